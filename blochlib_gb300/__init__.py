@@ -1,0 +1,375 @@
+"""blochlib_gb300: GB300-native powder-averaged MAS spin propagation (gamma-COMPUTE).
+
+Python mirror of BlochLib's host API for the spinning powder-FID path, over the C ABI in
+include/blochlib_gb300.h (libblochlib_gb300.so, built in-tree by blochlib_gb300/build.py):
+
+    SolidSys(lines)                    src/QMspins/sys.cc:40-42, read 120-204
+    SolidSys.Fx()/Fp()/Ix(k)/...       src/QMspins/spinsys.h:143-162
+    powder(powder.zcw, t, p[, g])      src/QMspins/driver/powder.cc:94-113, 248-280
+    powder.read(path)                  src/QMspins/driver/powder.cc:333-389
+    oneFID(sys, npts, sw, wr, rotb)    src/QMspins/driver/oneFID.h:103-108
+    oneFID.FID(powder, ro, det)        src/QMspins/driver/oneFID.h:200-208, 339-431
+    plotterFID(fid, file, dt)          src/utils/plotter.cc:49-135
+
+All compute runs in the CUDA library; there is no CPU fallback.  Loading fails loudly
+when the library is missing or cannot initialise a GPU.
+"""
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["SolidSys", "powder", "oneFID", "plotterFID", "Context", "Job", "BlochError", "library_path", "load"]
+
+_HERE = Path(__file__).resolve().parent
+_LIB = None
+
+
+def library_path():
+    return _HERE / "libblochlib_gb300.so"
+
+
+class BlochError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"bl_status {status}: {msg}")
+        self.status = status
+
+
+_SIGS = {
+    "bl_last_error": (ctypes.c_char_p, []),
+    "bl_version": (ctypes.c_char_p, []),
+    "bl_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_ctx_destroy": (None, [ctypes.c_void_p]),
+    "bl_ctx_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "bl_system_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_system_destroy": (None, [ctypes.c_void_p]),
+    "bl_system_dim": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_system_spins": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_system_operator": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p]),
+    "bl_system_blocks": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "bl_powder_zcw": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_powder_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_powder_from_arrays": (ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_powder_size": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_powder_get": (ctypes.c_int, [ctypes.c_void_p] * 5),
+    "bl_powder_destroy": (None, [ctypes.c_void_p]),
+    "bl_powder_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
+    "bl_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_job_run": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_job_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "bl_job_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_job_launches": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_job_flops": (ctypes.c_double, [ctypes.c_void_p]),
+    "bl_job_sw": (ctypes.c_double, [ctypes.c_void_p]),
+    "bl_job_describe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
+    "bl_job_destroy": (None, [ctypes.c_void_p]),
+    "bl_plotter_fid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_double]),
+    "bl_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "bl_job_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "bl_job_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bl_job_stage_flops": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "bl_job_reset_stage_times": (ctypes.c_int, [ctypes.c_void_p]),
+    "bl_job_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "bl_job_io_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
+    "bl_probe_fp64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+}
+
+STAGES = 8
+
+
+class FidParams(ctypes.Structure):
+    _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
+                ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int)]
+
+
+def load():
+    """Load the CUDA library (no fallback: raises if it is absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = library_path()
+    if not p.exists():
+        raise ImportError(f"{p} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(st):
+    if st != 0:
+        raise BlochError(st, load().bl_last_error().decode())
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _cmat(m, n):
+    m = np.ascontiguousarray(np.asarray(m, dtype=np.complex128))
+    if m.shape != (n, n):
+        raise ValueError(f"operator must be {n}x{n}, got {m.shape}")
+    return m
+
+
+class Context:
+    """One CUDA device + stream (bl_ctx)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.bl_ctx_create(int(device), int(hbm_budget), ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def stream(self):
+        return load().bl_ctx_stream(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bl_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(int(os.environ.get("BL_DEVICE", "0")))
+    return _default_ctx
+
+
+def probe_fp64_tflops(ctx=None):
+    """Measured DFMA throughput of the device (TFLOP/s)."""
+    t = ctypes.c_double()
+    _check(load().bl_probe_fp64((ctx or default_context())._h, ctypes.byref(t)))
+    return t.value
+
+
+class SolidSys:
+    """Spin system from the reference's text format (list of lines or one string)."""
+
+    def __init__(self, lines):
+        text = lines if isinstance(lines, str) else "\n".join(lines)
+        self.text = text
+        lib = load()
+        h = ctypes.c_void_p()
+        _check(lib.bl_system_create(text.encode(), ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                load().bl_system_destroy(self._h)
+        except Exception:
+            pass
+
+    def dim(self):
+        return load().bl_system_dim(self._h)
+
+    def spins(self):
+        return load().bl_system_spins(self._h)
+
+    def blocks(self):
+        lib = load()
+        n = ctypes.c_int()
+        _check(lib.bl_system_blocks(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        _check(lib.bl_system_blocks(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out.tolist()
+
+    def op(self, expr):
+        n = self.dim()
+        out = np.zeros((n, n), dtype=np.complex128)
+        _check(load().bl_system_operator(self._h, expr.encode(), _ptr(out)))
+        return out
+
+    # reference accessor names (spinsys.h:143-162)
+    def Fx(self): return self.op("Fx")
+    def Fy(self): return self.op("Fy")
+    def Fz(self): return self.op("Fz")
+    def Fp(self): return self.op("Fp")
+    def Fmi(self): return self.op("Fm")
+    def Fe(self): return self.op("Fe")
+    def Ix(self, k): return self.op(f"Ix {k}")
+    def Iy(self, k): return self.op(f"Iy {k}")
+    def Iz(self, k): return self.op(f"Iz {k}")
+    def Ip(self, k): return self.op(f"Ip {k}")
+    def Imi(self, k): return self.op(f"Im {k}")
+
+
+class powder:
+    """Powder angle set (theta, phi, gamma, weight), radians."""
+    zcw = "zcw"
+
+    def __init__(self, method=None, tstep=0, pstep=0, gstep=0, _handle=None):
+        lib = load()
+        if _handle is not None:
+            self._h = _handle
+        elif method == powder.zcw:
+            h = ctypes.c_void_p()
+            _check(lib.bl_powder_zcw(int(tstep), int(pstep), int(gstep), ctypes.byref(h)))
+            self._h = h
+        elif isinstance(method, (str, os.PathLike)):
+            h = ctypes.c_void_p()
+            _check(lib.bl_powder_read(str(method).encode(), ctypes.byref(h)))
+            self._h = h
+        else:
+            raise ValueError("powder(method): use powder.zcw or a powder file path")
+
+    @classmethod
+    def read(cls, path):
+        return cls(str(path))
+
+    @classmethod
+    def from_arrays(cls, theta, phi, gamma, weight):
+        th, ph, ga, w = (np.ascontiguousarray(np.asarray(x, dtype=np.float64)) for x in (theta, phi, gamma, weight))
+        if not (len(th) == len(ph) == len(ga) == len(w)):
+            raise ValueError("powder arrays differ in length")
+        h = ctypes.c_void_p()
+        _check(load().bl_powder_from_arrays(_ptr(th), _ptr(ph), _ptr(ga), _ptr(w), len(th), ctypes.byref(h)))
+        return cls(_handle=h)
+
+    def size(self):
+        return load().bl_powder_size(self._h)
+
+    def arrays(self):
+        n = self.size()
+        out = [np.zeros(n) for _ in range(4)]
+        _check(load().bl_powder_get(self._h, *(_ptr(a) for a in out)))
+        return tuple(out)  # theta, phi, gamma, weight
+
+    def __del__(self):
+        try:
+            if getattr(self, "_h", None):
+                load().bl_powder_destroy(self._h)
+        except Exception:
+            pass
+
+
+class Job:
+    """Resident job (bl_job): inputs on the device; run() recomputes the powder FID."""
+
+    def __init__(self, sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, ctx=None):
+        self.ctx = ctx or default_context()
+        n = sys.dim()
+        self._ro, self._det = _cmat(ro, n), _cmat(det, n)
+        self.params = FidParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision))
+        h = ctypes.c_void_p()
+        _check(load().bl_job_create(self.ctx._h, sys._h, pw._h, _ptr(self._ro), _ptr(self._det),
+                                    ctypes.byref(self.params), ctypes.byref(h)))
+        self._h = h
+        self.npts = int(npts)
+
+    def run(self):
+        _check(load().bl_job_run(self._h))
+
+    def read(self):
+        out = np.zeros(self.npts, dtype=np.complex128)
+        _check(load().bl_job_read(self._h, _ptr(out)))
+        return out
+
+    def sync(self):
+        _check(load().bl_job_sync(self._h))
+
+    @property
+    def launches(self):
+        return load().bl_job_launches(self._h)
+
+    @property
+    def flops(self):
+        return load().bl_job_flops(self._h)
+
+    @property
+    def sw(self):
+        return load().bl_job_sw(self._h)
+
+    def set_profiling(self, on=True):
+        _check(load().bl_job_set_profiling(self._h, int(bool(on))))
+
+    def stage_times(self):
+        """{stage name: (ms accumulated, launches)}"""
+        ms = np.zeros(STAGES)
+        nl = np.zeros(STAGES, dtype=np.int32)
+        _check(load().bl_job_stage_times(self._h, _ptr(ms), _ptr(nl)))
+        lib = load()
+        return {lib.bl_stage_name(i).decode(): (float(ms[i]), int(nl[i])) for i in range(STAGES)}
+
+    def stage_flops(self):
+        f = np.zeros(STAGES)
+        _check(load().bl_job_stage_flops(self._h, _ptr(f)))
+        lib = load()
+        return {lib.bl_stage_name(i).decode(): float(f[i]) for i in range(STAGES)}
+
+    def reset_stage_times(self):
+        _check(load().bl_job_reset_stage_times(self._h))
+
+    def run_timed(self, iters):
+        ms = ctypes.c_double()
+        _check(load().bl_job_run_timed(self._h, int(iters), ctypes.byref(ms)))
+        return ms.value
+
+    def io_bytes(self):
+        a, b = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(load().bl_job_io_bytes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def describe(self):
+        import json
+        buf = ctypes.create_string_buffer(4096)
+        load().bl_job_describe(self._h, buf, 4096)
+        return json.loads(buf.value.decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bl_job_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class oneFID:
+    """oneFID<SolidSys>(sys, npts, sw, wr, rotb_deg, startT)  (oneFID.h:103-108)."""
+
+    def __init__(self, sys, npts, sw=20000.0, wr=0.0, rotb=0.0, startT=0.0, precision=0, ctx=None):
+        self.sys, self.npts, self.sw, self.wr, self.rotb, self.startT = sys, int(npts), float(sw), float(wr), float(rotb), float(startT)
+        self.precision = precision
+        self.ctx = ctx
+        self.fid_ = np.zeros(self.npts, dtype=np.complex128)
+
+    def FID(self, pw, ro, det):
+        """Powder-summed FID, sum_c w_c FID_c (oneFID.h:200-208); updates self.sw to n*wr."""
+        ctx = self.ctx or default_context()
+        n = self.sys.dim()
+        ro, det = _cmat(ro, n), _cmat(det, n)
+        out = np.zeros(self.npts, dtype=np.complex128)
+        sw_out = np.zeros(1)
+        params = FidParams(self.npts, self.sw, self.wr, self.rotb, self.startT, int(self.precision))
+        _check(load().bl_powder_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
+                                    _ptr(out), _ptr(sw_out)))
+        self.sw = float(sw_out[0])
+        self.fid_ = out
+        return out
+
+
+def plotterFID(fid, datasave="fid", dt=1.0):
+    """7-column text file t, f, Re S, Im S, Re fid, Im fid, |S| (plotter.cc:49-135)."""
+    f = np.ascontiguousarray(np.asarray(fid, dtype=np.complex128))
+    _check(load().bl_plotter_fid(_ptr(f), len(f), str(datasave).encode(), float(dt)))
+    return str(datasave)

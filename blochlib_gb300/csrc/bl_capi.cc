@@ -1,0 +1,264 @@
+// C ABI of the engine (include/blochlib_gb300.h).  Converts exceptions to bl_status.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <memory>
+#include <string>
+
+#include "../../include/blochlib_gb300.h"
+#include "bl_engine.h"
+#include "bl_host.h"
+
+struct bl_ctx {
+  bl::Context c;
+};
+struct bl_system {
+  bl::SpinSystem s;
+};
+struct bl_powder {
+  bl::Powder p;
+};
+struct bl_job {
+  std::unique_ptr<bl::Job> j;
+};
+
+namespace {
+thread_local std::string g_err;
+
+bl_status fail(int code, const std::string &msg) {
+  g_err = msg;
+  return static_cast<bl_status>(code);
+}
+
+template <class F>
+bl_status guarded(F &&f) {
+  try {
+    g_err.clear();
+    f();
+    return BL_OK;
+  } catch (const bl::Error &e) {
+    return fail(e.code, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(BL_ERR_NOMEM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(BL_ERR_INVALID, e.what());
+  }
+}
+
+bl::CMatrix load_op(const double *m, int N) {
+  bl::CMatrix M(N);
+  for (size_t i = 0; i < M.a.size(); ++i) M.a[i] = bl::cplx(m[2 * i], m[2 * i + 1]);
+  return M;
+}
+
+bl::FidParams to_params(const bl_fid_params *p) {
+  bl::FidParams f;
+  f.npts = p->npts, f.sw = p->sw, f.wr = p->wr, f.rotb_deg = p->rotb_deg, f.start_t = p->start_t;
+  f.precision = p->precision;
+  return f;
+}
+}  // namespace
+
+extern "C" {
+
+const char *bl_last_error(void) { return g_err.c_str(); }
+const char *bl_version(void) { return "blochlib_gb300 0.1 (sm_103a, FP64 gamma-COMPUTE)"; }
+
+bl_status bl_ctx_create(int device, size_t hbm_budget, bl_ctx **out) {
+  if (!out) return fail(BL_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  return guarded([&] {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || device < 0 || device >= n)
+      throw bl::Error(BL_ERR_CUDA, std::string("no CUDA device ") + std::to_string(device) +
+                                       (e != cudaSuccess ? std::string(": ") + cudaGetErrorString(e) : ""));
+    if (cudaSetDevice(device) != cudaSuccess) throw bl::Error(BL_ERR_CUDA, "cudaSetDevice failed");
+    std::unique_ptr<bl_ctx> c(new bl_ctx);
+    c->c.device = device;
+    c->c.hbm_budget = hbm_budget;
+    if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess)
+      throw bl::Error(BL_ERR_CUDA, "cudaStreamCreate failed");
+    *out = c.release();
+  });
+}
+
+void bl_ctx_destroy(bl_ctx *ctx) { delete ctx; }
+void *bl_ctx_stream(bl_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+bl_status bl_system_create(const char *spin_text, bl_system **out) {
+  if (!spin_text || !out) return fail(BL_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] { *out = new bl_system{bl::SpinSystem::from_text(spin_text)}; });
+}
+
+void bl_system_destroy(bl_system *sys) { delete sys; }
+int bl_system_dim(const bl_system *sys) { return sys ? sys->s.dim() : 0; }
+int bl_system_spins(const bl_system *sys) { return sys ? sys->s.spins() : 0; }
+
+bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out) {
+  if (!sys || !expr || !out) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    bl::CMatrix M = sys->s.op(expr);
+    for (size_t i = 0; i < M.a.size(); ++i) out[2 * i] = M.a[i].real(), out[2 * i + 1] = M.a[i].imag();
+  });
+}
+
+bl_status bl_system_blocks(const bl_system *sys, int *sizes, int cap, int *nblocks) {
+  if (!sys || !nblocks) return fail(BL_ERR_INVALID, "null argument");
+  const auto &L = sys->s.layout();
+  *nblocks = int(L.size.size());
+  for (int k = 0; k < *nblocks && k < cap && sizes; ++k) sizes[k] = L.size[k];
+  return BL_OK;
+}
+
+bl_status bl_powder_zcw(int t, int p, int g, bl_powder **out) {
+  if (!out) return fail(BL_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  return guarded([&] { *out = new bl_powder{bl::powder_zcw(t, p, g)}; });
+}
+
+bl_status bl_powder_read(const char *path, bl_powder **out) {
+  if (!path || !out) return fail(BL_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] { *out = new bl_powder{bl::powder_read(path)}; });
+}
+
+bl_status bl_powder_from_arrays(const double *theta, const double *phi, const double *gamma, const double *weight,
+                                int n, bl_powder **out) {
+  if (!out || n < 0 || (n > 0 && (!theta || !phi || !weight))) return fail(BL_ERR_INVALID, "bad powder arrays");
+  *out = nullptr;
+  return guarded([&] {
+    bl::Powder P;
+    P.theta.assign(theta, theta + n);
+    P.phi.assign(phi, phi + n);
+    P.weight.assign(weight, weight + n);
+    if (gamma) P.gamma.assign(gamma, gamma + n);
+    else P.gamma.assign(n, 0.0);
+    *out = new bl_powder{P};
+  });
+}
+
+int bl_powder_size(const bl_powder *pw) { return pw ? pw->p.size() : 0; }
+
+bl_status bl_powder_get(const bl_powder *pw, double *theta, double *phi, double *gamma, double *weight) {
+  if (!pw) return fail(BL_ERR_INVALID, "null powder");
+  const auto &P = pw->p;
+  if (theta) std::memcpy(theta, P.theta.data(), sizeof(double) * P.size());
+  if (phi) std::memcpy(phi, P.phi.data(), sizeof(double) * P.size());
+  if (gamma) std::memcpy(gamma, P.gamma.data(), sizeof(double) * P.size());
+  if (weight) std::memcpy(weight, P.weight.data(), sizeof(double) * P.size());
+  return BL_OK;
+}
+
+void bl_powder_destroy(bl_powder *pw) { delete pw; }
+
+bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
+                        const bl_fid_params *params, bl_job **out) {
+  if (!ctx || !sys || !pw || !ro || !det || !params || !out) return fail(BL_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] {
+    int N = sys->s.dim();
+    std::unique_ptr<bl_job> j(new bl_job);
+    j->j.reset(new bl::Job(ctx->c, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
+    *out = j.release();
+  });
+}
+
+bl_status bl_job_run(bl_job *job) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  return guarded([&] { job->j->run(); });
+}
+
+bl_status bl_job_read(bl_job *job, double *fid_out) {
+  if (!job || !fid_out) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] { job->j->read(fid_out); });
+}
+
+bl_status bl_job_sync(bl_job *job) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  return guarded([&] {
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) throw bl::Error(BL_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  });
+}
+
+int bl_job_launches(const bl_job *job) { return job ? job->j->kernels_per_run() : 0; }
+double bl_job_flops(const bl_job *job) { return job ? job->j->flops() : 0.0; }
+double bl_job_sw(const bl_job *job) { return job ? job->j->sw_out() : 0.0; }
+
+int bl_job_describe(const bl_job *job, char *buf, int cap) {
+  if (!job || !buf || cap <= 0) return 0;
+  std::string s = job->j->describe();
+  int n = int(std::min<size_t>(s.size(), size_t(cap - 1)));
+  std::memcpy(buf, s.data(), n);
+  buf[n] = 0;
+  return n;
+}
+
+void bl_job_destroy(bl_job *job) { delete job; }
+
+const char *bl_stage_name(int stage) { return bl::Job::stage_name(stage); }
+
+bl_status bl_job_set_profiling(bl_job *job, int on) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  job->j->set_profiling(on != 0);
+  return BL_OK;
+}
+
+bl_status bl_job_stage_times(const bl_job *job, double *ms, int *launches) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  job->j->stage_times(ms, launches);
+  return BL_OK;
+}
+
+bl_status bl_job_stage_flops(const bl_job *job, double *flops) {
+  if (!job || !flops) return fail(BL_ERR_INVALID, "null argument");
+  job->j->stage_flops(flops);
+  return BL_OK;
+}
+
+bl_status bl_job_reset_stage_times(bl_job *job) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  job->j->reset_stage_times();
+  return BL_OK;
+}
+
+bl_status bl_job_run_timed(bl_job *job, int iters, double *ms_total) {
+  if (!job || !ms_total || iters < 0) return fail(BL_ERR_INVALID, "bad argument");
+  return guarded([&] { *ms_total = job->j->run_timed(iters); });
+}
+
+bl_status bl_job_io_bytes(const bl_job *job, size_t *h2d, size_t *d2h) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  if (h2d) *h2d = job->j->h2d_bytes();
+  if (d2h) *d2h = job->j->d2h_bytes();
+  return BL_OK;
+}
+
+bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] { *tflops = bl::probe_fp64_tflops(ctx->c); });
+}
+
+bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
+                        const bl_fid_params *params, double *fid_out, double *sw_out) {
+  if (!fid_out) return fail(BL_ERR_INVALID, "null output");
+  bl_job *job = nullptr;
+  bl_status st = bl_job_create(ctx, sys, pw, ro, det, params, &job);
+  if (st != BL_OK) return st;
+  st = bl_job_run(job);
+  if (st == BL_OK) st = bl_job_read(job, fid_out);
+  if (st == BL_OK && sw_out) *sw_out = job->j->sw_out();
+  std::string keep = g_err;
+  bl_job_destroy(job);
+  g_err = keep;
+  return st;
+}
+
+bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt) {
+  if (!fid || !path || npts <= 0) return fail(BL_ERR_INVALID, "bad arguments");
+  return guarded([&] { bl::write_fid_text(path, reinterpret_cast<const bl::cplx *>(fid), npts, dt); });
+}
+
+}  // extern "C"

@@ -1,0 +1,1203 @@
+// GPU engine: spinning powder FID by gamma-COMPUTE, all arithmetic FP64.
+//
+// Reference algorithm (paths inside the BlochLib tree):
+//   per crystallite  oneFID::singleSpinningFID   src/QMspins/driver/oneFID.h:419-431
+//   step loop        compute::calcUFID           src/QMspins/driver/compute.h:257-274
+//   H(t)             SolidSys::Hamiltonian       src/QMspins/sys.cc:749-770
+//   exp(-i2pi tau H) Mexp (Hermitian)            src/container/matrix/matexp.h:240-252
+//   reconstruction   compute::calcFID            src/QMspins/driver/compute.h:308-461
+//   powder sum       oneFID::spinningFID         src/QMspins/driver/oneFID.h:339-410
+//
+// GB300 layout.  Every per-crystallite array is stored with the crystallite index
+// fastest ([item][c], stride Cpad = C rounded up to 32) and every kernel maps the 32
+// lanes of a warp onto 32 consecutive crystallites, so loads/stores are coalesced and
+// all control flow (block sizes, steps, element indices) is warp-uniform.  The
+// Hamiltonian of every SolidSys commutes with total Fz, so H, U and the Dyson products
+// are block diagonal; the host finds the blocks (connected components of the operator
+// pattern) and the kernels work per block.  FP64 issue rate is the bound on GB300
+// (~1.2 TFLOP/s DFMA), so the kernels avoid FP64 work rather than memory traffic:
+//   k_step_prop  (c, block, step)   H_i block, Jacobi eigh, U_i = V e^{-i2pi tau L} V^T
+//   k_dyson      (c, block, column) A_{i+1} = U_i A_i, one column per thread
+//   k_floquet    (c, block)         unitary eig of A_n (Cayley transform + Jacobi)
+//   k_eigframe   (c, block, step)   W_i = A_{i+1} V_F  (in place)
+//   k_qr         (c, step, pair)    Q_i = W^H D W (and R_i = W^H rho W when needed)
+//   k_fave       (c, element, p)    G_p = sum_i q_{(i+p)%n} r_i (with the period twist)
+//   k_fid        (c, j, p)          fid[jn+p] = sum_e z_e^j G_p(e); weighted warp sum
+//   k_reduce     (k)                compensated sum of warp partials (fixed order)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <stdexcept>
+
+#include "bl_engine.h"
+
+namespace bl {
+
+namespace {
+
+constexpr int kMaxBlock = 8;      // largest Hamiltonian block handled by this engine
+constexpr int kMaxSweeps = 40;    // bound on Jacobi sweeps; exceeding it sets a status bit
+constexpr int kThreads = 128;
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kPi2 = 2.0 * kPi;
+
+enum StatusBits { kNoConvergeStep = 1, kNoConvergeFloquet = 2, kSingularCayley = 4 };
+
+#define CUDA_OK(x)                                                                          \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess) throw Error(3, std::string("CUDA: ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------------------ complex helpers
+__device__ __forceinline__ double2 cmk(double r, double i) { return make_double2(r, i); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return cmk(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return cmk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return cmk(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cconj(double2 a) { return cmk(a.x, -a.y); }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return cmk(a.x * s, a.y * s); }
+// acc + a*b
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 acc) {
+  return cmk(fma(a.x, b.x, fma(-a.y, b.y, acc.x)), fma(a.x, b.y, fma(a.y, b.x, acc.y)));
+}
+// acc + conj(a)*b
+__device__ __forceinline__ double2 cfmaconj(double2 a, double2 b, double2 acc) {
+  return cmk(fma(a.x, b.x, fma(a.y, b.y, acc.x)), fma(a.x, b.y, fma(-a.y, b.x, acc.y)));
+}
+__device__ __forceinline__ double2 cexp(double2 z) {
+  double s, c, e = exp(z.x);
+  sincos(z.y, &s, &c);
+  return cmk(e * c, e * s);
+}
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  double d = b.x * b.x + b.y * b.y;
+  return cmk((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+__device__ __forceinline__ double chop1(double v, double eps) { return fabs(v) < eps ? 0.0 : v; }
+
+// ------------------------------------------------------------------ job description
+struct DevSys {
+  int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym;
+  double tau, wr, sin_rotb, cos_rotb, scale;
+  // per block
+  const int *bs, *boff, *bpoff;
+  // per interaction: crystal tensor (xx xy xz yy yz zz), scale, packed operator
+  const double *pas, *iscale, *Tk, *Hc;
+  // Q pairs (D blocks) and R pairs (rho blocks)
+  int npq, npr;
+  const int *qa, *qb, *qoff, *doff;
+  const int *ra, *rb, *roff, *rhooff;
+  const double2 *Dblk, *Rhoblk;
+  // elements of the Fave/FID sums
+  const int *eq, *erev, *er, *erg, *esg;
+  // per crystallite (this batch): Rp (9 x Cpad), t0, weight
+  const double *Rp, *t0, *w;
+  // work buffers
+  double2 *U, *A, *VF, *L, *Q, *R, *G, *Z, *partial;
+  int warp_base;  // global warp index of this batch's first crystallite
+  int *status;
+};
+
+// ------------------------------------------------------------------ eigen-solvers
+// Cyclic Jacobi, real symmetric, B x B in registers.  a becomes diagonal, v the
+// eigenvectors (columns).  Returns false if kMaxSweeps was not enough.
+template <int B>
+__device__ bool jacobi_sym(double (&a)[B][B], double (&v)[B][B]) {
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = 0; q < B; ++q) v[p][q] = (p == q) ? 1.0 : 0.0;
+  if (B == 1) return true;
+  for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+    double off = 0, dg = 0;
+#pragma unroll
+    for (int p = 0; p < B; ++p) {
+      dg = fma(a[p][p], a[p][p], dg);
+#pragma unroll
+      for (int q = p + 1; q < B; ++q) off = fma(a[p][q], a[p][q], off);
+    }
+    if (off <= 1e-34 * dg || off == 0.0) return true;
+#pragma unroll
+    for (int p = 0; p < B - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < B; ++q) {
+        double apq = a[p][q];
+        if (apq != 0.0) {
+          double theta = (a[q][q] - a[p][p]) / (2.0 * apq);
+          double t;
+          if (fabs(theta) > 1e100) t = 0.5 / theta;
+          else t = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+          double c = rsqrt(fma(t, t, 1.0));
+          double s = t * c, tz = s / (1.0 + c);
+          a[p][p] = fma(-t, apq, a[p][p]);
+          a[q][q] = fma(t, apq, a[q][q]);
+          a[p][q] = 0.0;
+          a[q][p] = 0.0;
+#pragma unroll
+          for (int r = 0; r < B; ++r) {
+            if (r != p && r != q) {
+              double arp = a[r][p], arq = a[r][q];
+              double nrp = arp - s * fma(tz, arp, arq);
+              double nrq = arq + s * fma(-tz, arq, arp);
+              a[r][p] = nrp, a[p][r] = nrp;
+              a[r][q] = nrq, a[q][r] = nrq;
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < B; ++r) {
+            double vrp = v[r][p], vrq = v[r][q];
+            v[r][p] = vrp - s * fma(tz, vrp, vrq);
+            v[r][q] = vrq + s * fma(-tz, vrq, vrp);
+          }
+        }
+      }
+  }
+  return false;
+}
+
+// Cyclic Jacobi, complex Hermitian (B x B).  Same rotation as the oracle's.
+template <int B>
+__device__ bool jacobi_herm(double2 (&h)[B][B], double2 (&v)[B][B]) {
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = 0; q < B; ++q) v[p][q] = cmk(p == q ? 1.0 : 0.0, 0.0);
+  if (B == 1) return true;
+  for (int sweep = 0; sweep < kMaxSweeps; ++sweep) {
+    double off = 0, dg = 0;
+#pragma unroll
+    for (int p = 0; p < B; ++p) {
+      dg = fma(h[p][p].x, h[p][p].x, dg);
+#pragma unroll
+      for (int q = p + 1; q < B; ++q) off += h[p][q].x * h[p][q].x + h[p][q].y * h[p][q].y;
+    }
+    if (off <= 1e-34 * dg || off == 0.0) return true;
+#pragma unroll
+    for (int p = 0; p < B - 1; ++p)
+#pragma unroll
+      for (int q = p + 1; q < B; ++q) {
+        double2 hpq = h[p][q];
+        double ab = hypot(hpq.x, hpq.y);
+        if (ab != 0.0) {
+          double2 ph = cmk(hpq.x / ab, hpq.y / ab);
+          double theta = 0.5 * (h[q][q].x - h[p][p].x) / ab;
+          double t;
+          if (fabs(theta) > 1e100) t = 0.5 / theta;
+          else t = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+          double c = rsqrt(fma(t, t, 1.0)), s = t * c;
+          double2 sp = cscale(ph, s), spc = cconj(sp);
+#pragma unroll
+          for (int k = 0; k < B; ++k) {  // columns p, q
+            double2 hkp = h[k][p], hkq = h[k][q];
+            h[k][p] = csub(cscale(hkp, c), cmul(spc, hkq));
+            h[k][q] = cadd(cmul(sp, hkp), cscale(hkq, c));
+          }
+#pragma unroll
+          for (int k = 0; k < B; ++k) {  // rows p, q
+            double2 hpk = h[p][k], hqk = h[q][k];
+            h[p][k] = csub(cscale(hpk, c), cmul(sp, hqk));
+            h[q][k] = cadd(cmul(spc, hpk), cscale(hqk, c));
+          }
+          h[p][q] = cmk(0, 0);
+          h[q][p] = cmk(0, 0);
+          h[p][p].y = 0.0;
+          h[q][q].y = 0.0;
+#pragma unroll
+          for (int k = 0; k < B; ++k) {
+            double2 vkp = v[k][p], vkq = v[k][q];
+            v[k][p] = csub(cscale(vkp, c), cmul(spc, vkq));
+            v[k][q] = cadd(cmul(sp, vkp), cscale(vkq, c));
+          }
+        }
+      }
+  }
+  return false;
+}
+
+// Eigen-decomposition of a unitary U = V diag(lam) V^H via the Cayley transform of
+// W = e^{ia} U: K = i (I+W)^{-1} (I-W) is Hermitian with U's eigenvectors.  A first
+// pass (a = 0.5) locates the spectrum; the second puts -1 in its widest gap.
+template <int B>
+__device__ int unitary_eig(const double2 (&U)[B][B], double2 (&lam)[B], double2 (&V)[B][B]) {
+  int st = 0;
+  if (B == 1) {
+    lam[0] = U[0][0];
+    V[0][0] = cmk(1, 0);
+    return 0;
+  }
+  double a = 0.5;
+  for (int pass = 0; pass < 2; ++pass) {
+    double sa, ca;
+    sincos(a, &sa, &ca);
+    double2 ea = cmk(ca, sa);
+    double2 M[B][B], X[B][B];
+#pragma unroll
+    for (int r = 0; r < B; ++r)
+#pragma unroll
+      for (int c = 0; c < B; ++c) {
+        double2 w = cmul(ea, U[r][c]);
+        double id = (r == c) ? 1.0 : 0.0;
+        M[r][c] = cmk(id + w.x, w.y);
+        X[r][c] = cmk(id - w.x, -w.y);
+      }
+    // Gaussian elimination with partial pivoting: M X' = X
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      int piv = k;
+      double best = M[k][k].x * M[k][k].x + M[k][k].y * M[k][k].y;
+#pragma unroll
+      for (int i = k + 1; i < B; ++i) {
+        double m2 = M[i][k].x * M[i][k].x + M[i][k].y * M[i][k].y;
+        if (m2 > best) best = m2, piv = i;
+      }
+      if (best == 0.0) {
+        st |= kSingularCayley;
+        best = 1e-300;
+      }
+#pragma unroll
+      for (int i = k + 1; i < B; ++i) {
+        if (i == piv) {
+#pragma unroll
+          for (int j = 0; j < B; ++j) {
+            double2 t = M[k][j];
+            M[k][j] = M[i][j];
+            M[i][j] = t;
+            t = X[k][j];
+            X[k][j] = X[i][j];
+            X[i][j] = t;
+          }
+        }
+      }
+      double2 inv = cdiv(cmk(1, 0), M[k][k]);
+#pragma unroll
+      for (int i = k + 1; i < B; ++i) {
+        double2 f = cmul(M[i][k], inv);
+#pragma unroll
+        for (int j = k; j < B; ++j) M[i][j] = csub(M[i][j], cmul(f, M[k][j]));
+#pragma unroll
+        for (int j = 0; j < B; ++j) X[i][j] = csub(X[i][j], cmul(f, X[k][j]));
+      }
+    }
+#pragma unroll
+    for (int k = B - 1; k >= 0; --k) {
+      double2 inv = cdiv(cmk(1, 0), M[k][k]);
+#pragma unroll
+      for (int j = 0; j < B; ++j) {
+        double2 s = X[k][j];
+#pragma unroll
+        for (int i = k + 1; i < B; ++i) s = csub(s, cmul(M[k][i], X[i][j]));
+        X[k][j] = cmul(s, inv);
+      }
+    }
+    // K = i X, Hermitian part
+    double2 K[B][B];
+#pragma unroll
+    for (int r = 0; r < B; ++r)
+#pragma unroll
+      for (int c = 0; c < B; ++c) {
+        double2 krc = cmk(-X[r][c].y, X[r][c].x);
+        double2 kcr = cmk(-X[c][r].y, X[c][r].x);
+        K[r][c] = cscale(cadd(krc, cconj(kcr)), 0.5);
+      }
+    if (!jacobi_herm<B>(K, V)) st |= kNoConvergeFloquet;
+    // Rayleigh quotients
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      double2 s = cmk(0, 0);
+#pragma unroll
+      for (int k = 0; k < B; ++k) {
+        double2 uv = cmk(0, 0);
+#pragma unroll
+        for (int l = 0; l < B; ++l) uv = cfma(U[k][l], V[l][r], uv);
+        s = cfmaconj(V[k][r], uv, s);
+      }
+      lam[r] = s;
+    }
+    if (pass == 0) {
+      double th[B];
+#pragma unroll
+      for (int r = 0; r < B; ++r) th[r] = atan2(lam[r].y, lam[r].x);
+      // insertion sort
+#pragma unroll
+      for (int i = 1; i < B; ++i) {
+#pragma unroll
+        for (int j = i; j > 0; --j) {
+          if (th[j] < th[j - 1]) {
+            double t = th[j];
+            th[j] = th[j - 1];
+            th[j - 1] = t;
+          }
+        }
+      }
+      double best = -1, mid = 0;
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        double lo = th[r], hi = (r + 1 < B) ? th[r + 1] : th[0] + kPi2;
+        if (hi - lo > best) best = hi - lo, mid = 0.5 * (lo + hi);
+      }
+      a = kPi - mid;
+    }
+  }
+  return st;
+}
+
+// ------------------------------------------------------------------ kernels
+__device__ __forceinline__ size_t at(int item, int c, int Cpad) { return size_t(item) * Cpad + c; }
+
+// One thread per (crystallite, block k, step i): U_i block.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * s.n) return;
+  int i = int(rest % s.n);
+  int k = blist[rest / s.n];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  // rotor phase at the step midpoint (sys.cc:754-755)
+  double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
+  double tmid = (t2 - t1) / 2.0 + t1;
+  double sp, cp;
+  sincos(tmid * s.wr * kPi2, &sp, &cp);
+  // row 2 of R_rotor(phi, beta) times R_powder
+  double rr0 = sp * s.sin_rotb, rr1 = -cp * s.sin_rotb, rr2 = s.cos_rotb;
+  double r[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    r[j] = rr0 * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr1 * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
+           rr2 * s.Rp[at(2 * 3 + j, c, s.Cpad)];
+  double h[B][B];
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
+  for (int kk = 0; kk < s.nint; ++kk) {
+    const double *P = s.pas + 6 * kk;
+    // a = r^T PAS r  (the (2,2) element of M PAS M^T)
+    double a = r[0] * (P[0] * r[0] + P[1] * r[1] + P[2] * r[2]) + r[1] * (P[1] * r[0] + P[3] * r[1] + P[4] * r[2]) +
+               r[2] * (P[2] * r[0] + P[4] * r[1] + P[5] * r[2]);
+    double f = s.iscale[kk] * a;
+    const double *T = s.Tk + size_t(kk) * s.S2 + bp;
+#pragma unroll
+    for (int p = 0; p < B; ++p)
+#pragma unroll
+      for (int q = 0; q < B; ++q) h[p][q] = fma(f, T[p * B + q], h[p][q]);
+  }
+  double v[B][B];
+  if (!jacobi_sym<B>(h, v)) atomicOr(s.status, kNoConvergeStep);
+  double2 e[B];
+  const double tp = s.tau * kPi2;
+#pragma unroll
+  for (int j = 0; j < B; ++j) {
+    double sn, cs;
+    sincos(tp * h[j][j], &sn, &cs);
+    e[j] = cmk(chop1(cs, 1e-12), chop1(-sn, 1e-12));
+  }
+  double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      double2 u = cmk(0, 0);
+#pragma unroll
+      for (int j = 0; j < B; ++j) {
+        double vv = v[p][j] * v[q][j];
+        u.x = fma(vv, e[j].x, u.x);
+        u.y = fma(vv, e[j].y, u.y);
+      }
+      Ub[at(bp + p * B + q, c, s.Cpad)] = u;
+      if (q != p) Ub[at(bp + q * B + p, c, s.Cpad)] = u;
+    }
+}
+
+// One thread per (crystallite, block, column j): column j of A_{i+1} = U_i A_i.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_dyson(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * B) return;
+  int j = int(rest % B);
+  int k = blist[rest / B];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  double2 x[B];
+#pragma unroll
+  for (int r = 0; r < B; ++r) x[r] = cmk(r == j ? 1.0 : 0.0, 0.0);
+  for (int i = 0; i < s.n; ++i) {
+    const double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+    double2 y[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      double2 acc = cmk(0, 0);
+#pragma unroll
+      for (int l = 0; l < B; ++l) acc = cfma(Ub[at(bp + r * B + l, c, s.Cpad)], x[l], acc);
+      y[r] = acc;
+    }
+    double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      x[r] = y[r];
+      Ab[at(bp + r * B + j, c, s.Cpad)] = y[r];
+    }
+  }
+}
+
+// One thread per (crystallite, block): Floquet eigen-decomposition of A_n.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_floquet(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= nblist) return;
+  int k = blist[rest];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k], bo = s.boff[k];
+  const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
+  double2 U[B][B], lam[B], V[B][B];
+#pragma unroll
+  for (int r = 0; r < B; ++r)
+#pragma unroll
+    for (int q = 0; q < B; ++q) U[r][q] = An[at(bp + r * B + q, c, s.Cpad)];
+  int st = unitary_eig<B>(U, lam, V);
+  if (st) atomicOr(s.status, st);
+#pragma unroll
+  for (int r = 0; r < B; ++r) {
+#pragma unroll
+    for (int q = 0; q < B; ++q) s.VF[at(bp + r * B + q, c, s.Cpad)] = V[r][q];
+    // principal-branch log: (ln|lam|, atan2)   (complex.h:1058-1061)
+    s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
+  }
+}
+
+// One thread per (crystallite, block, step): W_i = A_{i+1} V_F, in place.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_eigframe(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * s.n) return;
+  int i = int(rest % s.n);
+  int k = blist[rest / s.n];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  double2 V[B][B];
+#pragma unroll
+  for (int r = 0; r < B; ++r)
+#pragma unroll
+    for (int q = 0; q < B; ++q) V[r][q] = s.VF[at(bp + r * B + q, c, s.Cpad)];
+  double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+#pragma unroll
+  for (int r = 0; r < B; ++r) {
+    double2 a[B];
+#pragma unroll
+    for (int l = 0; l < B; ++l) a[l] = Ab[at(bp + r * B + l, c, s.Cpad)];
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      double2 acc = cmk(0, 0);
+#pragma unroll
+      for (int l = 0; l < B; ++l) acc = cfma(a[l], V[l][q], acc);
+      Ab[at(bp + r * B + q, c, s.Cpad)] = acc;
+    }
+  }
+}
+
+// One thread per (crystallite, step, pair): Q^{ab} = W_a^H D_ab W_b  (and R pairs).
+// compute.h:378-383: Qs[i] = adjprop(evect, adjprop(As[i+1], det)).
+__global__ void __launch_bounds__(kThreads) k_qr(DevSys s) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  int npair = s.npq + s.npr;
+  if (rest >= long(npair) * s.n) return;
+  int i = int(rest % s.n);
+  int pr = int(rest / s.n);
+  if (c >= s.C) return;
+  bool isq = pr < s.npq;
+  int a, b, off, moff;
+  const double2 *M;
+  double2 *out;
+  int nitems;
+  if (isq) {
+    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = s.Q, nitems = s.nq;
+  } else {
+    int p2 = pr - s.npq;
+    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = s.R, nitems = s.nr;
+  }
+  const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
+  const double2 *W = s.A + size_t(i) * s.S2 * s.Cpad;
+  double2 X[kMaxBlock * kMaxBlock];
+  // X = M_ab W_b  (ba x bb)
+  for (int l = 0; l < ba; ++l)
+    for (int q = 0; q < bb; ++q) X[l * bb + q] = cmk(0, 0);
+  for (int l = 0; l < ba; ++l)
+    for (int m = 0; m < bb; ++m) {
+      double2 d = M[moff + l * bb + m];
+      if (d.x == 0.0 && d.y == 0.0) continue;
+      for (int q = 0; q < bb; ++q) X[l * bb + q] = cfma(d, W[at(pb + m * bb + q, c, s.Cpad)], X[l * bb + q]);
+    }
+  double2 *ob = out + size_t(i) * nitems * s.Cpad;
+  for (int r = 0; r < ba; ++r)
+    for (int q = 0; q < bb; ++q) {
+      double2 acc = cmk(0, 0);
+      for (int l = 0; l < ba; ++l) acc = cfmaconj(W[at(pa + l * ba + r, c, s.Cpad)], X[l * bb + q], acc);
+      ob[at(off + r * bb + q, c, s.Cpad)] = acc;
+    }
+}
+
+constexpr int kFavePT = 8;
+
+// One thread per (crystallite, element, tile of kFavePT values of p).
+// G_p = sum_{i<n-p} q_{i+p} r_i + z sum_{i>=n-p} q_{i+p-n} r_i with z = e^{i n tau w}.
+// Equals compute.h:406-427's Fave_p(r,s) times e^{i p tau w_rs}, so that
+// fid[jn+p] = sum_e z_e^j G_p(e) reproduces compute.h:440-459.
+__global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  int ntile = (s.n + kFavePT - 1) / kFavePT;
+  if (rest >= long(s.ne) * ntile) return;
+  int tile = int(rest % ntile);
+  int e = int(rest / ntile);
+  if (c >= s.C) return;
+  const int eq = s.eq[e], erev = s.erev[e], er = s.er[e];
+  // w_rs = chop((l_r - l_s)/(i n tau), 1e-10)   (compute.h:327-335)
+  double2 lr = s.L[at(s.erg[e], c, s.Cpad)], ls = s.L[at(s.esg[e], c, s.Cpad)];
+  double2 d = csub(lr, ls);
+  double nt = double(s.n) * s.tau;
+  double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+  // z = exp(i n tau w)
+  double2 z = cexp(cmk(-nt * w.y, nt * w.x));
+  if (tile == 0) {
+    for (int j = 0; j < s.J; ++j) {
+      double2 zj = cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x));
+      s.Z[at(j * s.ne + e, c, s.Cpad)] = zj;
+    }
+  }
+  const int p0 = tile * kFavePT;
+  double2 s1[kFavePT], s2[kFavePT];
+#pragma unroll
+  for (int t = 0; t < kFavePT; ++t) s1[t] = s2[t] = cmk(0, 0);
+  const size_t qstride = size_t(s.nq) * s.Cpad, rstride = size_t(s.nr) * s.Cpad;
+  for (int i = 0; i < s.n; ++i) {
+    double2 q = s.Q[i * qstride + at(eq, c, s.Cpad)];
+    double2 rho;
+    if (s.rosym) {
+      rho = cconj(q);
+      if (erev >= 0) rho = cadd(rho, s.Q[i * qstride + at(erev, c, s.Cpad)]);
+    } else {
+      rho = s.R[i * rstride + at(er, c, s.Cpad)];
+    }
+#pragma unroll
+    for (int t = 0; t < kFavePT; ++t) {
+      int p = p0 + t;
+      if (p < s.n) {
+        int j = i + p;
+        if (j < s.n) {
+          s1[t] = cfma(s.Q[j * qstride + at(eq, c, s.Cpad)], rho, s1[t]);
+        } else {
+          s2[t] = cfma(s.Q[(j - s.n) * qstride + at(eq, c, s.Cpad)], rho, s2[t]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < kFavePT; ++t) {
+    int p = p0 + t;
+    if (p < s.n) s.G[at(p * s.ne + e, c, s.Cpad)] = cfma(z, s2[t], s1[t]);
+  }
+}
+
+constexpr int kFidJT = 4, kFidPT = 4;
+
+// One thread per (crystallite, tile of kFidJT j's, tile of kFidPT p's); lanes are
+// 32 consecutive crystallites, reduced with the powder weights by warp shuffles.
+__global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  int npt = (s.n + kFidPT - 1) / kFidPT, njt = (s.J + kFidJT - 1) / kFidJT;
+  if (rest >= long(npt) * njt) return;  // warp-uniform: whole warp leaves together
+  int pt = int(rest % npt), jt = int(rest / npt);
+  int p0 = pt * kFidPT, j0 = jt * kFidJT;
+  double2 acc[kFidJT][kFidPT];
+#pragma unroll
+  for (int a = 0; a < kFidJT; ++a)
+#pragma unroll
+    for (int b = 0; b < kFidPT; ++b) acc[a][b] = cmk(0, 0);
+  if (c < s.C) {
+    for (int e = 0; e < s.ne; ++e) {
+      double2 zj[kFidJT], gp[kFidPT];
+#pragma unroll
+      for (int a = 0; a < kFidJT; ++a) zj[a] = (j0 + a < s.J) ? s.Z[at((j0 + a) * s.ne + e, c, s.Cpad)] : cmk(0, 0);
+#pragma unroll
+      for (int b = 0; b < kFidPT; ++b) gp[b] = (p0 + b < s.n) ? s.G[at((p0 + b) * s.ne + e, c, s.Cpad)] : cmk(0, 0);
+#pragma unroll
+      for (int a = 0; a < kFidJT; ++a)
+#pragma unroll
+        for (int b = 0; b < kFidPT; ++b) acc[a][b] = cfma(zj[a], gp[b], acc[a][b]);
+    }
+  }
+  double wc = (c < s.C) ? s.w[c] * s.scale : 0.0;
+  int lane = threadIdx.x & 31;
+  int wglob = s.warp_base + c / 32;
+#pragma unroll
+  for (int a = 0; a < kFidJT; ++a)
+#pragma unroll
+    for (int b = 0; b < kFidPT; ++b) {
+      double2 v = cscale(acc[a][b], wc);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+      }
+      int k = (j0 + a) * s.n + p0 + b;
+      if (lane == 0 && p0 + b < s.n && k < s.npts) s.partial[size_t(wglob) * s.npts + k] = v;
+    }
+}
+
+// Compensated (Kahan) sum of the warp partials in fixed order: deterministic.
+__global__ void k_reduce(const double2 *__restrict__ partial, int nw, int npts, double2 *__restrict__ fid) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= npts) return;
+  double sx = 0, sy = 0, cx = 0, cy = 0;
+  for (int w = 0; w < nw; ++w) {
+    double2 v = partial[size_t(w) * npts + k];
+    double yx = v.x - cx, tx = sx + yx;
+    cx = (tx - sx) - yx, sx = tx;
+    double yy = v.y - cy, ty = sy + yy;
+    cy = (ty - sy) - yy, sy = ty;
+  }
+  fid[k] = make_double2(sx, sy);
+}
+
+inline unsigned grid_for(long threads) { return unsigned((threads + kThreads - 1) / kThreads); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ host side
+Context::~Context() {
+  if (stream) cudaStreamDestroy(stream);
+}
+
+static size_t *g_upload_counter = nullptr;  // set while a Job uploads its inputs
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    n = count;
+    if (count) CUDA_OK(cudaMalloc(&p, count * sizeof(T)));
+  }
+  DevBuf() {}
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr, o.n = 0; }
+  void upload(const std::vector<T> &v, cudaStream_t st) {
+    alloc(v.size());
+    if (!v.empty()) CUDA_OK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+    if (g_upload_counter) *g_upload_counter += v.size() * sizeof(T);
+  }
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+struct JobImpl {
+  Context *ctx;
+  FidParams P;
+  int C = 0, n = 0, gammaloop = 1, J = 0, rosym = 0;
+  double tau = 0, sw_out = 0;
+  BlockLayout L;
+  int nint = 0, nq = 0, nr = 0, ne = 0, npq = 0, npr = 0;
+  int Cb = 0, nbatch = 0, nwarps_total = 0;
+  std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices
+  DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status;
+  std::vector<DevBuf<int>> blist;
+  DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
+  DevBuf<double2> Dblk, Rhoblk;
+  DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid;
+  DevBuf<double> Rp_b, t0_b, w_b;
+  std::vector<double> h_Rp, h_t0, h_w;  // all virtual crystallites (C * gammaloop)
+  int Ceff = 0;
+  double flops = 0;
+  int launches = 0;
+  size_t h2d = 0;
+  bool profiling = false;
+  double stage_ms[Job::kStages] = {0};
+  int stage_launch[Job::kStages] = {0};
+  double stage_fl[Job::kStages] = {0};
+  std::vector<cudaEvent_t> evpool;  // stage-boundary events (created when profiling)
+  struct Mark {
+    int stage, b, e, nlaunch;
+  };
+  std::vector<Mark> marks;
+  int evnext = 0;
+  ~JobImpl() {
+    for (auto &e : evpool) cudaEventDestroy(e);
+  }
+  double cos_rotb = 1, sin_rotb = 0;
+  DevSys base{};
+};
+
+static bool any_nonzero(const CMatrix &M, const BlockLayout &L, int a, int b) {
+  for (int r = 0; r < L.size[a]; ++r)
+    for (int s = 0; s < L.size[b]; ++s)
+      if (M(L.perm[L.off[a] + r], L.perm[L.off[b] + s]) != cplx(0, 0)) return true;
+  return false;
+}
+
+Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+         const FidParams &p)
+    : d_(new JobImpl) {
+  JobImpl &J = *d_;
+  J.ctx = &ctx;
+  J.P = p;
+  CUDA_OK(cudaSetDevice(ctx.device));
+  if (p.precision != 0) throw Error(5, "only the FP64 precision mode is implemented");
+  if (p.npts <= 0) throw Error(1, "npts must be positive");
+  if (p.wr == 0.0 || p.rotb_deg == 0.0)
+    throw Error(5, "static (non-spinning) powder FIDs are not implemented by the GPU engine");
+  if (pw.size() <= 0) throw Error(1, "empty powder");
+  const int N = sys.dim();
+  if (ro.n != N || det.n != N) throw Error(1, "rho/detect dimension does not match the spin system");
+  // compute::CalcComputeStep and the constructor (compute.h:86-97, 213-235)
+  J.n = int(std::floor(p.sw / p.wr + 0.5));
+  if (J.n < 1) throw Error(1, "sw/wr gives fewer than one step per rotor period");
+  int gamma_step = 10;
+  J.gammaloop = gamma_step >= J.n ? gamma_step / J.n : 1;
+  if (J.gammaloop < 1) J.gammaloop = 1;
+  J.sw_out = double(J.n * p.wr);
+  double tmin = p.start_t, tmax = p.start_t + 1.0 / p.wr;
+  J.tau = (tmax - tmin) / J.n;
+  if (!(J.tau > 0)) throw Error(1, "the propagator time step is not positive");
+  J.L = sys.layout();
+  const BlockLayout &L = J.L;
+  if (L.max_block > kMaxBlock)
+    throw Error(5, "Hamiltonian block of size " + std::to_string(L.max_block) + " exceeds this engine's limit of " +
+                       std::to_string(kMaxBlock));
+  const int nb = int(L.size.size());
+  // rosym: exact test ro == 0.5*(det + det^H)   (compute.h:75-83)
+  J.rosym = 1;
+  for (int r = 0; r < N && J.rosym; ++r)
+    for (int s = 0; s < N; ++s)
+      if (ro(r, s) != 0.5 * (det(r, s) + std::conj(det(s, r)))) {
+        J.rosym = 0;
+        break;
+      }
+  // Hamiltonian terms, packed per block
+  std::vector<double> pas, isc, Tk, Hc(L.S2, 0.0);
+  auto pack = [&](const std::vector<double> &M, double *dst) {
+    for (int k = 0; k < nb; ++k)
+      for (int r = 0; r < L.size[k]; ++r)
+        for (int q = 0; q < L.size[k]; ++q)
+          dst[L.poff[k] + r * L.size[k] + q] = M[size_t(L.perm[L.off[k] + r]) * N + L.perm[L.off[k] + q]];
+  };
+  pack(sys.h_const(), Hc.data());
+  const auto &ints = sys.interactions();
+  for (size_t kk = 0; kk < ints.size(); ++kk) {
+    if (ints[kk].kind == 'J') continue;
+    const auto &I = ints[kk];
+    pas.insert(pas.end(), {I.pas[0][0], I.pas[0][1], I.pas[0][2], I.pas[1][1], I.pas[1][2], I.pas[2][2]});
+    isc.push_back(I.op_scale);
+    size_t o = Tk.size();
+    Tk.resize(o + L.S2);
+    pack(sys.h_ops()[kk], Tk.data() + o);
+    ++J.nint;
+  }
+  // Q pairs (blocks of D) and R pairs (blocks of rho when rho != (D + D^H)/2)
+  std::vector<int> qa, qb, qoff, doff, ra, rb, roff, rhooff;
+  std::vector<double2> Dblk, Rhoblk;
+  std::vector<std::vector<int>> qpair(nb, std::vector<int>(nb, -1)), rpair(nb, std::vector<int>(nb, -1));
+  for (int a = 0; a < nb; ++a)
+    for (int b = 0; b < nb; ++b) {
+      if (any_nonzero(det, L, a, b)) {
+        qpair[a][b] = int(qa.size());
+        qa.push_back(a), qb.push_back(b), qoff.push_back(J.nq), doff.push_back(int(Dblk.size()));
+        for (int r = 0; r < L.size[a]; ++r)
+          for (int s = 0; s < L.size[b]; ++s) {
+            cplx v = det(L.perm[L.off[a] + r], L.perm[L.off[b] + s]);
+            Dblk.push_back(make_double2(v.real(), v.imag()));
+          }
+        J.nq += L.size[a] * L.size[b];
+      }
+      if (!J.rosym && any_nonzero(ro, L, a, b)) {
+        rpair[a][b] = int(ra.size());
+        ra.push_back(a), rb.push_back(b), roff.push_back(J.nr), rhooff.push_back(int(Rhoblk.size()));
+        for (int r = 0; r < L.size[a]; ++r)
+          for (int s = 0; s < L.size[b]; ++s) {
+            cplx v = ro(L.perm[L.off[a] + r], L.perm[L.off[b] + s]);
+            Rhoblk.push_back(make_double2(v.real(), v.imag()));
+          }
+        J.nr += L.size[a] * L.size[b];
+      }
+    }
+  J.npq = int(qa.size());
+  J.npr = int(ra.size());
+  // elements (r,s): Q(r,s) structurally non-zero and R(s,r) structurally non-zero
+  std::vector<int> eq, erev, er, erg, esg;
+  for (int pq = 0; pq < J.npq; ++pq) {
+    int a = qa[pq], b = qb[pq];
+    for (int r = 0; r < L.size[a]; ++r)
+      for (int s = 0; s < L.size[b]; ++s) {
+        int rv = -1, ri = -1;
+        if (J.rosym) {
+          if (qpair[b][a] >= 0) rv = qoff[qpair[b][a]] + s * L.size[a] + r;
+        } else {
+          if (rpair[b][a] < 0) continue;
+          ri = roff[rpair[b][a]] + s * L.size[a] + r;
+        }
+        eq.push_back(qoff[pq] + r * L.size[b] + s);
+        erev.push_back(rv);
+        er.push_back(ri);
+        erg.push_back(L.off[a] + r);
+        esg.push_back(L.off[b] + s);
+      }
+  }
+  J.ne = int(eq.size());
+  J.J = (p.npts + J.n - 1) / J.n;
+  // crystallites, expanded by the gamma loop (compute.h:294-306: fid summed over q)
+  J.C = pw.size();
+  J.Ceff = J.C * J.gammaloop;
+  const double d2r = kPi / 180.0;
+  for (int c = 0; c < J.C; ++c) {
+    double R[3][3];
+    rotation3(pw.phi[c], pw.theta[c], pw.gamma[c], R);  // setPowderAngles(phi, theta, gamma)
+    for (int q = 0; q < J.gammaloop; ++q) {
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) J.h_Rp.push_back(R[a][b]);
+      J.h_t0.push_back(tmin + kPi2 * double(q) / double(J.gammaloop * J.n) / p.wr);
+      J.h_w.push_back(pw.weight[c]);
+    }
+  }
+  J.cos_rotb = std::cos(p.rotb_deg * d2r);
+  J.sin_rotb = std::sin(p.rotb_deg * d2r);
+  // batch size from the memory budget
+  size_t per_c = sizeof(double2) * (size_t(J.n) * L.S2 * 2 + L.S2 + N + size_t(J.n) * (J.nq + J.nr + J.ne) +
+                                    size_t(J.J) * J.ne) +
+                 sizeof(double) * 11;
+  size_t budget = ctx.hbm_budget ? ctx.hbm_budget : (size_t(16) << 30);
+  long cb = long(budget / std::max<size_t>(per_c, 1));
+  cb = (cb / 32) * 32;
+  long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
+  if (cb < 32) throw Error(4, "job does not fit the device memory budget (one warp of crystallites)");
+  J.Cb = int(std::min(cb, cpad_all));
+  J.nbatch = int((cpad_all + J.Cb - 1) / J.Cb);
+  J.nwarps_total = J.nbatch * (J.Cb / 32);
+  // block lists by size
+  J.blocks_by_size.assign(kMaxBlock + 1, {});
+  for (int k = 0; k < nb; ++k) J.blocks_by_size[L.size[k]].push_back(k);
+  J.blist.resize(kMaxBlock + 1);
+  cudaStream_t st = ctx.stream;
+  g_upload_counter = &J.h2d;
+  struct CounterReset {
+    ~CounterReset() { g_upload_counter = nullptr; }
+  } counter_reset;
+  for (int b = 1; b <= kMaxBlock; ++b) J.blist[b].upload(J.blocks_by_size[b], st);
+  J.bs.upload(L.size, st), J.boff.upload(L.off, st), J.bpoff.upload(L.poff, st);
+  J.qa.upload(qa, st), J.qb.upload(qb, st), J.qoff.upload(qoff, st), J.doff.upload(doff, st);
+  J.ra.upload(ra, st), J.rb.upload(rb, st), J.roff.upload(roff, st), J.rhooff.upload(rhooff, st);
+  J.eq.upload(eq, st), J.erev.upload(erev, st), J.er.upload(er, st), J.erg.upload(erg, st), J.esg.upload(esg, st);
+  J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
+  J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
+  J.status.upload(std::vector<int>(1, 0), st);
+  // per-crystallite inputs, all batches, transposed to [item][c] per batch at run time
+  // (stored here already in batch-major, crystallite-fastest order)
+  {
+    std::vector<double> Rp(size_t(J.nbatch) * 9 * J.Cb, 0.0), t0(size_t(J.nbatch) * J.Cb, 0.0),
+        w(size_t(J.nbatch) * J.Cb, 0.0);
+    for (int cg = 0; cg < J.Ceff; ++cg) {
+      int bi = cg / J.Cb, c = cg % J.Cb;
+      for (int x = 0; x < 9; ++x) Rp[(size_t(bi) * 9 + x) * J.Cb + c] = J.h_Rp[size_t(cg) * 9 + x];
+      t0[size_t(bi) * J.Cb + c] = J.h_t0[cg];
+      w[size_t(bi) * J.Cb + c] = J.h_w[cg];
+    }
+    J.Rp_all.upload(Rp, st), J.t0_all.upload(t0, st), J.w_all.upload(w, st);
+  }
+  size_t Cb = J.Cb;
+  J.U.alloc(size_t(J.n) * L.S2 * Cb);
+  J.A.alloc(size_t(J.n) * L.S2 * Cb);
+  J.VF.alloc(size_t(L.S2) * Cb);
+  J.Lb.alloc(size_t(N) * Cb);
+  J.Q.alloc(std::max<size_t>(1, size_t(J.n) * J.nq * Cb));
+  J.R.alloc(std::max<size_t>(1, size_t(J.n) * J.nr * Cb));
+  J.G.alloc(std::max<size_t>(1, size_t(J.n) * J.ne * Cb));
+  J.Z.alloc(std::max<size_t>(1, size_t(J.J) * J.ne * Cb));
+  J.partial.alloc(size_t(J.nwarps_total) * p.npts);
+  J.fid.alloc(p.npts);
+  CUDA_OK(cudaMemsetAsync(J.partial.p, 0, J.partial.n * sizeof(double2), st));
+  CUDA_OK(cudaStreamSynchronize(st));
+  // algorithmic flop count (one complex MAC = 8 flop; eigh counted as 32 b^3, the
+  // Floquet eig as 100 b^3)
+  double S3 = 0;
+  for (int k = 0; k < nb; ++k) S3 += double(L.size[k]) * L.size[k] * L.size[k];
+  double pairs = 0;
+  for (int pq = 0; pq < J.npq + J.npr; ++pq) {
+    int a = pq < J.npq ? qa[pq] : ra[pq - J.npq], b = pq < J.npq ? qb[pq] : rb[pq - J.npq];
+    pairs += double(L.size[a]) * L.size[b] * (L.size[a] + L.size[b]);
+  }
+  double S2H = 0;  // H build: one FMA per operator entry per interaction
+  for (int k = 0; k < nb; ++k) S2H += double(L.size[k]) * L.size[k];
+  double Ce = J.Ceff;
+  J.stage_fl[0] = Ce * J.n * (11.0 * S3 + 2.0 * J.nint * S2H);  // eigh 9b^3 + U 2b^3 + H build
+  J.stage_fl[1] = Ce * J.n * 8.0 * S3;                          // Dyson
+  J.stage_fl[2] = Ce * 100.0 * S3;                              // Floquet eig
+  J.stage_fl[3] = Ce * J.n * 8.0 * S3;                          // W = A V_F
+  J.stage_fl[4] = Ce * J.n * 8.0 * pairs;                       // Q, R transforms
+  J.stage_fl[5] = Ce * 8.0 * J.n * J.n * J.ne;                  // Fave correlation
+  J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
+  J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total;                // compensated powder sum
+  J.flops = 0;
+  for (double f : J.stage_fl) J.flops += f;
+  // static part of the device description
+  DevSys &s = J.base;
+  s.n = J.n, s.npts = p.npts, s.N = N, s.nb = nb, s.S2 = L.S2, s.nint = J.nint, s.nq = J.nq, s.nr = J.nr;
+  s.ne = J.ne, s.J = J.J, s.rosym = J.rosym;
+  s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
+  s.scale = double(1. / double(J.n / (J.rosym ? 2 : 1)));
+  s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
+  s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
+  s.npq = J.npq, s.npr = J.npr;
+  s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
+  s.ra = J.ra.p, s.rb = J.rb.p, s.roff = J.roff.p, s.rhooff = J.rhooff.p;
+  s.Dblk = J.Dblk.p, s.Rhoblk = J.Rhoblk.p;
+  s.eq = J.eq.p, s.erev = J.erev.p, s.er = J.er.p, s.erg = J.erg.p, s.esg = J.esg.p;
+  s.U = J.U.p, s.A = J.A.p, s.VF = J.VF.p, s.L = J.Lb.p, s.Q = J.Q.p, s.R = J.R.p, s.G = J.G.p, s.Z = J.Z.p;
+  s.partial = J.partial.p;
+  s.status = J.status.p;
+  s.Cpad = J.Cb;
+}
+
+Job::~Job() {}
+
+template <int B>
+static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
+  const auto &lst = J.blocks_by_size[B];
+  if (lst.empty()) return;
+  int nl = int(lst.size());
+  const int *bl = J.blist[B].p;
+  cudaStream_t st = J.ctx->stream;
+  long Cp = s.Cpad;
+  switch (stage) {
+    case 0: k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl); break;
+    case 1: k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl); break;
+    case 2: k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl); break;
+    case 3: k_eigframe<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl); break;
+  }
+  ++J.launches;
+}
+
+static void launch_stage(JobImpl &J, DevSys &s, int stage) {
+  launch_block_kernels<1>(J, s, stage);
+  launch_block_kernels<2>(J, s, stage);
+  launch_block_kernels<3>(J, s, stage);
+  launch_block_kernels<4>(J, s, stage);
+  launch_block_kernels<5>(J, s, stage);
+  launch_block_kernels<6>(J, s, stage);
+  launch_block_kernels<7>(J, s, stage);
+  launch_block_kernels<8>(J, s, stage);
+}
+
+static void mark_begin(JobImpl &J, int stage);
+static void mark_end(JobImpl &J, int stage, int nlaunch);
+
+void Job::run() {
+  JobImpl &J = *d_;
+  CUDA_OK(cudaSetDevice(J.ctx->device));
+  cudaStream_t st = J.ctx->stream;
+  J.launches = 0;
+  J.marks.clear();
+  J.evnext = 0;
+  if (J.profiling && J.evpool.empty()) {
+    J.evpool.resize(size_t(2) * Job::kStages * (J.nbatch + 1));
+    for (auto &e : J.evpool) CUDA_OK(cudaEventCreate(&e));
+  }
+  CUDA_OK(cudaMemsetAsync(J.status.p, 0, sizeof(int), st));
+  for (int bi = 0; bi < J.nbatch; ++bi) {
+    DevSys s = J.base;
+    int c0 = bi * J.Cb;
+    s.C = std::min(J.Cb, J.Ceff - c0);
+    s.Cpad = J.Cb;
+    s.Rp = J.Rp_all.p + size_t(bi) * 9 * J.Cb;
+    s.t0 = J.t0_all.p + size_t(bi) * J.Cb;
+    s.w = J.w_all.p + size_t(bi) * J.Cb;
+    s.warp_base = c0 / 32;
+    for (int stage = 0; stage < 4; ++stage) {
+      mark_begin(J, stage);
+      int before = J.launches;
+      launch_stage(J, s, stage);
+      mark_end(J, stage, J.launches - before);
+    }
+    long Cp = s.Cpad;
+    mark_begin(J, 4);
+    if (J.npq + J.npr > 0) {
+      k_qr<<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
+      ++J.launches;
+    }
+    mark_end(J, 4, J.npq + J.npr > 0 ? 1 : 0);
+    mark_begin(J, 5);
+    if (J.ne > 0) {
+      int ntile = (J.n + kFavePT - 1) / kFavePT;
+      k_fave<<<grid_for(Cp * J.ne * ntile), kThreads, 0, st>>>(s);
+      ++J.launches;
+    }
+    mark_end(J, 5, J.ne > 0 ? 1 : 0);
+    // k_fid writes every (warp, k) of this batch, so partials need no clearing; it exits
+    // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
+    int npt = (J.n + kFidPT - 1) / kFidPT, njt = (J.J + kFidJT - 1) / kFidJT;
+    mark_begin(J, 6);
+    k_fid<<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
+    ++J.launches;
+    mark_end(J, 6, 1);
+  }
+  mark_begin(J, 7);
+  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, J.nwarps_total, J.P.npts, J.fid.p);
+  ++J.launches;
+  mark_end(J, 7, 1);
+  CUDA_OK(cudaGetLastError());
+  if (J.profiling && !J.marks.empty()) {
+    CUDA_OK(cudaEventSynchronize(J.evpool[J.marks.back().e]));
+    for (const auto &m : J.marks) {
+      float ms = 0;
+      CUDA_OK(cudaEventElapsedTime(&ms, J.evpool[m.b], J.evpool[m.e]));
+      J.stage_ms[m.stage] += ms;
+      J.stage_launch[m.stage] += m.nlaunch;
+    }
+  }
+}
+
+// Stage markers: with profiling on, an event pair on the launching stream brackets each
+// stage; run() folds the elapsed times into the per-stage totals once its last event
+// has completed (one synchronisation per run, none between stages).
+static void mark_begin(JobImpl &J, int stage) {
+  if (!J.profiling) return;
+  CUDA_OK(cudaEventRecord(J.evpool[J.evnext], J.ctx->stream));
+  J.marks.push_back({stage, J.evnext, -1, 0});
+  ++J.evnext;
+}
+
+static void mark_end(JobImpl &J, int stage, int nlaunch) {
+  if (!J.profiling) return;
+  CUDA_OK(cudaEventRecord(J.evpool[J.evnext], J.ctx->stream));
+  J.marks.back().e = J.evnext;
+  J.marks.back().nlaunch = nlaunch;
+  (void)stage;
+  ++J.evnext;
+}
+
+void Job::read(double *fid_out) {
+  JobImpl &J = *d_;
+  CUDA_OK(cudaMemcpyAsync(fid_out, J.fid.p, sizeof(double2) * J.P.npts, cudaMemcpyDeviceToHost, J.ctx->stream));
+  int status = 0;
+  CUDA_OK(cudaMemcpyAsync(&status, J.status.p, sizeof(int), cudaMemcpyDeviceToHost, J.ctx->stream));
+  CUDA_OK(cudaStreamSynchronize(J.ctx->stream));
+  if (status & (kNoConvergeStep | kNoConvergeFloquet))
+    throw Error(7, "an eigen-decomposition did not converge within its sweep limit");
+  if (status & kSingularCayley) throw Error(7, "singular Cayley transform in the Floquet eigen-decomposition");
+}
+
+const char *Job::stage_name(int s) {
+  static const char *names[kStages] = {"k_step_prop", "k_dyson",  "k_floquet", "k_eigframe",
+                                       "k_qr",        "k_fave",   "k_fid",     "k_reduce"};
+  return (s >= 0 && s < kStages) ? names[s] : "";
+}
+void Job::set_profiling(bool on) { d_->profiling = on; }
+void Job::stage_times(double *ms, int *launches) const {
+  for (int i = 0; i < kStages; ++i) {
+    if (ms) ms[i] = d_->stage_ms[i];
+    if (launches) launches[i] = d_->stage_launch[i];
+  }
+}
+void Job::stage_flops(double *f) const {
+  for (int i = 0; i < kStages; ++i) f[i] = d_->stage_fl[i];
+}
+void Job::reset_stage_times() {
+  for (int i = 0; i < kStages; ++i) d_->stage_ms[i] = 0, d_->stage_launch[i] = 0;
+}
+size_t Job::h2d_bytes() const { return d_->h2d; }
+size_t Job::d2h_bytes() const { return sizeof(double2) * d_->P.npts; }
+double Job::run_timed(int iters) {
+  JobImpl &J = *d_;
+  cudaEvent_t a, b;
+  CUDA_OK(cudaEventCreate(&a));
+  CUDA_OK(cudaEventCreate(&b));
+  CUDA_OK(cudaEventRecord(a, J.ctx->stream));
+  for (int i = 0; i < iters; ++i) run();
+  CUDA_OK(cudaEventRecord(b, J.ctx->stream));
+  CUDA_OK(cudaEventSynchronize(b));
+  float ms = 0;
+  CUDA_OK(cudaEventElapsedTime(&ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return ms;
+}
+
+namespace {
+// 8 independent DFMA chains per thread; 2*8*iters flop per thread.
+__global__ void k_dfma_probe(double *out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = threadIdx.x + c;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+  double s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace
+
+double probe_fp64_tflops(Context &ctx) {
+  CUDA_OK(cudaSetDevice(ctx.device));
+  int sms = 0;
+  CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  int blocks = sms * 4, threads = 256, iters = 4000;
+  DevBuf<double> out;
+  out.alloc(size_t(blocks) * threads);
+  cudaEvent_t a, b;
+  CUDA_OK(cudaEventCreate(&a));
+  CUDA_OK(cudaEventCreate(&b));
+  k_dfma_probe<<<blocks, threads, 0, ctx.stream>>>(out.p, 10, 0.999, 0.001);
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    CUDA_OK(cudaEventRecord(a, ctx.stream));
+    k_dfma_probe<<<blocks, threads, 0, ctx.stream>>>(out.p, iters, 0.999, 0.001);
+    CUDA_OK(cudaEventRecord(b, ctx.stream));
+    CUDA_OK(cudaEventSynchronize(b));
+    float ms = 0;
+    CUDA_OK(cudaEventElapsedTime(&ms, a, b));
+    best = std::max(best, 2.0 * 8 * double(iters) * blocks * threads / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
+
+double Job::sw_out() const { return d_->sw_out; }
+int Job::npts() const { return d_->P.npts; }
+int Job::kernels_per_run() const { return d_->launches; }
+const double *Job::device_fid() const { return reinterpret_cast<const double *>(d_->fid.p); }
+double Job::flops() const { return d_->flops; }
+
+std::string Job::describe() const {
+  const JobImpl &J = *d_;
+  std::ostringstream o;
+  o << "{\"N\": " << J.L.N << ", \"blocks\": [";
+  for (size_t k = 0; k < J.L.size.size(); ++k) o << (k ? ", " : "") << J.L.size[k];
+  o << "], \"S2\": " << J.L.S2 << ", \"n\": " << J.n << ", \"gammaloop\": " << J.gammaloop
+    << ", \"crystallites\": " << J.C << ", \"rosym\": " << J.rosym << ", \"q_pairs\": " << J.npq
+    << ", \"r_pairs\": " << J.npr << ", \"elements\": " << J.ne << ", \"batch\": " << J.Cb
+    << ", \"batches\": " << J.nbatch << ", \"flops\": " << J.flops << "}";
+  return o.str();
+}
+
+}  // namespace bl

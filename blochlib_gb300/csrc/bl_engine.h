@@ -1,0 +1,65 @@
+// GPU engine for the spinning powder FID (gamma-COMPUTE), internal C++ interface.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "bl_host.h"
+
+namespace bl {
+
+struct FidParams {
+  int npts = 0;
+  double sw = 0, wr = 0, rotb_deg = 0, start_t = 0;
+  int precision = 0;  // 0 = FP64 (the only mode implemented by this engine)
+};
+
+struct Context {
+  int device = 0;
+  size_t hbm_budget = 0;  // bytes the engine may hold for one job's work buffers
+  cudaStream_t stream = nullptr;
+  ~Context();
+};
+
+struct JobImpl;
+
+// A job with all inputs resident on the device; run() recomputes the powder FID.
+class Job {
+ public:
+  Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+      const FidParams &p);
+  ~Job();
+  void run();                       // enqueue all kernels on the context stream
+  void read(double *fid_out);       // device -> host (2*npts doubles), synchronises
+  double sw_out() const;
+  int npts() const;
+  int kernels_per_run() const;      // kernel launches one run() enqueues
+  const double *device_fid() const; // device pointer, 2*npts doubles
+  std::string describe() const;     // layout summary (JSON)
+  // algorithmic FP64 flop count of one run() (one complex MAC = 8 flop)
+  double flops() const;
+
+  // Per-stage CUDA-event timing of run() (stages: see stage_name), accumulated while on.
+  static constexpr int kStages = 8;
+  static const char *stage_name(int s);
+  void set_profiling(bool on);
+  void stage_times(double *ms, int *launches) const;  // kStages each, accumulated
+  void stage_flops(double *flops) const;              // algorithmic flop per run, per stage
+  void reset_stage_times();
+  // Host<->device bytes moved per bl_powder_fid call (upload at creation, FID read back)
+  size_t h2d_bytes() const;
+  size_t d2h_bytes() const;
+  // Runs run() 'iters' times between two events on the context stream; returns ms total.
+  double run_timed(int iters);
+
+ private:
+  std::unique_ptr<JobImpl> d_;
+};
+
+// Measured FP64 FMA throughput of the device (TFLOP/s), from a short DFMA probe kernel.
+double probe_fp64_tflops(Context &ctx);
+
+}  // namespace bl

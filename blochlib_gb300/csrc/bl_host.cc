@@ -1,0 +1,505 @@
+// Host-side spin-system model: parsing, spin operators, Hamiltonian terms, block
+// structure, powder sets and FID text output.  See bl_host.h for the reference map.
+#include "bl_host.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <numeric>
+#include <sstream>
+
+namespace bl {
+
+namespace {
+const double kPi = 3.14159265358979323846;
+const double kDeg2Rad = kPi / 180.0;
+
+std::vector<std::string> split_ws(const std::string &s) {
+  std::vector<std::string> out;
+  std::string cur;
+  for (char ch : s) {
+    if (ch == ' ' || ch == '\t' || ch == '\n' || ch == '\r' || ch == ',') {
+      if (!cur.empty()) out.push_back(cur), cur.clear();
+    } else {
+      cur.push_back(ch);
+    }
+  }
+  if (!cur.empty()) out.push_back(cur);
+  return out;
+}
+
+std::string trim(const std::string &s) {
+  size_t a = s.find_first_not_of(" \t\r\n");
+  if (a == std::string::npos) return "";
+  size_t b = s.find_last_not_of(" \t\r\n");
+  return s.substr(a, b - a + 1);
+}
+
+void mat3mul(const double A[3][3], const double B[3][3], double C[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i][j] = A[i][0] * B[0][j] + A[i][1] * B[1][j] + A[i][2] * B[2][j];
+}
+
+// PAS' = R diag(d) R^T, R = rotation3 of the interaction's Euler angles (degrees).
+void crystal_tensor(Interaction &it, double d0, double d1, double d2) {
+  double R[3][3], D[3][3] = {{d0, 0, 0}, {0, d1, 0}, {0, 0, d2}}, T[3][3], Rt[3][3];
+  rotation3(it.alpha * kDeg2Rad, it.beta * kDeg2Rad, it.gamma * kDeg2Rad, R);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Rt[i][j] = R[j][i];
+  mat3mul(R, D, T);
+  mat3mul(T, Rt, it.pas);
+}
+
+// Real part of a real-valued product of two expanded single-spin operators.
+std::vector<double> real_of(const CMatrix &m) {
+  std::vector<double> r(m.a.size());
+  for (size_t i = 0; i < r.size(); ++i) r[i] = m.a[i].real();
+  return r;
+}
+
+CMatrix mul(const CMatrix &x, const CMatrix &y) {
+  CMatrix z(x.n);
+  for (int i = 0; i < x.n; ++i)
+    for (int k = 0; k < x.n; ++k) {
+      cplx v = x(i, k);
+      if (v == cplx(0, 0)) continue;
+      for (int j = 0; j < x.n; ++j) z(i, j) += v * y(k, j);
+    }
+  return z;
+}
+}  // namespace
+
+double isotope_spin(const std::string &iso) {
+  // nuclear spin quantum numbers of common NMR isotopes (physical constants)
+  static const std::map<std::string, double> t = {
+      {"1H", 0.5},    {"2H", 1.0},    {"3H", 0.5},    {"3He", 0.5},   {"6Li", 1.0},   {"7Li", 1.5},
+      {"9Be", 1.5},   {"10B", 3.0},   {"11B", 1.5},   {"13C", 0.5},   {"14N", 1.0},   {"15N", 0.5},
+      {"17O", 2.5},   {"19F", 0.5},   {"21Ne", 1.5},  {"23Na", 1.5},  {"25Mg", 2.5},  {"27Al", 2.5},
+      {"29Si", 0.5},  {"31P", 0.5},   {"33S", 1.5},   {"35Cl", 1.5},  {"37Cl", 1.5},  {"39K", 1.5},
+      {"43Ca", 3.5},  {"45Sc", 3.5},  {"47Ti", 2.5},  {"49Ti", 3.5},  {"51V", 3.5},   {"53Cr", 1.5},
+      {"55Mn", 2.5},  {"57Fe", 0.5},  {"59Co", 3.5},  {"61Ni", 1.5},  {"63Cu", 1.5},  {"65Cu", 1.5},
+      {"67Zn", 2.5},  {"69Ga", 1.5},  {"71Ga", 1.5},  {"77Se", 0.5},  {"79Br", 1.5},  {"81Br", 1.5},
+      {"87Rb", 1.5},  {"89Y", 0.5},   {"93Nb", 4.5},  {"95Mo", 2.5},  {"103Rh", 0.5}, {"107Ag", 0.5},
+      {"109Ag", 0.5}, {"111Cd", 0.5}, {"113Cd", 0.5}, {"115In", 4.5}, {"117Sn", 0.5}, {"119Sn", 0.5},
+      {"125Te", 0.5}, {"127I", 2.5},  {"129Xe", 0.5}, {"131Xe", 1.5}, {"133Cs", 3.5}, {"183W", 0.5},
+      {"195Pt", 0.5}, {"199Hg", 0.5}, {"205Tl", 0.5}, {"207Pb", 0.5}, {"e", 0.5}};
+  auto it = t.find(iso);
+  if (it == t.end()) throw Error(2, "unknown isotope '" + iso + "'");
+  return it->second;
+}
+
+void rotation3(double a, double b, double g, double R[3][3]) {
+  double cg = std::cos(g), cb = std::cos(b), ca = std::cos(a);
+  double sg = std::sin(g), sb = std::sin(b), sa = std::sin(a);
+  R[0][0] = ca * cb * cg - sa * sg;
+  R[0][1] = sa * cb * cg + ca * sg;
+  R[0][2] = -sb * cg;
+  R[1][0] = -ca * cb * sg - sa * cg;
+  R[1][1] = -sa * cb * sg + ca * cg;
+  R[1][2] = sb * sg;
+  R[2][0] = ca * sb;
+  R[2][1] = sa * sb;
+  R[2][2] = cb;
+}
+
+void rotation2(double phi, double theta, double R[3][3]) {
+  double ct = std::cos(theta), cp = std::cos(phi), sp = std::sin(phi), st = std::sin(theta);
+  R[0][0] = cp;
+  R[0][1] = sp;
+  R[0][2] = 0.0;
+  R[1][0] = -ct * sp;
+  R[1][1] = cp * ct;
+  R[1][2] = st;
+  R[2][0] = sp * st;
+  R[2][1] = -cp * st;
+  R[2][2] = ct;
+}
+
+SpinSystem SpinSystem::from_text(const std::string &text) {
+  std::vector<std::string> lines;
+  std::stringstream ss(text);
+  std::string l;
+  while (std::getline(ss, l)) lines.push_back(l);
+  return SpinSystem(lines);
+}
+
+SpinSystem::SpinSystem(const std::vector<std::string> &lines) {
+  std::vector<std::pair<std::string, int>> types;
+  for (const auto &l : lines) {
+    auto t = split_ws(l);
+    if (t.size() >= 2 && (t[0] == "numspin" || t[0] == "spins")) nspin_ = std::atoi(t[1].c_str());
+    if (t.size() >= 1 && (t[0] == "T" || t[0] == "type" || t[0] == "Type")) {
+      if (t.size() < 3) throw Error(2, "'T' line needs: T <isotope> <spin>");
+      types.push_back({t[1], std::atoi(t[2].c_str())});
+    }
+  }
+  if (nspin_ < 1) throw Error(2, "numspin must be >= 1");
+  iso_.assign(nspin_, "1H");
+  for (auto &p : types) {
+    if (p.second < 0 || p.second >= nspin_) throw Error(2, "isotope assigned to a spin outside numspin");
+    iso_[p.second] = p.first;
+  }
+  dims_.resize(nspin_);
+  N_ = 1;
+  for (int i = 0; i < nspin_; ++i) {
+    dims_[i] = int(std::lround(2 * isotope_spin(iso_[i]) + 1));
+    N_ *= dims_[i];
+    if (N_ > 4096) throw Error(5, "Hilbert space dimension above 4096 is not supported");
+  }
+  std::vector<Interaction> csa, dip, jj, qua;
+  auto check_spin = [&](int s) {
+    if (s < 0 || s >= nspin_) throw Error(2, "interaction names a spin outside numspin");
+  };
+  for (const auto &l : lines) {
+    auto t = split_ws(l);
+    if (t.empty() || t[0][0] == '#') continue;
+    auto num = [&](size_t i) { return i < t.size() ? std::atof(t[i].c_str()) : 0.0; };
+    const std::string &k = t[0];
+    if (k == "C" || k == "CSA" || k == "csa") {
+      if (t.size() < 5) throw Error(2, "a CSA needs: C <iso> <del> <eta> <spin> [alpha beta gamma]");
+      Interaction it;
+      it.kind = 'C';
+      it.iso = num(1), it.del = num(2), it.eta = num(3), it.s1 = std::atoi(t[4].c_str());
+      it.alpha = num(5), it.beta = num(6), it.gamma = num(7);
+      check_spin(it.s1);
+      crystal_tensor(it, it.del * (it.eta - 1.0) / 2.0, -it.del * (it.eta + 1.0) / 2.0, 1.0 * it.del);
+      it.op_scale = 1.0;
+      csa.push_back(it);
+    } else if (k == "D" || k == "Dip" || k == "dip" || k == "DIP") {
+      if (t.size() < 4) throw Error(2, "a dipole needs: D <coupling> <spin1> <spin2> [alpha beta gamma]");
+      Interaction it;
+      it.kind = 'D';
+      it.del = num(1), it.s1 = int(num(2)), it.s2 = int(num(3));
+      it.alpha = num(4), it.beta = num(5), it.gamma = num(6);
+      check_spin(it.s1), check_spin(it.s2);
+      double r6 = std::pow(6.0, 0.5);
+      crystal_tensor(it, -0.5 * it.del * r6, -0.5 * it.del * r6, 1.0 * it.del * r6);
+      it.op_scale = 1.0;
+      dip.push_back(it);
+    } else if (k == "J" || k == "j" || k == "jcop" || k == "Jcop") {
+      if (t.size() < 4) throw Error(2, "a J coupling needs: J <coupling> <spin1> <spin2> [strong]");
+      Interaction it;
+      it.kind = 'J';
+      it.iso = num(1), it.s1 = std::atoi(t[2].c_str()), it.s2 = std::atoi(t[3].c_str());
+      it.strong = t.size() >= 5 ? std::atoi(t[4].c_str()) : 0;
+      check_spin(it.s1), check_spin(it.s2);
+      jj.push_back(it);
+    } else if (k == "Q" || k == "QUAD" || k == "Quad") {
+      if (t.size() < 4) throw Error(2, "a quadrupole needs: Q <coupling> <eta> <spin> [alpha beta gamma]");
+      Interaction it;
+      it.kind = 'Q';
+      it.del = num(1), it.eta = num(2), it.s1 = std::atoi(t[3].c_str());
+      it.alpha = num(4), it.beta = num(5), it.gamma = num(6);
+      check_spin(it.s1);
+      crystal_tensor(it, (it.eta - 1.0) / 2.0, -(it.eta + 1.0) / 2.0, 1.0);
+      qua.push_back(it);
+    }
+  }
+  // evaluation order of SolidSys::Hamiltonian: CSA, dipoles, J, quadrupoles
+  for (auto *v : {&csa, &dip, &jj, &qua}) ints_.insert(ints_.end(), v->begin(), v->end());
+  build();
+}
+
+CMatrix SpinSystem::single(char which, int spin) const {
+  if (spin < 0 || spin >= nspin_) throw Error(1, "spin index out of range");
+  int hs = dims_[spin];
+  CMatrix m(hs);
+  double q = (hs - 1.0) / 2.0, q1 = q * (q + 1.0);
+  if (which == 'z') {
+    double mm = q;
+    for (int k = 0; k < hs; ++k, mm -= 1) m(k, k) = mm;
+  } else if (which == 'e') {
+    for (int k = 0; k < hs; ++k) m(k, k) = 1.0;
+  } else {
+    double mm = q - 1;
+    for (int k = 0; k < hs - 1; ++k, mm -= 1) {
+      double c = std::sqrt(q1 - mm * (mm + 1));
+      if (which == 'x') m(k + 1, k) = c / 2, m(k, k + 1) = c / 2;
+      else if (which == 'y') m(k + 1, k) = cplx(0, c / 2), m(k, k + 1) = cplx(0, -c / 2);
+      else if (which == 'p') m(k, k + 1) = c;
+      else if (which == 'm') m(k + 1, k) = c;
+      else throw Error(1, "unknown single-spin operator");
+    }
+  }
+  // Kronecker expansion, spin 0 most significant (multispinop.cc:51-74)
+  int left = 1, right = 1;
+  for (int i = 0; i < spin; ++i) left *= dims_[i];
+  for (int i = spin + 1; i < nspin_; ++i) right *= dims_[i];
+  CMatrix out(N_);
+  for (int l = 0; l < left; ++l)
+    for (int r1 = 0; r1 < hs; ++r1)
+      for (int c1 = 0; c1 < hs; ++c1) {
+        cplx v = m(r1, c1);
+        if (v == cplx(0, 0)) continue;
+        for (int r = 0; r < right; ++r) {
+          int row = (l * hs + r1) * right + r, col = (l * hs + c1) * right + r;
+          out(row, col) = v;
+        }
+      }
+  return out;
+}
+
+CMatrix SpinSystem::op(const std::string &expr) const {
+  CMatrix acc(N_);
+  std::stringstream ss(expr);
+  std::string term;
+  bool any = false;
+  while (std::getline(ss, term, '+')) {
+    term = trim(term);
+    if (term.empty()) continue;
+    double coef = 1.0;
+    size_t star = term.find('*');
+    if (star != std::string::npos) {
+      char *end = nullptr;
+      std::string cs = trim(term.substr(0, star));
+      coef = std::strtod(cs.c_str(), &end);
+      if (end == cs.c_str()) throw Error(1, "bad coefficient in operator expression '" + expr + "'");
+      term = trim(term.substr(star + 1));
+    }
+    std::istringstream is(term);
+    std::string name;
+    int k = -1;
+    is >> name >> k;
+    CMatrix m(N_);
+    auto total = [&](char w) {
+      CMatrix t(N_);
+      for (int s = 0; s < nspin_; ++s) {
+        CMatrix x = single(w, s);
+        for (size_t i = 0; i < t.a.size(); ++i) t.a[i] += x.a[i];
+      }
+      return t;
+    };
+    if (name == "Fx") m = total('x');
+    else if (name == "Fy") m = total('y');
+    else if (name == "Fz") m = total('z');
+    else if (name == "Fp") m = total('p');
+    else if (name == "Fm") m = total('m');
+    else if (name == "Fe") { for (int i = 0; i < N_; ++i) m(i, i) = 1.0; }
+    else if (name.size() == 2 && name[0] == 'I' && std::string("xyzpm").find(name[1]) != std::string::npos) {
+      if (k < 0) throw Error(1, "single-spin operator '" + name + "' needs a spin index");
+      m = single(name[1], k);
+    } else {
+      throw Error(1, "unknown operator '" + name + "' in '" + expr + "'");
+    }
+    for (size_t i = 0; i < acc.a.size(); ++i) acc.a[i] += coef * m.a[i];
+    any = true;
+  }
+  if (!any) throw Error(1, "empty operator expression");
+  return acc;
+}
+
+void SpinSystem::build() {
+  size_t NN = size_t(N_) * N_;
+  hc_.assign(NN, 0.0);
+  hops_.clear();
+  const double inv_r3 = 1.0 / std::pow(3., 0.5), r3 = std::pow(3., 0.5);
+  for (auto &it : ints_) {
+    std::vector<double> T(NN, 0.0);
+    if (it.kind == 'C') {
+      // a*Iz + (1/sqrt3 Iz)(-sqrt3 iso)   (csa.cc:289-329, spin_ten.cc:211-236)
+      CMatrix Iz = single('z', it.s1);
+      for (int k = 0; k < N_; ++k) {
+        double z = Iz(k, k).real();
+        T[size_t(k) * N_ + k] = z;
+        if (it.iso != 0) hc_[size_t(k) * N_ + k] += (inv_r3 * z) * (-r3 * it.iso);
+      }
+    } else if (it.kind == 'D') {
+      // homonuclear sqrt(1/6)(2IzIz - IxIx - IyIy); heteronuclear sqrt(4/6) IzIz (spin_ten.cc:431-452)
+      CMatrix zz = mul(single('z', it.s1), single('z', it.s2));
+      if (iso_[it.s1] == iso_[it.s2]) {
+        CMatrix xx = mul(single('x', it.s1), single('x', it.s2));
+        CMatrix yy = mul(single('y', it.s1), single('y', it.s2));
+        double f = std::pow(1. / 6., 0.5);
+        for (size_t i = 0; i < NN; ++i) T[i] = f * (2.0 * zz.a[i].real() - xx.a[i].real() - yy.a[i].real());
+      } else {
+        double f = std::pow(4. / 6., 0.5);
+        for (size_t i = 0; i < NN; ++i) T[i] = f * zz.a[i].real();
+      }
+    } else if (it.kind == 'J') {
+      // iso*sqrt3 * (1/sqrt3)(IzIz [+IxIx+IyIy])   (j.cc:129-137, spin_ten.cc:455-465)
+      CMatrix zz = mul(single('z', it.s1), single('z', it.s2));
+      CMatrix xx, yy;
+      if (it.strong) xx = mul(single('x', it.s1), single('x', it.s2)), yy = mul(single('y', it.s1), single('y', it.s2));
+      for (size_t i = 0; i < NN; ++i) {
+        double v = zz.a[i].real();
+        if (it.strong) v = v + xx.a[i].real() + yy.a[i].real();
+        hc_[i] += (inv_r3 * v) * (it.iso * std::sqrt(3.));
+      }
+    } else if (it.kind == 'Q') {
+      // first order: Qp * a * 3 Iz^2, Qp = Q / (4 I (2I-1))   (qua.cc:219-267, spin_ten.cc:285-300)
+      double spin = isotope_spin(iso_[it.s1]);
+      if (spin < 1.0) throw Error(2, "a quadrupole needs a spin >= 1");
+      it.op_scale = it.del / (4.0 * spin * (2.0 * spin - 1.0));
+      CMatrix Iz = single('z', it.s1);
+      for (int k = 0; k < N_; ++k) {
+        double z = Iz(k, k).real();
+        T[size_t(k) * N_ + k] = 3.0 * (z * z);
+      }
+    }
+    hops_.push_back(T);
+  }
+  // Block structure: connected components of the union non-zero pattern.
+  std::vector<int> parent(N_);
+  std::iota(parent.begin(), parent.end(), 0);
+  auto find = [&](int x) {
+    while (parent[x] != x) x = parent[x] = parent[parent[x]];
+    return x;
+  };
+  auto scan = [&](const std::vector<double> &M) {
+    for (int r = 0; r < N_; ++r)
+      for (int c = r + 1; c < N_; ++c)
+        if (M[size_t(r) * N_ + c] != 0.0 || M[size_t(c) * N_ + r] != 0.0) {
+          int a = find(r), b = find(c);
+          if (a != b) parent[std::max(a, b)] = std::min(a, b);
+        }
+  };
+  scan(hc_);
+  for (auto &T : hops_) scan(T);
+  std::map<int, std::vector<int>> comps;
+  for (int s = 0; s < N_; ++s) comps[find(s)].push_back(s);
+  BlockLayout &L = layout_;
+  L = BlockLayout();
+  L.N = N_;
+  L.inv.assign(N_, -1);
+  for (auto &kv : comps) {
+    L.off.push_back(int(L.perm.size()));
+    L.size.push_back(int(kv.second.size()));
+    L.poff.push_back(L.S2);
+    L.S2 += int(kv.second.size() * kv.second.size());
+    L.max_block = std::max(L.max_block, int(kv.second.size()));
+    for (int s : kv.second) {
+      L.inv[s] = int(L.perm.size());
+      L.block_of.push_back(int(L.size.size()) - 1);
+      L.perm.push_back(s);
+    }
+  }
+}
+
+std::vector<double> SpinSystem::hamiltonian(const double Rp[3][3], double alpha_rot, double rotb_rad) const {
+  size_t NN = size_t(N_) * N_;
+  std::vector<double> H = hc_;
+  double Rr[3][3], M[3][3];
+  rotation2(alpha_rot, rotb_rad, Rr);
+  mat3mul(Rr, Rp, M);
+  for (size_t k = 0; k < ints_.size(); ++k) {
+    const Interaction &it = ints_[k];
+    if (it.kind == 'J') continue;
+    double a = 0;
+    for (int j = 0; j < 3; ++j)
+      for (int l = 0; l < 3; ++l) a += M[2][j] * it.pas[j][l] * M[2][l];
+    for (size_t i = 0; i < NN; ++i) H[i] += it.op_scale * a * hops_[k][i];
+  }
+  return H;
+}
+
+// ---------------------------------------------------------------- powder sets
+
+Powder powder_zcw(int tstep, int pstep, int gstep) {
+  static const int vt[10] = {21, 34, 55, 89, 144, 233, 377, 616, 987, 4184};
+  static const int vp[10] = {8, 13, 21, 34, 55, 89, 144, 233, 377, 2584};
+  bool gt = false, gp = false;
+  for (int i = 0; i < 10; ++i) {
+    if (tstep == vt[i]) gt = true;
+    if (pstep == vp[i]) gp = true;
+  }
+  if (!gt || !gp || tstep <= pstep)
+    throw Error(1, "ZCW needs Fibonacci theta_step/phi_step with theta_step > phi_step");
+  Powder P;
+  int gs = gstep <= 0 ? 1 : gstep;
+  for (int g = 0; g < gs; ++g) {
+    double gnow = gstep == 0 ? 0.0 : double(g) / double(gstep) * kPi;
+    for (int k = 1; k < tstep; ++k) {
+      double fac = double(k) / double(tstep);
+      double f0 = fac - std::floor(fac);
+      double f1 = double(fac * pstep);
+      f1 = f1 - std::floor(f1);
+      P.phi.push_back(2. * kPi * f0);
+      P.theta.push_back(kPi * f1);
+      P.weight.push_back(1.0 / double(tstep) * std::sin(kPi * f1));
+      P.gamma.push_back(gnow);
+    }
+  }
+  double s = 0;
+  for (double w : P.weight) s += w;
+  for (double &w : P.weight) w /= s;
+  return P;
+}
+
+Powder powder_read(const std::string &path) {
+  std::ifstream in(path);
+  if (!in) throw Error(1, "no powder file '" + path + "'");
+  Powder P;
+  std::string line;
+  while (std::getline(in, line)) {
+    auto t = split_ws(line);
+    if (t.empty() || t[0][0] == '#' || t[0][0] == '%') continue;
+    P.phi.push_back(std::atof(t[0].c_str()));
+    P.theta.push_back(t.size() >= 2 ? std::atof(t[1].c_str()) : 0.0);
+    if (t.size() == 3) {
+      P.weight.push_back(std::atof(t[2].c_str()));
+      P.gamma.push_back(0.0);
+    } else if (t.size() >= 4) {
+      P.gamma.push_back(std::atof(t[2].c_str()));
+      P.weight.push_back(std::atof(t[3].c_str()));
+    } else {
+      P.weight.push_back(1.0);
+      P.gamma.push_back(0.0);
+    }
+  }
+  return P;
+}
+
+// ---------------------------------------------------------------- FID output
+
+namespace {
+// Radix-2 transform with the reference's sign (+i) and no normalisation
+// (src/container/Vector/Vectoraux.h:113-160).
+std::vector<cplx> fft_pos(std::vector<cplx> d) {
+  int n = int(d.size());
+  for (int j = 0, i = 0; i < n; ++i) {
+    if (j > i) std::swap(d[i], d[j]);
+    int m = n / 2;
+    while (m > 1 && j >= m) j -= m, m /= 2;
+    j += m;
+  }
+  for (int mmax = 1; n > mmax; mmax *= 2) {
+    double theta = kPi / mmax, s2 = std::sin(theta * 0.5);
+    cplx wp(-2. * s2 * s2, std::sin(theta)), w(1, 0);
+    for (int ii = 0; ii < mmax; ++ii) {
+      for (int i = ii; i < n; i += 2 * mmax) {
+        int j = i + mmax;
+        cplx t = w * d[j];
+        d[j] = d[i] - t;
+        d[i] += t;
+      }
+      w += w * wp;
+    }
+  }
+  return d;
+}
+}  // namespace
+
+void write_fid_text(const std::string &path, const cplx *fid, int npts, double dt) {
+  int n = 1;
+  while (n < npts) n *= 2;
+  std::vector<cplx> tf(fid, fid + npts);
+  tf.resize(n, cplx(0, 0));
+  std::vector<cplx> sp = fft_pos(tf);
+  int sh = int(std::ceil(double(n) / 2.0));
+  std::vector<cplx> sh_sp(n);
+  for (int j = 0; j < n; ++j) sh_sp[j] = sp[(j + sh) % n];
+  std::ofstream oo(path);
+  if (!oo) throw Error(1, "cannot write '" + path + "'");
+  double dw = 1. / dt / n, minw = -1. / dt / 2., t = 0;
+  for (int i = 0; i < n; ++i) {
+    oo << t << " " << minw << " " << sh_sp[i].real() << " " << sh_sp[i].imag() << " " << tf[i].real() << " "
+       << tf[i].imag() << " " << std::abs(sh_sp[i]) << "\n";
+    minw += dw;
+    t += dt;
+  }
+}
+
+}  // namespace bl

@@ -1,0 +1,116 @@
+// Host-side model of a BlochLib solid-state spin system (the SolidSys / SpinSys /
+// Rotations / powder surface), prepared for the GPU engine.
+//
+// Reference behaviour mirrored here (paths inside the BlochLib tree):
+//   SolidSys::read                    src/QMspins/sys.cc:120-204
+//   read_csa / read_dip / read_js /   src/QMspins/csa.cc:400-440, dip.cc:285-323,
+//     read_qua                          j.cc:171-202, qua.cc:511-560
+//   single-spin and expanded ops      src/QMspins/singlespinop.cc:88-200,
+//                                     src/QMspins/multispinop.cc:51-74
+//   interaction PAS tensors           csa.cc:223-286, dip.cc:136-169, qua.cc:169-217
+//   spin tensors T20/T00/T_Dip/T_J    src/QMspins/spin_ten.cc:211-236, 285-372, 431-465
+//   Hamiltonian(t1,t2,wr)             src/QMspins/sys.cc:749-770
+//   powder generation / file reader   src/QMspins/driver/powder.cc:179-311, 333-389
+//   plotterFID text output            src/utils/plotter.cc:49-135
+#pragma once
+
+#include <complex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace bl {
+
+typedef std::complex<double> cplx;
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+// Dense complex N x N matrix, row-major.
+struct CMatrix {
+  int n = 0;
+  std::vector<cplx> a;
+  CMatrix() {}
+  explicit CMatrix(int n_) : n(n_), a(size_t(n_) * n_) {}
+  cplx &operator()(int r, int c) { return a[size_t(r) * n + c]; }
+  const cplx &operator()(int r, int c) const { return a[size_t(r) * n + c]; }
+};
+
+// One interaction line of the spin-system file.
+struct Interaction {
+  char kind = 'C';  // 'C' CSA, 'D' dipole, 'J' scalar coupling, 'Q' quadrupole
+  double iso = 0, del = 0, eta = 0;
+  double alpha = 0, beta = 0, gamma = 0;  // PAS Euler angles, degrees
+  int s1 = 0, s2 = 0, strong = 0;
+  double pas[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // crystal-frame tensor
+  double op_scale = 0;  // H term = op_scale * (R pas R^T)_22 * T
+};
+
+// Block structure of every Hamiltonian the system can produce: connected components of
+// the union of the non-zero patterns of its operator terms.  All SolidSys terms commute
+// with total Fz, so blocks sit inside magnetisation sectors (or finer).
+struct BlockLayout {
+  int N = 0;
+  std::vector<int> size, off, poff;  // per block: dimension, first permuted index, packed offset
+  std::vector<int> perm;             // permuted index -> Zeeman index
+  std::vector<int> inv;              // Zeeman index -> permuted index
+  std::vector<int> block_of;         // permuted index -> block
+  int S2 = 0;                        // sum of size^2
+  int max_block = 0;
+};
+
+class SpinSystem {
+ public:
+  explicit SpinSystem(const std::vector<std::string> &lines);
+  static SpinSystem from_text(const std::string &text);
+
+  int spins() const { return nspin_; }
+  int dim() const { return N_; }
+  const std::vector<std::string> &isotopes() const { return iso_; }
+  const std::vector<Interaction> &interactions() const { return ints_; }
+
+  // Operator from an expression: '+'-separated terms "[coef*]NAME [spin]" with NAME in
+  // Fx Fy Fz Fp Fm Fe Ix Iy Iz Ip Im.
+  CMatrix op(const std::string &expr) const;
+  CMatrix single(char which, int spin) const;  // x y z p m e
+
+  // Constant part of H (isotropic CSA, J couplings) and the operator multiplying each
+  // orientation-dependent interaction (index matches interactions(); zero for J).
+  const std::vector<double> &h_const() const { return hc_; }  // N*N real, row-major
+  const std::vector<std::vector<double>> &h_ops() const { return hops_; }
+  const BlockLayout &layout() const { return layout_; }
+
+  // Reference-order dense H at rotor phase 'alpha_rot' for powder rotation Rp (for tests).
+  std::vector<double> hamiltonian(const double Rp[3][3], double alpha_rot, double rotb_rad) const;
+
+ private:
+  void build();
+  int nspin_ = 1, N_ = 1;
+  std::vector<std::string> iso_;
+  std::vector<int> dims_;
+  std::vector<Interaction> ints_;
+  std::vector<double> hc_;
+  std::vector<std::vector<double>> hops_;
+  BlockLayout layout_;
+};
+
+double isotope_spin(const std::string &iso);
+
+// Cartesian rotations of the reference (src/QMspins/space_ten.cc:578-652)
+void rotation3(double a, double b, double g, double R[3][3]);
+void rotation2(double phi, double theta, double R[3][3]);
+
+// Powder angle sets (src/QMspins/driver/powder.cc)
+struct Powder {
+  std::vector<double> theta, phi, gamma, weight;
+  int size() const { return int(theta.size()); }
+};
+Powder powder_zcw(int tstep, int pstep, int gstep);  // powder.cc:248-280 + normalisation
+Powder powder_read(const std::string &path);        // powder.cc:333-389 (no renormalisation)
+
+// plotterFID-style 7-column text output (src/utils/plotter.cc:49-135)
+void write_fid_text(const std::string &path, const cplx *fid, int npts, double dt);
+
+}  // namespace bl

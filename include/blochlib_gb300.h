@@ -1,0 +1,129 @@
+/*
+ * blochlib_gb300 — C ABI of the GB300 powder-FID engine.
+ *
+ * Drop-in boundary for BlochLib's spinning powder-FID path (SolidSys + powder +
+ * oneFID<SolidSys>::FID + plotterFID).  Plain pointers and sizes only; every call returns
+ * a bl_status and never throws or aborts.  A per-thread message for the last failure is
+ * available from bl_last_error().  Complex arrays are interleaved (re, im) doubles;
+ * operator matrices are N x N, row-major, in the Zeeman product basis with spin 0 the
+ * most significant factor (the reference's Kronecker order).
+ *
+ * Reference interfaces replaced (paths inside the BlochLib tree):
+ *   bl_system_create      SolidSys::SolidSys(const Vector<string>&)  src/QMspins/sys.cc:40-42,120-204
+ *   bl_system_operator    SpinSys::Fx()/Fy()/Fz()/Fp()/Fmi()/Fe(), Ix(i)...Imi(i)
+ *                                                                    src/QMspins/spinsys.h:143-162
+ *   bl_powder_zcw         powder::powder(powder::zcw, t, p, g)       src/QMspins/driver/powder.cc:94-113,248-280
+ *   bl_powder_read        powder::read(file)                         src/QMspins/driver/powder.cc:333-389
+ *   bl_powder_from_arrays powder setters (theta/phi/gamma/weight)    src/QMspins/driver/powder.h:111-141
+ *   bl_powder_fid         oneFID<SolidSys>::FID(powder&, ro, det)    src/QMspins/driver/oneFID.h:103-108,200-208
+ *                         (spinning branch oneFID.h:339-431, compute.h:86-461)
+ *   bl_job_*              the same call split into upload / run / read, for callers that
+ *                         keep inputs resident on the GPU between calls (no reference twin;
+ *                         oneFID::FID recomputes from host data every call)
+ *   bl_plotter_fid        plotterFID(fid, file, dt)                  src/utils/plotter.cc:49-135
+ */
+#ifndef BLOCHLIB_GB300_H
+#define BLOCHLIB_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BL_OK = 0,
+  BL_ERR_INVALID = 1,     /* bad argument (sizes, null pointers, npts<=0, sw/wr<1) */
+  BL_ERR_PARSE = 2,       /* malformed spin-system text / unknown isotope */
+  BL_ERR_CUDA = 3,        /* CUDA runtime error (message in bl_last_error) */
+  BL_ERR_NOMEM = 4,       /* the job does not fit the context's device-memory budget */
+  BL_ERR_UNSUPPORTED = 5, /* valid input outside what the GPU engine implements */
+  BL_ERR_NUMERIC = 7      /* an eigen-solver exceeded its iteration bound */
+} bl_status;
+
+typedef struct bl_ctx bl_ctx;
+typedef struct bl_system bl_system;
+typedef struct bl_powder bl_powder;
+typedef struct bl_job bl_job;
+
+typedef struct {
+  int npts;        /* FID points */
+  double sw;       /* sweep width, Hz (rounded to n*wr, n = floor(sw/wr+0.5)) */
+  double wr;       /* rotor speed, Hz (0 = static; not implemented) */
+  double rotb_deg; /* rotor angle, degrees */
+  double start_t;  /* start time, s */
+  int precision;   /* 0 = FP64 */
+} bl_fid_params;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *bl_last_error(void);
+/* Library version string. */
+const char *bl_version(void);
+
+/* Context: one CUDA device and stream; hbm_budget bytes for work buffers (0 = 16 GiB). */
+bl_status bl_ctx_create(int device, size_t hbm_budget, bl_ctx **out);
+void bl_ctx_destroy(bl_ctx *ctx);
+
+/* Spin system from the reference's text format (numspin/T/C/D/J/Q lines). */
+bl_status bl_system_create(const char *spin_text, bl_system **out);
+void bl_system_destroy(bl_system *sys);
+int bl_system_dim(const bl_system *sys);
+int bl_system_spins(const bl_system *sys);
+/* Operator expression, e.g. "Fx", "Ip 0", "0.5*Fx + Iz 1"; out = 2*N*N doubles. */
+bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out);
+/* Block structure of the Hamiltonian: writes up to cap block sizes, returns the count
+ * through *nblocks. */
+bl_status bl_system_blocks(const bl_system *sys, int *sizes, int cap, int *nblocks);
+
+/* Powder sets. */
+bl_status bl_powder_zcw(int theta_steps, int phi_steps, int gamma_steps, bl_powder **out);
+bl_status bl_powder_read(const char *path, bl_powder **out);
+bl_status bl_powder_from_arrays(const double *theta, const double *phi, const double *gamma,
+                                const double *weight, int n, bl_powder **out);
+int bl_powder_size(const bl_powder *pw);
+/* Copies the angle columns (any pointer may be NULL). */
+bl_status bl_powder_get(const bl_powder *pw, double *theta, double *phi, double *gamma, double *weight);
+void bl_powder_destroy(bl_powder *pw);
+
+/* Powder FID: fid_out = 2*npts doubles; *sw_out = the sweep width actually used. */
+bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                        const double *det, const bl_fid_params *params, double *fid_out, double *sw_out);
+
+/* Resident job: inputs uploaded once, each run recomputes the FID on the device. */
+bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                        const double *det, const bl_fid_params *params, bl_job **out);
+bl_status bl_job_run(bl_job *job);                    /* enqueue on the context stream */
+bl_status bl_job_read(bl_job *job, double *fid_out);  /* synchronises; 2*npts doubles */
+bl_status bl_job_sync(bl_job *job);
+int bl_job_launches(const bl_job *job);               /* kernel launches per run */
+double bl_job_flops(const bl_job *job);               /* algorithmic FP64 flop per run */
+double bl_job_sw(const bl_job *job);
+/* JSON description of the job's layout; returns the length written (truncated to cap). */
+int bl_job_describe(const bl_job *job, char *buf, int cap);
+/* The context's CUDA stream (a cudaStream_t), for callers that time runs with events. */
+void *bl_ctx_stream(bl_ctx *ctx);
+void bl_job_destroy(bl_job *job);
+
+/* Instrumentation (no reference twin: BlochLib has no profiler hooks).  With profiling on,
+ * every stage of bl_job_run is bracketed by CUDA events on the context stream. */
+#define BL_STAGES 8
+const char *bl_stage_name(int stage);
+bl_status bl_job_set_profiling(bl_job *job, int on);
+bl_status bl_job_stage_times(const bl_job *job, double *ms, int *launches); /* BL_STAGES each */
+bl_status bl_job_stage_flops(const bl_job *job, double *flops);             /* BL_STAGES */
+bl_status bl_job_reset_stage_times(bl_job *job);
+/* Runs the job iters times between two events on the context stream. */
+bl_status bl_job_run_timed(bl_job *job, int iters, double *ms_total);
+/* Bytes bl_powder_fid moves for this job: host->device at creation, device->host read. */
+bl_status bl_job_io_bytes(const bl_job *job, size_t *h2d, size_t *d2h);
+/* Measured FP64 FMA throughput of the context's device (TFLOP/s), DFMA probe kernel. */
+bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops);
+
+/* plotterFID-style text file: t, f, Re S, Im S, Re fid, Im fid, |S| (7 columns). */
+bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BLOCHLIB_GB300_H */

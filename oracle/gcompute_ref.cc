@@ -667,6 +667,7 @@ Job parse_job(const std::string &text) {
     else if (key == "sw") J.P.sw = std::atof(val.c_str());
     else if (key == "wr") J.P.wr = std::atof(val.c_str());
     else if (key == "rotb") J.P.rotb = std::atof(val.c_str());
+    else if (key == "start") J.P.startT = std::atof(val.c_str());
     else if (key == "rho") J.rho = val;
     else if (key == "det") J.det = val;
   }

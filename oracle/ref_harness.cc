@@ -14,7 +14,9 @@
 // Job file format (one "key: value" per line, '#' comments):
 //   spin: <one line of the reference's spin-system format>   (repeatable, in order)
 //   powder: <path of a powder file in the reference's format>
-//   npts: <int>   sw: <Hz>   wr: <Hz>   rotb: <degrees>
+//   powder_zcw: <theta_steps> <phi_steps>      (instead of 'powder:'; powder.cc:248-280)
+//   dump_powder: <path>   (writes the powder as C rows of theta phi gamma weight doubles)
+//   npts: <int>   sw: <Hz>   wr: <Hz>   rotb: <degrees>   start: <s>
 //   rho: <operator expression>   det: <operator expression>
 // An operator expression is a '+'-separated sum of terms "[coef*]NAME [spin]" with NAME
 // one of Fx Fy Fz Fp Fm Fe Ix Iy Iz Ip Im (single-spin names take a spin index).
@@ -96,9 +98,9 @@ int main(int argc, char **argv) {
   std::ifstream in(argv[1]);
   if (!in) { std::cerr << "ref_harness: cannot open " << argv[1] << "\n"; return 2; }
   Vector<std::string> spin_lines;
-  std::string powder_file, rho_s, det_s;
-  int npts = 0;
-  double sw = 0, wr = 0, rotb = 0;
+  std::string powder_file, rho_s, det_s, dump_file;
+  int npts = 0, zcw_t = 0, zcw_p = 0;
+  double sw = 0, wr = 0, rotb = 0, start = 0;
   std::string line;
   while (std::getline(in, line)) {
     std::string l = trim(line);
@@ -108,6 +110,9 @@ int main(int argc, char **argv) {
     std::string key = trim(l.substr(0, c)), val = trim(l.substr(c + 1));
     if (key == "spin") spin_lines.push_back(val + "\n");
     else if (key == "powder") powder_file = val;
+    else if (key == "powder_zcw") std::sscanf(val.c_str(), "%d %d", &zcw_t, &zcw_p);
+    else if (key == "dump_powder") dump_file = val;
+    else if (key == "start") start = std::atof(val.c_str());
     else if (key == "npts") npts = std::atoi(val.c_str());
     else if (key == "sw") sw = std::atof(val.c_str());
     else if (key == "wr") wr = std::atof(val.c_str());
@@ -117,10 +122,21 @@ int main(int argc, char **argv) {
   }
   SolidSys sys(spin_lines);
   powder pw;
-  pw.read(powder_file);
+  if (zcw_t > 0) pw = powder(powder::zcw, zcw_t, zcw_p);
+  else pw.read(powder_file);
+  if (!dump_file.empty()) {
+    FILE *fp = std::fopen(dump_file.c_str(), "wb");
+    powder::iterator it(pw);
+    while (it) {
+      double row[4] = {it.theta(), it.phi(), it.gamma(), it.weight()};
+      std::fwrite(row, sizeof(double), 4, fp);
+      ++it;
+    }
+    std::fclose(fp);
+  }
   matrix ro = op_expr(sys, rho_s);
   matrix det = op_expr(sys, det_s);
-  oneFID<SolidSys> driver(sys, npts, sw, wr, rotb);
+  oneFID<SolidSys> driver(sys, npts, sw, wr, rotb, start);
   Vector<complex> fid = driver.FID(pw, ro, det);
   FILE *f = std::fopen(argv[2], "wb");
   if (!f) { std::cerr << "ref_harness: cannot write " << argv[2] << "\n"; return 2; }

@@ -1,0 +1,117 @@
+#!/usr/bin/env python3
+"""Generates the golden FID fixtures by running the BlochLib reference itself.
+
+Run here, where the reference tree is mounted (BLOCHLIB_REF, default /root/reference):
+    oracle/build_ref.sh all && python3 tests/golden/make_golden.py
+
+Each case is a seeded job in the text format of oracle/ref_harness.cc.  For every case
+the fixture holds the job text, the crystallites (phi, theta, gamma, weight rows), the
+FID of the reference built with its QL eigen-iteration in double (ref_fid64, the FP64
+oracle) and as shipped (ref_fid, float QL), and the sweep width the reference reports.
+Also recorded: the reference's built-in 2-angle ZCW sets, and sample rows of its
+3-angle ZCW powder files (to check the closed-form generator in workloads.py).
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from blochlib_gb300 import workloads as W  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+REF = Path(os.environ.get("BLOCHLIB_REF", "/root/reference"))
+BIN64 = ROOT / "oracle" / "_ref" / "ref_fid64"
+BIN32 = ROOT / "oracle" / "_ref" / "ref_fid"
+
+
+def run_ref(binary, job_text, rows):
+    with tempfile.TemporaryDirectory() as td:
+        pw = Path(td) / "powder.txt"
+        with open(pw, "w") as f:
+            for r in rows:
+                f.write(" ".join("%.17g" % x for x in r) + "\n")
+        job = Path(td) / "job.txt"
+        job.write_text(job_text + f"powder: {pw}\n")
+        out = Path(td) / "out.bin"
+        subprocess.run([str(binary), str(job), str(out)], check=True)
+        a = np.fromfile(out, dtype=np.float64)
+    return float(a[0]), a[1:].view(np.complex128).copy()
+
+
+def spread(n_total, k):
+    return np.linspace(0, n_total - 1, k).round().astype(int)
+
+
+def powder_rows(pw, idx):
+    phi, theta, gamma, w = pw
+    return np.stack([phi[idx], theta[idx], gamma[idx], w[idx]], axis=1)
+
+
+def cases():
+    c0 = W.config(0)
+    yield "c0_sub16", W.job_text(c0), powder_rows(c0["powder"], spread(1154, 16))
+    c1 = W.config(1)
+    yield "c1_sub8", W.job_text(c1), powder_rows(c1["powder"], spread(3722, 8))
+    c1n = dict(c1, rho="Fx+Fz", npts=512)
+    yield "c1_nonsym_sub4", W.job_text(c1n), powder_rows(c1["powder"], spread(3722, 4))
+    quad = dict(lines=["numspin 2", "T 2H 0", "T 13C 1", "Q 120000 0.3 0 10 20 30",
+                       "C 500 4000 0.2 1 5 6 7", "D 2000 0 1 30 40 50", "J 50 0 1"],
+                rho="Ix 0", det="Ip 0", npts=300, wr=5000.0, sw=200000.0, rotb=W.MAGIC_ANGLE)
+    yield "quad_2h13c", W.job_text(quad), powder_rows(c0["powder"], spread(1154, 8))
+    js = dict(lines=["numspin 3", "T 1H 0", "T 1H 1", "T 1H 2", "C 120 3000 0.4 0 10 20 30",
+                     "C -80 2500 0.7 1 40 50 60", "C 0 1800 0.1 2 70 80 90", "D -15000 0 1 0 30 0",
+                     "D -9000 1 2 50 60 0", "D -6000 0 2 120 100 0", "J 140 0 1 1", "J 70 1 2"],
+              rho="Ix 0", det="Ix 0", npts=400, wr=15000.0, sw=96 * 15000.0, rotb=W.MAGIC_ANGLE)
+    yield "jstrong_3h", W.job_text(js), powder_rows(c0["powder"], spread(1154, 6))
+    gl = dict(lines=["numspin 2", "T 13C 0", "T 1H 1", "C 1500 6000 0.5 0 10 70 30", "D 8000 0 1 20 30 40"],
+              rho="Ix 0", det="Ip 0", npts=64, wr=10000.0, sw=40000.0, rotb=W.MAGIC_ANGLE)
+    yield "gammaloop_n4", W.job_text(gl), powder_rows(c0["powder"], spread(1154, 8))
+    het = dict(lines=["numspin 3", "T 13C 0", "T 1H 1", "T 1H 2", "C 900 7000 0.6 0 33 44 55",
+                      "D 9000 0 1 10 20 30", "D 7000 0 2 40 50 60", "D -20000 1 2 70 80 0"],
+               rho="Ix 0", det="Ip 0", npts=512, wr=12000.0, sw=80 * 12000.0, rotb=30.0)
+    yield "hetero_13c2h_30deg", W.job_text(het), powder_rows(c0["powder"], spread(1154, 6))
+    st = dict(c0, npts=256)
+    yield "c0_start_t", W.job_text(st) + "start: 1.7e-05\n", powder_rows(c0["powder"], spread(1154, 4))
+
+
+def main():
+    if not BIN64.exists():
+        sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
+    manifest = {}
+    for name, job, rows in cases():
+        sw64, f64 = run_ref(BIN64, job, rows)
+        sw32, f32 = run_ref(BIN32, job, rows)
+        np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f32,
+                            sw=np.array(sw64))
+        manifest[name] = {"crystallites": len(rows), "npts": len(f64), "sw": sw64,
+                          "float_ql_rel_dev": float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))}
+        print(name, manifest[name])
+    # built-in 2-angle ZCW sets (powder.cc:248-280)
+    zcw = {}
+    for t, p in [(144, 89), (233, 144), (21, 8)]:
+        with tempfile.TemporaryDirectory() as td:
+            dump = Path(td) / "pw.bin"
+            job = "spin: numspin 1\nspin: T 1H 0\nnpts: 1\nsw: 1000\nwr: 100\nrotb: 54.7356\nrho: Fx\ndet: Fp\n"
+            jf = Path(td) / "job.txt"
+            jf.write_text(job + f"powder_zcw: {t} {p}\ndump_powder: {dump}\n")
+            subprocess.run([str(BIN64), str(jf), str(Path(td) / "o.bin")], check=True)
+            zcw[f"{t}_{p}"] = np.fromfile(dump).reshape(-1, 4)
+    np.savez_compressed(OUT / "zcw_builtin.npz", **zcw)
+    # sample rows of the 3-angle ZCW powder files shipped with the reference
+    samples = {}
+    for n in (1154, 3722):
+        rows = np.loadtxt(REF / "crystals" / f"ZCW_3_{n}")
+        idx = [0, 1, 2, 3, 100, n // 2, n - 2, n - 1]
+        samples[str(n)] = {"index": idx, "rows": rows[idx].tolist(), "count": int(len(rows))}
+    (OUT / "zcw3_samples.json").write_text(json.dumps(samples, indent=1))
+    (OUT / "manifest.json").write_text(json.dumps(manifest, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+"""CUDA engine vs the reference (golden fixtures) and vs the CPU oracle, through the C ABI.
+
+Tolerance: the plain FP64 path must reproduce the reference's FP64 FID to <= 1e-10
+relative L2 error (||fid - ref|| / ||ref||)."""
+import numpy as np
+import pytest
+
+import blochlib_gb300 as bl
+from blochlib_gb300 import workloads as W
+from helpers import gpu_fid, golden_cases, load_golden, oracle_fid, parse_job, rel
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_matches_reference_golden(case):
+    job, rows, fid64, fid32, sw = load_golden(case)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True)
+    assert sw_g == sw
+    assert rel(fid, fid64) <= TOL, rel(fid, fid64)
+
+
+def random_system(seed):
+    rng = np.random.default_rng(seed)
+    kind = seed % 3
+    if kind == 0:   # homonuclear 1H, 2-4 spins
+        n = int(rng.integers(2, 5))
+        iso = ["1H"] * n
+    elif kind == 1:  # heteronuclear mix
+        n = int(rng.integers(2, 5))
+        iso = [str(rng.choice(["1H", "13C", "15N"])) for _ in range(n)]
+    else:            # spin-1 quadrupole with protons
+        n = int(rng.integers(2, 4))
+        iso = ["2H"] + ["1H"] * (n - 1)
+    lines = [f"numspin {n}"] + [f"T {iso[k]} {k}" for k in range(n)]
+    for k in range(n):
+        a = rng.uniform(0, 360, 3)
+        lines.append(f"C {rng.uniform(-3e3, 3e3):.9g} {rng.uniform(-8e3, 8e3):.9g} {rng.uniform(0, 1):.9g} {k} "
+                     f"{a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    for i in range(n):
+        for j in range(i + 1, n):
+            a = rng.uniform(0, 360, 3)
+            lines.append(f"D {rng.uniform(-2e4, 2e4):.9g} {i} {j} {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+            if rng.uniform() < 0.5:
+                lines.append(f"J {rng.uniform(0, 200):.9g} {i} {j} {int(rng.uniform() < 0.3)}")
+    if kind == 2:
+        a = rng.uniform(0, 360, 3)
+        lines.append(f"Q {rng.uniform(5e4, 2e5):.9g} {rng.uniform(0, 1):.9g} 0 {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    rho, det = [("Fx", "Fp"), ("Fx+Fz", "Fp"), ("Ix 0", "Ix 0"), ("Iy 0", "Ip 0")][seed % 4]
+    wr = float(rng.uniform(5e3, 30e3))
+    n_steps = int(rng.integers(12, 70))
+    job = "\n".join(f"spin: {l}" for l in lines) + (
+        f"\nnpts: {int(rng.integers(50, 300))}\nsw: {n_steps * wr!r}\nwr: {wr!r}\nrotb: {rng.uniform(30, 70)!r}\n"
+        f"rho: {rho}\ndet: {det}\n")
+    c = int(rng.integers(1, 40))
+    rows = np.stack([rng.uniform(0, 2 * np.pi, c), np.arccos(rng.uniform(-1, 1, c)), rng.uniform(0, 2 * np.pi, c),
+                     rng.uniform(0.1, 1, c)], axis=1)
+    return job, rows
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_gpu_matches_oracle_random_systems(seed):
+    job, rows = random_system(seed)
+    ref, sw = oracle_fid(job, rows)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True)
+    assert sw_g == sw
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
+def test_c0_full_powder_matches_oracle():
+    cfg = W.config(0)
+    job = W.job_text(cfg)
+    rows = np.stack(cfg["powder"], axis=1)
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows)
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
+def _c1_job(count=None):
+    cfg = W.config(1)
+    rows = np.stack(cfg["powder"], axis=1)
+    if count:
+        rows = rows[:count]
+    return W.job_text(cfg), rows
+
+
+def test_batched_run_is_bitwise_identical_to_single_batch():
+    job, rows = _c1_job(200)
+    one = gpu_fid(job, rows)
+    small = bl.Context(0, hbm_budget=40 << 20)  # forces several crystallite batches
+    many = gpu_fid(job, rows, ctx=small)
+    np.testing.assert_array_equal(one, many)
+
+
+def test_crystallite_alone_equals_crystallite_in_batch():
+    job, rows = _c1_job(96)
+    c = 37
+    alone = gpu_fid(job, rows[c:c + 1])
+    masked = rows.copy()
+    masked[:, 3] = 0.0
+    masked[c, 3] = rows[c, 3]
+    inbatch = gpu_fid(job, masked)
+    np.testing.assert_array_equal(alone, inbatch)
+
+
+def test_c1_full_size_properties():
+    """Full c1 (3722 crystallites, 2048 points): size-independent checks."""
+    job, rows = _c1_job()
+    full = gpu_fid(job, rows)
+    # rho = Fx = (D + D^H)/2 with D = F+ (D^2 = 0): fid[0] = 2 Tr(D D^H) sum(w)
+    lines, kv = parse_job(job)
+    s = bl.SolidSys(lines)
+    D = s.op("Fp")
+    expect0 = 2 * np.trace(D @ D.conj().T).real * rows[:, 3].sum()
+    assert abs(full[0] - expect0) <= 1e-12 * abs(expect0)
+    # linearity in the powder weights: two halves sum to the whole
+    a, b = rows.copy(), rows.copy()
+    a[1861:, 3] = 0.0
+    b[:1861, 3] = 0.0
+    assert rel(gpu_fid(job, a) + gpu_fid(job, b), full) <= 1e-13
+    # the first 8 crystallites against the oracle
+    ref8, _ = oracle_fid(job, rows[:8])
+    assert rel(gpu_fid(job, rows[:8]), ref8) <= TOL
+
+
+def test_unsupported_inputs_return_status():
+    cfg = W.config(0)
+    rows = np.stack(cfg["powder"], axis=1)[:4]
+    static_job = W.job_text(dict(cfg, wr=0.0))
+    with pytest.raises(bl.BlochError) as e:
+        gpu_fid(static_job, rows)
+    assert e.value.status == 5
+    big = "\n".join(f"spin: {l}" for l in ["numspin 5"] + [f"D -5000 {i} {j}" for i in range(5) for j in range(i + 1, 5)])
+    big += "\nnpts: 16\nsw: 100000\nwr: 10000\nrotb: 54.7356\nrho: Fx\ndet: Fp\n"
+    with pytest.raises(bl.BlochError) as e:
+        gpu_fid(big, rows)
+    assert e.value.status == 5
+    too_slow = W.job_text(dict(cfg, sw=1000.0))  # sw/wr rounds to zero steps
+    with pytest.raises(bl.BlochError) as e:
+        gpu_fid(too_slow, rows)
+    assert e.value.status == 1
+
+
+def test_resident_job_reruns_identically():
+    job, rows = _c1_job(64)
+    lines, kv = parse_job(job)
+    s = bl.SolidSys(lines)
+    pw = bl.powder.from_arrays(rows[:, 1], rows[:, 0], rows[:, 2], rows[:, 3])
+    j = bl.Job(s, pw, s.op(kv["rho"]), s.op(kv["det"]), int(kv["npts"]), float(kv["sw"]), float(kv["wr"]),
+               float(kv["rotb"]))
+    j.run()
+    a = j.read()
+    j.set_profiling(True)
+    j.run()
+    b = j.read()
+    np.testing.assert_array_equal(a, b)
+    st = j.stage_times()
+    assert st["k_fave"][1] >= 1 and st["k_step_prop"][0] > 0
+    assert j.launches >= 8

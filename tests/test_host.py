@@ -1,0 +1,121 @@
+"""Host side of the boundary through the C ABI: spin systems, operators, blocks, powders,
+FID text output and error statuses.  No GPU needed."""
+import numpy as np
+import pytest
+
+import blochlib_gb300 as bl
+from blochlib_gb300 import workloads as W
+from helpers import GOLDEN
+
+
+def single(spin, which):
+    hs = int(round(2 * spin + 1))
+    q = (hs - 1) / 2
+    m = np.zeros((hs, hs), dtype=complex)
+    if which == "z":
+        return np.diag(q - np.arange(hs)).astype(complex)
+    for k in range(hs - 1):
+        mm = q - 1 - k
+        c = np.sqrt(q * (q + 1) - mm * (mm + 1))
+        if which == "p":
+            m[k, k + 1] = c
+        elif which == "m":
+            m[k + 1, k] = c
+        elif which == "x":
+            m[k, k + 1] = m[k + 1, k] = c / 2
+        elif which == "y":
+            m[k + 1, k], m[k, k + 1] = 0.5j * c, -0.5j * c
+    return m
+
+
+def expand(spins, k, op):
+    out = np.eye(1, dtype=complex)
+    for i, s in enumerate(spins):
+        out = np.kron(out, op if i == k else np.eye(int(round(2 * s + 1))))
+    return out
+
+
+def test_operators_match_kronecker_construction():
+    sys_ = bl.SolidSys(["numspin 3", "T 1H 0", "T 2H 1", "T 13C 2"])
+    spins = [0.5, 1.0, 0.5]
+    assert sys_.dim() == 12 and sys_.spins() == 3
+    for k in range(3):
+        for w, name in [("x", "Ix"), ("y", "Iy"), ("z", "Iz"), ("p", "Ip"), ("m", "Im")]:
+            np.testing.assert_array_equal(sys_.op(f"{name} {k}"), expand(spins, k, single(spins[k], w)))
+    tot = sum(expand(spins, k, single(spins[k], "p")) for k in range(3))
+    np.testing.assert_array_equal(sys_.Fp(), tot)
+    np.testing.assert_array_equal(sys_.op("0.5*Fx + Iz 1"),
+                                  0.5 * sum(expand(spins, k, single(spins[k], "x")) for k in range(3))
+                                  + expand(spins, 1, single(1.0, "z")))
+
+
+def test_block_structure_follows_magnetisation_sectors():
+    c1 = W.config(1)
+    assert sorted(bl.SolidSys(c1["lines"]).blocks()) == [1, 1, 4, 4, 6]
+    c0 = W.config(0)  # heteronuclear, secular: H is diagonal
+    assert bl.SolidSys(c0["lines"]).blocks() == [1, 1, 1, 1]
+    c2 = W.config(2)
+    assert sorted(bl.SolidSys(c2["lines"]).blocks()) == [1, 1, 8, 8, 28, 28, 56, 56, 70]
+
+
+def test_zcw_builtin_matches_reference():
+    ref = np.load(GOLDEN / "zcw_builtin.npz")
+    for key in ref.files:
+        t, p = map(int, key.split("_"))
+        th, ph, ga, w = bl.powder(bl.powder.zcw, t, p).arrays()
+        r = ref[key]
+        np.testing.assert_allclose(th, r[:, 0], rtol=0, atol=1e-15)
+        np.testing.assert_allclose(ph, r[:, 1], rtol=0, atol=1e-15)
+        np.testing.assert_array_equal(ga, r[:, 2])
+        np.testing.assert_allclose(w, r[:, 3], rtol=1e-14, atol=0)
+
+
+def test_powder_file_reader_column_rules(tmp_path):
+    f = tmp_path / "p.txt"
+    f.write_text("# comment\n% other comment\n0.1 0.2 0.3 0.4\n0.5 0.6 0.7\n0.8 0.9\n1.1\n")
+    th, ph, ga, w = bl.powder.read(f).arrays()
+    np.testing.assert_array_equal(ph, [0.1, 0.5, 0.8, 1.1])   # column 0 -> phi
+    np.testing.assert_array_equal(th, [0.2, 0.6, 0.9, 0.0])   # column 1 -> theta
+    np.testing.assert_array_equal(ga, [0.3, 0.0, 0.0, 0.0])   # 4 columns: gamma then weight
+    np.testing.assert_array_equal(w, [0.4, 0.7, 1.0, 1.0])    # 3 columns: weight; fewer: 1
+
+
+def test_plotter_fid_text(tmp_path):
+    rng = np.random.default_rng(1)
+    fid = rng.normal(size=100) + 1j * rng.normal(size=100)
+    path = tmp_path / "fid.txt"
+    bl.plotterFID(fid, path, 1e-5)
+    d = np.loadtxt(path)
+    n = 128  # zero-filled to the next power of two
+    assert d.shape == (n, 7)
+    x = np.concatenate([fid, np.zeros(n - 100)])
+    S = np.fft.ifft(x) * n  # the reference's FFT has the +i sign and no scaling
+    S = np.roll(S, -(n // 2))
+    np.testing.assert_allclose(d[:, 0], np.arange(n) * 1e-5, rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(d[:, 1], -0.5 / 1e-5 + np.arange(n) / (1e-5 * n), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(d[:, 2] + 1j * d[:, 3], S, rtol=2e-5, atol=1e-4)
+    np.testing.assert_allclose(d[:, 4] + 1j * d[:, 5], x, rtol=2e-5, atol=1e-5)
+    np.testing.assert_allclose(d[:, 6], np.abs(S), rtol=2e-5, atol=1e-4)
+
+
+@pytest.mark.parametrize("lines,status", [
+    (["numspin 2", "T 1H 0", "T 1H 5"], 2),
+    (["numspin 2", "T 1H 0", "T Xx9 1"], 2),
+    (["numspin 2", "C 1 2 0.1"], 2),
+    (["numspin 2", "D 100 0 7"], 2),
+    (["numspin 1", "T 1H 0", "Q 1000 0 0"], 2),
+])
+def test_malformed_systems_return_parse_status(lines, status):
+    with pytest.raises(bl.BlochError) as e:
+        bl.SolidSys(lines)
+    assert e.value.status == status
+
+
+def test_bad_zcw_and_operator_return_invalid():
+    with pytest.raises(bl.BlochError) as e:
+        bl.powder(bl.powder.zcw, 100, 7)
+    assert e.value.status == 1
+    s = bl.SolidSys(["numspin 1"])
+    with pytest.raises(bl.BlochError) as e:
+        s.op("Foo")
+    assert e.value.status == 1
