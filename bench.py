@@ -222,6 +222,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--crystallites", type=int, default=0,
+                    help="use only the first N crystallites (smaller case for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -230,6 +232,8 @@ def main():
     d = Dist()
     ctx = bl.Context(d.local)
     cfg = workload(args.config)
+    if args.crystallites:
+        cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
     s, pw, ro, det, job = make_job(bl, cfg, ctx)
     for _ in range(args.warmup):
         job.run()

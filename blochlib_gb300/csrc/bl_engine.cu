@@ -1059,7 +1059,8 @@ void Job::run() {
     mark_end(J, 6, 1);
   }
   mark_begin(J, 7);
-  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, J.nwarps_total, J.P.npts, J.fid.p);
+  // only warps that hold crystallites: the sum is then independent of the batch size
+  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, (J.Ceff + 31) / 32, J.P.npts, J.fid.p);
   ++J.launches;
   mark_end(J, 7, 1);
   CUDA_OK(cudaGetLastError());
