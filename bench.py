@@ -124,12 +124,12 @@ def workload(name):
     return W.config(idx)
 
 
-def make_job(bl, cfg, ctx):
+def make_job(bl, cfg, ctx, step_method=None):
     s = bl.SolidSys(cfg["lines"])
     phi, theta, gamma, w = cfg["powder"]
     pw = bl.powder.from_arrays(theta, phi, gamma, w)
     ro, det = s.op(cfg["rho"]), s.op(cfg["det"])
-    job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx)
+    job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=step_method)
     return s, pw, ro, det, job
 
 
@@ -192,10 +192,12 @@ def run_reference(args):
     cfg = workload(args.config)
     binary, kind = _ref_binary()
     vals = []
+    # each step is a bounded sample; the whole run stays within about two minutes
+    step_s = max(1.0, min(args.cpu_seconds, 120.0 / max(args.steps, 1)))
     for i in range(args.warmup):
         cpu_baseline(cfg, target_s=1.0)
     for i in range(args.steps):
-        vals.append(cpu_baseline(cfg, target_s=args.cpu_seconds)["value"])
+        vals.append(cpu_baseline(cfg, target_s=step_s)["value"])
     v = statistics.median(vals)
     last = cpu_baseline(cfg, target_s=1.0)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -222,6 +224,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--step-method", default=None, choices=["eigh", "taylor"],
+                    help="FP64 step exponential (default: BL_STEP_METHOD or eigh)")
     ap.add_argument("--crystallites", type=int, default=0,
                     help="use only the first N crystallites (smaller case for profiler captures)")
     args = ap.parse_args()
@@ -234,7 +238,7 @@ def main():
     cfg = workload(args.config)
     if args.crystallites:
         cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
-    s, pw, ro, det, job = make_job(bl, cfg, ctx)
+    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method)
     for _ in range(args.warmup):
         job.run()
     job.sync()
@@ -267,7 +271,7 @@ def main():
             traffic = None
     launches_per_run = job.launches
     # e2e through the reference-facing call with host buffers
-    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx)
+    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method)
     drv.FID(pw, ro, det)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):

@@ -55,6 +55,7 @@ bl::FidParams to_params(const bl_fid_params *p) {
   bl::FidParams f;
   f.npts = p->npts, f.sw = p->sw, f.wr = p->wr, f.rotb_deg = p->rotb_deg, f.start_t = p->start_t;
   f.precision = p->precision;
+  f.step_method = p->step_method;
   return f;
 }
 }  // namespace

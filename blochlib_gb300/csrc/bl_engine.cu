@@ -83,7 +83,7 @@ __device__ __forceinline__ double chop1(double v, double eps) { return fabs(v) <
 
 // ------------------------------------------------------------------ job description
 struct DevSys {
-  int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym;
+  int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
   double tau, wr, sin_rotb, cos_rotb, scale;
   // per block
   const int *bs, *boff, *bpoff;
@@ -350,18 +350,10 @@ __device__ int unitary_eig(const double2 (&U)[B][B], double2 (&lam)[B], double2 
 // ------------------------------------------------------------------ kernels
 __device__ __forceinline__ size_t at(int item, int c, int Cpad) { return size_t(item) * Cpad + c; }
 
-// One thread per (crystallite, block k, step i): U_i block.
+// H_i block at the midpoint of step i (sys.cc:749-770): rotor phase 2 pi wr t_mid,
+// a = (M PAS M^T)_22 with M = R_rotor R_powder, H = Hc + sum_k scale_k a_k T_k.
 template <int B>
-__global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__restrict__ blist, int nblist) {
-  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  int c = int(tid % s.Cpad);
-  long rest = tid / s.Cpad;
-  if (rest >= long(nblist) * s.n) return;
-  int i = int(rest % s.n);
-  int k = blist[rest / s.n];
-  if (c >= s.C) return;
-  const int bp = s.bpoff[k];
-  // rotor phase at the step midpoint (sys.cc:754-755)
+__device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, double (&h)[B][B]) {
   double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
   double tmid = (t2 - t1) / 2.0 + t1;
   double sp, cp;
@@ -373,14 +365,12 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
   for (int j = 0; j < 3; ++j)
     r[j] = rr0 * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr1 * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
            rr2 * s.Rp[at(2 * 3 + j, c, s.Cpad)];
-  double h[B][B];
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
     for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
   for (int kk = 0; kk < s.nint; ++kk) {
     const double *P = s.pas + 6 * kk;
-    // a = r^T PAS r  (the (2,2) element of M PAS M^T)
     double a = r[0] * (P[0] * r[0] + P[1] * r[1] + P[2] * r[2]) + r[1] * (P[1] * r[0] + P[3] * r[1] + P[4] * r[2]) +
                r[2] * (P[2] * r[0] + P[4] * r[1] + P[5] * r[2]);
     double f = s.iscale[kk] * a;
@@ -390,6 +380,23 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
 #pragma unroll
       for (int q = 0; q < B; ++q) h[p][q] = fma(f, T[p * B + q], h[p][q]);
   }
+}
+
+// One thread per (crystallite, block k, step i): U_i = V diag(chop(e^{-i 2pi tau L})) V^T
+// from a cyclic Jacobi eigen-decomposition of the real symmetric H_i block (the
+// reference's method, matexp.h:240-252).
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * s.n) return;
+  int i = int(rest % s.n);
+  int k = blist[rest / s.n];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  double h[B][B];
+  build_h<B>(s, c, i, bp, h);
   double v[B][B];
   if (!jacobi_sym<B>(h, v)) atomicOr(s.status, kNoConvergeStep);
   double2 e[B];
@@ -412,6 +419,106 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
         u.x = fma(vv, e[j].x, u.x);
         u.y = fma(vv, e[j].y, u.y);
       }
+      Ub[at(bp + p * B + q, c, s.Cpad)] = u;
+      if (q != p) Ub[at(bp + q * B + p, c, s.Cpad)] = u;
+    }
+}
+
+constexpr int kTaylorTerms = 15;  // ||x|| <= 1/2: remainder 0.5^16/16! < 1e-18
+
+// Upper-triangle index of a symmetric B x B matrix stored packed.
+template <int B>
+__device__ __forceinline__ constexpr int sx(int p, int q) {
+  return p <= q ? p * B - p * (p - 1) / 2 + (q - p) : q * B - q * (q - 1) / 2 + (p - q);
+}
+
+// C = X Y for commuting real symmetric X, Y (the product is symmetric): upper triangle.
+template <int B>
+__device__ __forceinline__ void sym_mul(const double *X, const double *Y, double *C, double scale) {
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      double acc = 0;
+#pragma unroll
+      for (int l = 0; l < B; ++l) acc = fma(X[sx<B>(p, l)], Y[sx<B>(l, q)], acc);
+      C[sx<B>(p, q)] = acc * scale;
+    }
+}
+
+// One thread per (crystallite, block k, step i): U_i = exp(-i 2pi tau H_i) by a Taylor
+// series of the scaled real symmetric block plus repeated squaring.  Real and imaginary
+// parts of U are polynomials in H, hence symmetric and commuting, so every product is a
+// real symmetric one (B^2(B+1)/2 FMA) and no division or square root is needed.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * s.n) return;
+  int i = int(rest % s.n);
+  int k = blist[rest / s.n];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  constexpr int NP = B * (B + 1) / 2;
+  double h[B][B];
+  build_h<B>(s, c, i, bp, h);
+  const double tp = s.tau * kPi2;
+  double nrm = 0;
+#pragma unroll
+  for (int p = 0; p < B; ++p) {
+    double rs = 0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) rs += fabs(h[p][q]);
+    nrm = fmax(nrm, rs);
+  }
+  nrm *= tp;
+  int sq = 0;
+  if (nrm > 0.5) {
+    frexp(nrm / 0.5, &sq);  // nrm / 0.5 < 2^sq
+    sq = min(sq, 60);
+  }
+  const double sc = ldexp(tp, -sq);
+  double X[NP], P[NP], Q[NP], R[NP], I[NP];
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      X[sx<B>(p, q)] = sc * h[p][q];
+      P[sx<B>(p, q)] = X[sx<B>(p, q)];
+      R[sx<B>(p, q)] = (p == q) ? 1.0 : 0.0;
+      I[sx<B>(p, q)] = -P[sx<B>(p, q)];  // k = 1 term: -i X
+    }
+  // terms k = 2..: P_k = P_{k-1} X / k; (-i)^k cycles -1, +i, +1, -i
+#pragma unroll
+  for (int kt = 2; kt <= kTaylorTerms; ++kt) {
+    sym_mul<B>(P, X, Q, 1.0 / kt);
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+      P[j] = Q[j];
+      if ((kt & 3) == 2) R[j] -= Q[j];
+      else if ((kt & 3) == 3) I[j] += Q[j];
+      else if ((kt & 3) == 0) R[j] += Q[j];
+      else I[j] -= Q[j];
+    }
+  }
+  // (R + iI)^2 = (R R - I I) + i 2 R I
+  for (int t = 0; t < sq; ++t) {
+    sym_mul<B>(R, R, P, 1.0);
+    sym_mul<B>(I, I, Q, 1.0);
+    sym_mul<B>(R, I, X, 2.0);
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+      R[j] = P[j] - Q[j];
+      I[j] = X[j];
+    }
+  }
+  double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      double2 u = cmk(R[sx<B>(p, q)], I[sx<B>(p, q)]);
       Ub[at(bp + p * B + q, c, s.Cpad)] = u;
       if (q != p) Ub[at(bp + q * B + p, c, s.Cpad)] = u;
     }
@@ -581,37 +688,66 @@ __global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
       s.Z[at(j * s.ne + e, c, s.Cpad)] = zj;
     }
   }
-  const int p0 = tile * kFavePT;
-  double2 s1[kFavePT], s2[kFavePT];
-#pragma unroll
-  for (int t = 0; t < kFavePT; ++t) s1[t] = s2[t] = cmk(0, 0);
+  // Three phases over i for the tile p0..p0+PT-1: all j = i+p < n (no wrap), the mixed
+  // band of at most PT-1 steps, and all wrapped.  Only the band tests j < n per p, so
+  // the bulk issues exactly one complex FMA per (i, p).  q_{(i+p) mod n} for the tile
+  // sits in a register window that shifts by one element per step.
+  const int n = s.n, p0 = tile * kFavePT;
   const size_t qstride = size_t(s.nq) * s.Cpad, rstride = size_t(s.nr) * s.Cpad;
-  for (int i = 0; i < s.n; ++i) {
-    double2 q = s.Q[i * qstride + at(eq, c, s.Cpad)];
-    double2 rho;
-    if (s.rosym) {
-      rho = cconj(q);
-      if (erev >= 0) rho = cadd(rho, s.Q[i * qstride + at(erev, c, s.Cpad)]);
-    } else {
-      rho = s.R[i * rstride + at(er, c, s.Cpad)];
+  const double2 *qb = s.Q + at(eq, c, s.Cpad);
+  const double2 *qr = s.Q + at(erev >= 0 ? erev : 0, c, s.Cpad);
+  const double2 *rb = s.R + at(er >= 0 ? er : 0, c, s.Cpad);
+  const bool rosym = s.rosym != 0, has_rev = erev >= 0;
+  double2 s1[kFavePT], s2[kFavePT], win[kFavePT];
+#pragma unroll
+  for (int t = 0; t < kFavePT; ++t) {
+    s1[t] = s2[t] = cmk(0, 0);
+    win[t] = qb[size_t((p0 + t) % n) * qstride];
+  }
+  int jl = (p0 + kFavePT) % n;  // next window element to load
+  auto rho_at = [&](int i) -> double2 {
+    if (rosym) {
+      double2 r = cconj(qb[size_t(i) * qstride]);
+      if (has_rev) r = cadd(r, qr[size_t(i) * qstride]);
+      return r;
     }
+    return rb[size_t(i) * rstride];
+  };
+  auto shift = [&]() {
+#pragma unroll
+    for (int t = 0; t < kFavePT - 1; ++t) win[t] = win[t + 1];
+    win[kFavePT - 1] = qb[size_t(jl) * qstride];
+    jl = (jl + 1 == n) ? 0 : jl + 1;
+  };
+  int iA = n - p0 - (kFavePT - 1);
+  if (iA < 0) iA = 0;
+  const int iC = n - p0;
+  int i = 0;
+  for (; i < iA; ++i) {
+    double2 rho = rho_at(i);
+#pragma unroll
+    for (int t = 0; t < kFavePT; ++t) s1[t] = cfma(win[t], rho, s1[t]);
+    shift();
+  }
+  for (; i < iC; ++i) {
+    double2 rho = rho_at(i);
 #pragma unroll
     for (int t = 0; t < kFavePT; ++t) {
-      int p = p0 + t;
-      if (p < s.n) {
-        int j = i + p;
-        if (j < s.n) {
-          s1[t] = cfma(s.Q[j * qstride + at(eq, c, s.Cpad)], rho, s1[t]);
-        } else {
-          s2[t] = cfma(s.Q[(j - s.n) * qstride + at(eq, c, s.Cpad)], rho, s2[t]);
-        }
-      }
+      if (i + p0 + t < n) s1[t] = cfma(win[t], rho, s1[t]);
+      else s2[t] = cfma(win[t], rho, s2[t]);
     }
+    shift();
+  }
+  for (; i < n; ++i) {
+    double2 rho = rho_at(i);
+#pragma unroll
+    for (int t = 0; t < kFavePT; ++t) s2[t] = cfma(win[t], rho, s2[t]);
+    shift();
   }
 #pragma unroll
   for (int t = 0; t < kFavePT; ++t) {
     int p = p0 + t;
-    if (p < s.n) s.G[at(p * s.ne + e, c, s.Cpad)] = cfma(z, s2[t], s1[t]);
+    if (p < n) s.G[at(p * s.ne + e, c, s.Cpad)] = cfma(z, s2[t], s1[t]);
   }
 }
 
@@ -763,6 +899,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.P = p;
   CUDA_OK(cudaSetDevice(ctx.device));
   if (p.precision != 0) throw Error(5, "only the FP64 precision mode is implemented");
+  if (p.step_method != 0 && p.step_method != 1) throw Error(1, "step_method must be 0 (eigh) or 1 (Taylor)");
   if (p.npts <= 0) throw Error(1, "npts must be positive");
   if (p.wr == 0.0 || p.rotb_deg == 0.0)
     throw Error(5, "static (non-spinning) powder FIDs are not implemented by the GPU engine");
@@ -960,7 +1097,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   // static part of the device description
   DevSys &s = J.base;
   s.n = J.n, s.npts = p.npts, s.N = N, s.nb = nb, s.S2 = L.S2, s.nint = J.nint, s.nq = J.nq, s.nr = J.nr;
-  s.ne = J.ne, s.J = J.J, s.rosym = J.rosym;
+  s.ne = J.ne, s.J = J.J, s.rosym = J.rosym, s.step_method = p.step_method;
   s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
   s.scale = double(1. / double(J.n / (J.rosym ? 2 : 1)));
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
@@ -987,7 +1124,10 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
   cudaStream_t st = J.ctx->stream;
   long Cp = s.Cpad;
   switch (stage) {
-    case 0: k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl); break;
+    case 0:
+      if (s.step_method == 1) k_step_taylor<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      else k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      break;
     case 1: k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl); break;
     case 2: k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl); break;
     case 3: k_eigframe<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl); break;

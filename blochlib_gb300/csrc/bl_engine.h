@@ -15,6 +15,7 @@ struct FidParams {
   int npts = 0;
   double sw = 0, wr = 0, rotb_deg = 0, start_t = 0;
   int precision = 0;  // 0 = FP64 (the only mode implemented by this engine)
+  int step_method = 0;  // step exponential: 0 Jacobi eigen-decomposition, 1 Taylor + squaring
 };
 
 struct Context {

@@ -53,6 +53,8 @@ typedef struct {
   double rotb_deg; /* rotor angle, degrees */
   double start_t;  /* start time, s */
   int precision;   /* 0 = FP64 */
+  int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
+                      1 = Taylor series with scaling and squaring; both FP64 */
 } bl_fid_params;
 
 /* Message of the calling thread's last failed call ("" if none). */

@@ -13,10 +13,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-10
 
 
+@pytest.mark.parametrize("method", ["eigh", "taylor"])
 @pytest.mark.parametrize("case", golden_cases())
-def test_gpu_matches_reference_golden(case):
+def test_gpu_matches_reference_golden(case, method):
     job, rows, fid64, fid32, sw = load_golden(case)
-    fid, sw_g = gpu_fid(job, rows, return_sw=True)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
     assert sw_g == sw
     assert rel(fid, fid64) <= TOL, rel(fid, fid64)
 
@@ -59,21 +60,23 @@ def random_system(seed):
     return job, rows
 
 
+@pytest.mark.parametrize("method", ["eigh", "taylor"])
 @pytest.mark.parametrize("seed", range(12))
-def test_gpu_matches_oracle_random_systems(seed):
+def test_gpu_matches_oracle_random_systems(seed, method):
     job, rows = random_system(seed)
     ref, sw = oracle_fid(job, rows)
-    fid, sw_g = gpu_fid(job, rows, return_sw=True)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
     assert sw_g == sw
     assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
-def test_c0_full_powder_matches_oracle():
+@pytest.mark.parametrize("method", ["eigh", "taylor"])
+def test_c0_full_powder_matches_oracle(method):
     cfg = W.config(0)
     job = W.job_text(cfg)
     rows = np.stack(cfg["powder"], axis=1)
     ref, _ = oracle_fid(job, rows)
-    fid = gpu_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method=method)
     assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
