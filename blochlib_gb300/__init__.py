@@ -73,6 +73,7 @@ _SIGS = {
     "bl_job_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "bl_job_io_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "bl_probe_fp64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "bl_powder_fid_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 8),
 }
 
 STAGES = 8

@@ -257,6 +257,16 @@ bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
   return st;
 }
 
+bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                                const double *det, const bl_fid_params *params, double *fid_out, double *sw_out) {
+  if (!ctx || !sys || !pw || !ro || !det || !params || !fid_out) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    int N = sys->s.dim();
+    bl::powder_fid_noalloc(ctx->c, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out,
+                           sw_out);
+  });
+}
+
 bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt) {
   if (!fid || !path || npts <= 0) return fail(BL_ERR_INVALID, "bad arguments");
   return guarded([&] { bl::write_fid_text(path, reinterpret_cast<const bl::cplx *>(fid), npts, dt); });

@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <sstream>
 #include <stdexcept>
 
@@ -825,25 +826,46 @@ Context::~Context() {
 
 static size_t *g_upload_counter = nullptr;  // set while a Job uploads its inputs
 
+// Bump allocator over a caller-provided device region.  Only the allocation-free entry
+// point (powder_fid_noalloc, below) installs one, for the duration of its own call.
+struct ScratchArena {
+  char *base = nullptr;
+  size_t cap = 0, used = 0;
+};
+static thread_local ScratchArena *g_arena = nullptr;
+
 template <class T>
 struct DevBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool owned = true;  // false: carved from a ScratchArena, never freed here
   void alloc(size_t count) {
     n = count;
-    if (count) CUDA_OK(cudaMalloc(&p, count * sizeof(T)));
+    if (!count) return;
+    if (g_arena) {
+      size_t off = (g_arena->used + 255) & ~size_t(255);
+      size_t bytes = count * sizeof(T);
+      if (off + bytes > g_arena->cap)
+        throw Error(4, "job needs more than the " + std::to_string(g_arena->cap >> 20) +
+                           " MiB static device scratch of the allocation-free entry point");
+      p = reinterpret_cast<T *>(g_arena->base + off);
+      g_arena->used = off + bytes;
+      owned = false;
+      return;
+    }
+    CUDA_OK(cudaMalloc(&p, count * sizeof(T)));
   }
   DevBuf() {}
   DevBuf(const DevBuf &) = delete;
   DevBuf &operator=(const DevBuf &) = delete;
-  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr, o.n = 0; }
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), owned(o.owned) { o.p = nullptr, o.n = 0; }
   void upload(const std::vector<T> &v, cudaStream_t st) {
     alloc(v.size());
     if (!v.empty()) CUDA_OK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st));
     if (g_upload_counter) *g_upload_counter += v.size() * sizeof(T);
   }
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
   }
 };
 
@@ -1339,6 +1361,84 @@ std::string Job::describe() const {
     << ", \"r_pairs\": " << J.npr << ", \"elements\": " << J.ne << ", \"batch\": " << J.Cb
     << ", \"batches\": " << J.nbatch << ", \"flops\": " << J.flops << "}";
   return o.str();
+}
+
+// ------------------------------------------------------------------ allocation-free entry
+// Some callers may not allocate device memory at all: a host program that reserves the
+// GPU's memory for itself up front and forbids other allocators, or a timing-critical loop
+// in which cudaMalloc/cudaFree (which synchronise the device) are not allowed.  For them
+// powder_fid_noalloc runs the same pipeline with every device buffer (inputs, tables, work
+// buffers, warp partials, FID, status word) carved from one static device array of
+// kNoAllocScratch bytes; larger jobs are processed in crystallite batches that fit it, and
+// a job whose smallest batch does not fit is rejected with BL_ERR_NOMEM.  Every GPU that
+// loads this library holds the array until the process exits.  All calls share it and it
+// keeps the previous call's contents: each call zeroes what must start at zero (the status
+// word and the warp partials), and calls that overlap on the GPU race on it.
+namespace {
+constexpr size_t kNoAllocScratch = size_t(64) << 20;
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch];
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+void *g_noalloc_addr[kNoAllocMaxDevices] = {};
+}  // namespace
+
+size_t noalloc_scratch_bytes() { return kNoAllocScratch; }
+
+// Device address of the static array on the current device, looked up once per device
+// (host code may not use the symbol itself as a device pointer).  The first call on a
+// device performs this lookup, so it should come before any stream capture.
+static char *noalloc_base(int device) {
+  if (device < 0 || device >= kNoAllocMaxDevices) throw Error(1, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[device]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) throw Error(3, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    g_noalloc_addr[device] = ptr;
+  }
+  return static_cast<char *>(g_noalloc_addr[device]);
+}
+
+void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+                        const FidParams &p, double *fid_out, double *sw_out) {
+  CUDA_OK(cudaSetDevice(ctx.device));
+  ScratchArena arena;
+  arena.base = noalloc_base(ctx.device);
+  arena.cap = kNoAllocScratch;
+  // Space outside the batch-sized work buffers: tables, per-crystallite inputs (11
+  // doubles each, padded by up to one batch), warp partials and the FID.
+  long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
+  long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
+  size_t ceff = size_t(pw.size()) * size_t(g) + 32;
+  size_t fixed = (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
+                 (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
+  if (fixed >= kNoAllocScratch)
+    throw Error(4, "job needs more than the " + std::to_string(kNoAllocScratch >> 20) +
+                       " MiB static device scratch of the allocation-free entry point");
+  Context view;  // same device and stream; budget = what the scratch leaves for work buffers
+  view.device = ctx.device;
+  view.stream = ctx.stream;
+  view.hbm_budget = kNoAllocScratch - fixed;
+  struct Release {
+    Context &c;
+    ~Release() { c.stream = nullptr; }  // the stream belongs to the caller's context
+  } release{view};
+  struct Scope {
+    ScratchArena *prev;
+    explicit Scope(ScratchArena *a) : prev(g_arena) { g_arena = a; }
+    ~Scope() { g_arena = prev; }
+  } scope(&arena);
+  try {
+    Job job(view, sys, pw, ro, det, p);
+    job.run();
+    job.read(fid_out);
+    if (sw_out) *sw_out = job.sw_out();
+  } catch (const Error &e) {
+    if (e.code == 4 && std::string(e.what()).find("static device scratch") == std::string::npos)
+      throw Error(4, std::string("job does not fit the ") + std::to_string(kNoAllocScratch >> 20) +
+                         " MiB static device scratch of the allocation-free entry point: " + e.what());
+    throw;
+  }
 }
 
 }  // namespace bl

@@ -63,4 +63,10 @@ class Job {
 // Measured FP64 FMA throughput of the device (TFLOP/s), from a short DFMA probe kernel.
 double probe_fp64_tflops(Context &ctx);
 
+// The powder FID with every device buffer taken from one static device array (no device
+// allocation or free during the call); see bl_powder_fid_noalloc.
+void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+                        const FidParams &p, double *fid_out, double *sw_out);
+size_t noalloc_scratch_bytes();
+
 }  // namespace bl

@@ -121,6 +121,24 @@ bl_status bl_job_io_bytes(const bl_job *job, size_t *h2d, size_t *d2h);
 /* Measured FP64 FMA throughput of the context's device (TFLOP/s), DFMA probe kernel. */
 bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops);
 
+/* Allocation-free powder FID.  No counterpart in the reference: BlochLib has no GPU and
+ * no device memory.  Same inputs, outputs and results as bl_powder_fid, for callers that
+ * must not allocate device memory during a call: a host program that claims the GPU's
+ * memory up front and forbids any other allocator, or a timing-critical loop where
+ * cudaMalloc/cudaFree are off limits because they synchronise the whole device.
+ * Every device buffer of the call comes from one static device array of
+ * BL_NOALLOC_SCRATCH_BYTES that each GPU loading this library keeps until the process
+ * exits; nothing is allocated or freed.  Larger powders are processed in crystallite
+ * batches that fit it; a job whose smallest batch (32 crystallites plus tables) does not
+ * fit returns BL_ERR_NOMEM.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share
+ * the array and it keeps the previous call's contents (each call clears what must start
+ * at zero); calls that overlap on the GPU, from any thread or context, race on it. */
+#define BL_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                                const double *det, const bl_fid_params *params, double *fid_out,
+                                double *sw_out);
+
 /* plotterFID-style text file: t, f, Re S, Im S, Re fid, Im fid, |S| (7 columns). */
 bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt);
 
