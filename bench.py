@@ -124,12 +124,13 @@ def workload(name):
     return W.config(idx)
 
 
-def make_job(bl, cfg, ctx, step_method=None):
+def make_job(bl, cfg, ctx, step_method=None, fave_method=None):
     s = bl.SolidSys(cfg["lines"])
     phi, theta, gamma, w = cfg["powder"]
     pw = bl.powder.from_arrays(theta, phi, gamma, w)
     ro, det = s.op(cfg["rho"]), s.op(cfg["det"])
-    job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=step_method)
+    job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=step_method,
+                 fave_method=fave_method)
     return s, pw, ro, det, job
 
 
@@ -224,6 +225,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fave-method", default=None, choices=["auto", "direct", "fft"])
     ap.add_argument("--step-method", default=None, choices=["eigh", "taylor"],
                     help="FP64 step exponential (default: BL_STEP_METHOD or eigh)")
     ap.add_argument("--crystallites", type=int, default=0,
@@ -238,7 +240,7 @@ def main():
     cfg = workload(args.config)
     if args.crystallites:
         cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
-    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method)
+    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method)
     for _ in range(args.warmup):
         job.run()
     job.sync()
@@ -271,7 +273,8 @@ def main():
             traffic = None
     launches_per_run = job.launches
     # e2e through the reference-facing call with host buffers
-    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method)
+    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method,
+                    fave_method=args.fave_method)
     drv.FID(pw, ro, det)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):

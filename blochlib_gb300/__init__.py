@@ -92,10 +92,22 @@ def _step_method(m):
     return int(m)
 
 
+FAVE_AUTO, FAVE_DIRECT, FAVE_FFT = 0, 1, 2
+
+
+def _fave_method(m):
+    """Fave correlation: 'auto' (0), 'direct' (1) or 'fft' (2); default BL_FAVE_METHOD or auto."""
+    if m is None:
+        m = os.environ.get("BL_FAVE_METHOD", "auto")
+    if isinstance(m, str):
+        m = {"auto": FAVE_AUTO, "direct": FAVE_DIRECT, "fft": FAVE_FFT}[m]
+    return int(m)
+
+
 class FidParams(ctypes.Structure):
     _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
                 ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
-                ("step_method", ctypes.c_int)]
+                ("step_method", ctypes.c_int), ("fave_method", ctypes.c_int)]
 
 
 def load():
@@ -277,12 +289,13 @@ class powder:
 class Job:
     """Resident job (bl_job): inputs on the device; run() recomputes the powder FID."""
 
-    def __init__(self, sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, ctx=None, step_method=None):
+    def __init__(self, sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, ctx=None, step_method=None,
+                 fave_method=None):
         self.ctx = ctx or default_context()
         n = sys.dim()
         self._ro, self._det = _cmat(ro, n), _cmat(det, n)
         self.params = FidParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
-                                _step_method(step_method))
+                                _step_method(step_method), _fave_method(fave_method))
         h = ctypes.c_void_p()
         _check(load().bl_job_create(self.ctx._h, sys._h, pw._h, _ptr(self._ro), _ptr(self._det),
                                     ctypes.byref(self.params), ctypes.byref(h)))
@@ -363,10 +376,12 @@ class Job:
 class oneFID:
     """oneFID<SolidSys>(sys, npts, sw, wr, rotb_deg, startT)  (oneFID.h:103-108)."""
 
-    def __init__(self, sys, npts, sw=20000.0, wr=0.0, rotb=0.0, startT=0.0, precision=0, ctx=None, step_method=None):
+    def __init__(self, sys, npts, sw=20000.0, wr=0.0, rotb=0.0, startT=0.0, precision=0, ctx=None, step_method=None,
+                 fave_method=None):
         self.sys, self.npts, self.sw, self.wr, self.rotb, self.startT = sys, int(npts), float(sw), float(wr), float(rotb), float(startT)
         self.precision = precision
         self.step_method = step_method
+        self.fave_method = fave_method
         self.ctx = ctx
         self.fid_ = np.zeros(self.npts, dtype=np.complex128)
 
@@ -378,7 +393,7 @@ class oneFID:
         out = np.zeros(self.npts, dtype=np.complex128)
         sw_out = np.zeros(1)
         params = FidParams(self.npts, self.sw, self.wr, self.rotb, self.startT, int(self.precision),
-                           _step_method(self.step_method))
+                           _step_method(self.step_method), _fave_method(self.fave_method))
         _check(load().bl_powder_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
                                     _ptr(out), _ptr(sw_out)))
         self.sw = float(sw_out[0])

@@ -56,6 +56,7 @@ bl::FidParams to_params(const bl_fid_params *p) {
   f.npts = p->npts, f.sw = p->sw, f.wr = p->wr, f.rotb_deg = p->rotb_deg, f.start_t = p->start_t;
   f.precision = p->precision;
   f.step_method = p->step_method;
+  f.fave_method = p->fave_method;
   return f;
 }
 }  // namespace

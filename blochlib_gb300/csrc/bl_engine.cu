@@ -85,6 +85,8 @@ __device__ __forceinline__ double chop1(double v, double eps) { return fabs(v) <
 // ------------------------------------------------------------------ job description
 struct DevSys {
   int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
+  int M, logM, fave_method;  // FFT length (pow2 >= 2n) for the Fave correlation; 0 direct, 1 FFT
+  const double2 *tw;         // exp(-2 pi i k / M), k < M/2
   double tau, wr, sin_rotb, cos_rotb, scale;
   // per block
   const int *bs, *boff, *bpoff;
@@ -752,6 +754,116 @@ __global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
   }
 }
 
+// In-place radix-2 decimation-in-time FFT (negative exponent) of CG interleaved sequences
+// of length M = 2^logM held in shared memory as X[i * CG + cc], input in bit-reversed
+// order, output in natural order.  tw[k] = exp(-2 pi i k / M), k < M/2.  Y (optional) is
+// transformed alongside X.  Ends with a barrier.
+template <int CG>
+__device__ void fft_dit(double2 *X, double2 *Y, int M, int logM, const double2 *__restrict__ tw) {
+  const int nb = (M / 2) * CG;
+  for (int st = 0; st < logM; ++st) {
+    const int h = 1 << st, tstride = M >> (st + 1);
+    for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
+      const int cc = idx % CG, b = idx / CG;
+      const int pos = b & (h - 1), grp = b >> st;
+      const int i0 = ((grp << (st + 1)) + pos) * CG + cc, i1 = i0 + h * CG;
+      if (st == 0) {
+        double2 a = X[i0], d = X[i1];
+        X[i0] = cadd(a, d), X[i1] = csub(a, d);
+        if (Y) {
+          a = Y[i0], d = Y[i1];
+          Y[i0] = cadd(a, d), Y[i1] = csub(a, d);
+        }
+      } else {
+        const double2 w = tw[pos * tstride];
+        double2 a = X[i0], t = cmul(w, X[i1]);
+        X[i0] = cadd(a, t), X[i1] = csub(a, t);
+        if (Y) {
+          a = Y[i0], t = cmul(w, Y[i1]);
+          Y[i0] = cadd(a, t), Y[i1] = csub(a, t);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Fave by FFT.  One CTA per (element e, group of CG crystallites).  With q zero outside
+// [0, n), Lin_d = sum_i q_{i+d} r_i for |d| < n is the linear cross-correlation, obtained
+// from zero-padded transforms of length M >= 2n:  Lin = IFFT(FFT(q) . conj(FFT(conj r))).
+// Then G_p = Lin_p + z Lin_{p-n} (the same G as k_fave).  When r = conj(q) (rho = (D+D^H)/2
+// and D has no block pair (b,a) for this element) the product is |FFT(q)|^2 and the second
+// forward transform is skipped.
+template <int CG>
+__global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
+  extern __shared__ double2 smem[];
+  const int M = s.M, logM = s.logM, n = s.n;
+  double2 *X = smem, *Y = smem + size_t(M) * CG;
+  __shared__ double2 zc[CG];
+  const int groups = s.Cpad / CG;
+  const int e = blockIdx.x / groups;
+  const int c0 = (blockIdx.x % groups) * CG;
+  const int eq = s.eq[e], erev = s.erev[e], er = s.er[e];
+  const bool autoc = s.rosym && erev < 0;
+  const size_t qstride = size_t(s.nq) * s.Cpad, rstride = size_t(s.nr) * s.Cpad;
+  const double nt = double(n) * s.tau;
+  // per crystallite of the group: w_rs = chop((l_r - l_s)/(i n tau), 1e-10), z = e^{i n tau w},
+  // and the powers z^j of the FID reconstruction
+  for (int idx = threadIdx.x; idx < CG * (s.J + 1); idx += blockDim.x) {
+    const int cc = idx % CG, j = idx / CG, c = c0 + cc;
+    if (c >= s.C) continue;
+    double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
+    double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+    if (j == s.J) zc[cc] = cexp(cmk(-nt * w.y, nt * w.x));
+    else s.Z[at(j * s.ne + e, c, s.Cpad)] = cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x));
+  }
+  // load q (and conj r) zero-padded, bit-reversed
+  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+    const int cc = idx % CG, i = idx / CG, c = c0 + cc;
+    const int ri = int(__brev(unsigned(i)) >> (32 - logM));
+    double2 q = cmk(0, 0), y = cmk(0, 0);
+    if (i < n && c < s.C) {
+      q = s.Q[i * qstride + at(eq, c, s.Cpad)];
+      if (!autoc) {
+        double2 r;
+        if (s.rosym) r = cadd(cconj(q), s.Q[i * qstride + at(erev, c, s.Cpad)]);
+        else r = s.R[i * rstride + at(er, c, s.Cpad)];
+        y = cconj(r);
+      }
+    }
+    X[ri * CG + cc] = q;
+    if (!autoc) Y[ri * CG + cc] = y;
+  }
+  __syncthreads();
+  fft_dit<CG>(X, autoc ? nullptr : Y, M, logM, s.tw);
+  // conj of the cross spectrum, in place in X (same index read and written)
+  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+    double2 x = X[idx];
+    if (autoc) X[idx] = cmk(x.x * x.x + x.y * x.y, 0.0);
+    else X[idx] = cconj(cmul(x, cconj(Y[idx])));
+  }
+  __syncthreads();
+  // bit-reverse into Y, forward transform: conj(result)/M is the inverse transform
+  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+    const int cc = idx % CG, f = idx / CG;
+    Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
+  }
+  __syncthreads();
+  fft_dit<CG>(Y, nullptr, M, logM, s.tw);
+  const double invM = 1.0 / double(M);
+  for (int idx = threadIdx.x; idx < n * CG; idx += blockDim.x) {
+    const int cc = idx % CG, p = idx / CG, c = c0 + cc;
+    if (c >= s.C) continue;
+    double2 lp = cscale(cconj(Y[p * CG + cc]), invM);
+    double2 g = lp;
+    if (p > 0) {
+      double2 lm = cscale(cconj(Y[(M + p - n) * CG + cc]), invM);
+      g = cfma(zc[cc], lm, lp);
+    }
+    s.G[at(p * s.ne + e, c, s.Cpad)] = g;
+  }
+}
+
 constexpr int kFidJT = 4, kFidPT = 4;
 
 // One thread per (crystallite, tile of kFidJT j's, tile of kFidPT p's); lanes are
@@ -882,7 +994,7 @@ struct JobImpl {
   std::vector<DevBuf<int>> blist;
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
   DevBuf<double2> Dblk, Rhoblk;
-  DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid;
+  DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<double> Rp_b, t0_b, w_b;
   std::vector<double> h_Rp, h_t0, h_w;  // all virtual crystallites (C * gammaloop)
   int Ceff = 0;
@@ -922,6 +1034,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   CUDA_OK(cudaSetDevice(ctx.device));
   if (p.precision != 0) throw Error(5, "only the FP64 precision mode is implemented");
   if (p.step_method != 0 && p.step_method != 1) throw Error(1, "step_method must be 0 (eigh) or 1 (Taylor)");
+  if (p.fave_method < 0 || p.fave_method > 2) throw Error(1, "fave_method must be 0 (auto), 1 (direct) or 2 (FFT)");
   if (p.npts <= 0) throw Error(1, "npts must be positive");
   if (p.wr == 0.0 || p.rotb_deg == 0.0)
     throw Error(5, "static (non-spinning) powder FIDs are not implemented by the GPU engine");
@@ -1111,7 +1224,20 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.stage_fl[2] = Ce * 100.0 * S3;                              // Floquet eig
   J.stage_fl[3] = Ce * J.n * 8.0 * S3;                          // W = A V_F
   J.stage_fl[4] = Ce * J.n * 8.0 * pairs;                       // Q, R transforms
-  J.stage_fl[5] = Ce * 8.0 * J.n * J.n * J.ne;                  // Fave correlation
+  {
+    // Fave correlation: direct 8 n^2 per element; FFT: 5 M log2 M per length-M transform
+    // (two when r = conj(q), three otherwise), 8 M for the spectrum product, 8 n for G
+    int lm = 1;
+    while ((1 << lm) < 2 * J.n) ++lm;
+    double M = double(1 << lm), fftf = 5.0 * M * lm;
+    bool fft = p.fave_method != 1 && M <= 4096;
+    double per = 0;
+    for (int e = 0; e < J.ne; ++e) {
+      bool autoc = J.rosym && erev[e] < 0;
+      per += fft ? (autoc ? 2 : 3) * fftf + 8.0 * M + 8.0 * J.n : 8.0 * J.n * J.n;
+    }
+    J.stage_fl[5] = Ce * per;
+  }
   J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
   J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total;                // compensated powder sum
   J.flops = 0;
@@ -1120,6 +1246,28 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   DevSys &s = J.base;
   s.n = J.n, s.npts = p.npts, s.N = N, s.nb = nb, s.S2 = L.S2, s.nint = J.nint, s.nq = J.nq, s.nr = J.nr;
   s.ne = J.ne, s.J = J.J, s.rosym = J.rosym, s.step_method = p.step_method;
+  s.logM = 1;
+  while ((1 << s.logM) < 2 * J.n) ++s.logM;
+  s.M = 1 << s.logM;
+  // FFT correlation up to M = 4096 (its shared-memory tile is M * max(1, 2048/M) * 32 B)
+  if (p.fave_method == 2 && s.M > 4096) throw Error(5, "FFT Fave supports at most 2048 steps per period");
+  s.fave_method = (p.fave_method != 1 && s.M <= 4096) ? 1 : 0;
+  {
+    std::vector<double2> tw(s.M / 2);
+    for (int k = 0; k < s.M / 2; ++k) {
+      double a = kPi2 * double(k) / double(s.M);
+      tw[k] = make_double2(std::cos(a), -std::sin(a));
+    }
+    g_upload_counter = &J.h2d;
+    J.tw.upload(tw, st);
+    g_upload_counter = nullptr;
+    s.tw = J.tw.p;
+    size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * std::max(1, std::min(8, 2048 / s.M));
+    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+  }
   s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
   s.scale = double(1. / double(J.n / (J.rosym ? 2 : 1)));
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
@@ -1207,8 +1355,20 @@ void Job::run() {
     mark_end(J, 4, J.npq + J.npr > 0 ? 1 : 0);
     mark_begin(J, 5);
     if (J.ne > 0) {
-      int ntile = (J.n + kFavePT - 1) / kFavePT;
-      k_fave<<<grid_for(Cp * J.ne * ntile), kThreads, 0, st>>>(s);
+      if (s.fave_method == 1) {
+        int cg = std::max(1, std::min(8, 2048 / s.M));
+        size_t shm = sizeof(double2) * size_t(s.M) * cg * 2;
+        unsigned grid = unsigned(J.ne) * unsigned(Cp / cg);
+        switch (cg) {
+          case 8: k_fave_fft<8><<<grid, 128, shm, st>>>(s); break;
+          case 4: k_fave_fft<4><<<grid, 128, shm, st>>>(s); break;
+          case 2: k_fave_fft<2><<<grid, 128, shm, st>>>(s); break;
+          default: k_fave_fft<1><<<grid, 128, shm, st>>>(s); break;
+        }
+      } else {
+        int ntile = (J.n + kFavePT - 1) / kFavePT;
+        k_fave<<<grid_for(Cp * J.ne * ntile), kThreads, 0, st>>>(s);
+      }
       ++J.launches;
     }
     mark_end(J, 5, J.ne > 0 ? 1 : 0);

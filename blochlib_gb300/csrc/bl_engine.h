@@ -16,6 +16,7 @@ struct FidParams {
   double sw = 0, wr = 0, rotb_deg = 0, start_t = 0;
   int precision = 0;  // 0 = FP64 (the only mode implemented by this engine)
   int step_method = 0;  // step exponential: 0 Jacobi eigen-decomposition, 1 Taylor + squaring
+  int fave_method = 0;  // Fave correlation: 0 auto (FFT when n <= 2048), 1 direct, 2 FFT
 };
 
 struct Context {

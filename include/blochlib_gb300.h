@@ -55,6 +55,8 @@ typedef struct {
   int precision;   /* 0 = FP64 */
   int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
                       1 = Taylor series with scaling and squaring; both FP64 */
+  int fave_method; /* correlation over the rotor period: 0 = automatic (FFT for n <= 2048),
+                      1 = direct O(n^2) sum, 2 = zero-padded FFT; both FP64 */
 } bl_fid_params;
 
 /* Message of the calling thread's last failed call ("" if none). */

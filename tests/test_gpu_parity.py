@@ -13,11 +13,11 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-10
 
 
-@pytest.mark.parametrize("method", ["eigh", "taylor"])
+@pytest.mark.parametrize("method,fave", [("eigh", "fft"), ("taylor", "fft"), ("eigh", "direct")])
 @pytest.mark.parametrize("case", golden_cases())
-def test_gpu_matches_reference_golden(case, method):
+def test_gpu_matches_reference_golden(case, method, fave):
     job, rows, fid64, fid32, sw = load_golden(case)
-    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method, fave_method=fave)
     assert sw_g == sw
     assert rel(fid, fid64) <= TOL, rel(fid, fid64)
 
@@ -60,12 +60,12 @@ def random_system(seed):
     return job, rows
 
 
-@pytest.mark.parametrize("method", ["eigh", "taylor"])
+@pytest.mark.parametrize("method,fave", [("eigh", "fft"), ("taylor", "fft"), ("taylor", "direct")])
 @pytest.mark.parametrize("seed", range(12))
-def test_gpu_matches_oracle_random_systems(seed, method):
+def test_gpu_matches_oracle_random_systems(seed, method, fave):
     job, rows = random_system(seed)
     ref, sw = oracle_fid(job, rows)
-    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method, fave_method=fave)
     assert sw_g == sw
     assert rel(fid, ref) <= TOL, rel(fid, ref)
 
