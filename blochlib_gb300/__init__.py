@@ -74,6 +74,8 @@ _SIGS = {
     "bl_job_io_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "bl_probe_fp64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "bl_powder_fid_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 8),
+    "bl_rotation3": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "bl_rotation2": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
 }
 
 STAGES = 8
@@ -399,6 +401,16 @@ class oneFID:
         self.sw = float(sw_out[0])
         self.fid_ = out
         return out
+
+
+def rotationMatrix3D(a, b, g=None):
+    """Cartesian rotation of the reference: (alpha, beta, gamma) or the rotor's (phi, theta)."""
+    R = np.zeros(9)
+    if g is None:
+        _check(load().bl_rotation2(float(a), float(b), _ptr(R)))
+    else:
+        _check(load().bl_rotation3(float(a), float(b), float(g), _ptr(R)))
+    return R.reshape(3, 3)
 
 
 def plotterFID(fid, datasave="fid", dt=1.0):

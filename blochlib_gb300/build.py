@@ -76,6 +76,24 @@ def build_library(verbose=False, force=False):
     return LIB
 
 
+EXAMPLES = PKG / "examples"
+
+
+def build_examples(force=False):
+    """C++ programs written against include/blochlib_gb300.hpp (linked to the library)."""
+    out = EXAMPLES / "_build"
+    out.mkdir(exist_ok=True)
+    built = []
+    for src in sorted(EXAMPLES.glob("*.cc")):
+        exe = out / src.stem
+        deps = [src, ROOT / "include" / "blochlib_gb300.hpp", ROOT / "include" / "blochlib_gb300.h", LIB]
+        if force or _stale(exe, deps):
+            _run(["g++", "-O2", "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{PKG}",
+                  "-lblochlib_gb300", f"-Wl,-rpath,{PKG}"])
+        built.append(exe)
+    return built
+
+
 def build_oracle(force=False):
     """Oracle (test infrastructure): shared library for ctypes and the CLI binary."""
     ORACLE_BUILD.mkdir(parents=True, exist_ok=True)
@@ -104,3 +122,4 @@ if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_library(verbose="-v" in sys.argv, force=force))
     print(build_oracle(force=force))
+    print(build_examples(force=force))

@@ -274,3 +274,23 @@ bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double d
 }
 
 }  // extern "C"
+
+extern "C" {
+
+bl_status bl_rotation3(double alpha, double beta, double gamma, double *R9) {
+  if (!R9) return fail(BL_ERR_INVALID, "null output");
+  double R[3][3];
+  bl::rotation3(alpha, beta, gamma, R);
+  for (int i = 0; i < 9; ++i) R9[i] = R[i / 3][i % 3];
+  return BL_OK;
+}
+
+bl_status bl_rotation2(double phi, double theta, double *R9) {
+  if (!R9) return fail(BL_ERR_INVALID, "null output");
+  double R[3][3];
+  bl::rotation2(phi, theta, R);
+  for (int i = 0; i < 9; ++i) R9[i] = R[i / 3][i % 3];
+  return BL_OK;
+}
+
+}  // extern "C"

@@ -323,6 +323,14 @@ __device__ int unitary_eig(const double2 (&U)[B][B], double2 (&lam)[B], double2 
       lam[r] = s;
     }
     if (pass == 0) {
+      // well conditioned already (every |1 + e^{ia} lambda| >= 1/4): keep this pass
+      double mind = 4.0;
+#pragma unroll
+      for (int r = 0; r < B; ++r) {
+        double2 w = cmul(ea, lam[r]);
+        mind = fmin(mind, (1.0 + w.x) * (1.0 + w.x) + w.y * w.y);
+      }
+      if (mind >= 0.0625) break;
       double th[B];
 #pragma unroll
       for (int r = 0; r < B; ++r) th[r] = atan2(lam[r].y, lam[r].x);
@@ -381,7 +389,10 @@ __device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, d
 #pragma unroll
     for (int p = 0; p < B; ++p)
 #pragma unroll
-      for (int q = 0; q < B; ++q) h[p][q] = fma(f, T[p * B + q], h[p][q]);
+      for (int q = 0; q < B; ++q) {
+        const double t = T[p * B + q];  // same for every lane: the skip is warp-uniform
+        if (t != 0.0) h[p][q] = fma(f, t, h[p][q]);
+      }
   }
 }
 

@@ -21,6 +21,7 @@
  *                         keep inputs resident on the GPU between calls (no reference twin;
  *                         oneFID::FID recomputes from host data every call)
  *   bl_plotter_fid        plotterFID(fid, file, dt)                  src/utils/plotter.cc:49-135
+ *   bl_rotation3/2        rotationMatrix3D(a,b,g) / (phi,theta)      src/QMspins/space_ten.cc:578-652
  */
 #ifndef BLOCHLIB_GB300_H
 #define BLOCHLIB_GB300_H
@@ -140,6 +141,11 @@ bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops);
 bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
                                 const double *det, const bl_fid_params *params, double *fid_out,
                                 double *sw_out);
+
+/* Cartesian rotation matrices of the reference, row-major 3x3 (radians):
+ * 3-angle (powder orientation) and 2-angle (rotor phase phi, rotor tilt theta). */
+bl_status bl_rotation3(double alpha, double beta, double gamma, double *R9);
+bl_status bl_rotation2(double phi, double theta, double *R9);
 
 /* plotterFID-style text file: t, f, Re S, Im S, Re fid, Im fid, |S| (7 columns). */
 bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt);

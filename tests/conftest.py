@@ -17,5 +17,6 @@ def _built():
     """Build (if stale) the CUDA library and the CPU oracle before any test."""
     from blochlib_gb300 import build
     build.build_library()
+    build.build_examples()
     build.build_oracle()
     yield

@@ -119,3 +119,23 @@ def test_bad_zcw_and_operator_return_invalid():
     with pytest.raises(bl.BlochError) as e:
         s.op("Foo")
     assert e.value.status == 1
+
+
+def test_rotation_matrices_match_reference_formulas():
+    a, b, g = 0.3, 1.1, 2.0
+    ca, sa, cb, sb, cg, sg = np.cos(a), np.sin(a), np.cos(b), np.sin(b), np.cos(g), np.sin(g)
+    R3 = np.array([[ca * cb * cg - sa * sg, sa * cb * cg + ca * sg, -sb * cg],
+                   [-ca * cb * sg - sa * cg, -sa * cb * sg + ca * cg, sb * sg],
+                   [ca * sb, sa * sb, cb]])
+    np.testing.assert_allclose(bl.rotationMatrix3D(a, b, g), R3, atol=1e-15)
+    R2 = np.array([[np.cos(a), np.sin(a), 0], [-np.cos(b) * np.sin(a), np.cos(a) * np.cos(b), np.sin(b)],
+                   [np.sin(a) * np.sin(b), -np.cos(a) * np.sin(b), np.cos(b)]])
+    np.testing.assert_allclose(bl.rotationMatrix3D(a, b), R2, atol=1e-15)
+    for R in (bl.rotationMatrix3D(a, b, g), bl.rotationMatrix3D(a, b)):
+        np.testing.assert_allclose(R @ R.T, np.eye(3), atol=1e-14)
+
+
+def test_cpp_host_api_example_builds():
+    from blochlib_gb300 import build
+    exes = build.build_examples()
+    assert exes and all(e.exists() for e in exes)
