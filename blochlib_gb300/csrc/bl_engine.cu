@@ -86,6 +86,9 @@ __device__ __forceinline__ double chop1(double v, double eps) { return fabs(v) <
 struct DevSys {
   int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
   int M, logM, fave_method;  // FFT length (pow2 >= 2n) for the Fave correlation; 0 direct, 1 FFT
+  int is_static;             // static powder FID (oneFID.h:292-336): dt = 1/sw, n = p-period
+  double dt;
+  const int *srp, *seo;      // per D pair (a,b): the rho pair (b,a) and first element, or -1
   const double2 *tw;         // exp(-2 pi i k / M), k < M/2
   double tau, wr, sin_rotb, cos_rotb, scale;
   // per block
@@ -364,12 +367,8 @@ __device__ __forceinline__ size_t at(int item, int c, int Cpad) { return size_t(
 // H_i block at the midpoint of step i (sys.cc:749-770): rotor phase 2 pi wr t_mid,
 // a = (M PAS M^T)_22 with M = R_rotor R_powder, H = Hc + sum_k scale_k a_k T_k.
 template <int B>
-__device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, double (&h)[B][B]) {
-  double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
-  double tmid = (t2 - t1) / 2.0 + t1;
-  double sp, cp;
-  sincos(tmid * s.wr * kPi2, &sp, &cp);
-  // row 2 of R_rotor(phi, beta) times R_powder
+__device__ __forceinline__ void build_h_at(const DevSys &s, int c, double sp, double cp, int bp, double (&h)[B][B]) {
+  // row 2 of R_rotor(phi, beta) times R_powder, phi the rotor phase (sin sp, cos cp)
   double rr0 = sp * s.sin_rotb, rr1 = -cp * s.sin_rotb, rr2 = s.cos_rotb;
   double r[3];
 #pragma unroll
@@ -394,6 +393,110 @@ __device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, d
         if (t != 0.0) h[p][q] = fma(f, t, h[p][q]);
       }
   }
+}
+
+template <int B>
+__device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, double (&h)[B][B]) {
+  double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
+  double tmid = (t2 - t1) / 2.0 + t1;
+  double sp, cp;
+  sincos(tmid * s.wr * kPi2, &sp, &cp);
+  build_h_at<B>(s, c, sp, cp, bp, h);
+}
+
+// Static powder FID, step 1 (oneFID.h:301-311): one thread per (crystallite, block): H at
+// rotor phase 0 (Hamiltonian(0, dt), wr = 0), Jacobi eigen-decomposition; V (real) goes to
+// VF, the eigenvalues to L.x.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_static_eig(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= nblist) return;
+  int k = blist[rest];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k], bo = s.boff[k];
+  double h[B][B], v[B][B];
+  build_h_at<B>(s, c, 0.0, 1.0, bp, h);
+  if (!jacobi_sym<B>(h, v)) atomicOr(s.status, kNoConvergeStep);
+#pragma unroll
+  for (int r = 0; r < B; ++r) {
+#pragma unroll
+    for (int q = 0; q < B; ++q) s.VF[at(bp + r * B + q, c, s.Cpad)] = cmk(v[r][q], 0.0);
+    s.L[at(bo + r, c, s.Cpad)] = cmk(h[r][r], 0.0);
+  }
+}
+
+// Static powder FID, step 2 (oneFID.h:312-334): one thread per (crystallite, block pair
+// (a,b) of D with rho_ba != 0).  Do = V_a^T D_ab V_b, sig0 = V_b^T rho_ba V_a,
+// A_ij = Do(i,j) sig0(j,i) (dropped when |A|^2 <= 1e-10, as the reference does),
+// B_ij = conj(e_i) e_j with e = exp(-2 pi i dt lambda).  fid[k] = sum A B^k is written for
+// the reconstruction kernel as G_p = A B^p (p < ns) and Z_j = (B^ns)^j.
+__global__ void __launch_bounds__(kThreads) k_static_elems(DevSys s) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= s.npq) return;
+  const int pq = int(rest);
+  if (c >= s.C || s.srp[pq] < 0) return;
+  const int a = s.qa[pq], b = s.qb[pq], rp = s.srp[pq], e0 = s.seo[pq];
+  const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
+  const double2 *D = s.Dblk + s.doff[pq], *Rh = s.Rhoblk + s.rhooff[rp];  // D_ab (ba x bb), rho_ba (bb x ba)
+  double2 X[kMaxBlock * kMaxBlock], Do[kMaxBlock * kMaxBlock];
+  // Do = V_a^T (D_ab V_b)
+  for (int l = 0; l < ba; ++l)
+    for (int q = 0; q < bb; ++q) {
+      double2 acc = cmk(0, 0);
+      for (int m = 0; m < bb; ++m) {
+        double2 d = D[l * bb + m];
+        if (d.x == 0.0 && d.y == 0.0) continue;
+        acc = cfma(d, cmk(s.VF[at(pb + m * bb + q, c, s.Cpad)].x, 0.0), acc);
+      }
+      X[l * bb + q] = acc;
+    }
+  for (int r = 0; r < ba; ++r)
+    for (int q = 0; q < bb; ++q) {
+      double2 acc = cmk(0, 0);
+      for (int l = 0; l < ba; ++l) acc = cfma(cmk(s.VF[at(pa + l * ba + r, c, s.Cpad)].x, 0.0), X[l * bb + q], acc);
+      Do[r * bb + q] = acc;
+    }
+  // sig0_ba = V_b^T (rho_ba V_a)   (bb x ba)
+  for (int m = 0; m < bb; ++m)
+    for (int r = 0; r < ba; ++r) {
+      double2 acc = cmk(0, 0);
+      for (int l = 0; l < ba; ++l) {
+        double2 d = Rh[m * ba + l];
+        if (d.x == 0.0 && d.y == 0.0) continue;
+        acc = cfma(d, cmk(s.VF[at(pa + l * ba + r, c, s.Cpad)].x, 0.0), acc);
+      }
+      X[m * ba + r] = acc;
+    }
+  const double z = s.dt * kPi2;
+  for (int i = 0; i < ba; ++i)
+    for (int j = 0; j < bb; ++j) {
+      double2 sg = cmk(0, 0);
+      for (int m = 0; m < bb; ++m) sg = cfma(cmk(s.VF[at(pb + m * bb + j, c, s.Cpad)].x, 0.0), X[m * ba + i], sg);
+      double2 A = cmul(Do[i * bb + j], sg);
+      if (A.x * A.x + A.y * A.y <= 1.0e-10) A = cmk(0, 0);
+      double si, ci, sj, cj;
+      sincos(z * s.L[at(s.boff[a] + i, c, s.Cpad)].x, &si, &ci);
+      sincos(z * s.L[at(s.boff[b] + j, c, s.Cpad)].x, &sj, &cj);
+      const double2 B = cmul(cmk(ci, si), cmk(cj, -sj));  // conj(e_i) e_j
+      const int e = e0 + i * bb + j;
+      double2 g = A;
+      for (int p = 0; p < s.n; ++p) {
+        s.G[at(p * s.ne + e, c, s.Cpad)] = g;
+        g = cmul(g, B);
+      }
+      // g = A B^ns now; Z_j = (B^ns)^j
+      double2 bn = cmk(1, 0);
+      for (int p = 0; p < s.n; ++p) bn = cmul(bn, B);
+      double2 zj = cmk(1, 0);
+      for (int j2 = 0; j2 < s.J; ++j2) {
+        s.Z[at(j2 * s.ne + e, c, s.Cpad)] = zj;
+        zj = cmul(zj, bn);
+      }
+    }
 }
 
 // One thread per (crystallite, block k, step i): U_i = V diag(chop(e^{-i 2pi tau L})) V^T
@@ -995,13 +1098,13 @@ struct DevBuf {
 struct JobImpl {
   Context *ctx;
   FidParams P;
-  int C = 0, n = 0, gammaloop = 1, J = 0, rosym = 0;
-  double tau = 0, sw_out = 0;
+  int C = 0, n = 0, gammaloop = 1, J = 0, rosym = 0, is_static = 0;
+  double tau = 0, sw_out = 0, dt = 0;
   BlockLayout L;
   int nint = 0, nq = 0, nr = 0, ne = 0, npq = 0, npr = 0;
   int Cb = 0, nbatch = 0, nwarps_total = 0;
   std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices
-  DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status;
+  DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status, srp, seo;
   std::vector<DevBuf<int>> blist;
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
   DevBuf<double2> Dblk, Rhoblk;
@@ -1047,21 +1150,33 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   if (p.step_method != 0 && p.step_method != 1) throw Error(1, "step_method must be 0 (eigh) or 1 (Taylor)");
   if (p.fave_method < 0 || p.fave_method > 2) throw Error(1, "fave_method must be 0 (auto), 1 (direct) or 2 (FFT)");
   if (p.npts <= 0) throw Error(1, "npts must be positive");
-  if (p.wr == 0.0 || p.rotb_deg == 0.0)
-    throw Error(5, "static (non-spinning) powder FIDs are not implemented by the GPU engine");
   if (pw.size() <= 0) throw Error(1, "empty powder");
   const int N = sys.dim();
   if (ro.n != N || det.n != N) throw Error(1, "rho/detect dimension does not match the spin system");
-  // compute::CalcComputeStep and the constructor (compute.h:86-97, 213-235)
-  J.n = int(std::floor(p.sw / p.wr + 0.5));
-  if (J.n < 1) throw Error(1, "sw/wr gives fewer than one step per rotor period");
-  int gamma_step = 10;
-  J.gammaloop = gamma_step >= J.n ? gamma_step / J.n : 1;
-  if (J.gammaloop < 1) J.gammaloop = 1;
-  J.sw_out = double(J.n * p.wr);
-  double tmin = p.start_t, tmax = p.start_t + 1.0 / p.wr;
-  J.tau = (tmax - tmin) / J.n;
-  if (!(J.tau > 0)) throw Error(1, "the propagator time step is not positive");
+  // oneFID::FID dispatch (oneFID.h:206): no spinning or rotor angle 0 -> static powder FID
+  J.is_static = (p.wr == 0.0 || p.rotb_deg == 0.0) ? 1 : 0;
+  double tmin = p.start_t;
+  if (J.is_static) {
+    // oneFID::singleStaticFID (oneFID.h:292-336): dt = 1/sw as given; the FID index k is
+    // split as k = j*ns + p for the reconstruction kernel
+    if (!(p.sw > 0)) throw Error(1, "sw must be positive");
+    J.n = std::min(64, p.npts);
+    J.gammaloop = 1;
+    J.sw_out = p.sw;
+    J.tau = 0.0;
+    J.dt = 1.0 / p.sw;
+  } else {
+    // compute::CalcComputeStep and the constructor (compute.h:86-97, 213-235)
+    J.n = int(std::floor(p.sw / p.wr + 0.5));
+    if (J.n < 1) throw Error(1, "sw/wr gives fewer than one step per rotor period");
+    int gamma_step = 10;
+    J.gammaloop = gamma_step >= J.n ? gamma_step / J.n : 1;
+    if (J.gammaloop < 1) J.gammaloop = 1;
+    J.sw_out = double(J.n * p.wr);
+    double tmax = p.start_t + 1.0 / p.wr;
+    J.tau = (tmax - tmin) / J.n;
+    if (!(J.tau > 0)) throw Error(1, "the propagator time step is not positive");
+  }
   J.L = sys.layout();
   const BlockLayout &L = J.L;
   if (L.max_block > kMaxBlock)
@@ -1076,6 +1191,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         J.rosym = 0;
         break;
       }
+  if (J.is_static) J.rosym = 0;  // the static FID always transforms rho itself
   // Hamiltonian terms, packed per block
   std::vector<double> pas, isc, Tk, Hc(L.S2, 0.0);
   auto pack = [&](const std::vector<double> &M, double *dst) {
@@ -1126,9 +1242,10 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.npq = int(qa.size());
   J.npr = int(ra.size());
   // elements (r,s): Q(r,s) structurally non-zero and R(s,r) structurally non-zero
-  std::vector<int> eq, erev, er, erg, esg;
+  std::vector<int> eq, erev, er, erg, esg, srp(J.npq, -1), seo(J.npq, -1);
   for (int pq = 0; pq < J.npq; ++pq) {
     int a = qa[pq], b = qb[pq];
+    if (!J.rosym && rpair[b][a] >= 0) srp[pq] = rpair[b][a], seo[pq] = int(eq.size());
     for (int r = 0; r < L.size[a]; ++r)
       for (int s = 0; s < L.size[b]; ++s) {
         int rv = -1, ri = -1;
@@ -1164,7 +1281,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.cos_rotb = std::cos(p.rotb_deg * d2r);
   J.sin_rotb = std::sin(p.rotb_deg * d2r);
   // batch size from the memory budget
-  size_t per_c = sizeof(double2) * (size_t(J.n) * L.S2 * 2 + L.S2 + N + size_t(J.n) * (J.nq + J.nr + J.ne) +
+  const size_t nsteps = J.is_static ? 0 : size_t(J.n);  // U, A, Q, R exist only when spinning
+  size_t per_c = sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + nsteps * (J.nq + J.nr) + size_t(J.n) * J.ne +
                                     size_t(J.J) * J.ne) +
                  sizeof(double) * 11;
   size_t budget = ctx.hbm_budget ? ctx.hbm_budget : (size_t(16) << 30);
@@ -1189,6 +1307,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.qa.upload(qa, st), J.qb.upload(qb, st), J.qoff.upload(qoff, st), J.doff.upload(doff, st);
   J.ra.upload(ra, st), J.rb.upload(rb, st), J.roff.upload(roff, st), J.rhooff.upload(rhooff, st);
   J.eq.upload(eq, st), J.erev.upload(erev, st), J.er.upload(er, st), J.erg.upload(erg, st), J.esg.upload(esg, st);
+  J.srp.upload(srp, st), J.seo.upload(seo, st);
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
@@ -1206,12 +1325,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.Rp_all.upload(Rp, st), J.t0_all.upload(t0, st), J.w_all.upload(w, st);
   }
   size_t Cb = J.Cb;
-  J.U.alloc(size_t(J.n) * L.S2 * Cb);
-  J.A.alloc(size_t(J.n) * L.S2 * Cb);
+  J.U.alloc(std::max<size_t>(1, nsteps * L.S2 * Cb));
+  J.A.alloc(std::max<size_t>(1, nsteps * L.S2 * Cb));
   J.VF.alloc(size_t(L.S2) * Cb);
   J.Lb.alloc(size_t(N) * Cb);
-  J.Q.alloc(std::max<size_t>(1, size_t(J.n) * J.nq * Cb));
-  J.R.alloc(std::max<size_t>(1, size_t(J.n) * J.nr * Cb));
+  J.Q.alloc(std::max<size_t>(1, nsteps * J.nq * Cb));
+  J.R.alloc(std::max<size_t>(1, nsteps * J.nr * Cb));
   J.G.alloc(std::max<size_t>(1, size_t(J.n) * J.ne * Cb));
   J.Z.alloc(std::max<size_t>(1, size_t(J.J) * J.ne * Cb));
   J.partial.alloc(size_t(J.nwarps_total) * p.npts);
@@ -1230,11 +1349,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   double S2H = 0;  // H build: one FMA per operator entry per interaction
   for (int k = 0; k < nb; ++k) S2H += double(L.size[k]) * L.size[k];
   double Ce = J.Ceff;
-  J.stage_fl[0] = Ce * J.n * (11.0 * S3 + 2.0 * J.nint * S2H);  // eigh 9b^3 + U 2b^3 + H build
-  J.stage_fl[1] = Ce * J.n * 8.0 * S3;                          // Dyson
-  J.stage_fl[2] = Ce * 100.0 * S3;                              // Floquet eig
-  J.stage_fl[3] = Ce * J.n * 8.0 * S3;                          // W = A V_F
-  J.stage_fl[4] = Ce * J.n * 8.0 * pairs;                       // Q, R transforms
+  J.stage_fl[0] = Ce * (J.is_static ? 1 : J.n) * (11.0 * S3 + 2.0 * J.nint * S2H);  // eigh + U + H build
+  const double spin_steps = J.is_static ? 0.0 : double(J.n);
+  J.stage_fl[1] = Ce * spin_steps * 8.0 * S3;                   // Dyson
+  J.stage_fl[2] = J.is_static ? 0.0 : Ce * 100.0 * S3;          // Floquet eig
+  J.stage_fl[3] = Ce * spin_steps * 8.0 * S3;                   // W = A V_F
+  J.stage_fl[4] = Ce * spin_steps * 8.0 * pairs;               // Q, R transforms
   {
     // Fave correlation: direct 8 n^2 per element; FFT: 5 M log2 M per length-M transform
     // (two when r = conj(q), three otherwise), 8 M for the spectrum product, 8 n for G
@@ -1247,7 +1367,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       bool autoc = J.rosym && erev[e] < 0;
       per += fft ? (autoc ? 2 : 3) * fftf + 8.0 * M + 8.0 * J.n : 8.0 * J.n * J.n;
     }
-    J.stage_fl[5] = Ce * per;
+    J.stage_fl[5] = J.is_static ? Ce * (16.0 * pairs + 8.0 * J.n * J.ne) : Ce * per;
   }
   J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
   J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total;                // compensated powder sum
@@ -1280,7 +1400,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     CUDA_OK(cudaFuncSetAttribute(k_fave_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
   }
   s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
-  s.scale = double(1. / double(J.n / (J.rosym ? 2 : 1)));
+  s.is_static = J.is_static, s.dt = J.dt, s.srp = J.srp.p, s.seo = J.seo.p;
+  s.scale = J.is_static ? 1.0 : double(1. / double(J.n / (J.rosym ? 2 : 1)));
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
   s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
   s.npq = J.npq, s.npr = J.npr;
@@ -1304,6 +1425,12 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
   const int *bl = J.blist[B].p;
   cudaStream_t st = J.ctx->stream;
   long Cp = s.Cpad;
+  if (s.is_static) {
+    if (stage == 0) k_static_eig<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl);
+    else return;
+    ++J.launches;
+    return;
+  }
   switch (stage) {
     case 0:
       if (s.step_method == 1) k_step_taylor<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
@@ -1359,13 +1486,16 @@ void Job::run() {
     }
     long Cp = s.Cpad;
     mark_begin(J, 4);
-    if (J.npq + J.npr > 0) {
+    if (!J.is_static && J.npq + J.npr > 0) {
       k_qr<<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
       ++J.launches;
     }
-    mark_end(J, 4, J.npq + J.npr > 0 ? 1 : 0);
+    mark_end(J, 4, !J.is_static && J.npq + J.npr > 0 ? 1 : 0);
     mark_begin(J, 5);
-    if (J.ne > 0) {
+    if (J.is_static && J.ne > 0) {
+      k_static_elems<<<grid_for(Cp * J.npq), kThreads, 0, st>>>(s);
+      ++J.launches;
+    } else if (J.ne > 0) {
       if (s.fave_method == 1) {
         int cg = std::max(1, std::min(8, 2048 / s.M));
         size_t shm = sizeof(double2) * size_t(s.M) * cg * 2;

@@ -21,6 +21,7 @@
 //   gamma-COMPUTE                  src/QMspins/driver/compute.h:86-97, 213-235, 257-274,
 //                                  294-306, 308-461
 //   powder loop                    src/QMspins/driver/oneFID.h:200-208, 339-431
+//   static powder FID              src/QMspins/driver/oneFID.h:220-336
 //   powder file reader             src/QMspins/driver/powder.cc:333-389
 //
 // Eigen-solvers are this file's own: cyclic complex Jacobi for Hermitian matrices, and
@@ -698,14 +699,53 @@ void read_powder(const std::string &file, std::vector<double> &th, std::vector<d
   }
 }
 
+// oneFID::singleStaticFID (oneFID.h:292-336): H at rotor phase 0 (Hamiltonian(0, dt) with
+// wr = 0), one eigen-decomposition, fid[k] = sum A_ij B_ij^k over |A_ij|^2 > 1e-10 with
+// A_ij = Do(i,j) sig0(j,i), B_ij = conj(e_i) e_j, e = exp(-2 pi i dt lambda), dt = 1/sw.
+std::vector<cplx> single_static_fid(const System &S, const Params &P, double theta, double phi, double gamma,
+                                    const CMat &ro, const CMat &det) {
+  double dt = 1. / P.sw;
+  double Rp[3][3];
+  rot3(phi, theta, gamma, Rp);
+  CMat H = hamiltonian(S, Rp, 0.0, P.rotb * kDeg2Rad);
+  std::vector<double> w;
+  CMat V;
+  jacobi_herm(H, w, V);
+  CMat sig0 = adjprop(V, ro), Do = adjprop(V, det);
+  int hs = S.N;
+  std::vector<cplx> e(hs), A, B;
+  cplx z(0.0, -dt * 2.0 * kPi);
+  for (int i = 0; i < hs; ++i) e[i] = std::exp(z * w[i]);
+  for (int i = 0; i < hs; ++i)
+    for (int j = 0; j < hs; ++j) {
+      cplx a = Do(i, j) * sig0(j, i);
+      if (std::norm(a) > 1.0e-10) {
+        A.push_back(a);
+        B.push_back(std::conj(e[i]) * e[j]);
+      }
+    }
+  std::vector<cplx> fid(P.npts);
+  for (int k = 0; k < P.npts; ++k) {
+    cplx acc = 0;
+    for (size_t p = 0; p < A.size(); ++p) {
+      acc += A[p];
+      A[p] *= B[p];
+    }
+    fid[k] = acc;
+  }
+  return fid;
+}
+
 int run(const Job &J, const double *pw, int C, double *out, double *sw_out) {
   System S = parse_system(J.spin);
   CMat ro = op_expr(S, J.rho), det = op_expr(S, J.det);
   std::vector<cplx> acc(J.P.npts, cplx(0, 0));
   double sw = J.P.sw;
+  const bool stat = J.P.wr == 0.0 || J.P.rotb == 0.0;  // oneFID::FID dispatch (oneFID.h:206)
   for (int c = 0; c < C; ++c) {
     double phi = pw[4 * c + 0], theta = pw[4 * c + 1], gamma = pw[4 * c + 2], w = pw[4 * c + 3];
-    std::vector<cplx> f = single_fid(S, J.P, theta, phi, gamma, ro, det, sw);
+    std::vector<cplx> f = stat ? single_static_fid(S, J.P, theta, phi, gamma, ro, det)
+                               : single_fid(S, J.P, theta, phi, gamma, ro, det, sw);
     for (int k = 0; k < J.P.npts; ++k) acc[k] += w * f[k];
   }
   for (int k = 0; k < J.P.npts; ++k) {

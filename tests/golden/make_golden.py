@@ -78,6 +78,15 @@ def cases():
     yield "hetero_13c2h_30deg", W.job_text(het), powder_rows(c0["powder"], spread(1154, 6))
     st = dict(c0, npts=256)
     yield "c0_start_t", W.job_text(st) + "start: 1.7e-05\n", powder_rows(c0["powder"], spread(1154, 4))
+    # static powder FIDs (oneFID.h:220-336): no spinning, and spinning with rotor angle 0
+    s1 = dict(c1, wr=0.0, sw=200000.0, npts=512)
+    yield "static_c1_wr0", W.job_text(s1), powder_rows(c1["powder"], spread(3722, 6))
+    s0 = dict(c0, rotb=0.0, sw=250000.0, npts=400)
+    yield "static_c0_rotb0", W.job_text(s0), powder_rows(c0["powder"], spread(1154, 8))
+    sq = dict(quad, wr=0.0, rotb=35.0, sw=500000.0, npts=256)
+    yield "static_quad_tilted", W.job_text(sq), powder_rows(c0["powder"], spread(1154, 5))
+    sn = dict(js, wr=0.0, rho="Fx+Fz", det="Fp", sw=300000.0, npts=300)
+    yield "static_jstrong_nonsym", W.job_text(sn), powder_rows(c0["powder"], spread(1154, 5))
 
 
 def main():

@@ -130,10 +130,6 @@ def test_c1_full_size_properties():
 def test_unsupported_inputs_return_status():
     cfg = W.config(0)
     rows = np.stack(cfg["powder"], axis=1)[:4]
-    static_job = W.job_text(dict(cfg, wr=0.0))
-    with pytest.raises(bl.BlochError) as e:
-        gpu_fid(static_job, rows)
-    assert e.value.status == 5
     big = "\n".join(f"spin: {l}" for l in ["numspin 5"] + [f"D -5000 {i} {j}" for i in range(5) for j in range(i + 1, 5)])
     big += "\nnpts: 16\nsw: 100000\nwr: 10000\nrotb: 54.7356\nrho: Fx\ndet: Fp\n"
     with pytest.raises(bl.BlochError) as e:
@@ -143,6 +139,18 @@ def test_unsupported_inputs_return_status():
     with pytest.raises(bl.BlochError) as e:
         gpu_fid(too_slow, rows)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("wr,rotb", [(0.0, 54.7356), (10000.0, 0.0), (0.0, 0.0)])
+def test_static_powder_fid_matches_oracle(wr, rotb):
+    """oneFID::FID takes the static branch when wr == 0 or the rotor angle is 0."""
+    cfg = W.config(1)
+    rows = np.stack(cfg["powder"], axis=1)[:40]
+    job = W.job_text(dict(cfg, wr=wr, rotb=rotb, sw=250000.0, npts=700))
+    ref, sw = oracle_fid(job, rows)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True)
+    assert sw_g == sw == 250000.0
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
 def test_resident_job_reruns_identically():
