@@ -1,0 +1,486 @@
+// Large-block kernels (Hamiltonian blocks of kMaxBlock < b <= kMaxBigBlock), included by
+// bl_engine.cu after DevSys and the complex helpers.  One CTA of kBigThreads threads works
+// on one crystallite's block with the matrices in shared memory; products are CTA-wide
+// FP64 GEMMs with 2x2 register tiles.  Same arithmetic as the small-block kernels:
+//   k_big_step      (c, step)   H_i, U_i = exp(-i 2pi tau H_i) by Taylor + squaring
+//   k_big_dyson     (c)         A_{i+1} = U_i A_i for i < n (A stays in shared memory)
+//   k_big_floquet   (c)         A_n = V diag(lam) V^H: Cayley transform, parallel Jacobi
+//   k_big_eigframe  (c)         W_i = A_{i+1} V_F for i < n
+//   k_big_qr        (c, step, pair)  Q = W_a^H M_ab W_b for block pairs with a big block
+
+constexpr int kMaxBigBlock = 74;   // 5 real b x b matrices fit 227 KB of shared memory
+constexpr int kBigThreads = 256;
+constexpr int kBigTiles = 6;       // ceil((74/2)^2 / 256) 2x2 output tiles per thread
+constexpr int kMaxInt = 128;       // interactions per system on the large-block path
+
+// C (m x n) = alpha * A (m x k) * B (k x n), real, shared memory, row-major with lds.
+__device__ void cta_mm_real(const double *A, int lda, const double *B, int ldb, double *C, int ldc, int m, int n,
+                            int k, double alpha) {
+  const int tm = (m + 1) / 2, tn = (n + 1) / 2;
+  for (int t = threadIdx.x; t < tm * tn; t += blockDim.x) {
+    const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
+    const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, n - 1);
+    double c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+    for (int l = 0; l < k; ++l) {
+      const double a0 = A[i0 * lda + l], a1 = A[i1 * lda + l];
+      const double b0 = B[l * ldb + j0], b1 = B[l * ldb + j1];
+      c00 = fma(a0, b0, c00), c01 = fma(a0, b1, c01), c10 = fma(a1, b0, c10), c11 = fma(a1, b1, c11);
+    }
+    C[i0 * ldc + j0] = alpha * c00;
+    if (j0 + 1 < n) C[i0 * ldc + j0 + 1] = alpha * c01;
+    if (i0 + 1 < m) {
+      C[(i0 + 1) * ldc + j0] = alpha * c10;
+      if (j0 + 1 < n) C[(i0 + 1) * ldc + j0 + 1] = alpha * c11;
+    }
+  }
+}
+
+// Complex 2x2-tiled product into per-thread registers: acc[t] for this thread's tiles.
+// CONJ_A: use A^H (A stored k x m).  Tiles are numbered t = threadIdx.x + q*blockDim.x.
+template <bool CONJ_A>
+__device__ void cta_mm_cplx_regs(const double2 *A, int lda, const double2 *B, int ldb, int m, int n, int k,
+                                 double2 (&acc)[kBigTiles][4]) {
+  const int tm = (m + 1) / 2, tn = (n + 1) / 2;
+#pragma unroll
+  for (int q = 0; q < kBigTiles; ++q) {
+    const int t = threadIdx.x + q * blockDim.x;
+    acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = cmk(0, 0);
+    if (t >= tm * tn) continue;
+    const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
+    const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, n - 1);
+    double2 c00 = cmk(0, 0), c01 = c00, c10 = c00, c11 = c00;
+    for (int l = 0; l < k; ++l) {
+      double2 a0, a1;
+      if (CONJ_A) {
+        a0 = cconj(A[l * lda + i0]), a1 = cconj(A[l * lda + i1]);
+      } else {
+        a0 = A[i0 * lda + l], a1 = A[i1 * lda + l];
+      }
+      const double2 b0 = B[l * ldb + j0], b1 = B[l * ldb + j1];
+      c00 = cfma(a0, b0, c00), c01 = cfma(a0, b1, c01), c10 = cfma(a1, b0, c10), c11 = cfma(a1, b1, c11);
+    }
+    acc[q][0] = c00, acc[q][1] = c01, acc[q][2] = c10, acc[q][3] = c11;
+  }
+}
+
+// Visits this thread's tile outputs: f(row, col, value).
+template <class F>
+__device__ void cta_tiles_store(int m, int n, const double2 (&acc)[kBigTiles][4], F f) {
+  const int tm = (m + 1) / 2, tn = (n + 1) / 2;
+#pragma unroll
+  for (int q = 0; q < kBigTiles; ++q) {
+    const int t = threadIdx.x + q * blockDim.x;
+    if (t >= tm * tn) continue;
+    const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
+    f(i0, j0, acc[q][0]);
+    if (j0 + 1 < n) f(i0, j0 + 1, acc[q][1]);
+    if (i0 + 1 < m) {
+      f(i0 + 1, j0, acc[q][2]);
+      if (j0 + 1 < n) f(i0 + 1, j0 + 1, acc[q][3]);
+    }
+  }
+}
+
+// One CTA per (crystallite, step): U_i of a large block by Taylor series + squaring.
+__global__ void __launch_bounds__(kBigThreads) k_big_step(DevSys s, int k) {
+  extern __shared__ double bsm[];
+  __shared__ double fk[kMaxInt];
+  __shared__ double red[kMaxBigBlock];
+  __shared__ double scl[2];
+  const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  double *X = bsm, *P = X + bb, *Q = P + bb, *R = Q + bb, *I = R + bb;
+  if (threadIdx.x == 0) {
+    double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
+    double tmid = (t2 - t1) / 2.0 + t1;
+    double sp, cp;
+    sincos(tmid * s.wr * kPi2, &sp, &cp);
+    double rr0 = sp * s.sin_rotb, rr1 = -cp * s.sin_rotb, rr2 = s.cos_rotb, r[3];
+    for (int j = 0; j < 3; ++j)
+      r[j] = rr0 * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr1 * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
+             rr2 * s.Rp[at(2 * 3 + j, c, s.Cpad)];
+    for (int kk = 0; kk < s.nint; ++kk) {
+      const double *Pa = s.pas + 6 * kk;
+      double a = r[0] * (Pa[0] * r[0] + Pa[1] * r[1] + Pa[2] * r[2]) +
+                 r[1] * (Pa[1] * r[0] + Pa[3] * r[1] + Pa[4] * r[2]) + r[2] * (Pa[2] * r[0] + Pa[4] * r[1] + Pa[5] * r[2]);
+      fk[kk] = s.iscale[kk] * a;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    double h = s.Hc[bp + e];
+    for (int kk = 0; kk < s.nint; ++kk) {
+      const double t = s.Tk[size_t(kk) * s.S2 + bp + e];
+      if (t != 0.0) h = fma(fk[kk], t, h);
+    }
+    X[e] = h;
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < b; p += blockDim.x) {
+    double rs = 0;
+    for (int q = 0; q < b; ++q) rs += fabs(X[p * b + q]);
+    red[p] = rs;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double nrm = 0;
+    for (int p = 0; p < b; ++p) nrm = fmax(nrm, red[p]);
+    const double tp = s.tau * kPi2;
+    nrm *= tp;
+    int sq = 0;
+    if (nrm > 0.5) {
+      frexp(nrm / 0.5, &sq);
+      sq = min(sq, 60);
+    }
+    scl[0] = ldexp(tp, -sq);
+    scl[1] = double(sq);
+  }
+  __syncthreads();
+  const double sc = scl[0];
+  const int sq = int(scl[1]);
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    const double x = sc * X[e];
+    X[e] = x, P[e] = x;
+    R[e] = (e / b == e % b) ? 1.0 : 0.0;
+    I[e] = -x;
+  }
+  __syncthreads();
+  for (int kt = 2; kt <= kTaylorTerms; ++kt) {
+    cta_mm_real(P, b, X, b, Q, b, b, b, b, 1.0 / kt);
+    __syncthreads();
+    const int m4 = kt & 3;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const double v = Q[e];
+      if (m4 == 2) R[e] -= v;
+      else if (m4 == 3) I[e] += v;
+      else if (m4 == 0) R[e] += v;
+      else I[e] -= v;
+    }
+    double *t = P;
+    P = Q, Q = t;
+    __syncthreads();
+  }
+  for (int t = 0; t < sq; ++t) {  // (R + iI)^2 = (RR - II) + i 2RI; X is free here
+    cta_mm_real(R, b, R, b, P, b, b, b, b, 1.0);
+    cta_mm_real(I, b, I, b, Q, b, b, b, b, 1.0);
+    cta_mm_real(R, b, I, b, X, b, b, b, b, 2.0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) R[e] = P[e] - Q[e], I[e] = X[e];
+    __syncthreads();
+  }
+  double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) Ub[at(bp + e, c, s.Cpad)] = cmk(R[e], I[e]);
+}
+
+// One CTA per crystallite: A_{i+1} = U_i A_i for all steps; A lives in shared memory.
+__global__ void __launch_bounds__(kBigThreads) k_big_dyson(DevSys s, int k) {
+  extern __shared__ double2 bsc[];
+  const int c = blockIdx.x;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  double2 *Us = bsc, *As = Us + bb;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = cmk(e / b == e % b ? 1.0 : 0.0, 0.0);
+  double2 acc[kBigTiles][4];
+  for (int i = 0; i < s.n; ++i) {
+    const double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) Us[e] = Ub[at(bp + e, c, s.Cpad)];
+    __syncthreads();
+    cta_mm_cplx_regs<false>(Us, b, As, b, b, b, b, acc);
+    __syncthreads();
+    double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+    cta_tiles_store(b, b, acc, [&](int r, int q, double2 v) {
+      As[r * b + q] = v;
+      Ab[at(bp + r * b + q, c, s.Cpad)] = v;
+    });
+    __syncthreads();
+  }
+}
+
+// One CTA per crystallite: W_i = A_{i+1} V_F, in place.
+__global__ void __launch_bounds__(kBigThreads) k_big_eigframe(DevSys s, int k) {
+  extern __shared__ double2 bsc[];
+  const int c = blockIdx.x;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  double2 *Vs = bsc, *As = Vs + bb;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) Vs[e] = s.VF[at(bp + e, c, s.Cpad)];
+  double2 acc[kBigTiles][4];
+  for (int i = 0; i < s.n; ++i) {
+    double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = Ab[at(bp + e, c, s.Cpad)];
+    __syncthreads();
+    cta_mm_cplx_regs<false>(As, b, Vs, b, b, b, b, acc);
+    cta_tiles_store(b, b, acc, [&](int r, int q, double2 v) { Ab[at(bp + r * b + q, c, s.Cpad)] = v; });
+    __syncthreads();
+  }
+}
+
+// One CTA per (crystallite, step, big pair): Q^{ab} = W_a^H (M_ab W_b), M = D (or rho).
+__global__ void __launch_bounds__(kBigThreads) k_big_qr(DevSys s, const int *__restrict__ plist, int npl) {
+  extern __shared__ double2 bsc[];
+  const int pidx = blockIdx.x / (s.C * s.n);
+  const int rem = blockIdx.x % (s.C * s.n);
+  const int c = rem % s.C, i = rem / s.C;
+  const int pr = plist[pidx];
+  const bool isq = pr < s.npq;
+  int a, b, off, moff, nitems;
+  const double2 *M;
+  double2 *out;
+  if (isq) {
+    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = s.Q, nitems = s.nq;
+  } else {
+    const int p2 = pr - s.npq;
+    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = s.R, nitems = s.nr;
+  }
+  const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
+  const double2 *W = s.A + size_t(i) * s.S2 * s.Cpad;
+  double2 *Wa = bsc, *X = Wa + ba * ba;
+  for (int e = threadIdx.x; e < ba * ba; e += blockDim.x) Wa[e] = W[at(pa + e, c, s.Cpad)];
+  // X = M_ab W_b (M sparse: its zero entries are skipped, uniformly across the CTA)
+  for (int e = threadIdx.x; e < ba * bb; e += blockDim.x) {
+    const int l = e / bb, q = e % bb;
+    double2 acc = cmk(0, 0);
+    for (int m = 0; m < bb; ++m) {
+      const double2 d = M[moff + l * bb + m];
+      if (d.x == 0.0 && d.y == 0.0) continue;
+      acc = cfma(d, W[at(pb + m * bb + q, c, s.Cpad)], acc);
+    }
+    X[e] = acc;
+  }
+  __syncthreads();
+  double2 acc[kBigTiles][4];
+  cta_mm_cplx_regs<true>(Wa, ba, X, bb, ba, bb, ba, acc);
+  double2 *ob = out + size_t(i) * nitems * s.Cpad;
+  cta_tiles_store(ba, bb, acc, [&](int r, int q, double2 v) { ob[at(off + r * bb + q, c, s.Cpad)] = v; });
+}
+
+// One CTA per crystallite: unitary eigen-decomposition of the big block of A_n by the
+// Cayley transform K = i (I+W)^{-1}(I-W), W = e^{ia} A_n, and a parallel (round-robin)
+// complex Jacobi on K; a second pass moves -1 into the widest spectral gap when the first
+// is ill conditioned.  Shared memory: two complex b x b matrices.
+__global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
+  extern __shared__ double2 bsc[];
+  __shared__ double2 rot[kMaxBigBlock / 2 + 1][2];  // (c, 0), (s e^{i ph}) per pair
+  __shared__ int rpair[kMaxBigBlock / 2 + 1][2];
+  __shared__ double2 fv[kMaxBigBlock];
+  __shared__ double2 lam[kMaxBigBlock];
+  __shared__ double red[kBigThreads];
+  __shared__ int piv_s;
+  __shared__ double a_s;
+  __shared__ int done_s;
+  const int c = blockIdx.x;
+  const int b = s.bs[k], bp = s.bpoff[k], bo = s.boff[k], bb = b * b;
+  double2 *Mm = bsc, *Xk = Mm + bb;
+  const double2 *U = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;  // U(r,q) = U[at(bp + r*b + q, c)]
+  auto Ug = [&](int r, int q) { return U[at(bp + r * b + q, c, s.Cpad)]; };
+  if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    double sa, ca;
+    sincos(a_s, &sa, &ca);
+    const double2 ea = cmk(ca, sa);
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const double2 w = cmul(ea, Ug(e / b, e % b));
+      const double id = (e / b == e % b) ? 1.0 : 0.0;
+      Mm[e] = cmk(id + w.x, w.y);
+      Xk[e] = cmk(id - w.x, -w.y);
+    }
+    __syncthreads();
+    // Gaussian elimination with partial pivoting: Mm Xk' = Xk
+    for (int kc = 0; kc < b; ++kc) {
+      if (threadIdx.x == 0) {
+        int pv = kc;
+        double best = -1;
+        for (int r = kc; r < b; ++r) {
+          const double2 v = Mm[r * b + kc];
+          const double m2 = v.x * v.x + v.y * v.y;
+          if (m2 > best) best = m2, pv = r;
+        }
+        piv_s = pv;
+        if (best == 0.0) atomicOr(s.status, kSingularCayley);
+      }
+      __syncthreads();
+      const int pv = piv_s;
+      if (pv != kc)
+        for (int j = threadIdx.x; j < 2 * b; j += blockDim.x) {
+          double2 *Mx = j < b ? Mm : Xk;
+          const int jj = j < b ? j : j - b;
+          const double2 t = Mx[kc * b + jj];
+          Mx[kc * b + jj] = Mx[pv * b + jj];
+          Mx[pv * b + jj] = t;
+        }
+      __syncthreads();
+      const double2 inv = cdiv(cmk(1, 0), Mm[kc * b + kc]);
+      for (int r = kc + 1 + threadIdx.x; r < b; r += blockDim.x) fv[r] = cmul(Mm[r * b + kc], inv);
+      __syncthreads();
+      const int rows = b - kc - 1;
+      for (int e = threadIdx.x; e < rows * (2 * b); e += blockDim.x) {
+        const int r = kc + 1 + e / (2 * b), j = e % (2 * b);
+        if (j < b) {
+          if (j > kc) Mm[r * b + j] = csub(Mm[r * b + j], cmul(fv[r], Mm[kc * b + j]));
+        } else {
+          Xk[r * b + (j - b)] = csub(Xk[r * b + (j - b)], cmul(fv[r], Xk[kc * b + (j - b)]));
+        }
+      }
+      __syncthreads();
+    }
+    for (int kr = b - 1; kr >= 0; --kr) {  // back substitution, columns in parallel
+      const double2 inv = cdiv(cmk(1, 0), Mm[kr * b + kr]);
+      for (int j = threadIdx.x; j < b; j += blockDim.x) {
+        double2 acc = Xk[kr * b + j];
+        for (int r = kr + 1; r < b; ++r) acc = csub(acc, cmul(Mm[kr * b + r], Xk[r * b + j]));
+        Xk[kr * b + j] = cmul(acc, inv);
+      }
+      __syncthreads();
+    }
+    // K = Hermitian part of i X, in Xk; V = I in Mm
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const int r = e / b, q = e % b;
+      if (r <= q) {
+        const double2 xrq = Xk[r * b + q], xqr = Xk[q * b + r];
+        const double2 krq = cmk(-xrq.y, xrq.x), kqr = cmk(-xqr.y, xqr.x);
+        const double2 h = cscale(cadd(krq, cconj(kqr)), 0.5);
+        Xk[r * b + q] = h;
+        Xk[q * b + r] = cconj(h);
+      }
+    }
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) Mm[e] = cmk(e / b == e % b ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < b; e += blockDim.x) Xk[e * b + e].y = 0.0;
+    __syncthreads();
+    const int bq = b + (b & 1);  // players in the round-robin (one dummy when b is odd)
+    const int np = bq / 2;
+    bool conv = false;
+    for (int sweep = 0; sweep < kMaxSweeps && !conv; ++sweep) {
+      double off = 0, dg = 0;
+      for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+        const int r = e / b, q = e % b;
+        const double2 v = Xk[e];
+        if (r < q) off += v.x * v.x + v.y * v.y;
+        else if (r == q) dg += v.x * v.x;
+      }
+      red[threadIdx.x] = off;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double so = 0;
+        for (int t = 0; t < blockDim.x; ++t) so += red[t];
+        red[0] = so;
+      }
+      __syncthreads();
+      const double offs = red[0];
+      __syncthreads();
+      red[threadIdx.x] = dg;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double sd = 0;
+        for (int t = 0; t < blockDim.x; ++t) sd += red[t];
+        red[0] = sd;
+      }
+      __syncthreads();
+      const double dgs = red[0];
+      __syncthreads();
+      if (offs <= 1e-34 * dgs || offs == 0.0) {
+        conv = true;
+        break;
+      }
+      for (int round = 0; round < bq - 1; ++round) {
+        for (int t = threadIdx.x; t < np; t += blockDim.x) {
+          auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (bq - 1); };
+          int p = player(t), q = player(bq - 1 - t);
+          if (p > q) {
+            int tmp = p;
+            p = q, q = tmp;
+          }
+          rpair[t][0] = p, rpair[t][1] = q;
+          rot[t][0] = cmk(1, 0), rot[t][1] = cmk(0, 0);
+          if (q < b) {
+            const double2 hpq = Xk[p * b + q];
+            const double ab = hypot(hpq.x, hpq.y);
+            if (ab != 0.0) {
+              const double2 ph = cmk(hpq.x / ab, hpq.y / ab);
+              const double theta = 0.5 * (Xk[q * b + q].x - Xk[p * b + p].x) / ab;
+              double tt;
+              if (fabs(theta) > 1e100) tt = 0.5 / theta;
+              else tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+              const double cc = rsqrt(fma(tt, tt, 1.0));
+              rot[t][0] = cmk(cc, 0.0);
+              rot[t][1] = cscale(ph, tt * cc);
+            }
+          }
+        }
+        __syncthreads();
+        // columns p, q of K and V:  K <- K G, V <- V G  with G = [[c, sp], [-conj(sp), c]]
+        for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
+          const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
+          double2 *Mx = rem2 < b ? Xk : Mm;
+          const int p = rpair[t][0], q = rpair[t][1];
+          if (q >= b) continue;
+          const double cc = rot[t][0].x;
+          const double2 sp = rot[t][1], spc = cconj(sp);
+          const double2 xkp = Mx[kk * b + p], xkq = Mx[kk * b + q];
+          Mx[kk * b + p] = csub(cscale(xkp, cc), cmul(spc, xkq));
+          Mx[kk * b + q] = cadd(cmul(sp, xkp), cscale(xkq, cc));
+        }
+        __syncthreads();
+        // rows p, q of K:  K <- G^H K
+        for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
+          const int t = e / b, kk = e % b;
+          const int p = rpair[t][0], q = rpair[t][1];
+          if (q >= b) continue;
+          const double cc = rot[t][0].x;
+          const double2 sp = rot[t][1], spc = cconj(sp);
+          const double2 xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
+          Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
+          Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < np; t += blockDim.x) {
+          const int p = rpair[t][0], q = rpair[t][1];
+          if (q >= b || (rot[t][1].x == 0.0 && rot[t][1].y == 0.0)) continue;
+          Xk[p * b + q] = cmk(0, 0), Xk[q * b + p] = cmk(0, 0);
+          Xk[p * b + p].y = 0.0, Xk[q * b + q].y = 0.0;
+        }
+        __syncthreads();
+      }
+    }
+    if (!conv) atomicOr(s.status, kNoConvergeFloquet);
+    // Rayleigh quotients lam_r = v_r^H U v_r
+    for (int r = threadIdx.x; r < b; r += blockDim.x) {
+      double2 acc = cmk(0, 0);
+      for (int kk = 0; kk < b; ++kk) {
+        double2 uv = cmk(0, 0);
+        for (int l = 0; l < b; ++l) uv = cfma(Ug(kk, l), Mm[l * b + r], uv);
+        acc = cfmaconj(Mm[kk * b + r], uv, acc);
+      }
+      lam[r] = acc;
+    }
+    __syncthreads();
+    if (pass == 1) break;
+    if (threadIdx.x == 0) {
+      double mind = 4.0;
+      for (int r = 0; r < b; ++r) {
+        const double2 w = cmul(ea, lam[r]);
+        mind = fmin(mind, (1.0 + w.x) * (1.0 + w.x) + w.y * w.y);
+      }
+      done_s = mind >= 0.0625;
+      if (!done_s) {
+        // widest gap of the eigenphases: sort them (insertion sort into red[])
+        for (int r = 0; r < b; ++r) {
+          const double th = atan2(lam[r].y, lam[r].x);
+          int j = r;
+          while (j > 0 && red[j - 1] > th) red[j] = red[j - 1], --j;
+          red[j] = th;
+        }
+        double best = -1, mid = 0;
+        for (int r = 0; r < b; ++r) {
+          const double lo = red[r], hi = (r + 1 < b) ? red[r + 1] : red[0] + kPi2;
+          if (hi - lo > best) best = hi - lo, mid = 0.5 * (lo + hi);
+        }
+        a_s = kPi - mid;
+      }
+    }
+    __syncthreads();
+    if (done_s) break;
+  }
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) s.VF[at(bp + e, c, s.Cpad)] = Mm[e];
+  for (int r = threadIdx.x; r < b; r += blockDim.x)
+    s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
+}

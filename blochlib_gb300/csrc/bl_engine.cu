@@ -756,6 +756,7 @@ __global__ void __launch_bounds__(kThreads) k_qr(DevSys s) {
     a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = s.R, nitems = s.nr;
   }
   const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
+  if (ba > kMaxBlock || bb > kMaxBlock) return;  // k_big_qr handles pairs with a large block
   const double2 *W = s.A + size_t(i) * s.S2 * s.Cpad;
   double2 X[kMaxBlock * kMaxBlock];
   // X = M_ab W_b  (ba x bb)
@@ -978,6 +979,8 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   }
 }
 
+#include "bl_big.cuh"
+
 constexpr int kFidJT = 4, kFidPT = 4;
 
 // One thread per (crystallite, tile of kFidJT j's, tile of kFidPT p's); lanes are
@@ -1103,7 +1106,11 @@ struct JobImpl {
   BlockLayout L;
   int nint = 0, nq = 0, nr = 0, ne = 0, npq = 0, npr = 0;
   int Cb = 0, nbatch = 0, nwarps_total = 0;
-  std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices
+  std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices (size <= kMaxBlock)
+  std::vector<int> big_blocks;                   // blocks larger than kMaxBlock
+  std::vector<int> big_pairs_h;                  // Q/R pairs with a block larger than kMaxBlock
+  DevBuf<int> big_pairs;
+  size_t big_smem_step = 0, big_smem_mat = 0, big_smem_qr = 0;
   DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status, srp, seo;
   std::vector<DevBuf<int>> blist;
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
@@ -1179,9 +1186,11 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   J.L = sys.layout();
   const BlockLayout &L = J.L;
-  if (L.max_block > kMaxBlock)
+  if (L.max_block > kMaxBigBlock)
     throw Error(5, "Hamiltonian block of size " + std::to_string(L.max_block) + " exceeds this engine's limit of " +
-                       std::to_string(kMaxBlock));
+                       std::to_string(kMaxBigBlock));
+  if (J.is_static && L.max_block > kMaxBlock)
+    throw Error(5, "static powder FIDs support Hamiltonian blocks up to " + std::to_string(kMaxBlock));
   const int nb = int(L.size.size());
   // rosym: exact test ro == 0.5*(det + det^H)   (compute.h:75-83)
   J.rosym = 1;
@@ -1295,7 +1304,30 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.nwarps_total = J.nbatch * (J.Cb / 32);
   // block lists by size
   J.blocks_by_size.assign(kMaxBlock + 1, {});
-  for (int k = 0; k < nb; ++k) J.blocks_by_size[L.size[k]].push_back(k);
+  for (int k = 0; k < nb; ++k) {
+    if (L.size[k] <= kMaxBlock) J.blocks_by_size[L.size[k]].push_back(k);
+    else J.big_blocks.push_back(k);
+  }
+  if (!J.big_blocks.empty()) {
+    if (J.nint > kMaxInt) throw Error(5, "more than " + std::to_string(kMaxInt) + " anisotropic interactions");
+    int bmax = 0;
+    for (int k : J.big_blocks) bmax = std::max(bmax, L.size[k]);
+    J.big_smem_step = sizeof(double) * 5 * size_t(bmax) * bmax;
+    J.big_smem_mat = sizeof(double2) * 2 * size_t(bmax) * bmax;
+    for (int pr = 0; pr < J.npq + J.npr; ++pr) {
+      int a = pr < J.npq ? qa[pr] : ra[pr - J.npq], b = pr < J.npq ? qb[pr] : rb[pr - J.npq];
+      if (L.size[a] > kMaxBlock || L.size[b] > kMaxBlock) {
+        J.big_pairs_h.push_back(pr);
+        J.big_smem_qr = std::max(J.big_smem_qr, sizeof(double2) * size_t(L.size[a]) * (L.size[a] + L.size[b]));
+      }
+    }
+    CUDA_OK(cudaFuncSetAttribute(k_big_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_step)));
+    CUDA_OK(cudaFuncSetAttribute(k_big_dyson, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
+    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
+    CUDA_OK(cudaFuncSetAttribute(k_big_floquet, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
+    if (J.big_smem_qr)
+      CUDA_OK(cudaFuncSetAttribute(k_big_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_qr)));
+  }
   J.blist.resize(kMaxBlock + 1);
   cudaStream_t st = ctx.stream;
   g_upload_counter = &J.h2d;
@@ -1308,6 +1340,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.ra.upload(ra, st), J.rb.upload(rb, st), J.roff.upload(roff, st), J.rhooff.upload(rhooff, st);
   J.eq.upload(eq, st), J.erev.upload(erev, st), J.er.upload(er, st), J.erg.upload(erg, st), J.esg.upload(esg, st);
   J.srp.upload(srp, st), J.seo.upload(seo, st);
+  J.big_pairs.upload(J.big_pairs_h, st);
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
@@ -1452,6 +1485,21 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
   launch_block_kernels<6>(J, s, stage);
   launch_block_kernels<7>(J, s, stage);
   launch_block_kernels<8>(J, s, stage);
+  // blocks larger than kMaxBlock: one CTA per crystallite (per step for the exponential)
+  cudaStream_t st = J.ctx->stream;
+  for (int k : J.big_blocks) {
+    const int b = J.L.size[k];
+    const size_t smat = sizeof(double2) * 2 * size_t(b) * b;
+    switch (stage) {
+      case 0:
+        k_big_step<<<unsigned(s.C) * unsigned(s.n), kBigThreads, sizeof(double) * 5 * size_t(b) * b, st>>>(s, k);
+        break;
+      case 1: k_big_dyson<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
+      case 2: k_big_floquet<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
+      case 3: k_big_eigframe<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
+    }
+    ++J.launches;
+  }
 }
 
 static void mark_begin(JobImpl &J, int stage);
@@ -1489,6 +1537,11 @@ void Job::run() {
     if (!J.is_static && J.npq + J.npr > 0) {
       k_qr<<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
       ++J.launches;
+      if (!J.big_pairs_h.empty()) {
+        unsigned grid = unsigned(J.big_pairs_h.size()) * unsigned(s.C) * unsigned(J.n);
+        k_big_qr<<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
+        ++J.launches;
+      }
     }
     mark_end(J, 4, !J.is_static && J.npq + J.npr > 0 ? 1 : 0);
     mark_begin(J, 5);

@@ -89,9 +89,34 @@ def cases():
     yield "static_jstrong_nonsym", W.job_text(sn), powder_rows(c0["powder"], spread(1154, 5))
 
 
+def big_cases():
+    """Systems with Hamiltonian blocks larger than 8 (5, 6 and 8 like spins)."""
+    c0 = W.config(0)
+    c3 = W.config(3, 1)  # a seeded c3 system
+    for nspin, seed, name in [(5, 11, "big_5h"), (6, 12, "big_6h")]:
+        rng = np.random.default_rng(W.SEED0 + seed)
+        xyz = W._proton_cluster(rng, nspin, 5.0, min_sep=1.5)
+        lines = [f"numspin {nspin}"] + [f"T 1H {k}" for k in range(nspin)] + W._csa_lines(rng, nspin) + \
+            W._dipole_lines(xyz) + ["J 85 0 1"]
+        cfg = dict(lines=lines, rho="Fx", det="Fp", npts=512, wr=25000.0, sw=50 * 25000.0, rotb=W.MAGIC_ANGLE)
+        yield name, W.job_text(cfg), powder_rows(c0["powder"], spread(1154, 3 if nspin == 5 else 2))
+    c2 = W.config(2)
+    yield "c2_sub1", W.job_text(c2), powder_rows(c2["powder"], spread(1154, 1))
+
+
 def main():
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
+    if "--big" in sys.argv:
+        man = json.loads((OUT / "manifest.json").read_text())
+        for name, job, rows in big_cases():
+            sw64, f64 = run_ref(BIN64, job, rows)
+            np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,
+                                sw=np.array(sw64))
+            man[name] = {"crystallites": len(rows), "npts": len(f64), "sw": sw64, "float_ql_rel_dev": None}
+            print(name, man[name], flush=True)
+        (OUT / "manifest.json").write_text(json.dumps(man, indent=1))
+        return
     manifest = {}
     for name, job, rows in cases():
         sw64, f64 = run_ref(BIN64, job, rows)

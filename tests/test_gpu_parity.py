@@ -169,3 +169,50 @@ def test_resident_job_reruns_identically():
     st = j.stage_times()
     assert st["k_fave"][1] >= 1 and st["k_step_prop"][0] > 0
     assert j.launches >= 8
+
+
+def big_system(seed, nspin, rho, det):
+    rng = np.random.default_rng(1000 + seed)
+    iso = ["1H"] * nspin if seed % 2 == 0 else ["1H"] * (nspin - 1) + ["13C"]
+    lines = [f"numspin {nspin}"] + [f"T {iso[k]} {k}" for k in range(nspin)]
+    for k in range(nspin):
+        a = rng.uniform(0, 360, 3)
+        lines.append(f"C {rng.uniform(-2e3, 2e3):.9g} {rng.uniform(-6e3, 6e3):.9g} {rng.uniform(0, 1):.9g} {k} "
+                     f"{a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    for i in range(nspin):
+        for j in range(i + 1, nspin):
+            a = rng.uniform(0, 360, 3)
+            lines.append(f"D {rng.uniform(-1.5e4, 1.5e4):.9g} {i} {j} {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    lines.append("J 90 0 1 1")
+    wr = float(rng.uniform(8e3, 30e3))
+    n_steps = int(rng.integers(10, 40))
+    job = "\n".join(f"spin: {l}" for l in lines) + (
+        f"\nnpts: 300\nsw: {n_steps * wr!r}\nwr: {wr!r}\nrotb: {W.MAGIC_ANGLE!r}\nrho: {rho}\ndet: {det}\n")
+    c = 2 if nspin < 7 else 1
+    rows = np.stack([rng.uniform(0, 2 * np.pi, c), np.arccos(rng.uniform(-1, 1, c)), rng.uniform(0, 2 * np.pi, c),
+                     rng.uniform(0.1, 1, c)], axis=1)
+    return job, rows
+
+
+@pytest.mark.parametrize("seed,nspin,rho,det", [(0, 5, "Fx", "Fp"), (1, 5, "Fx+Fz", "Fp"), (2, 6, "Ix 0", "Ix 0"),
+                                                (3, 6, "Fx", "Fp"), (4, 7, "Fx", "Fp")])
+def test_big_blocks_match_oracle(seed, nspin, rho, det):
+    """Hamiltonian blocks larger than 8 (5-7 spins) run on the CTA-per-block kernels."""
+    job, rows = big_system(seed, nspin, rho, det)
+    lines, _ = parse_job(job)
+    assert max(bl.SolidSys(lines).blocks()) > 8
+    ref, sw = oracle_fid(job, rows)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method="taylor")
+    assert sw_g == sw
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
+def test_c2_subset_batches_consistently():
+    """c2 (8 x 1H, blocks up to 70): 64 crystallites in one batch and in two."""
+    cfg = W.config(2)
+    rows = np.stack(cfg["powder"], axis=1)[:64]
+    job = W.job_text(cfg)
+    one = gpu_fid(job, rows)
+    small = bl.Context(0, hbm_budget=6 << 30)  # ~160 MB per crystallite: forces two batches
+    two = gpu_fid(job, rows, ctx=small)
+    np.testing.assert_array_equal(one, two)
