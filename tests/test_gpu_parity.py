@@ -130,7 +130,8 @@ def test_c1_full_size_properties():
 def test_unsupported_inputs_return_status():
     cfg = W.config(0)
     rows = np.stack(cfg["powder"], axis=1)[:4]
-    big = "\n".join(f"spin: {l}" for l in ["numspin 5"] + [f"D -5000 {i} {j}" for i in range(5) for j in range(i + 1, 5)])
+    # 9 like spins: the M = 1/2 sector is a block of 126 > 74
+    big = "\n".join(f"spin: {l}" for l in ["numspin 9"] + [f"D -5000 {i} {i + 1}" for i in range(8)])
     big += "\nnpts: 16\nsw: 100000\nwr: 10000\nrotb: 54.7356\nrho: Fx\ndet: Fp\n"
     with pytest.raises(bl.BlochError) as e:
         gpu_fid(big, rows)
@@ -173,7 +174,8 @@ def test_resident_job_reruns_identically():
 
 def big_system(seed, nspin, rho, det):
     rng = np.random.default_rng(1000 + seed)
-    iso = ["1H"] * nspin if seed % 2 == 0 else ["1H"] * (nspin - 1) + ["13C"]
+    # one 13C among >= 5 protons still leaves proton blocks larger than 8
+    iso = ["1H"] * nspin if (seed % 2 == 0 or nspin < 6) else ["1H"] * (nspin - 1) + ["13C"]
     lines = [f"numspin {nspin}"] + [f"T {iso[k]} {k}" for k in range(nspin)]
     for k in range(nspin):
         a = rng.uniform(0, 360, 3)
