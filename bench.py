@@ -124,13 +124,13 @@ def workload(name):
     return W.config(idx)
 
 
-def make_job(bl, cfg, ctx, step_method=None, fave_method=None):
+def make_job(bl, cfg, ctx, step_method=None, fave_method=None, precision=0):
     s = bl.SolidSys(cfg["lines"])
     phi, theta, gamma, w = cfg["powder"]
     pw = bl.powder.from_arrays(theta, phi, gamma, w)
     ro, det = s.op(cfg["rho"]), s.op(cfg["det"])
     job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=step_method,
-                 fave_method=fave_method)
+                 fave_method=fave_method, precision=precision)
     return s, pw, ro, det, job
 
 
@@ -215,6 +215,10 @@ def run_reference(args):
     return 0
 
 
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -225,22 +229,26 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--fave-method", default=None, choices=["auto", "direct", "fft"])
-    ap.add_argument("--step-method", default=None, choices=["eigh", "taylor"],
-                    help="FP64 step exponential (default: BL_STEP_METHOD or eigh)")
     ap.add_argument("--crystallites", type=int, default=0,
                     help="use only the first N crystallites (smaller case for profiler captures)")
+    ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
+                    help="path timed for 'value' (default: fp64 for c0/c1, mixed for c2)")
+    ap.add_argument("--no-compare", action="store_true", help="skip the other precision form")
+    ap.add_argument("--fave-method", default=None, choices=["auto", "direct", "fft"])
+    ap.add_argument("--step-method", default="taylor", choices=["eigh", "taylor"],
+                    help="FP64 step exponential (default taylor: the faster exact form)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     args.warmup = max(args.warmup, 3)
+    prec = args.precision or ("mixed" if args.config == "c2" else "fp64")
     import blochlib_gb300 as bl
     d = Dist()
     ctx = bl.Context(d.local)
     cfg = workload(args.config)
     if args.crystallites:
         cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
-    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method)
+    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if prec == "mixed" else 0)
     for _ in range(args.warmup):
         job.run()
     job.sync()
@@ -259,6 +267,7 @@ def main():
     clk = clocks.stop()
     ms_max = d.max(ms_total)
     value = d.world * args.steps / (ms_max / 1e3)
+    fid_main = job.read()
     stages = job.stage_times()
     sflops = job.stage_flops()
     dom = max(stages, key=lambda k: stages[k][0])
@@ -272,9 +281,24 @@ def main():
         except (ValueError, AttributeError):
             traffic = None
     launches_per_run = job.launches
+    job.set_profiling(False)
+    forms = {prec: {"fids_per_s": value, "ms_per_fid": ms_max / args.steps}}
+    if not args.no_compare:
+        other = "fp64" if prec == "mixed" else "mixed"
+        _, _, _, _, job2 = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if other == "mixed" else 0)
+        job2.run()
+        job2.sync()
+        k2 = max(1, min(args.steps, 10))
+        ms2 = job2.run_timed(k2) / k2
+        fid_other = job2.read()
+        forms[other] = {"fids_per_s": 1e3 / ms2, "ms_per_fid": ms2}
+        f64, fmx = (fid_main, fid_other) if prec == "fp64" else (fid_other, fid_main)
+        forms["mixed"]["rel_err_vs_fp64"] = _rel(fmx, f64)
+        forms["mixed_speedup_vs_fp64"] = forms["mixed"]["fids_per_s"] / forms["fp64"]["fids_per_s"]
+        job2.close()
     # e2e through the reference-facing call with host buffers
     drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method,
-                    fave_method=args.fave_method)
+                    fave_method=args.fave_method, precision=1 if prec == "mixed" else 0)
     drv.FID(pw, ro, det)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
@@ -284,17 +308,21 @@ def main():
     h2d += 8 * 4 * len(cfg["powder"][0]) + 2 * ro.nbytes  # the caller's powder arrays and rho/det
     if d.rank != 0:
         return 0
+    dtype = "f64" if prec == "fp64" else "f64+f32 (f64: step exponential, Dyson, Floquet, powder sum)"
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded spin systems and ZCW powder, workloads.py)",
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded spin systems and ZCW powder, workloads.py)",
         "config": {"workload": f"{cfg['name']}: {cfg['lines'][0]} ({' '.join(cfg['lines'][1:2])}...), "
                                f"dim {s.dim()}, {len(cfg['powder'][0])} crystallites, "
-                               f"n={int(round(cfg['sw'] / cfg['wr']))} steps/period, npts={cfg['npts']}, plain FP64",
+                               f"n={int(round(cfg['sw'] / cfg['wr']))} steps/period, npts={cfg['npts']}, "
+                               f"{'plain FP64' if prec == 'fp64' else 'mixed precision'}",
+                   "precision": prec, "step_method": args.step_method,
                    "parallelism": f"replicas x{d.world}",
-                   "l2": "inputs larger than L2: each step streams ~2 GB of per-crystallite work buffers",
+                   "l2": "inputs larger than L2: each step streams the per-crystallite work buffers (GBs)",
                    "layout": job.describe()},
         "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
+        "precision_forms": forms,
         "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": traffic,
                      "peak_source": "measured live: DFMA probe kernel (MEASURED_PEAKS.json has no FP64 figure)",

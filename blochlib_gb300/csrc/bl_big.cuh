@@ -37,26 +37,25 @@ __device__ void cta_mm_real(const double *A, int lda, const double *B, int ldb, 
 
 // Complex 2x2-tiled product into per-thread registers: acc[t] for this thread's tiles.
 // CONJ_A: use A^H (A stored k x m).  Tiles are numbered t = threadIdx.x + q*blockDim.x.
-template <bool CONJ_A>
-__device__ void cta_mm_cplx_regs(const double2 *A, int lda, const double2 *B, int ldb, int m, int n, int k,
-                                 double2 (&acc)[kBigTiles][4]) {
+template <bool CONJ_A, class C>
+__device__ void cta_mm_cplx_regs(const C *A, int lda, const C *B, int ldb, int m, int n, int k, C (&acc)[kBigTiles][4]) {
   const int tm = (m + 1) / 2, tn = (n + 1) / 2;
 #pragma unroll
   for (int q = 0; q < kBigTiles; ++q) {
     const int t = threadIdx.x + q * blockDim.x;
-    acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = cmk(0, 0);
+    acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = mkc<C>(0, 0);
     if (t >= tm * tn) continue;
     const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
     const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, n - 1);
-    double2 c00 = cmk(0, 0), c01 = c00, c10 = c00, c11 = c00;
+    C c00 = mkc<C>(0, 0), c01 = c00, c10 = c00, c11 = c00;
     for (int l = 0; l < k; ++l) {
-      double2 a0, a1;
+      C a0, a1;
       if (CONJ_A) {
         a0 = cconj(A[l * lda + i0]), a1 = cconj(A[l * lda + i1]);
       } else {
         a0 = A[i0 * lda + l], a1 = A[i1 * lda + l];
       }
-      const double2 b0 = B[l * ldb + j0], b1 = B[l * ldb + j1];
+      const C b0 = B[l * ldb + j0], b1 = B[l * ldb + j1];
       c00 = cfma(a0, b0, c00), c01 = cfma(a0, b1, c01), c10 = cfma(a1, b0, c10), c11 = cfma(a1, b1, c11);
     }
     acc[q][0] = c00, acc[q][1] = c01, acc[q][2] = c10, acc[q][3] = c11;
@@ -64,8 +63,8 @@ __device__ void cta_mm_cplx_regs(const double2 *A, int lda, const double2 *B, in
 }
 
 // Visits this thread's tile outputs: f(row, col, value).
-template <class F>
-__device__ void cta_tiles_store(int m, int n, const double2 (&acc)[kBigTiles][4], F f) {
+template <class C, class F>
+__device__ void cta_tiles_store(int m, int n, const C (&acc)[kBigTiles][4], F f) {
   const int tm = (m + 1) / 2, tn = (n + 1) / 2;
 #pragma unroll
   for (int q = 0; q < kBigTiles; ++q) {
@@ -184,7 +183,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big_dyson(DevSys s, int k) {
     const double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) Us[e] = Ub[at(bp + e, c, s.Cpad)];
     __syncthreads();
-    cta_mm_cplx_regs<false>(Us, b, As, b, b, b, b, acc);
+    cta_mm_cplx_regs<false, double2>(Us, b, As, b, b, b, b, acc);
     __syncthreads();
     double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
     cta_tiles_store(b, b, acc, [&](int r, int q, double2 v) {
@@ -195,27 +194,31 @@ __global__ void __launch_bounds__(kBigThreads) k_big_dyson(DevSys s, int k) {
   }
 }
 
-// One CTA per crystallite: W_i = A_{i+1} V_F, in place.
+// One CTA per crystallite: W_i = A_{i+1} V_F (in place over A in FP64; into the
+// single-precision W array in the mixed form).
+template <class C>
 __global__ void __launch_bounds__(kBigThreads) k_big_eigframe(DevSys s, int k) {
-  extern __shared__ double2 bsc[];
+  extern __shared__ __align__(16) unsigned char bsr[];
   const int c = blockIdx.x;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
-  double2 *Vs = bsc, *As = Vs + bb;
-  for (int e = threadIdx.x; e < bb; e += blockDim.x) Vs[e] = s.VF[at(bp + e, c, s.Cpad)];
-  double2 acc[kBigTiles][4];
+  C *Vs = reinterpret_cast<C *>(bsr), *As = Vs + bb;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) Vs[e] = cvt<C>(s.VF[at(bp + e, c, s.Cpad)]);
+  C acc[kBigTiles][4];
   for (int i = 0; i < s.n; ++i) {
-    double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
-    for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = Ab[at(bp + e, c, s.Cpad)];
+    const double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+    C *Wb = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = cvt<C>(Ab[at(bp + e, c, s.Cpad)]);
     __syncthreads();
-    cta_mm_cplx_regs<false>(As, b, Vs, b, b, b, b, acc);
-    cta_tiles_store(b, b, acc, [&](int r, int q, double2 v) { Ab[at(bp + r * b + q, c, s.Cpad)] = v; });
+    cta_mm_cplx_regs<false, C>(As, b, Vs, b, b, b, b, acc);
+    cta_tiles_store(b, b, acc, [&](int r, int q, C v) { Wb[at(bp + r * b + q, c, s.Cpad)] = v; });
     __syncthreads();
   }
 }
 
 // One CTA per (crystallite, step, big pair): Q^{ab} = W_a^H (M_ab W_b), M = D (or rho).
+template <class C>
 __global__ void __launch_bounds__(kBigThreads) k_big_qr(DevSys s, const int *__restrict__ plist, int npl) {
-  extern __shared__ double2 bsc[];
+  extern __shared__ __align__(16) unsigned char bsr[];
   const int pidx = blockIdx.x / (s.C * s.n);
   const int rem = blockIdx.x % (s.C * s.n);
   const int c = rem % s.C, i = rem / s.C;
@@ -223,33 +226,34 @@ __global__ void __launch_bounds__(kBigThreads) k_big_qr(DevSys s, const int *__r
   const bool isq = pr < s.npq;
   int a, b, off, moff, nitems;
   const double2 *M;
-  double2 *out;
+  C *out;
   if (isq) {
-    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = s.Q, nitems = s.nq;
+    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = Bufs<C>::Q(s), nitems = s.nq;
   } else {
     const int p2 = pr - s.npq;
-    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = s.R, nitems = s.nr;
+    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = Bufs<C>::R(s);
+    nitems = s.nr;
   }
   const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
-  const double2 *W = s.A + size_t(i) * s.S2 * s.Cpad;
-  double2 *Wa = bsc, *X = Wa + ba * ba;
+  const C *W = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
+  C *Wa = reinterpret_cast<C *>(bsr), *X = Wa + ba * ba;
   for (int e = threadIdx.x; e < ba * ba; e += blockDim.x) Wa[e] = W[at(pa + e, c, s.Cpad)];
   // X = M_ab W_b (M sparse: its zero entries are skipped, uniformly across the CTA)
   for (int e = threadIdx.x; e < ba * bb; e += blockDim.x) {
     const int l = e / bb, q = e % bb;
-    double2 acc = cmk(0, 0);
+    C acc = mkc<C>(0, 0);
     for (int m = 0; m < bb; ++m) {
       const double2 d = M[moff + l * bb + m];
       if (d.x == 0.0 && d.y == 0.0) continue;
-      acc = cfma(d, W[at(pb + m * bb + q, c, s.Cpad)], acc);
+      acc = cfma(cvt<C>(d), W[at(pb + m * bb + q, c, s.Cpad)], acc);
     }
     X[e] = acc;
   }
   __syncthreads();
-  double2 acc[kBigTiles][4];
-  cta_mm_cplx_regs<true>(Wa, ba, X, bb, ba, bb, ba, acc);
-  double2 *ob = out + size_t(i) * nitems * s.Cpad;
-  cta_tiles_store(ba, bb, acc, [&](int r, int q, double2 v) { ob[at(off + r * bb + q, c, s.Cpad)] = v; });
+  C acc[kBigTiles][4];
+  cta_mm_cplx_regs<true, C>(Wa, ba, X, bb, ba, bb, ba, acc);
+  C *ob = out + size_t(i) * nitems * s.Cpad;
+  cta_tiles_store(ba, bb, acc, [&](int r, int q, C v) { ob[at(off + r * bb + q, c, s.Cpad)] = v; });
 }
 
 // One CTA per crystallite: unitary eigen-decomposition of the big block of A_n by the

@@ -82,6 +82,31 @@ __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
 }
 __device__ __forceinline__ double chop1(double v, double eps) { return fabs(v) < eps ? 0.0 : v; }
 
+// Single-precision twins for the mixed-precision form (same names, float2 arguments).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 acc) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
+}
+__device__ __forceinline__ float2 cfmaconj(float2 a, float2 b, float2 acc) {
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, acc.y)));
+}
+template <class C>
+__device__ __forceinline__ C mkc(double r, double i);
+template <>
+__device__ __forceinline__ double2 mkc<double2>(double r, double i) { return make_double2(r, i); }
+template <>
+__device__ __forceinline__ float2 mkc<float2>(double r, double i) { return make_float2(float(r), float(i)); }
+template <class C>
+__device__ __forceinline__ C cvt(double2 v) { return mkc<C>(v.x, v.y); }
+template <class C>
+__device__ __forceinline__ double2 todbl(C v) { return make_double2(double(v.x), double(v.y)); }
+
 // ------------------------------------------------------------------ job description
 struct DevSys {
   int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
@@ -106,8 +131,31 @@ struct DevSys {
   const double *Rp, *t0, *w;
   // work buffers
   double2 *U, *A, *VF, *L, *Q, *R, *G, *Z, *partial;
+  // mixed-precision form: eigenframe, Q/R, Fave and FID arrays in single precision
+  int mixed;
+  float2 *Wf, *Qf, *Rf, *Gf, *Zf;
+  const float2 *twf;
   int warp_base;  // global warp index of this batch's first crystallite
   int *status;
+};
+
+// Precision-dependent arrays: W (eigenframe; in place over A in FP64), Q, R, G, Z, twiddles.
+template <class C> struct Bufs;
+template <> struct Bufs<double2> {
+  static __device__ double2 *W(const DevSys &s) { return s.A; }
+  static __device__ double2 *Q(const DevSys &s) { return s.Q; }
+  static __device__ double2 *R(const DevSys &s) { return s.R; }
+  static __device__ double2 *G(const DevSys &s) { return s.G; }
+  static __device__ double2 *Z(const DevSys &s) { return s.Z; }
+  static __device__ const double2 *tw(const DevSys &s) { return s.tw; }
+};
+template <> struct Bufs<float2> {
+  static __device__ float2 *W(const DevSys &s) { return s.Wf; }
+  static __device__ float2 *Q(const DevSys &s) { return s.Qf; }
+  static __device__ float2 *R(const DevSys &s) { return s.Rf; }
+  static __device__ float2 *G(const DevSys &s) { return s.Gf; }
+  static __device__ float2 *Z(const DevSys &s) { return s.Zf; }
+  static __device__ const float2 *tw(const DevSys &s) { return s.twf; }
 };
 
 // ------------------------------------------------------------------ eigen-solvers
@@ -701,8 +749,9 @@ __global__ void __launch_bounds__(kThreads) k_floquet(DevSys s, const int *__res
   }
 }
 
-// One thread per (crystallite, block, step): W_i = A_{i+1} V_F, in place.
-template <int B>
+// One thread per (crystallite, block, step): W_i = A_{i+1} V_F (in place over A in FP64;
+// into the single-precision W array in the mixed form).
+template <int B, class C>
 __global__ void __launch_bounds__(kThreads) k_eigframe(DevSys s, const int *__restrict__ blist, int nblist) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
   int c = int(tid % s.Cpad);
@@ -712,29 +761,31 @@ __global__ void __launch_bounds__(kThreads) k_eigframe(DevSys s, const int *__re
   int k = blist[rest / s.n];
   if (c >= s.C) return;
   const int bp = s.bpoff[k];
-  double2 V[B][B];
+  C V[B][B];
 #pragma unroll
   for (int r = 0; r < B; ++r)
 #pragma unroll
-    for (int q = 0; q < B; ++q) V[r][q] = s.VF[at(bp + r * B + q, c, s.Cpad)];
-  double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+    for (int q = 0; q < B; ++q) V[r][q] = cvt<C>(s.VF[at(bp + r * B + q, c, s.Cpad)]);
+  const double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+  C *Wb = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
 #pragma unroll
   for (int r = 0; r < B; ++r) {
-    double2 a[B];
+    C a[B];
 #pragma unroll
-    for (int l = 0; l < B; ++l) a[l] = Ab[at(bp + r * B + l, c, s.Cpad)];
+    for (int l = 0; l < B; ++l) a[l] = cvt<C>(Ab[at(bp + r * B + l, c, s.Cpad)]);
 #pragma unroll
     for (int q = 0; q < B; ++q) {
-      double2 acc = cmk(0, 0);
+      C acc = mkc<C>(0, 0);
 #pragma unroll
       for (int l = 0; l < B; ++l) acc = cfma(a[l], V[l][q], acc);
-      Ab[at(bp + r * B + q, c, s.Cpad)] = acc;
+      Wb[at(bp + r * B + q, c, s.Cpad)] = acc;
     }
   }
 }
 
 // One thread per (crystallite, step, pair): Q^{ab} = W_a^H D_ab W_b  (and R pairs).
 // compute.h:378-383: Qs[i] = adjprop(evect, adjprop(As[i+1], det)).
+template <class C>
 __global__ void __launch_bounds__(kThreads) k_qr(DevSys s) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
   int c = int(tid % s.Cpad);
@@ -747,31 +798,33 @@ __global__ void __launch_bounds__(kThreads) k_qr(DevSys s) {
   bool isq = pr < s.npq;
   int a, b, off, moff;
   const double2 *M;
-  double2 *out;
+  C *out;
   int nitems;
   if (isq) {
-    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = s.Q, nitems = s.nq;
+    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = Bufs<C>::Q(s), nitems = s.nq;
   } else {
     int p2 = pr - s.npq;
-    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = s.R, nitems = s.nr;
+    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = Bufs<C>::R(s);
+    nitems = s.nr;
   }
   const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
   if (ba > kMaxBlock || bb > kMaxBlock) return;  // k_big_qr handles pairs with a large block
-  const double2 *W = s.A + size_t(i) * s.S2 * s.Cpad;
-  double2 X[kMaxBlock * kMaxBlock];
+  const C *W = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
+  C X[kMaxBlock * kMaxBlock];
   // X = M_ab W_b  (ba x bb)
   for (int l = 0; l < ba; ++l)
-    for (int q = 0; q < bb; ++q) X[l * bb + q] = cmk(0, 0);
+    for (int q = 0; q < bb; ++q) X[l * bb + q] = mkc<C>(0, 0);
   for (int l = 0; l < ba; ++l)
     for (int m = 0; m < bb; ++m) {
-      double2 d = M[moff + l * bb + m];
-      if (d.x == 0.0 && d.y == 0.0) continue;
+      double2 d2 = M[moff + l * bb + m];
+      if (d2.x == 0.0 && d2.y == 0.0) continue;
+      const C d = cvt<C>(d2);
       for (int q = 0; q < bb; ++q) X[l * bb + q] = cfma(d, W[at(pb + m * bb + q, c, s.Cpad)], X[l * bb + q]);
     }
-  double2 *ob = out + size_t(i) * nitems * s.Cpad;
+  C *ob = out + size_t(i) * nitems * s.Cpad;
   for (int r = 0; r < ba; ++r)
     for (int q = 0; q < bb; ++q) {
-      double2 acc = cmk(0, 0);
+      C acc = mkc<C>(0, 0);
       for (int l = 0; l < ba; ++l) acc = cfmaconj(W[at(pa + l * ba + r, c, s.Cpad)], X[l * bb + q], acc);
       ob[at(off + r * bb + q, c, s.Cpad)] = acc;
     }
@@ -873,8 +926,8 @@ __global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
 // of length M = 2^logM held in shared memory as X[i * CG + cc], input in bit-reversed
 // order, output in natural order.  tw[k] = exp(-2 pi i k / M), k < M/2.  Y (optional) is
 // transformed alongside X.  Ends with a barrier.
-template <int CG>
-__device__ void fft_dit(double2 *X, double2 *Y, int M, int logM, const double2 *__restrict__ tw) {
+template <int CG, class C>
+__device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw) {
   const int nb = (M / 2) * CG;
   for (int st = 0; st < logM; ++st) {
     const int h = 1 << st, tstride = M >> (st + 1);
@@ -883,15 +936,15 @@ __device__ void fft_dit(double2 *X, double2 *Y, int M, int logM, const double2 *
       const int pos = b & (h - 1), grp = b >> st;
       const int i0 = ((grp << (st + 1)) + pos) * CG + cc, i1 = i0 + h * CG;
       if (st == 0) {
-        double2 a = X[i0], d = X[i1];
+        C a = X[i0], d = X[i1];
         X[i0] = cadd(a, d), X[i1] = csub(a, d);
         if (Y) {
           a = Y[i0], d = Y[i1];
           Y[i0] = cadd(a, d), Y[i1] = csub(a, d);
         }
       } else {
-        const double2 w = tw[pos * tstride];
-        double2 a = X[i0], t = cmul(w, X[i1]);
+        const C w = tw[pos * tstride];
+        C a = X[i0], t = cmul(w, X[i1]);
         X[i0] = cadd(a, t), X[i1] = csub(a, t);
         if (Y) {
           a = Y[i0], t = cmul(w, Y[i1]);
@@ -909,40 +962,41 @@ __device__ void fft_dit(double2 *X, double2 *Y, int M, int logM, const double2 *
 // Then G_p = Lin_p + z Lin_{p-n} (the same G as k_fave).  When r = conj(q) (rho = (D+D^H)/2
 // and D has no block pair (b,a) for this element) the product is |FFT(q)|^2 and the second
 // forward transform is skipped.
-template <int CG>
+template <int CG, class C>
 __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
-  extern __shared__ double2 smem[];
+  extern __shared__ __align__(16) unsigned char fsm_raw[];
   const int M = s.M, logM = s.logM, n = s.n;
-  double2 *X = smem, *Y = smem + size_t(M) * CG;
-  __shared__ double2 zc[CG];
+  C *X = reinterpret_cast<C *>(fsm_raw), *Y = X + size_t(M) * CG;
+  __shared__ C zc[CG];
   const int groups = s.Cpad / CG;
   const int e = blockIdx.x / groups;
   const int c0 = (blockIdx.x % groups) * CG;
   const int eq = s.eq[e], erev = s.erev[e], er = s.er[e];
   const bool autoc = s.rosym && erev < 0;
   const size_t qstride = size_t(s.nq) * s.Cpad, rstride = size_t(s.nr) * s.Cpad;
+  const C *Qb = Bufs<C>::Q(s), *Rb = Bufs<C>::R(s);
   const double nt = double(n) * s.tau;
   // per crystallite of the group: w_rs = chop((l_r - l_s)/(i n tau), 1e-10), z = e^{i n tau w},
-  // and the powers z^j of the FID reconstruction
+  // and the powers z^j of the FID reconstruction (always computed in FP64)
   for (int idx = threadIdx.x; idx < CG * (s.J + 1); idx += blockDim.x) {
     const int cc = idx % CG, j = idx / CG, c = c0 + cc;
     if (c >= s.C) continue;
     double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
     double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
-    if (j == s.J) zc[cc] = cexp(cmk(-nt * w.y, nt * w.x));
-    else s.Z[at(j * s.ne + e, c, s.Cpad)] = cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x));
+    if (j == s.J) zc[cc] = cvt<C>(cexp(cmk(-nt * w.y, nt * w.x)));
+    else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x)));
   }
   // load q (and conj r) zero-padded, bit-reversed
   for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
     const int cc = idx % CG, i = idx / CG, c = c0 + cc;
     const int ri = int(__brev(unsigned(i)) >> (32 - logM));
-    double2 q = cmk(0, 0), y = cmk(0, 0);
+    C q = mkc<C>(0, 0), y = mkc<C>(0, 0);
     if (i < n && c < s.C) {
-      q = s.Q[i * qstride + at(eq, c, s.Cpad)];
+      q = Qb[i * qstride + at(eq, c, s.Cpad)];
       if (!autoc) {
-        double2 r;
-        if (s.rosym) r = cadd(cconj(q), s.Q[i * qstride + at(erev, c, s.Cpad)]);
-        else r = s.R[i * rstride + at(er, c, s.Cpad)];
+        C r;
+        if (s.rosym) r = cadd(cconj(q), Qb[i * qstride + at(erev, c, s.Cpad)]);
+        else r = Rb[i * rstride + at(er, c, s.Cpad)];
         y = cconj(r);
       }
     }
@@ -950,11 +1004,11 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     if (!autoc) Y[ri * CG + cc] = y;
   }
   __syncthreads();
-  fft_dit<CG>(X, autoc ? nullptr : Y, M, logM, s.tw);
+  fft_dit<CG, C>(X, autoc ? nullptr : Y, M, logM, Bufs<C>::tw(s));
   // conj of the cross spectrum, in place in X (same index read and written)
   for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
-    double2 x = X[idx];
-    if (autoc) X[idx] = cmk(x.x * x.x + x.y * x.y, 0.0);
+    C x = X[idx];
+    if (autoc) X[idx] = mkc<C>(x.x * x.x + x.y * x.y, 0.0);
     else X[idx] = cconj(cmul(x, cconj(Y[idx])));
   }
   __syncthreads();
@@ -964,18 +1018,19 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
   }
   __syncthreads();
-  fft_dit<CG>(Y, nullptr, M, logM, s.tw);
+  fft_dit<CG, C>(Y, nullptr, M, logM, Bufs<C>::tw(s));
   const double invM = 1.0 / double(M);
+  C *Gb = Bufs<C>::G(s);
   for (int idx = threadIdx.x; idx < n * CG; idx += blockDim.x) {
     const int cc = idx % CG, p = idx / CG, c = c0 + cc;
     if (c >= s.C) continue;
-    double2 lp = cscale(cconj(Y[p * CG + cc]), invM);
-    double2 g = lp;
+    C lp = cscale(cconj(Y[p * CG + cc]), invM);
+    C g = lp;
     if (p > 0) {
-      double2 lm = cscale(cconj(Y[(M + p - n) * CG + cc]), invM);
+      C lm = cscale(cconj(Y[(M + p - n) * CG + cc]), invM);
       g = cfma(zc[cc], lm, lp);
     }
-    s.G[at(p * s.ne + e, c, s.Cpad)] = g;
+    Gb[at(p * s.ne + e, c, s.Cpad)] = g;
   }
 }
 
@@ -985,6 +1040,7 @@ constexpr int kFidJT = 4, kFidPT = 4;
 
 // One thread per (crystallite, tile of kFidJT j's, tile of kFidPT p's); lanes are
 // 32 consecutive crystallites, reduced with the powder weights by warp shuffles.
+template <class C>
 __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
   int c = int(tid % s.Cpad);
@@ -993,18 +1049,19 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   if (rest >= long(npt) * njt) return;  // warp-uniform: whole warp leaves together
   int pt = int(rest % npt), jt = int(rest / npt);
   int p0 = pt * kFidPT, j0 = jt * kFidJT;
-  double2 acc[kFidJT][kFidPT];
+  C acc[kFidJT][kFidPT];
 #pragma unroll
   for (int a = 0; a < kFidJT; ++a)
 #pragma unroll
-    for (int b = 0; b < kFidPT; ++b) acc[a][b] = cmk(0, 0);
+    for (int b = 0; b < kFidPT; ++b) acc[a][b] = mkc<C>(0, 0);
+  const C *Zb = Bufs<C>::Z(s), *Gb = Bufs<C>::G(s);
   if (c < s.C) {
     for (int e = 0; e < s.ne; ++e) {
-      double2 zj[kFidJT], gp[kFidPT];
+      C zj[kFidJT], gp[kFidPT];
 #pragma unroll
-      for (int a = 0; a < kFidJT; ++a) zj[a] = (j0 + a < s.J) ? s.Z[at((j0 + a) * s.ne + e, c, s.Cpad)] : cmk(0, 0);
+      for (int a = 0; a < kFidJT; ++a) zj[a] = (j0 + a < s.J) ? Zb[at((j0 + a) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
-      for (int b = 0; b < kFidPT; ++b) gp[b] = (p0 + b < s.n) ? s.G[at((p0 + b) * s.ne + e, c, s.Cpad)] : cmk(0, 0);
+      for (int b = 0; b < kFidPT; ++b) gp[b] = (p0 + b < s.n) ? Gb[at((p0 + b) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
       for (int a = 0; a < kFidJT; ++a)
 #pragma unroll
@@ -1018,7 +1075,7 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   for (int a = 0; a < kFidJT; ++a)
 #pragma unroll
     for (int b = 0; b < kFidPT; ++b) {
-      double2 v = cscale(acc[a][b], wc);
+      double2 v = cscale(todbl(acc[a][b]), wc);  // powder weight and the warp sum in FP64
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
@@ -1116,6 +1173,8 @@ struct JobImpl {
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
+  DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
+  int mixed = 0;
   DevBuf<double> Rp_b, t0_b, w_b;
   std::vector<double> h_Rp, h_t0, h_w;  // all virtual crystallites (C * gammaloop)
   int Ceff = 0;
@@ -1153,7 +1212,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.ctx = &ctx;
   J.P = p;
   CUDA_OK(cudaSetDevice(ctx.device));
-  if (p.precision != 0) throw Error(5, "only the FP64 precision mode is implemented");
+  if (p.precision != 0 && p.precision != 1) throw Error(1, "precision must be 0 (FP64) or 1 (mixed)");
   if (p.step_method != 0 && p.step_method != 1) throw Error(1, "step_method must be 0 (eigh) or 1 (Taylor)");
   if (p.fave_method < 0 || p.fave_method > 2) throw Error(1, "fave_method must be 0 (auto), 1 (direct) or 2 (FFT)");
   if (p.npts <= 0) throw Error(1, "npts must be positive");
@@ -1291,9 +1350,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.sin_rotb = std::sin(p.rotb_deg * d2r);
   // batch size from the memory budget
   const size_t nsteps = J.is_static ? 0 : size_t(J.n);  // U, A, Q, R exist only when spinning
-  size_t per_c = sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + nsteps * (J.nq + J.nr) + size_t(J.n) * J.ne +
-                                    size_t(J.J) * J.ne) +
-                 sizeof(double) * 11;
+  // mixed form (spinning only): eigenframe W, Q/R, Fave G and z powers Z in single precision
+  J.mixed = (p.precision == 1 && !J.is_static) ? 1 : 0;
+  const size_t wide = nsteps * (J.nq + J.nr) + size_t(J.n) * J.ne + size_t(J.J) * J.ne;
+  size_t per_c = J.mixed ? sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N) + sizeof(float2) * (nsteps * L.S2 + wide)
+                         : sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + wide);
+  per_c += sizeof(double) * 11;
   size_t budget = ctx.hbm_budget ? ctx.hbm_budget : (size_t(16) << 30);
   long cb = long(budget / std::max<size_t>(per_c, 1));
   cb = (cb / 32) * 32;
@@ -1323,10 +1385,14 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     }
     CUDA_OK(cudaFuncSetAttribute(k_big_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_step)));
     CUDA_OK(cudaFuncSetAttribute(k_big_dyson, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
-    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
+    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(J.big_smem_mat)));
+    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(J.big_smem_mat)));
     CUDA_OK(cudaFuncSetAttribute(k_big_floquet, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
     if (J.big_smem_qr)
-      CUDA_OK(cudaFuncSetAttribute(k_big_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_qr)));
+      for (auto f : {k_big_qr<double2>, k_big_qr<float2>})
+        CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_qr)));
   }
   J.blist.resize(kMaxBlock + 1);
   cudaStream_t st = ctx.stream;
@@ -1362,10 +1428,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.A.alloc(std::max<size_t>(1, nsteps * L.S2 * Cb));
   J.VF.alloc(size_t(L.S2) * Cb);
   J.Lb.alloc(size_t(N) * Cb);
-  J.Q.alloc(std::max<size_t>(1, nsteps * J.nq * Cb));
-  J.R.alloc(std::max<size_t>(1, nsteps * J.nr * Cb));
-  J.G.alloc(std::max<size_t>(1, size_t(J.n) * J.ne * Cb));
-  J.Z.alloc(std::max<size_t>(1, size_t(J.J) * J.ne * Cb));
+  const size_t nQ = std::max<size_t>(1, nsteps * J.nq * Cb), nR = std::max<size_t>(1, nsteps * J.nr * Cb);
+  const size_t nG = std::max<size_t>(1, size_t(J.n) * J.ne * Cb), nZ = std::max<size_t>(1, size_t(J.J) * J.ne * Cb);
+  if (J.mixed) {
+    J.Wf.alloc(std::max<size_t>(1, nsteps * L.S2 * Cb));
+    J.Qf.alloc(nQ), J.Rf.alloc(nR), J.Gf.alloc(nG), J.Zf.alloc(nZ);
+    J.Q.alloc(1), J.R.alloc(1), J.G.alloc(1), J.Z.alloc(1);
+  } else {
+    J.Q.alloc(nQ), J.R.alloc(nR), J.G.alloc(nG), J.Z.alloc(nZ);
+  }
   J.partial.alloc(size_t(J.nwarps_total) * p.npts);
   J.fid.alloc(p.npts);
   CUDA_OK(cudaMemsetAsync(J.partial.p, 0, J.partial.n * sizeof(double2), st));
@@ -1416,21 +1487,25 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   // FFT correlation up to M = 4096 (its shared-memory tile is M * max(1, 2048/M) * 32 B)
   if (p.fave_method == 2 && s.M > 4096) throw Error(5, "FFT Fave supports at most 2048 steps per period");
   s.fave_method = (p.fave_method != 1 && s.M <= 4096) ? 1 : 0;
+  if (J.mixed && !s.fave_method) throw Error(5, "the mixed form needs the FFT correlation (at most 2048 steps)");
   {
     std::vector<double2> tw(s.M / 2);
     for (int k = 0; k < s.M / 2; ++k) {
       double a = kPi2 * double(k) / double(s.M);
       tw[k] = make_double2(std::cos(a), -std::sin(a));
     }
+    std::vector<float2> twf(tw.size());
+    for (size_t k = 0; k < tw.size(); ++k) twf[k] = make_float2(float(tw[k].x), float(tw[k].y));
     g_upload_counter = &J.h2d;
     J.tw.upload(tw, st);
+    J.twf.upload(twf, st);
     g_upload_counter = nullptr;
     s.tw = J.tw.p;
+    s.twf = J.twf.p;
     size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * std::max(1, std::min(8, 2048 / s.M));
-    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
-    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
-    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
-    CUDA_OK(cudaFuncSetAttribute(k_fave_fft<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+    for (auto f : {k_fave_fft<8, double2>, k_fave_fft<4, double2>, k_fave_fft<2, double2>, k_fave_fft<1, double2>,
+                   k_fave_fft<8, float2>, k_fave_fft<4, float2>, k_fave_fft<2, float2>, k_fave_fft<1, float2>})
+      CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
   }
   s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
   s.is_static = J.is_static, s.dt = J.dt, s.srp = J.srp.p, s.seo = J.seo.p;
@@ -1441,6 +1516,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
   s.ra = J.ra.p, s.rb = J.rb.p, s.roff = J.roff.p, s.rhooff = J.rhooff.p;
   s.Dblk = J.Dblk.p, s.Rhoblk = J.Rhoblk.p;
+  s.mixed = J.mixed;
+  s.Wf = J.Wf.p, s.Qf = J.Qf.p, s.Rf = J.Rf.p, s.Gf = J.Gf.p, s.Zf = J.Zf.p;
   s.eq = J.eq.p, s.erev = J.erev.p, s.er = J.er.p, s.erg = J.erg.p, s.esg = J.esg.p;
   s.U = J.U.p, s.A = J.A.p, s.VF = J.VF.p, s.L = J.Lb.p, s.Q = J.Q.p, s.R = J.R.p, s.G = J.G.p, s.Z = J.Z.p;
   s.partial = J.partial.p;
@@ -1471,7 +1548,10 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
       break;
     case 1: k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl); break;
     case 2: k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl); break;
-    case 3: k_eigframe<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl); break;
+    case 3:
+      if (s.mixed) k_eigframe<B, float2><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      else k_eigframe<B, double2><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      break;
   }
   ++J.launches;
 }
@@ -1496,7 +1576,10 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         break;
       case 1: k_big_dyson<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
       case 2: k_big_floquet<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
-      case 3: k_big_eigframe<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
+      case 3:
+        if (s.mixed) k_big_eigframe<float2><<<unsigned(s.C), kBigThreads, smat, st>>>(s, k);
+        else k_big_eigframe<double2><<<unsigned(s.C), kBigThreads, smat, st>>>(s, k);
+        break;
     }
     ++J.launches;
   }
@@ -1535,11 +1618,15 @@ void Job::run() {
     long Cp = s.Cpad;
     mark_begin(J, 4);
     if (!J.is_static && J.npq + J.npr > 0) {
-      k_qr<<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
+      if (s.mixed) k_qr<float2><<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
+      else k_qr<double2><<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
       ++J.launches;
       if (!J.big_pairs_h.empty()) {
         unsigned grid = unsigned(J.big_pairs_h.size()) * unsigned(s.C) * unsigned(J.n);
-        k_big_qr<<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
+        if (s.mixed)
+          k_big_qr<float2><<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
+        else
+          k_big_qr<double2><<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
         ++J.launches;
       }
     }
@@ -1554,10 +1641,22 @@ void Job::run() {
         size_t shm = sizeof(double2) * size_t(s.M) * cg * 2;
         unsigned grid = unsigned(J.ne) * unsigned(Cp / cg);
         switch (cg) {
-          case 8: k_fave_fft<8><<<grid, 128, shm, st>>>(s); break;
-          case 4: k_fave_fft<4><<<grid, 128, shm, st>>>(s); break;
-          case 2: k_fave_fft<2><<<grid, 128, shm, st>>>(s); break;
-          default: k_fave_fft<1><<<grid, 128, shm, st>>>(s); break;
+          case 8:
+            if (s.mixed) k_fave_fft<8, float2><<<grid, 128, shm / 2, st>>>(s);
+            else k_fave_fft<8, double2><<<grid, 128, shm, st>>>(s);
+            break;
+          case 4:
+            if (s.mixed) k_fave_fft<4, float2><<<grid, 128, shm / 2, st>>>(s);
+            else k_fave_fft<4, double2><<<grid, 128, shm, st>>>(s);
+            break;
+          case 2:
+            if (s.mixed) k_fave_fft<2, float2><<<grid, 128, shm / 2, st>>>(s);
+            else k_fave_fft<2, double2><<<grid, 128, shm, st>>>(s);
+            break;
+          default:
+            if (s.mixed) k_fave_fft<1, float2><<<grid, 128, shm / 2, st>>>(s);
+            else k_fave_fft<1, double2><<<grid, 128, shm, st>>>(s);
+            break;
         }
       } else {
         int ntile = (J.n + kFavePT - 1) / kFavePT;
@@ -1570,7 +1669,8 @@ void Job::run() {
     // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
     int npt = (J.n + kFidPT - 1) / kFidPT, njt = (J.J + kFidJT - 1) / kFidJT;
     mark_begin(J, 6);
-    k_fid<<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
+    if (s.mixed) k_fid<float2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
+    else k_fid<double2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
     ++J.launches;
     mark_end(J, 6, 1);
   }

@@ -49,7 +49,7 @@ def oracle_fid(job_text, rows):
     return out.view(np.complex128), float(sw[0])
 
 
-def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_method=None):
+def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_method=None, precision=0):
     """The CUDA path through the C ABI (oneFID.FID)."""
     import blochlib_gb300 as bl
     lines, kv = parse_job(job_text)
@@ -57,7 +57,8 @@ def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_me
     rows = np.asarray(rows, dtype=np.float64)
     pw = bl.powder.from_arrays(theta=rows[:, 1], phi=rows[:, 0], gamma=rows[:, 2], weight=rows[:, 3])
     drv = bl.oneFID(sys_, int(kv["npts"]), float(kv["sw"]), float(kv["wr"]), float(kv["rotb"]),
-                    float(kv.get("start", 0.0)), ctx=ctx, step_method=step_method, fave_method=fave_method)
+                    float(kv.get("start", 0.0)), precision=precision, ctx=ctx, step_method=step_method,
+                    fave_method=fave_method)
     fid = drv.FID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]))
     return (fid, drv.sw) if return_sw else fid
 
