@@ -76,6 +76,13 @@ _SIGS = {
     "bl_powder_fid_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_rotation3": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "bl_rotation2": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "bl_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_server_destroy": (None, [ctypes.c_void_p]),
+    "bl_server_submit": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_longlong)]),
+    "bl_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "bl_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
+    "bl_server_stats": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_longlong)] * 3),
 }
 
 STAGES = 8
@@ -401,6 +408,67 @@ class oneFID:
         self.sw = float(sw_out[0])
         self.fid_ = out
         return out
+
+
+class Server:
+    """Serving loop with continuous batching (bl_server): slots of device memory, one
+    stream each; submit() returns a ticket, poll()/result() collect the FID and latency."""
+    QUEUED, RUNNING, DONE, FAILED, CANCELLED = 0, 1, 2, 3, 4
+
+    def __init__(self, device=0, slots=8, slot_bytes=1 << 30):
+        h = ctypes.c_void_p()
+        _check(load().bl_server_create(int(device), int(slots), int(slot_bytes), ctypes.byref(h)))
+        self._h = h
+        self._npts = {}
+
+    def submit(self, sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, step_method=None,
+               fave_method=None):
+        n = sys.dim()
+        ro, det = _cmat(ro, n), _cmat(det, n)
+        p = FidParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
+                      _step_method(step_method), _fave_method(fave_method))
+        t = ctypes.c_longlong()
+        _check(load().bl_server_submit(self._h, sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(p), ctypes.byref(t)))
+        self._npts[t.value] = int(npts)
+        return t.value
+
+    def state(self, ticket):
+        st = ctypes.c_int()
+        _check(load().bl_server_poll(self._h, int(ticket), ctypes.byref(st), None, None, None))
+        return st.value
+
+    def result(self, ticket):
+        """(state, fid, sw, latency_ms) once finished (releases the ticket), else (state, None, None, None)."""
+        st = ctypes.c_int()
+        fid = np.zeros(self._npts[ticket], dtype=np.complex128)
+        sw, lat = ctypes.c_double(), ctypes.c_double()
+        _check(load().bl_server_poll(self._h, int(ticket), ctypes.byref(st), _ptr(fid), ctypes.byref(sw),
+                                     ctypes.byref(lat)))
+        if st.value >= self.DONE:
+            self._npts.pop(ticket, None)
+            if st.value == self.FAILED:
+                raise BlochError(5, load().bl_last_error().decode())
+            return st.value, (fid if st.value == self.DONE else None), sw.value, lat.value
+        return st.value, None, None, None
+
+    def cancel(self, ticket):
+        _check(load().bl_server_cancel(self._h, int(ticket)))
+
+    def stats(self):
+        q, r, d = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        _check(load().bl_server_stats(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(d)))
+        return q.value, r.value, d.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bl_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def rotationMatrix3D(a, b, g=None):

@@ -58,6 +58,7 @@ def build_library(verbose=False, force=False):
                                  "-Xptxas", "-v" if verbose else "-O3"]),
         (CSRC / "bl_host.cc", ["g++", "-O2", "-std=c++17", "-fPIC"]),
         (CSRC / "bl_capi.cc", ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{cuda / 'include'}"]),
+        (CSRC / "bl_server.cc", ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{cuda / 'include'}"]),
     ]
     objs = []
     jobs = []
@@ -66,7 +67,7 @@ def build_library(verbose=False, force=False):
         objs.append(obj)
         if force or _stale(obj, [src, *headers]):
             jobs.append(cmd + ["-c", str(src), "-o", str(obj)])
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    with ThreadPoolExecutor(max_workers=4) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
         for o in outs:

@@ -8,6 +8,7 @@
 #include "../../include/blochlib_gb300.h"
 #include "bl_engine.h"
 #include "bl_host.h"
+#include "bl_server.h"
 
 struct bl_ctx {
   bl::Context c;
@@ -290,6 +291,62 @@ bl_status bl_rotation2(double phi, double theta, double *R9) {
   double R[3][3];
   bl::rotation2(phi, theta, R);
   for (int i = 0; i < 9; ++i) R9[i] = R[i / 3][i % 3];
+  return BL_OK;
+}
+
+}  // extern "C"
+
+struct bl_server {
+  std::unique_ptr<bl::Server> s;
+};
+
+extern "C" {
+
+bl_status bl_server_create(int device, int slots, size_t slot_bytes, bl_server **out) {
+  if (!out) return fail(BL_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  return guarded([&] {
+    std::unique_ptr<bl_server> h(new bl_server);
+    h->s.reset(new bl::Server(device, slots, slot_bytes));
+    *out = h.release();
+  });
+}
+
+void bl_server_destroy(bl_server *srv) { delete srv; }
+
+bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
+                           const double *det, const bl_fid_params *params, long long *ticket) {
+  if (!srv || !sys || !pw || !ro || !det || !params || !ticket) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    int N = sys->s.dim();
+    if (params->npts <= 0) throw bl::Error(BL_ERR_INVALID, "npts must be positive");
+    *ticket = srv->s->submit(sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params));
+  });
+}
+
+bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *fid_out, double *sw_out,
+                         double *latency_ms) {
+  if (!srv || !state) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    std::string err;
+    *state = srv->s->poll(ticket, fid_out, sw_out, latency_ms, &err);
+    if (*state == 3) g_err = err;
+  });
+}
+
+bl_status bl_server_cancel(bl_server *srv, long long ticket) {
+  if (!srv) return fail(BL_ERR_INVALID, "null server");
+  if (!srv->s->cancel(ticket)) return fail(BL_ERR_INVALID, "ticket is not queued");
+  return BL_OK;
+}
+
+bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done) {
+  if (!srv) return fail(BL_ERR_INVALID, "null server");
+  int64_t q = 0, r = 0, d = 0;
+  srv->s->stats(&q, &r, &d);
+  if (queued) *queued = q;
+  if (running) *running = r;
+  if (done) *done = d;
   return BL_OK;
 }
 

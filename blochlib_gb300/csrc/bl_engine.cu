@@ -1131,7 +1131,7 @@ Context::~Context() {
   if (stream) cudaStreamDestroy(stream);
 }
 
-static size_t *g_upload_counter = nullptr;  // set while a Job uploads its inputs
+static thread_local size_t *g_upload_counter = nullptr;  // set while a Job uploads its inputs
 
 // Bump allocator over a caller-provided device region.  Only the allocation-free entry
 // point (powder_fid_noalloc, below) installs one, for the duration of its own call.
@@ -1914,6 +1914,30 @@ void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, c
                          " MiB static device scratch of the allocation-free entry point: " + e.what());
     throw;
   }
+}
+
+// A resident Job whose every device buffer lives in [base, base + bytes): the serving loop
+// gives each slot such a region, so admitting a request allocates nothing.  The caller's
+// Context (device, stream) must outlive the Job; its hbm_budget is set here.
+std::unique_ptr<Job> job_in_region(Context &ctx, void *base, size_t bytes, const SpinSystem &sys, const Powder &pw,
+                                   const CMatrix &ro, const CMatrix &det, const FidParams &p) {
+  CUDA_OK(cudaSetDevice(ctx.device));
+  ScratchArena arena;
+  arena.base = static_cast<char *>(base);
+  arena.cap = bytes;
+  long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
+  long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
+  size_t ceff = size_t(pw.size()) * size_t(g) + 32;
+  size_t fixed = (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
+                 (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
+  if (fixed >= bytes) throw Error(4, "job does not fit a serving slot of " + std::to_string(bytes >> 20) + " MiB");
+  ctx.hbm_budget = bytes - fixed;
+  struct Scope {
+    ScratchArena *prev;
+    explicit Scope(ScratchArena *a) : prev(g_arena) { g_arena = a; }
+    ~Scope() { g_arena = prev; }
+  } scope(&arena);
+  return std::unique_ptr<Job>(new Job(ctx, sys, pw, ro, det, p));
 }
 
 }  // namespace bl

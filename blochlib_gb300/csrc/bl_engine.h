@@ -70,4 +70,8 @@ void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, c
                         const FidParams &p, double *fid_out, double *sw_out);
 size_t noalloc_scratch_bytes();
 
+// A Job whose device buffers are all carved from [base, base + bytes) (no allocation).
+std::unique_ptr<Job> job_in_region(Context &ctx, void *base, size_t bytes, const SpinSystem &sys, const Powder &pw,
+                                   const CMatrix &ro, const CMatrix &det, const FidParams &p);
+
 }  // namespace bl

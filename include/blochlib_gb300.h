@@ -142,6 +142,27 @@ bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powd
                                 const double *det, const bl_fid_params *params, double *fid_out,
                                 double *sw_out);
 
+/* Serving loop with continuous batching.  No counterpart in the reference beyond its MPI
+ * crystallite farm (src/QMspins/driver/oneFID.h:230-286, examples/solid-2.0/src/
+ * sequencerun.cc:435-526), which hands work to whichever worker finishes first; here whole
+ * jobs go to slots of device memory.  One device allocation of slots x slot_bytes at
+ * creation; a submitted job is admitted (FIFO) when a slot is free, built inside that slot
+ * (no further allocation; crystallites batched to fit it), and run on the slot's stream, so
+ * jobs in different slots overlap on the GPU.  A job whose 32-crystallite batch does not fit
+ * a slot fails with BL_ERR_NOMEM.  Inputs are copied at submission.
+ * Ticket states: 0 queued, 1 running, 2 done, 3 failed, 4 cancelled; -1 unknown ticket. */
+typedef struct bl_server bl_server;
+bl_status bl_server_create(int device, int slots, size_t slot_bytes, bl_server **out);
+void bl_server_destroy(bl_server *srv);  /* waits for running jobs */
+bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
+                           const double *det, const bl_fid_params *params, long long *ticket);
+/* *state as above.  When the job is done (or failed/cancelled) and fid_out is non-NULL, the
+ * FID (2*npts doubles) is copied and the ticket is released.  latency_ms: submit to done. */
+bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *fid_out, double *sw_out,
+                         double *latency_ms);
+bl_status bl_server_cancel(bl_server *srv, long long ticket);  /* queued jobs only */
+bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done);
+
 /* Cartesian rotation matrices of the reference, row-major 3x3 (radians):
  * 3-angle (powder orientation) and 2-angle (rotor phase phi, rotor tilt theta). */
 bl_status bl_rotation3(double alpha, double beta, double gamma, double *R9);

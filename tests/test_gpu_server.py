@@ -1,0 +1,71 @@
+"""The serving loop (bl_server): continuous batching of whole jobs over memory slots."""
+import time
+
+import numpy as np
+import pytest
+
+import blochlib_gb300 as bl
+from blochlib_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _job(cfg, count):
+    s = bl.SolidSys(cfg["lines"])
+    phi, theta, gamma, w = (np.asarray(x)[:count] for x in cfg["powder"])
+    pw = bl.powder.from_arrays(theta, phi, gamma, w)
+    return dict(sys=s, pw=pw, ro=s.op(cfg["rho"]), det=s.op(cfg["det"]), npts=cfg["npts"], sw=cfg["sw"],
+                wr=cfg["wr"], rotb=cfg["rotb"])
+
+
+def _wait(srv, tickets, timeout=120.0):
+    out, t0 = {}, time.time()
+    while len(out) < len(tickets):
+        for t in tickets:
+            if t in out:
+                continue
+            st, fid, sw, lat = srv.result(t)
+            if st >= srv.DONE:
+                out[t] = (st, fid, lat)
+        assert time.time() - t0 < timeout, "serving loop timed out"
+        time.sleep(0.002)
+    return out
+
+
+def test_result_is_the_same_alone_and_in_the_mix():
+    srv = bl.Server(0, slots=6, slot_bytes=512 << 20)
+    probe = _job(W.config(1), 128)
+    t = srv.submit(**probe)
+    alone = _wait(srv, [t])[t][1]
+    mix = [_job(W.config(3, i), 96) for i in range(24)]
+    tickets = []
+    for i, j in enumerate(mix):
+        tickets.append(srv.submit(**j))
+        if i == 11:
+            tp = srv.submit(**probe)
+    res = _wait(srv, tickets + [tp])
+    assert all(r[0] == srv.DONE for r in res.values())
+    np.testing.assert_array_equal(res[tp][1], alone)
+    # and equal to the direct (non-served) call
+    direct = bl.oneFID(probe["sys"], probe["npts"], probe["sw"], probe["wr"], probe["rotb"]).FID(
+        probe["pw"], probe["ro"], probe["det"])
+    np.testing.assert_array_equal(alone, direct)
+    q, r, d = srv.stats()
+    assert q == 0 and r == 0 and d >= 26
+    srv.close()
+
+
+def test_cancel_queued_and_reject_oversized():
+    srv = bl.Server(0, slots=1, slot_bytes=64 << 20)
+    j = _job(W.config(0), 64)
+    tickets = [srv.submit(**j) for _ in range(6)]
+    srv.cancel(tickets[-1])  # still queued behind five jobs on one slot
+    res = _wait(srv, tickets[:-1])
+    assert all(r[0] == srv.DONE for r in res.values())
+    st, fid, _, _ = srv.result(tickets[-1])
+    assert st == srv.CANCELLED and fid is None
+    big = _job(dict(W.config(1), sw=2000 * 20e3), 64)  # one warp needs > 64 MiB
+    tb = srv.submit(**big)
+    with pytest.raises(bl.BlochError):
+        _wait(srv, [tb])
+    srv.close()
