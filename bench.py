@@ -219,13 +219,168 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+# ------------------------------------------------------------------ batching and serving forms
+def _job_inputs(bl, cfg):
+    s = bl.SolidSys(cfg["lines"])
+    phi, theta, gamma, w = cfg["powder"]
+    pw = bl.powder.from_arrays(theta, phi, gamma, w)
+    return dict(sys=s, pw=pw, ro=s.op(cfg["rho"]), det=s.op(cfg["det"]), npts=cfg["npts"], sw=cfg["sw"],
+                wr=cfg["wr"], rotb=cfg["rotb"])
+
+
+def _drain(srv, tickets, timeout):
+    """Polls until every ticket finished or timeout; returns {ticket: (state, fid, latency)}."""
+    out, t0 = {}, time.perf_counter()
+    pending = list(tickets)
+    while pending and time.perf_counter() - t0 < timeout:
+        pending = [t for t in pending if not _collect(srv, t, out)]
+        if pending:
+            time.sleep(0.001)
+    return out, pending
+
+
+def _collect(srv, t, out):
+    """Stores (state, fid, latency_ms) of a finished ticket in out; False while it runs."""
+    if srv.state(t) < srv.DONE:
+        return False
+    import blochlib_gb300 as bl
+    try:
+        st, fid, _, lat = srv.result(t)
+    except bl.BlochError:
+        st, fid, lat = srv.FAILED, None, None
+    out[t] = (st, fid, lat)
+    return True
+
+
+def run_batch(args):
+    """c3: a set of seeded spin systems (2..7 1H, n 64..256, 1024 points, powders of 144..1154)
+    submitted at once to the serving loop; FIDs/s of the whole batch, mixed and FP64."""
+    import blochlib_gb300 as bl
+    from blochlib_gb300 import workloads as W
+    rank, world, local = dist_env()
+    cfgs = [W.config(3, i) for i in range(args.systems)]
+    jobs = [_job_inputs(bl, c) for c in cfgs]
+    peak = bl.probe_fp64_tflops(bl.Context(local))
+    clocks = Clocks(local)
+    clocks.start()
+    forms, fids = {}, {}
+    for prec in ("mixed", "fp64"):
+        srv = bl.Server(local, lanes=args.lanes, pool_bytes=args.pool_gib << 30)
+        warm = srv.submit(**jobs[0], precision=1 if prec == "mixed" else 0, step_method="taylor")
+        _drain(srv, [warm], 300)
+        flops0 = srv.stats()[3]
+        t0 = time.perf_counter()
+        tickets = [srv.submit(**j, precision=1 if prec == "mixed" else 0, step_method="taylor") for j in jobs]
+        res, pending = _drain(srv, tickets, 3600)
+        dt = time.perf_counter() - t0
+        flops = srv.stats()[3] - flops0
+        ok = [t for t in tickets if t in res and res[t][0] == srv.DONE]
+        lat = [res[t][2] for t in ok]
+        forms[prec] = {"fids_per_s": len(ok) / dt, "seconds": dt, "completed": len(ok), "failed": len(tickets) - len(ok),
+                       "tflops_algorithmic": flops / dt / 1e12,
+                       "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
+        fids[prec] = [res[t][1] for t in tickets]
+        srv.close()
+    clk = clocks.stop()
+    errs = [_rel(a, b) for a, b in zip(fids["mixed"], fids["fp64"]) if a is not None and b is not None]
+    forms["mixed"]["rel_err_vs_fp64_max"] = max(errs) if errs else None
+    forms["mixed_speedup_vs_fp64"] = forms["mixed"]["fids_per_s"] / forms["fp64"]["fids_per_s"]
+    if rank != 0:
+        return 0
+    dims = sorted({2 ** int(c["lines"][0].split()[1]) for c in cfgs})
+    print(json.dumps({
+        "metric": METRIC, "value": forms["mixed"]["fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["seconds"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded, workloads.py config 3)",
+        "config": {"workload": f"c3 batching form: {len(cfgs)} seeded systems, dims {dims}, n 64-256, 1024 points, "
+                               "powders 144/320/678/1154, all submitted at once", "lanes": args.lanes,
+                   "pool_gib": args.pool_gib, "precision": "mixed (FP64 row for comparison)"},
+        "latency_ms": forms["mixed"]["latency_ms"], "precision_forms": forms,
+        "roofline": {"bound": "fp64", "kernel": "whole batch (all stages)", "form": "fp64",
+                     "achieved": forms["fp64"]["tflops_algorithmic"], "peak": peak, "unit": "TFLOP/s",
+                     "frac": forms["fp64"]["tflops_algorithmic"] / peak if peak else None, "traffic": None,
+                     "peak_source": "measured live: DFMA probe kernel"},
+        "clocks": clk}))
+    return 0
+
+
+def run_serving(args):
+    """c4: Poisson request stream (seeded) of c3-like jobs plus 10% large (8 x 1H, dim 256, 100
+    crystallites; 9-10 spin jobs exceed the engine's block limit), for a fixed window; the
+    backlog left at the end is cancelled and reported.  Mixed and FP64 on the same stream."""
+    import blochlib_gb300 as bl
+    from blochlib_gb300 import workloads as W
+    rank, world, local = dist_env()
+    rng = np.random.default_rng(W.SEED0 + 4)
+    small = [_job_inputs(bl, W.config(3, 1000 + i)) for i in range(48)]
+    c2 = W.config(2)
+    large = [_job_inputs(bl, dict(c2, powder=W.subset(c2["powder"], 100, 100 * i))) for i in range(4)]
+    n_req = int(args.rate * args.duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
+    picks = [(large[rng.integers(len(large))] if rng.uniform() < 0.1 else small[rng.integers(len(small))])
+             for _ in range(n_req)]
+    forms = {}
+    for prec in ("mixed", "fp64"):
+        srv = bl.Server(local, lanes=args.lanes, pool_bytes=args.pool_gib << 30)
+        warm = srv.submit(**small[0], precision=1 if prec == "mixed" else 0, step_method="taylor")
+        _drain(srv, [warm], 300)
+        t0 = time.perf_counter()
+        done, open_ = {}, []
+        i = 0
+        while i < n_req:
+            now = time.perf_counter() - t0
+            while i < n_req and arrivals[i] <= now:
+                open_.append(srv.submit(**picks[i], precision=1 if prec == "mixed" else 0, step_method="taylor"))
+                i += 1
+            open_ = [t for t in open_ if not _collect(srv, t, done)]
+            time.sleep(0.0005)
+        window = time.perf_counter() - t0
+        drained, pending = _drain(srv, open_, args.drain)
+        done.update(drained)
+        cancelled = 0
+        for t in pending:
+            try:
+                srv.cancel(t)
+                cancelled += 1
+            except bl.BlochError:
+                pass  # already running: it finishes below
+        late, _ = _drain(srv, pending, 600)
+        total = time.perf_counter() - t0
+        ok = [v[2] for v in done.values() if v[0] == srv.DONE]
+        forms[prec] = {"offered_per_s": args.rate, "submitted": n_req, "completed": len(ok),
+                       "cancelled_backlog": cancelled,
+                       "finished_after_drain": sum(v[0] == srv.DONE for v in late.values()), "achieved_fids_per_s": len(ok) / total,
+                       "window_s": window, "total_s": total,
+                       "latency_ms": {"p50": float(np.percentile(ok, 50)) if ok else None,
+                                      "p99": float(np.percentile(ok, 99)) if ok else None}}
+        srv.close()
+    forms["mixed_speedup_vs_fp64"] = forms["mixed"]["achieved_fids_per_s"] / forms["fp64"]["achieved_fids_per_s"]
+    if rank != 0:
+        return 0
+    print(json.dumps({
+        "metric": METRIC, "value": forms["mixed"]["achieved_fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
+        "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["total_s"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic seeded Poisson stream (workloads.py)",
+        "config": {"workload": f"c4 serving form: Poisson {args.rate}/s for {args.duration} s, 90% c3-like, 10% "
+                               "8 x 1H dim 256 on 100 crystallites", "lanes": args.lanes, "pool_gib": args.pool_gib,
+                   "drain_s": args.drain},
+        "latency_ms": forms["mixed"]["latency_ms"], "precision_forms": forms}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"])
+    ap.add_argument("--systems", type=int, default=128, help="c3: number of seeded systems in the batch")
+    ap.add_argument("--lanes", type=int, default=16, help="c3/c4: serving lanes (CUDA streams)")
+    ap.add_argument("--pool-gib", type=int, default=128, help="c3/c4: serving memory pool (GiB)")
+    ap.add_argument("--rate", type=float, default=200.0, help="c4: offered requests per second")
+    ap.add_argument("--duration", type=float, default=10.0, help="c4: arrival window (s)")
+    ap.add_argument("--drain", type=float, default=20.0, help="c4: wait after the window (s)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -240,6 +395,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "c3":
+        return run_batch(args)
+    if args.config == "c4":
+        return run_serving(args)
     args.warmup = max(args.warmup, 3)
     prec = args.precision or ("mixed" if args.config == "c2" else "fp64")
     import blochlib_gb300 as bl

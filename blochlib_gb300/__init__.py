@@ -76,13 +76,15 @@ _SIGS = {
     "bl_powder_fid_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_rotation3": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "bl_rotation2": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
+    "bl_job_bytes": (ctypes.c_int, [ctypes.c_int] + [ctypes.c_void_p] * 5 + [ctypes.POINTER(ctypes.c_size_t)] * 2),
     "bl_server_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "bl_server_destroy": (None, [ctypes.c_void_p]),
     "bl_server_submit": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_longlong)]),
     "bl_server_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.POINTER(ctypes.c_int),
                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "bl_server_cancel": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
-    "bl_server_stats": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_longlong)] * 3),
+    "bl_server_stats": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_longlong)] * 3 +
+                        [ctypes.POINTER(ctypes.c_double)]),
 }
 
 STAGES = 8
@@ -410,14 +412,29 @@ class oneFID:
         return out
 
 
+def job_bytes(sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, step_method=None, fave_method=None,
+              device=0):
+    """(min_bytes, full_bytes): device memory of the job with 32 crystallites per batch and
+    with all crystallites in one batch (bl_job_bytes; host-side planning only)."""
+    n = sys.dim()
+    ro, det = _cmat(ro, n), _cmat(det, n)
+    p = FidParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
+                  _step_method(step_method), _fave_method(fave_method))
+    lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
+    _check(load().bl_job_bytes(int(device), sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(p), ctypes.byref(lo),
+                               ctypes.byref(hi)))
+    return lo.value, hi.value
+
+
 class Server:
-    """Serving loop with continuous batching (bl_server): slots of device memory, one
-    stream each; submit() returns a ticket, poll()/result() collect the FID and latency."""
+    """Serving loop with continuous batching (bl_server): `lanes` CUDA streams sharing one
+    pool of device memory; requests are sized at submit() and admitted first come first
+    served by free memory; poll()/result() collect the FID and latency."""
     QUEUED, RUNNING, DONE, FAILED, CANCELLED = 0, 1, 2, 3, 4
 
-    def __init__(self, device=0, slots=8, slot_bytes=1 << 30):
+    def __init__(self, device=0, lanes=8, pool_bytes=16 << 30):
         h = ctypes.c_void_p()
-        _check(load().bl_server_create(int(device), int(slots), int(slot_bytes), ctypes.byref(h)))
+        _check(load().bl_server_create(int(device), int(lanes), int(pool_bytes), ctypes.byref(h)))
         self._h = h
         self._npts = {}
 
@@ -455,9 +472,10 @@ class Server:
         _check(load().bl_server_cancel(self._h, int(ticket)))
 
     def stats(self):
-        q, r, d = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
-        _check(load().bl_server_stats(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(d)))
-        return q.value, r.value, d.value
+        """(queued, running, finished, algorithmic flop of the completed jobs)."""
+        q, r, d, f = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_double()
+        _check(load().bl_server_stats(self._h, ctypes.byref(q), ctypes.byref(r), ctypes.byref(d), ctypes.byref(f)))
+        return q.value, r.value, d.value, f.value
 
     def close(self):
         if getattr(self, "_h", None):

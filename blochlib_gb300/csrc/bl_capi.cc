@@ -302,12 +302,21 @@ struct bl_server {
 
 extern "C" {
 
-bl_status bl_server_create(int device, int slots, size_t slot_bytes, bl_server **out) {
+bl_status bl_job_bytes(int device, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
+                       const bl_fid_params *params, size_t *min_bytes, size_t *full_bytes) {
+  if (!sys || !pw || !ro || !det || !params) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    int N = sys->s.dim();
+    bl::job_bytes(device, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params), min_bytes, full_bytes);
+  });
+}
+
+bl_status bl_server_create(int device, int lanes, size_t pool_bytes, bl_server **out) {
   if (!out) return fail(BL_ERR_INVALID, "null output pointer");
   *out = nullptr;
   return guarded([&] {
     std::unique_ptr<bl_server> h(new bl_server);
-    h->s.reset(new bl::Server(device, slots, slot_bytes));
+    h->s.reset(new bl::Server(device, lanes, pool_bytes));
     *out = h.release();
   });
 }
@@ -340,13 +349,16 @@ bl_status bl_server_cancel(bl_server *srv, long long ticket) {
   return BL_OK;
 }
 
-bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done) {
+bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done,
+                          double *flops_done) {
   if (!srv) return fail(BL_ERR_INVALID, "null server");
   int64_t q = 0, r = 0, d = 0;
-  srv->s->stats(&q, &r, &d);
+  double f = 0;
+  srv->s->stats(&q, &r, &d, &f);
   if (queued) *queued = q;
   if (running) *running = r;
   if (done) *done = d;
+  if (flops_done) *flops_done = f;
   return BL_OK;
 }
 

@@ -1133,13 +1133,21 @@ Context::~Context() {
 
 static thread_local size_t *g_upload_counter = nullptr;  // set while a Job uploads its inputs
 
-// Bump allocator over a caller-provided device region.  Only the allocation-free entry
-// point (powder_fid_noalloc, below) installs one, for the duration of its own call.
+// Bump allocator over a caller-provided device region.  The allocation-free entry point
+// (powder_fid_noalloc) and job_in_region install one while they build a Job.
 struct ScratchArena {
   char *base = nullptr;
   size_t cap = 0, used = 0;
+  const char *label = "static device scratch of the allocation-free entry point";
 };
 static thread_local ScratchArena *g_arena = nullptr;
+// Set by job_bytes: the Job constructor records its memory plan here and returns before
+// touching the device.
+struct JobSizing {
+  size_t per_c = 0;
+  long cpad = 0;
+};
+static thread_local JobSizing *g_sizing = nullptr;
 
 template <class T>
 struct DevBuf {
@@ -1153,8 +1161,7 @@ struct DevBuf {
       size_t off = (g_arena->used + 255) & ~size_t(255);
       size_t bytes = count * sizeof(T);
       if (off + bytes > g_arena->cap)
-        throw Error(4, "job needs more than the " + std::to_string(g_arena->cap >> 20) +
-                           " MiB static device scratch of the allocation-free entry point");
+        throw Error(4, "job needs more than the " + std::to_string(g_arena->cap >> 20) + " MiB " + g_arena->label);
       p = reinterpret_cast<T *>(g_arena->base + off);
       g_arena->used = off + bytes;
       owned = false;
@@ -1232,7 +1239,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   JobImpl &J = *d_;
   J.ctx = &ctx;
   J.P = p;
-  CUDA_OK(cudaSetDevice(ctx.device));
+  if (!g_sizing) CUDA_OK(cudaSetDevice(ctx.device));
   if (p.precision != 0 && p.precision != 1) throw Error(1, "precision must be 0 (FP64) or 1 (mixed)");
   if (p.step_method != 0 && p.step_method != 1) throw Error(1, "step_method must be 0 (eigh) or 1 (Taylor)");
   if (p.fave_method < 0 || p.fave_method > 2) throw Error(1, "fave_method must be 0 (auto), 1 (direct) or 2 (FFT)");
@@ -1377,10 +1384,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   size_t per_c = J.mixed ? sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N) + sizeof(float2) * (nsteps * L.S2 + wide)
                          : sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + wide);
   per_c += sizeof(double) * 11;
+  long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
+  if (g_sizing) {
+    g_sizing->per_c = per_c;
+    g_sizing->cpad = cpad_all;
+    return;
+  }
   size_t budget = ctx.hbm_budget ? ctx.hbm_budget : (size_t(16) << 30);
   long cb = long(budget / std::max<size_t>(per_c, 1));
   cb = (cb / 32) * 32;
-  long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
   if (cb < 32) throw Error(4, "job does not fit the device memory budget (one warp of crystallites)");
   J.Cb = int(std::min(cb, cpad_all));
   J.nbatch = int((cpad_all + J.Cb - 1) / J.Cb);
@@ -1874,19 +1886,40 @@ static char *noalloc_base(int device) {
   return static_cast<char *>(g_noalloc_addr[device]);
 }
 
+// Device bytes outside the batch-sized work buffers: tables, per-crystallite inputs (11
+// doubles each, padded by up to one batch), warp partials and the FID.
+static size_t fixed_bytes(const Powder &pw, const FidParams &p) {
+  long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
+  long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
+  size_t ceff = size_t(pw.size()) * size_t(g) + 32;
+  return (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
+         (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
+}
+
+void job_bytes(int device, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+               const FidParams &p, size_t *min_bytes, size_t *full_bytes) {
+  Context ctx;
+  ctx.device = device;
+  JobSizing plan;
+  struct Scope {
+    JobSizing *prev;
+    explicit Scope(JobSizing *z) : prev(g_sizing) { g_sizing = z; }
+    ~Scope() { g_sizing = prev; }
+  } scope(&plan);
+  Job job(ctx, sys, pw, ro, det, p);
+  // work buffers are carved with 256-byte alignment: allow for it on each of ~40 buffers
+  size_t fixed = fixed_bytes(pw, p) + 40 * 256;
+  if (min_bytes) *min_bytes = fixed + plan.per_c * 32;
+  if (full_bytes) *full_bytes = fixed + plan.per_c * size_t(plan.cpad);
+}
+
 void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
                         const FidParams &p, double *fid_out, double *sw_out) {
   CUDA_OK(cudaSetDevice(ctx.device));
   ScratchArena arena;
   arena.base = noalloc_base(ctx.device);
   arena.cap = kNoAllocScratch;
-  // Space outside the batch-sized work buffers: tables, per-crystallite inputs (11
-  // doubles each, padded by up to one batch), warp partials and the FID.
-  long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
-  long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
-  size_t ceff = size_t(pw.size()) * size_t(g) + 32;
-  size_t fixed = (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
-                 (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
+  size_t fixed = fixed_bytes(pw, p);
   if (fixed >= kNoAllocScratch)
     throw Error(4, "job needs more than the " + std::to_string(kNoAllocScratch >> 20) +
                        " MiB static device scratch of the allocation-free entry point");
@@ -1925,12 +1958,9 @@ std::unique_ptr<Job> job_in_region(Context &ctx, void *base, size_t bytes, const
   ScratchArena arena;
   arena.base = static_cast<char *>(base);
   arena.cap = bytes;
-  long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
-  long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
-  size_t ceff = size_t(pw.size()) * size_t(g) + 32;
-  size_t fixed = (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
-                 (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
-  if (fixed >= bytes) throw Error(4, "job does not fit a serving slot of " + std::to_string(bytes >> 20) + " MiB");
+  arena.label = "device region given to the job";
+  size_t fixed = fixed_bytes(pw, p);
+  if (fixed >= bytes) throw Error(4, "job does not fit a device region of " + std::to_string(bytes >> 20) + " MiB");
   ctx.hbm_budget = bytes - fixed;
   struct Scope {
     ScratchArena *prev;

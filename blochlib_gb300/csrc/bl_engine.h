@@ -14,7 +14,8 @@ namespace bl {
 struct FidParams {
   int npts = 0;
   double sw = 0, wr = 0, rotb_deg = 0, start_t = 0;
-  int precision = 0;  // 0 = FP64 (the only mode implemented by this engine)
+  int precision = 0;  // 0 = FP64; 1 = mixed (FP64 step, Dyson, Floquet and powder sum;
+                      // single-precision eigenframe, Q/R, Fave and FID terms)
   int step_method = 0;  // step exponential: 0 Jacobi eigen-decomposition, 1 Taylor + squaring
   int fave_method = 0;  // Fave correlation: 0 auto (FFT when n <= 2048), 1 direct, 2 FFT
 };
@@ -69,6 +70,11 @@ double probe_fp64_tflops(Context &ctx);
 void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
                         const FidParams &p, double *fid_out, double *sw_out);
 size_t noalloc_scratch_bytes();
+
+// Device bytes a job needs: *min_bytes with one warp (32) of crystallites per batch,
+// *full_bytes with all crystallites in one batch.  Plans the job on the host only.
+void job_bytes(int device, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+               const FidParams &p, size_t *min_bytes, size_t *full_bytes);
 
 // A Job whose device buffers are all carved from [base, base + bytes) (no allocation).
 std::unique_ptr<Job> job_in_region(Context &ctx, void *base, size_t bytes, const SpinSystem &sys, const Powder &pw,

@@ -3,28 +3,66 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 namespace bl {
 
 namespace {
 void cuda_ok(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw Error(3, std::string(what) + ": " + cudaGetErrorString(e));
 }
+constexpr size_t kAlign = 256;
+size_t round_up(size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); }
 }  // namespace
 
-Server::Server(int device, int slots, size_t slot_bytes) : device_(device), slot_bytes_(slot_bytes) {
-  if (slots < 1 || slot_bytes < (size_t(16) << 20)) throw Error(1, "need >= 1 slot of >= 16 MiB");
+bool RangePool::take(size_t bytes, size_t *off) {
+  for (auto it = free_.begin(); it != free_.end(); ++it) {
+    if (it->second < bytes) continue;
+    *off = it->first;
+    size_t rest = it->second - bytes;
+    size_t at = it->first + bytes;
+    free_.erase(it);
+    if (rest) free_[at] = rest;
+    return true;
+  }
+  return false;
+}
+
+void RangePool::give(size_t off, size_t bytes) {
+  auto it = free_.emplace(off, bytes).first;
+  auto nx = std::next(it);
+  if (nx != free_.end() && it->first + it->second == nx->first) {
+    it->second += nx->second;
+    free_.erase(nx);
+  }
+  if (it != free_.begin()) {
+    auto pv = std::prev(it);
+    if (pv->first + pv->second == it->first) {
+      pv->second += it->second;
+      free_.erase(it);
+    }
+  }
+}
+
+size_t RangePool::free_bytes() const {
+  size_t t = 0;
+  for (auto &kv : free_) t += kv.second;
+  return t;
+}
+
+Server::Server(int device, int lanes, size_t pool_bytes)
+    : device_(device), pool_bytes_(pool_bytes & ~(kAlign - 1)), ranges_(pool_bytes & ~(kAlign - 1)) {
+  if (lanes < 1 || pool_bytes < (size_t(16) << 20)) throw Error(1, "need >= 1 lane and a pool of >= 16 MiB");
   cuda_ok(cudaSetDevice(device), "cudaSetDevice");
-  cuda_ok(cudaMalloc(&pool_, size_t(slots) * slot_bytes), "cudaMalloc (serving pool)");
-  for (int i = 0; i < slots; ++i) {
-    std::unique_ptr<Slot> s(new Slot);
+  cuda_ok(cudaMalloc(&pool_, pool_bytes_), "cudaMalloc (serving pool)");
+  for (int i = 0; i < lanes; ++i) {
+    std::unique_ptr<Lane> s(new Lane);
     s->ctx.device = device;
     cuda_ok(cudaStreamCreateWithFlags(&s->ctx.stream, cudaStreamNonBlocking), "cudaStreamCreate");
     cudaEvent_t ev;
     cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
     s->event = ev;
-    s->base = static_cast<char *>(pool_) + size_t(i) * slot_bytes;
-    s->bytes = slot_bytes;
-    slots_.push_back(std::move(s));
+    lanes_.push_back(std::move(s));
   }
   worker_ = std::thread([this] { loop(); });
 }
@@ -37,19 +75,28 @@ Server::~Server() {
   cv_.notify_all();
   if (worker_.joinable()) worker_.join();
   cudaSetDevice(device_);
-  for (auto &s : slots_) {
+  for (auto &s : lanes_) {
     if (s->ctx.stream) cudaStreamSynchronize(s->ctx.stream);
     s->job.reset();
     if (s->event) cudaEventDestroy(static_cast<cudaEvent_t>(s->event));
   }
-  slots_.clear();  // Context destructors release the streams
+  lanes_.clear();  // Context destructors release the streams
   if (pool_) cudaFree(pool_);
+}
+
+size_t Server::grant(const ServeRequest &r) const {
+  size_t share = pool_bytes_ / lanes_.size();
+  return round_up(std::min(r.full_bytes, std::max(r.min_bytes, share)));
 }
 
 int64_t Server::submit(const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
                        const FidParams &p) {
   auto r = std::make_shared<ServeRequest>(sys, pw, ro, det, p);
   r->t_submit = std::chrono::steady_clock::now();
+  job_bytes(device_, sys, pw, ro, det, p, &r->min_bytes, &r->full_bytes);
+  if (round_up(r->min_bytes) > pool_bytes_)
+    throw Error(4, "job needs " + std::to_string(r->min_bytes >> 20) + " MiB for one warp of crystallites; the pool has " +
+                       std::to_string(pool_bytes_ >> 20) + " MiB");
   {
     std::lock_guard<std::mutex> lk(mu_);
     r->id = next_id_++;
@@ -89,7 +136,7 @@ bool Server::cancel(int64_t id) {
   return true;
 }
 
-void Server::stats(int64_t *queued, int64_t *running, int64_t *done) const {
+void Server::stats(int64_t *queued, int64_t *running, int64_t *done, double *flops_done) const {
   std::lock_guard<std::mutex> lk(mu_);
   int64_t q = 0, r = 0;
   for (auto &kv : all_) {
@@ -99,6 +146,7 @@ void Server::stats(int64_t *queued, int64_t *running, int64_t *done) const {
   if (queued) *queued = q;
   if (running) *running = r;
   if (done) *done = n_done_;
+  if (flops_done) *flops_done = flops_done_;
 }
 
 void Server::loop() {
@@ -106,8 +154,8 @@ void Server::loop() {
   for (;;) {
     bool progress = false;
     // completions
-    for (auto &sp : slots_) {
-      Slot &s = *sp;
+    for (auto &sp : lanes_) {
+      Lane &s = *sp;
       if (!s.req) continue;
       cudaError_t q = cudaEventQuery(static_cast<cudaEvent_t>(s.event));
       if (q == cudaErrorNotReady) continue;
@@ -120,7 +168,9 @@ void Server::loop() {
         err = e.what();
       }
       double sw = s.job ? s.job->sw_out() : 0;
+      double fl = s.job ? s.job->flops() : 0;
       s.job.reset();
+      ranges_.give(s.off, s.bytes);
       {
         std::lock_guard<std::mutex> lk(mu_);
         s.req->t_done = std::chrono::steady_clock::now();
@@ -128,6 +178,7 @@ void Server::loop() {
         s.req->sw = sw;
         s.req->err = err;
         s.req->state = err.empty() ? 2 : 3;
+        if (err.empty()) flops_done_ += fl;
         ++n_done_;
       }
       s.req.reset();
@@ -138,30 +189,35 @@ void Server::loop() {
       std::lock_guard<std::mutex> lk(mu_);
       stopping = stop_;
     }
-    // admissions, first come first served, while a slot is free
-    for (auto &sp : slots_) {
+    // admissions, first come first served, while a lane is idle and the head's grant fits
+    for (auto &sp : lanes_) {
       if (stopping) break;
-      Slot &s = *sp;
+      Lane &s = *sp;
       if (s.req) continue;
       std::shared_ptr<ServeRequest> r;
+      size_t bytes = 0, off = 0;
       {
         std::lock_guard<std::mutex> lk(mu_);
-        while (!queue_.empty() && !r) {
-          r = queue_.front();
-          queue_.pop_front();
-          if (r->state != 0) r.reset();  // cancelled while queued
-        }
-        if (!r) break;
+        while (!queue_.empty() && queue_.front()->state != 0) queue_.pop_front();  // cancelled
+        if (queue_.empty()) break;
+        bytes = grant(*queue_.front());
+        if (!ranges_.take(bytes, &off)) break;  // wait for a completion to free memory
+        r = queue_.front();
+        queue_.pop_front();
         r->state = 1;
         r->t_start = std::chrono::steady_clock::now();
       }
       try {
-        s.job = job_in_region(s.ctx, s.base, s.bytes, r->sys, r->pw, r->ro, r->det, r->p);
+        s.off = off;
+        s.bytes = bytes;
+        s.job = job_in_region(s.ctx, static_cast<char *>(pool_) + off, bytes, r->sys, r->pw, r->ro, r->det, r->p);
         s.job->run();
         cuda_ok(cudaEventRecord(static_cast<cudaEvent_t>(s.event), s.ctx.stream), "cudaEventRecord");
         s.req = r;
       } catch (const std::exception &e) {
         s.job.reset();
+        cudaStreamSynchronize(s.ctx.stream);  // nothing of the failed job may still use the range
+        ranges_.give(off, bytes);
         std::lock_guard<std::mutex> lk(mu_);
         r->err = e.what();
         r->state = 3;
@@ -173,7 +229,7 @@ void Server::loop() {
     std::unique_lock<std::mutex> lk(mu_);
     if (stop_) {
       bool busy = false;
-      for (auto &sp : slots_) busy = busy || bool(sp->req);
+      for (auto &sp : lanes_) busy = busy || bool(sp->req);
       if (!busy) break;
     }
     if (!progress) cv_.wait_for(lk, std::chrono::microseconds(100));

@@ -1,23 +1,32 @@
-// Serving loop: continuous batching of powder-FID jobs on one GPU.
+// Serving loop: continuous batching of powder-FID jobs on one GPU, admission by free
+// device memory.
 //
 // The reference has no server; its closest analogue is the MPI master/worker farm that
 // hands crystallites to free workers as they finish (src/QMspins/driver/oneFID.h:230-286,
 // examples/solid-2.0/src/sequencerun.cc:435-526).  Here the unit handed out is a whole
-// job (spin system + powder + rho/detect + parameters) and the workers are slots of device
-// memory, each with its own CUDA stream:
-//   * one device allocation at start, cut into `slots` regions of `slot_bytes`;
-//   * a request is admitted (FIFO) as soon as a slot is free: its job is built inside the
-//     slot's region (no further allocation), enqueued on the slot's stream, and its
-//     completion recorded with an event, so jobs in different slots overlap on the GPU;
-//   * a worker thread polls completions, copies the FID back and frees the slot;
+// job (spin system + powder + rho/detect + parameters) and the workers are CUDA streams
+// ("lanes") sharing one pool of device memory:
+//   * one device allocation at start (the pool) and `lanes` non-blocking streams;
+//   * each request is sized when it is submitted (job_bytes: the bytes for one warp of
+//     crystallites per batch and for all crystallites at once); a request whose one-warp
+//     size exceeds the pool is refused at submission;
+//   * admission is first come first served: the head of the queue is admitted when a lane
+//     is idle and the pool holds a free range of its grant, grant = its full size capped at
+//     pool/lanes but never below its one-warp size.  The job is built inside that range (no
+//     further allocation), batching its crystallites to fit, enqueued on the lane's stream,
+//     and its completion recorded with an event;
+//   * a worker thread polls completions, copies the FID back and returns the range;
 //   * latency = completion - submission, measured on the host steady clock.
-// Jobs never share arithmetic, so a result does not depend on what else is in flight.
+// Jobs never share arithmetic and the crystallite batching does not change the powder sum
+// (warp partials are reduced in a fixed order), so a result is bitwise the same alone, in
+// the mix, and from a direct call.
 #pragma once
 
 #include <chrono>
 #include <condition_variable>
 #include <cstdint>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -35,6 +44,7 @@ struct ServeRequest {
   Powder pw;
   CMatrix ro, det;
   FidParams p;
+  size_t min_bytes = 0, full_bytes = 0;
   std::chrono::steady_clock::time_point t_submit, t_start, t_done;
   int state = 0;  // 0 queued, 1 running, 2 done, 3 failed, 4 cancelled
   std::vector<double> fid;
@@ -44,35 +54,53 @@ struct ServeRequest {
       : sys(s), pw(w), ro(r), det(d), p(q) {}
 };
 
+// First-fit ranges of the pool, free neighbours merged on release.
+class RangePool {
+ public:
+  explicit RangePool(size_t bytes) { free_[0] = bytes; }
+  bool take(size_t bytes, size_t *off);
+  void give(size_t off, size_t bytes);
+  size_t free_bytes() const;
+
+ private:
+  std::map<size_t, size_t> free_;  // offset -> size
+};
+
 class Server {
  public:
-  Server(int device, int slots, size_t slot_bytes);
+  Server(int device, int lanes, size_t pool_bytes);
   ~Server();
+  // sizes the job (throws Error 4 when one warp of it exceeds the pool) and queues it
   int64_t submit(const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det, const FidParams &p);
   // state of a ticket; when done and fid_out is given, copies the FID and forgets the ticket
   int poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err);
   bool cancel(int64_t id);
-  void stats(int64_t *queued, int64_t *running, int64_t *done) const;
+  // requests queued/running, finished (any outcome), and the algorithmic flop of the
+  // completed ones (one complex multiply-add = 8 flop)
+  void stats(int64_t *queued, int64_t *running, int64_t *done, double *flops_done) const;
+  size_t pool_bytes() const { return pool_bytes_; }
 
  private:
-  struct Slot {
+  struct Lane {
     Context ctx;
-    char *base = nullptr;
-    size_t bytes = 0;
     std::unique_ptr<Job> job;
     std::shared_ptr<ServeRequest> req;
+    size_t off = 0, bytes = 0;
     void *event = nullptr;  // cudaEvent_t
   };
   void loop();
+  size_t grant(const ServeRequest &r) const;
   int device_;
-  size_t slot_bytes_;
+  size_t pool_bytes_;
   void *pool_ = nullptr;
-  std::vector<std::unique_ptr<Slot>> slots_;
+  RangePool ranges_;
+  std::vector<std::unique_ptr<Lane>> lanes_;
   mutable std::mutex mu_;
   std::condition_variable cv_;
   std::deque<std::shared_ptr<ServeRequest>> queue_;
   std::unordered_map<int64_t, std::shared_ptr<ServeRequest>> all_;
   int64_t next_id_ = 1, n_done_ = 0;
+  double flops_done_ = 0;
   bool stop_ = false;
   std::thread worker_;
 };

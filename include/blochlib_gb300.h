@@ -142,17 +142,26 @@ bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powd
                                 const double *det, const bl_fid_params *params, double *fid_out,
                                 double *sw_out);
 
-/* Serving loop with continuous batching.  No counterpart in the reference beyond its MPI
- * crystallite farm (src/QMspins/driver/oneFID.h:230-286, examples/solid-2.0/src/
- * sequencerun.cc:435-526), which hands work to whichever worker finishes first; here whole
- * jobs go to slots of device memory.  One device allocation of slots x slot_bytes at
- * creation; a submitted job is admitted (FIFO) when a slot is free, built inside that slot
- * (no further allocation; crystallites batched to fit it), and run on the slot's stream, so
- * jobs in different slots overlap on the GPU.  A job whose 32-crystallite batch does not fit
- * a slot fails with BL_ERR_NOMEM.  Inputs are copied at submission.
+/* Device bytes one powder FID needs (host-side planning, no device work): *min_bytes with
+ * 32 crystallites per batch, *full_bytes with all crystallites in one batch.  Either output
+ * may be NULL.  The serving loop sizes every request with this. */
+bl_status bl_job_bytes(int device, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
+                       const bl_fid_params *params, size_t *min_bytes, size_t *full_bytes);
+
+/* Serving loop with continuous batching and admission by free device memory.  No
+ * counterpart in the reference beyond its MPI crystallite farm (src/QMspins/driver/
+ * oneFID.h:230-286, examples/solid-2.0/src/sequencerun.cc:435-526), which hands work to
+ * whichever worker finishes first; here whole jobs go to CUDA streams ("lanes") sharing one
+ * pool of device memory allocated at creation.  A submitted job is sized (bl_job_bytes) and
+ * refused with BL_ERR_NOMEM if 32 of its crystallites do not fit the pool; otherwise it is
+ * queued and admitted first come first served when a lane is idle and the pool has a free
+ * range of its grant (its full size, capped at pool_bytes/lanes but never below its
+ * 32-crystallite size).  The job is built inside that range (no further allocation;
+ * crystallites batched to fit) and runs on the lane's stream, overlapping the other lanes.
+ * Inputs are copied at submission.
  * Ticket states: 0 queued, 1 running, 2 done, 3 failed, 4 cancelled; -1 unknown ticket. */
 typedef struct bl_server bl_server;
-bl_status bl_server_create(int device, int slots, size_t slot_bytes, bl_server **out);
+bl_status bl_server_create(int device, int lanes, size_t pool_bytes, bl_server **out);
 void bl_server_destroy(bl_server *srv);  /* waits for running jobs */
 bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
                            const double *det, const bl_fid_params *params, long long *ticket);
@@ -161,7 +170,10 @@ bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder
 bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *fid_out, double *sw_out,
                          double *latency_ms);
 bl_status bl_server_cancel(bl_server *srv, long long ticket);  /* queued jobs only */
-bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done);
+/* queued and running requests, finished ones (any outcome), and the algorithmic FP64 flop of
+ * the completed ones (as bl_job_flops).  Any output may be NULL. */
+bl_status bl_server_stats(bl_server *srv, long long *queued, long long *running, long long *done,
+                          double *flops_done);
 
 /* Cartesian rotation matrices of the reference, row-major 3x3 (radians):
  * 3-angle (powder orientation) and 2-angle (rotor phase phi, rotor tilt theta). */

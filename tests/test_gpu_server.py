@@ -33,7 +33,8 @@ def _wait(srv, tickets, timeout=120.0):
 
 
 def test_result_is_the_same_alone_and_in_the_mix():
-    srv = bl.Server(0, slots=6, slot_bytes=512 << 20)
+    # 6 lanes over 12 GiB: 2 GiB grants, so the larger c3 systems run in several batches
+    srv = bl.Server(0, lanes=6, pool_bytes=12 << 30)
     probe = _job(W.config(1), 128)
     t = srv.submit(**probe)
     alone = _wait(srv, [t])[t][1]
@@ -50,22 +51,38 @@ def test_result_is_the_same_alone_and_in_the_mix():
     direct = bl.oneFID(probe["sys"], probe["npts"], probe["sw"], probe["wr"], probe["rotb"]).FID(
         probe["pw"], probe["ro"], probe["det"])
     np.testing.assert_array_equal(alone, direct)
-    q, r, d = srv.stats()
-    assert q == 0 and r == 0 and d >= 26
+    q, r, d, fl = srv.stats()
+    assert q == 0 and r == 0 and d >= 26 and fl > 0
     srv.close()
 
 
 def test_cancel_queued_and_reject_oversized():
-    srv = bl.Server(0, slots=1, slot_bytes=64 << 20)
+    srv = bl.Server(0, lanes=1, pool_bytes=64 << 20)
     j = _job(W.config(0), 64)
     tickets = [srv.submit(**j) for _ in range(6)]
-    srv.cancel(tickets[-1])  # still queued behind five jobs on one slot
+    srv.cancel(tickets[-1])  # still queued behind five jobs on one lane
     res = _wait(srv, tickets[:-1])
     assert all(r[0] == srv.DONE for r in res.values())
     st, fid, _, _ = srv.result(tickets[-1])
     assert st == srv.CANCELLED and fid is None
     big = _job(dict(W.config(1), sw=2000 * 20e3), 64)  # one warp needs > 64 MiB
-    tb = srv.submit(**big)
-    with pytest.raises(bl.BlochError):
-        _wait(srv, [tb])
+    with pytest.raises(bl.BlochError) as e:
+        srv.submit(**big)
+    assert e.value.status == 4
+    srv.close()
+
+
+def test_admission_waits_for_memory():
+    """Two lanes but a pool that holds one grant: jobs run one at a time, all complete,
+    results equal the direct call."""
+    cfg = W.config(3, 0)
+    j = _job(cfg, 64)
+    lo, hi = bl.job_bytes(**j)
+    srv = bl.Server(0, lanes=2, pool_bytes=int(lo * 1.5))
+    tickets = [srv.submit(**j) for _ in range(3)]
+    res = _wait(srv, tickets, timeout=300)
+    assert all(r[0] == srv.DONE for r in res.values())
+    direct = bl.oneFID(j["sys"], j["npts"], j["sw"], j["wr"], j["rotb"]).FID(j["pw"], j["ro"], j["det"])
+    for t in tickets:
+        np.testing.assert_array_equal(res[t][1], direct)
     srv.close()

@@ -139,3 +139,25 @@ def test_cpp_host_api_example_builds():
     from blochlib_gb300 import build
     exes = build.build_examples()
     assert exes and all(e.exists() for e in exes)
+
+
+def _sized(cfg, count=None, **kw):
+    s = bl.SolidSys(cfg["lines"])
+    phi, theta, gamma, w = (np.asarray(x)[:count] for x in cfg["powder"])
+    pw = bl.powder.from_arrays(theta, phi, gamma, w)
+    return bl.job_bytes(s, pw, s.op(cfg["rho"]), s.op(cfg["det"]), cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"],
+                        **kw)
+
+
+def test_job_bytes_plans_on_the_host():
+    """bl_job_bytes runs without a device: one-warp size <= full size, full size grows by one
+    warp's worth per 32 crystallites, the mixed form needs less, bigger systems need more."""
+    c1 = W.config(1)
+    lo32, hi32 = _sized(c1, 32)
+    lo64, hi64 = _sized(c1, 64)
+    lo96, hi96 = _sized(c1, 96)
+    assert lo32 <= hi32 and lo64 < hi64
+    assert hi96 - hi64 == hi64 - hi32 > 0
+    assert _sized(c1, 64, precision=1)[1] < hi64
+    small, big = _sized(W.config(3, 5), 64), _sized(W.config(3, 0), 64)  # 3 vs 7 protons
+    assert big[0] > small[0]
