@@ -1,21 +1,32 @@
 // Large-block kernels (Hamiltonian blocks of kMaxBlock < b <= kMaxBigBlock), included by
-// bl_engine.cu after DevSys and the complex helpers.  One CTA of kBigThreads threads works
-// on one crystallite's block with the matrices in shared memory; products are CTA-wide
-// FP64 GEMMs with 2x2 register tiles.  Same arithmetic as the small-block kernels:
+// bl_engine.cu after DevSys and the complex helpers.  One CTA works on one crystallite's
+// block with the matrices in shared memory; products are CTA-wide FP64 GEMMs with 2x2
+// output tiles, one tile per thread (NT = 1) or two (NT = 2, blocks above 64), and CTAs of
+// about one thread per tile so that registers stay low and several CTAs share an SM.
+// Same arithmetic as the small-block kernels:
 //   k_big_step      (c, step)   H_i, U_i = exp(-i 2pi tau H_i) by Taylor + squaring
 //   k_big_dyson     (c)         A_{i+1} = U_i A_i for i < n (A stays in shared memory)
 //   k_big_floquet   (c)         A_n = V diag(lam) V^H: Cayley transform, parallel Jacobi
 //   k_big_eigframe  (c)         W_i = A_{i+1} V_F for i < n
-//   k_big_qr        (c, step, pair)  Q = W_a^H M_ab W_b for block pairs with a big block
+//   k_big_qr        (c, step) per pair  Q = W_a^H M_ab W_b for block pairs with a big block
 
 constexpr int kMaxBigBlock = 74;   // 5 real b x b matrices fit 227 KB of shared memory
-constexpr int kBigThreads = 256;
-constexpr int kBigTiles = 6;       // ceil((74/2)^2 / 256) 2x2 output tiles per thread
+constexpr int kBigThreads = 256;   // k_big_floquet
+constexpr int kBigPSMax = 63;      // 7 real b x b matrices (Paterson-Stockmeyer step) fit
 constexpr int kMaxInt = 128;       // interactions per system on the large-block path
 
-// C (m x n) = alpha * A (m x k) * B (k x n), real, shared memory, row-major with lds.
+__host__ __device__ constexpr int big_tiles(int m, int n) { return ((m + 1) / 2) * ((n + 1) / 2); }
+// tiles per thread of an m x n product, and the CTA size that gives each thread NT tiles
+__host__ __device__ constexpr int big_nt(int m, int n) { return big_tiles(m, n) <= 1024 ? 1 : 2; }
+__host__ __device__ constexpr int big_threads(int m, int n) {
+  return ((big_tiles(m, n) + big_nt(m, n) - 1) / big_nt(m, n) + 31) / 32 * 32;
+}
+
+// C (m x n) = alpha * A (m x k) * B (k x n) (+ epilogue), real, shared memory, row-major.
+// ep(e, v) returns the value stored at C[e] for the product value v.
+template <class EP>
 __device__ void cta_mm_real(const double *A, int lda, const double *B, int ldb, double *C, int ldc, int m, int n,
-                            int k, double alpha) {
+                            int k, double alpha, EP ep) {
   const int tm = (m + 1) / 2, tn = (n + 1) / 2;
   for (int t = threadIdx.x; t < tm * tn; t += blockDim.x) {
     const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
@@ -26,22 +37,74 @@ __device__ void cta_mm_real(const double *A, int lda, const double *B, int ldb, 
       const double b0 = B[l * ldb + j0], b1 = B[l * ldb + j1];
       c00 = fma(a0, b0, c00), c01 = fma(a0, b1, c01), c10 = fma(a1, b0, c10), c11 = fma(a1, b1, c11);
     }
-    C[i0 * ldc + j0] = alpha * c00;
-    if (j0 + 1 < n) C[i0 * ldc + j0 + 1] = alpha * c01;
+    C[i0 * ldc + j0] = ep(i0 * ldc + j0, alpha * c00);
+    if (j0 + 1 < n) C[i0 * ldc + j0 + 1] = ep(i0 * ldc + j0 + 1, alpha * c01);
     if (i0 + 1 < m) {
-      C[(i0 + 1) * ldc + j0] = alpha * c10;
-      if (j0 + 1 < n) C[(i0 + 1) * ldc + j0 + 1] = alpha * c11;
+      C[(i0 + 1) * ldc + j0] = ep((i0 + 1) * ldc + j0, alpha * c10);
+      if (j0 + 1 < n) C[(i0 + 1) * ldc + j0 + 1] = ep((i0 + 1) * ldc + j0 + 1, alpha * c11);
     }
   }
 }
+__device__ __forceinline__ void cta_mm_real(const double *A, int lda, const double *B, int ldb, double *C, int ldc,
+                                            int m, int n, int k, double alpha) {
+  cta_mm_real(A, lda, B, ldb, C, ldc, m, n, k, alpha, [](int, double v) { return v; });
+}
 
-// Complex 2x2-tiled product into per-thread registers: acc[t] for this thread's tiles.
-// CONJ_A: use A^H (A stored k x m).  Tiles are numbered t = threadIdx.x + q*blockDim.x.
-template <bool CONJ_A, class C>
-__device__ void cta_mm_cplx_regs(const C *A, int lda, const C *B, int ldb, int m, int n, int k, C (&acc)[kBigTiles][4]) {
+// Upper-triangle 2x2 tiles of an m x m matrix: tile t -> (ti, tj), ti <= tj, t < big_sym_tiles.
+// Rows pr and tm-1-pr together hold tm+1 tiles; an odd tm's middle row comes last.
+__host__ __device__ constexpr int big_sym_tiles(int m) { return ((m + 1) / 2) * ((m + 1) / 2 + 1) / 2; }
+__device__ __forceinline__ void sym_tile(int t, int tm, int &ti, int &tj) {
+  const int h = tm / 2, pr = t / (tm + 1), q = t % (tm + 1);
+  if (pr < h) {
+    if (q < tm - pr) ti = pr, tj = pr + q;
+    else ti = tm - 1 - pr, tj = ti + (q - (tm - pr));
+  } else {
+    ti = h, tj = h + (t - h * (tm + 1));
+  }
+}
+
+// C = alpha * A * B (+ epilogue) for m x m real A, B that are symmetric and commute, so
+// that C is symmetric: only upper-triangle tiles are computed, each value stored at (i, j)
+// and (j, i).  ep(e, v) gives the stored value for the upper element e = i*m + j (called
+// once per upper element, by the thread that stores it and its mirror).
+template <class EP>
+__device__ void cta_mm_sym(const double *A, const double *B, double *C, int m, double alpha, EP ep) {
+  const int tm = (m + 1) / 2;
+  for (int t = threadIdx.x; t < big_sym_tiles(m); t += blockDim.x) {
+    int ti, tj;
+    sym_tile(t, tm, ti, tj);
+    const int i0 = 2 * ti, j0 = 2 * tj;
+    const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, m - 1);
+    double c00 = 0, c01 = 0, c10 = 0, c11 = 0;
+    for (int l = 0; l < m; ++l) {
+      const double a0 = A[i0 * m + l], a1 = A[i1 * m + l];
+      const double b0 = B[l * m + j0], b1 = B[l * m + j1];
+      c00 = fma(a0, b0, c00), c01 = fma(a0, b1, c01), c10 = fma(a1, b0, c10), c11 = fma(a1, b1, c11);
+    }
+    auto put = [&](int i, int j, double v) {
+      const double x = ep(i * m + j, alpha * v);
+      C[i * m + j] = x;
+      if (i != j) C[j * m + i] = x;
+    };
+    put(i0, j0, c00);
+    if (j0 + 1 < m) put(i0, j0 + 1, c01);
+    if (i0 + 1 < m) {
+      if (ti != tj) put(i0 + 1, j0, c10);  // on a diagonal tile (i0+1, i0) mirrors c01
+      if (j0 + 1 < m) put(i0 + 1, j0 + 1, c11);
+    }
+  }
+}
+__device__ __forceinline__ void cta_mm_sym(const double *A, const double *B, double *C, int m, double alpha) {
+  cta_mm_sym(A, B, C, m, alpha, [](int, double v) { return v; });
+}
+
+// Complex 2x2-tiled product into per-thread registers: acc[q] for the tiles
+// t = threadIdx.x + q*blockDim.x.  CONJ_A: use A^H (A stored k x m).
+template <int NT, bool CONJ_A, class C>
+__device__ void cta_mm_cplx_regs(const C *A, int lda, const C *B, int ldb, int m, int n, int k, C (&acc)[NT][4]) {
   const int tm = (m + 1) / 2, tn = (n + 1) / 2;
 #pragma unroll
-  for (int q = 0; q < kBigTiles; ++q) {
+  for (int q = 0; q < NT; ++q) {
     const int t = threadIdx.x + q * blockDim.x;
     acc[q][0] = acc[q][1] = acc[q][2] = acc[q][3] = mkc<C>(0, 0);
     if (t >= tm * tn) continue;
@@ -63,11 +126,11 @@ __device__ void cta_mm_cplx_regs(const C *A, int lda, const C *B, int ldb, int m
 }
 
 // Visits this thread's tile outputs: f(row, col, value).
-template <class C, class F>
-__device__ void cta_tiles_store(int m, int n, const C (&acc)[kBigTiles][4], F f) {
+template <int NT, class C, class F>
+__device__ void cta_tiles_store(int m, int n, const C (&acc)[NT][4], F f) {
   const int tm = (m + 1) / 2, tn = (n + 1) / 2;
 #pragma unroll
-  for (int q = 0; q < kBigTiles; ++q) {
+  for (int q = 0; q < NT; ++q) {
     const int t = threadIdx.x + q * blockDim.x;
     if (t >= tm * tn) continue;
     const int i0 = (t / tn) * 2, j0 = (t % tn) * 2;
@@ -80,15 +143,25 @@ __device__ void cta_tiles_store(int m, int n, const C (&acc)[kBigTiles][4], F f)
   }
 }
 
-// One CTA per (crystallite, step): U_i of a large block by Taylor series + squaring.
-__global__ void __launch_bounds__(kBigThreads) k_big_step(DevSys s, int k) {
+// Shared memory of k_big_step for a block of size b.
+__host__ __device__ constexpr size_t big_step_smem(int b) {
+  return sizeof(double) * size_t(b <= kBigPSMax ? 7 : 5) * size_t(b) * size_t(b);
+}
+
+// One CTA per (crystallite, step): U_i of a large block, exp(-iX) with X = 2pi tau H_i / 2^sq
+// (||X||_inf <= 1/2) by its degree-15 Taylor polynomial, then sq squarings.
+// Blocks up to kBigPSMax evaluate the polynomial as cos X = C(Y), sin X = X S(Y), Y = X^2,
+// C and S of degree 7 in Y by Paterson-Stockmeyer with Y^4 (Y, Y^2, Y^3, Y^4, C, S, X S:
+// 7 real products); larger blocks accumulate the terms one product at a time (14).  All
+// factors are polynomials in X, hence symmetric and commuting: products are symmetric
+// and only their upper triangles are computed (cta_mm_sym).
+__global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
   extern __shared__ double bsm[];
   __shared__ double fk[kMaxInt];
   __shared__ double red[kMaxBigBlock];
   __shared__ double scl[2];
   const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
-  double *X = bsm, *P = X + bb, *Q = P + bb, *R = Q + bb, *I = R + bb;
   if (threadIdx.x == 0) {
     double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
     double tmid = (t2 - t1) / 2.0 + t1;
@@ -106,6 +179,7 @@ __global__ void __launch_bounds__(kBigThreads) k_big_step(DevSys s, int k) {
     }
   }
   __syncthreads();
+  double *X = bsm;
   for (int e = threadIdx.x; e < bb; e += blockDim.x) {
     double h = s.Hc[bp + e];
     for (int kk = 0; kk < s.nint; ++kk) {
@@ -137,34 +211,74 @@ __global__ void __launch_bounds__(kBigThreads) k_big_step(DevSys s, int k) {
   __syncthreads();
   const double sc = scl[0];
   const int sq = int(scl[1]);
-  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
-    const double x = sc * X[e];
-    X[e] = x, P[e] = x;
-    R[e] = (e / b == e % b) ? 1.0 : 0.0;
-    I[e] = -x;
+  double *R, *I, *F0, *F1, *F2;  // result R + iI and three free b x b buffers for squaring
+  if (b <= kBigPSMax) {
+    double *Y = X + bb, *Y2 = Y + bb, *Y3 = Y2 + bb, *Y4 = Y3 + bb, *T = Y4 + bb;
+    R = T + bb;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) X[e] *= sc;
+    __syncthreads();
+    cta_mm_sym(X, X, Y, b, 1.0);
+    __syncthreads();
+    cta_mm_sym(Y, Y, Y2, b, 1.0);
+    __syncthreads();
+    cta_mm_sym(Y2, Y, Y3, b, 1.0);
+    cta_mm_sym(Y2, Y2, Y4, b, 1.0);
+    // c0 I + c1 Y + c2 Y^2 + c3 Y^3 at element e; cos: (-1)^j / (2j)!, sin: (-1)^j / (2j+1)!
+    auto low = [&](double c0, double c1, double c2, double c3, int e) {
+      const double d = (e / b == e % b) ? c0 : 0.0;
+      return fma(c3, Y3[e], fma(c2, Y2[e], fma(c1, Y[e], d)));
+    };
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x)
+      T[e] = low(1.0 / 40320, -1.0 / 3628800, 1.0 / 479001600, -1.0 / 87178291200.0, e);
+    __syncthreads();
+    cta_mm_sym(Y4, T, R, b, 1.0,
+                [&](int e, double v) { return v + low(1.0, -1.0 / 2, 1.0 / 24, -1.0 / 720, e); });
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x)
+      T[e] = low(1.0 / 362880, -1.0 / 39916800, 1.0 / 6227020800.0, -1.0 / 1307674368000.0, e);
+    __syncthreads();
+    // S(Y) over Y3 in place: element e's epilogue reads Y3[e] before the same thread writes it
+    cta_mm_sym(Y4, T, Y3, b, 1.0,
+                [&](int e, double v) { return v + low(1.0, -1.0 / 6, 1.0 / 120, -1.0 / 5040, e); });
+    __syncthreads();
+    I = Y;  // -sin X = -X S(Y)
+    cta_mm_sym(X, Y3, I, b, -1.0);
+    F0 = Y2, F1 = Y4, F2 = T;
+  } else {
+    double *P = X + bb, *Q = P + bb;
+    R = Q + bb, I = R + bb;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const double x = sc * X[e];
+      X[e] = x, P[e] = x;
+      R[e] = (e / b == e % b) ? 1.0 : 0.0;
+      I[e] = -x;
+    }
+    __syncthreads();
+    for (int kt = 2; kt <= kTaylorTerms; ++kt) {
+      cta_mm_sym(P, X, Q, b, 1.0 / kt);
+      __syncthreads();
+      const int m4 = kt & 3;
+      for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+        const double v = Q[e];
+        if (m4 == 2) R[e] -= v;
+        else if (m4 == 3) I[e] += v;
+        else if (m4 == 0) R[e] += v;
+        else I[e] -= v;
+      }
+      double *t = P;
+      P = Q, Q = t;
+      __syncthreads();
+    }
+    F0 = P, F1 = Q, F2 = X;
   }
   __syncthreads();
-  for (int kt = 2; kt <= kTaylorTerms; ++kt) {
-    cta_mm_real(P, b, X, b, Q, b, b, b, b, 1.0 / kt);
+  for (int t = 0; t < sq; ++t) {  // (R + iI)^2 = (RR - II) + i 2RI
+    cta_mm_sym(R, R, F0, b, 1.0);
+    cta_mm_sym(I, I, F1, b, 1.0);
+    cta_mm_sym(R, I, F2, b, 2.0);
     __syncthreads();
-    const int m4 = kt & 3;
-    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
-      const double v = Q[e];
-      if (m4 == 2) R[e] -= v;
-      else if (m4 == 3) I[e] += v;
-      else if (m4 == 0) R[e] += v;
-      else I[e] -= v;
-    }
-    double *t = P;
-    P = Q, Q = t;
-    __syncthreads();
-  }
-  for (int t = 0; t < sq; ++t) {  // (R + iI)^2 = (RR - II) + i 2RI; X is free here
-    cta_mm_real(R, b, R, b, P, b, b, b, b, 1.0);
-    cta_mm_real(I, b, I, b, Q, b, b, b, b, 1.0);
-    cta_mm_real(R, b, I, b, X, b, b, b, b, 2.0);
-    __syncthreads();
-    for (int e = threadIdx.x; e < bb; e += blockDim.x) R[e] = P[e] - Q[e], I[e] = X[e];
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) R[e] = F0[e] - F1[e], I[e] = F2[e];
     __syncthreads();
   }
   double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
@@ -172,21 +286,22 @@ __global__ void __launch_bounds__(kBigThreads) k_big_step(DevSys s, int k) {
 }
 
 // One CTA per crystallite: A_{i+1} = U_i A_i for all steps; A lives in shared memory.
-__global__ void __launch_bounds__(kBigThreads) k_big_dyson(DevSys s, int k) {
+template <int NT>
+__global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_dyson(DevSys s, int k) {
   extern __shared__ double2 bsc[];
   const int c = blockIdx.x;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
   double2 *Us = bsc, *As = Us + bb;
   for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = cmk(e / b == e % b ? 1.0 : 0.0, 0.0);
-  double2 acc[kBigTiles][4];
+  double2 acc[NT][4];
   for (int i = 0; i < s.n; ++i) {
     const double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) Us[e] = Ub[at(bp + e, c, s.Cpad)];
     __syncthreads();
-    cta_mm_cplx_regs<false, double2>(Us, b, As, b, b, b, b, acc);
+    cta_mm_cplx_regs<NT, false, double2>(Us, b, As, b, b, b, b, acc);
     __syncthreads();
     double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
-    cta_tiles_store(b, b, acc, [&](int r, int q, double2 v) {
+    cta_tiles_store<NT>(b, b, acc, [&](int r, int q, double2 v) {
       As[r * b + q] = v;
       Ab[at(bp + r * b + q, c, s.Cpad)] = v;
     });
@@ -196,64 +311,72 @@ __global__ void __launch_bounds__(kBigThreads) k_big_dyson(DevSys s, int k) {
 
 // One CTA per crystallite: W_i = A_{i+1} V_F (in place over A in FP64; into the
 // single-precision W array in the mixed form).
-template <class C>
-__global__ void __launch_bounds__(kBigThreads) k_big_eigframe(DevSys s, int k) {
+template <int NT, class C>
+__global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_eigframe(DevSys s, int k) {
   extern __shared__ __align__(16) unsigned char bsr[];
   const int c = blockIdx.x;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
   C *Vs = reinterpret_cast<C *>(bsr), *As = Vs + bb;
   for (int e = threadIdx.x; e < bb; e += blockDim.x) Vs[e] = cvt<C>(s.VF[at(bp + e, c, s.Cpad)]);
-  C acc[kBigTiles][4];
+  C acc[NT][4];
   for (int i = 0; i < s.n; ++i) {
     const double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
     C *Wb = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = cvt<C>(Ab[at(bp + e, c, s.Cpad)]);
     __syncthreads();
-    cta_mm_cplx_regs<false, C>(As, b, Vs, b, b, b, b, acc);
-    cta_tiles_store(b, b, acc, [&](int r, int q, C v) { Wb[at(bp + r * b + q, c, s.Cpad)] = v; });
+    cta_mm_cplx_regs<NT, false, C>(As, b, Vs, b, b, b, b, acc);
+    cta_tiles_store<NT>(b, b, acc, [&](int r, int q, C v) { Wb[at(bp + r * b + q, c, s.Cpad)] = v; });
     __syncthreads();
   }
 }
 
-// One CTA per (crystallite, step, big pair): Q^{ab} = W_a^H (M_ab W_b), M = D (or rho).
+// One big Q/R block pair as the kernel sees it: blocks a, b, the output offset, and the
+// non-zeros of M_ab (D or rho) by row: row l holds entries [rp[l], rp[l+1]) of (ci, cv).
+struct BigPair {
+  int a, b, off, nitems, isq, wchunk;
+  const int *rp, *ci;
+  const double2 *cv;
+};
+
+// Shared memory of k_big_qr: W_a, a column chunk of W_b and of X = M_ab W_b.
 template <class C>
-__global__ void __launch_bounds__(kBigThreads) k_big_qr(DevSys s, const int *__restrict__ plist, int npl) {
+__host__ __device__ constexpr size_t big_qr_smem(int ba, int bb, int w) {
+  return sizeof(C) * (size_t(ba) * ba + size_t(bb) * w + size_t(ba) * w);
+}
+
+// One CTA per (crystallite, step) of one block pair: Q^{ab} = W_a^H (M_ab W_b), M = D (or
+// rho), over column chunks of width wchunk; M's non-zeros come from the host.
+template <int NT, class C>
+__global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_qr(DevSys s, BigPair bp2) {
   extern __shared__ __align__(16) unsigned char bsr[];
-  const int pidx = blockIdx.x / (s.C * s.n);
-  const int rem = blockIdx.x % (s.C * s.n);
-  const int c = rem % s.C, i = rem / s.C;
-  const int pr = plist[pidx];
-  const bool isq = pr < s.npq;
-  int a, b, off, moff, nitems;
-  const double2 *M;
-  C *out;
-  if (isq) {
-    a = s.qa[pr], b = s.qb[pr], off = s.qoff[pr], moff = s.doff[pr], M = s.Dblk, out = Bufs<C>::Q(s), nitems = s.nq;
-  } else {
-    const int p2 = pr - s.npq;
-    a = s.ra[p2], b = s.rb[p2], off = s.roff[p2], moff = s.rhooff[p2], M = s.Rhoblk, out = Bufs<C>::R(s);
-    nitems = s.nr;
-  }
-  const int ba = s.bs[a], bb = s.bs[b], pa = s.bpoff[a], pb = s.bpoff[b];
+  const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
+  const int ba = s.bs[bp2.a], bb = s.bs[bp2.b], pa = s.bpoff[bp2.a], pb = s.bpoff[bp2.b];
+  const int w = bp2.wchunk;
+  C *out = bp2.isq ? Bufs<C>::Q(s) : Bufs<C>::R(s);
   const C *W = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
-  C *Wa = reinterpret_cast<C *>(bsr), *X = Wa + ba * ba;
+  C *Wa = reinterpret_cast<C *>(bsr), *Wb = Wa + ba * ba, *X = Wb + bb * w;
   for (int e = threadIdx.x; e < ba * ba; e += blockDim.x) Wa[e] = W[at(pa + e, c, s.Cpad)];
-  // X = M_ab W_b (M sparse: its zero entries are skipped, uniformly across the CTA)
-  for (int e = threadIdx.x; e < ba * bb; e += blockDim.x) {
-    const int l = e / bb, q = e % bb;
-    C acc = mkc<C>(0, 0);
-    for (int m = 0; m < bb; ++m) {
-      const double2 d = M[moff + l * bb + m];
-      if (d.x == 0.0 && d.y == 0.0) continue;
-      acc = cfma(cvt<C>(d), W[at(pb + m * bb + q, c, s.Cpad)], acc);
+  C *ob = out + size_t(i) * bp2.nitems * s.Cpad;
+  C acc[NT][4];
+  for (int q0 = 0; q0 < bb; q0 += w) {
+    const int wc = min(w, bb - q0);
+    for (int e = threadIdx.x; e < bb * wc; e += blockDim.x) {
+      const int m = e / wc, q = e % wc;
+      Wb[e] = W[at(pb + m * bb + q0 + q, c, s.Cpad)];
     }
-    X[e] = acc;
+    __syncthreads();
+    for (int e = threadIdx.x; e < ba * wc; e += blockDim.x) {
+      const int l = e / wc, q = e % wc;
+      C x = mkc<C>(0, 0);
+      for (int j = __ldg(bp2.rp + l); j < __ldg(bp2.rp + l + 1); ++j)
+        x = cfma(cvt<C>(__ldg(bp2.cv + j)), Wb[__ldg(bp2.ci + j) * wc + q], x);
+      X[e] = x;
+    }
+    __syncthreads();
+    cta_mm_cplx_regs<NT, true, C>(Wa, ba, X, wc, ba, wc, ba, acc);
+    cta_tiles_store<NT>(ba, wc, acc, [&](int r, int q, C v) { ob[at(bp2.off + r * bb + q0 + q, c, s.Cpad)] = v; });
+    __syncthreads();
   }
-  __syncthreads();
-  C acc[kBigTiles][4];
-  cta_mm_cplx_regs<true, C>(Wa, ba, X, bb, ba, bb, ba, acc);
-  C *ob = out + size_t(i) * nitems * s.Cpad;
-  cta_tiles_store(ba, bb, acc, [&](int r, int q, C v) { ob[at(off + r * bb + q, c, s.Cpad)] = v; });
 }
 
 // One CTA per crystallite: unitary eigen-decomposition of the big block of A_n by the

@@ -591,6 +591,22 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
 
 constexpr int kTaylorTerms = 15;  // ||x|| <= 1/2: remainder 0.5^16/16! < 1e-18
 
+// Taylor degree for exp(-iX) with ||X||_inf = x <= 1/2: the smallest K whose first omitted
+// term bound x^(K+1)/(K+1)! is at most 2^-56, i.e. x <= ((K+1)! 2^-56)^(1/(K+1)) (table for
+// K = 1..14; K = 15 covers x <= 0.601).
+__device__ __forceinline__ int taylor_degree(double x) {
+  constexpr double thr[14] = {5.268356063861754e-09, 4.3667382909901915e-06, 0.00013509300777591815,
+                              0.0011073892359697527, 0.004640970307744106,   0.013203184215395692,
+                              0.029408989058618194,  0.05554895835340547,    0.09337020827678472,
+                              0.14404487618659187,   0.2082354986608797,     0.2861946964536857,
+                              0.3778659482136564,    0.4829712994609099};
+  int K = kTaylorTerms;
+#pragma unroll
+  for (int j = 13; j >= 0; --j)
+    if (x <= thr[j]) K = j + 1;
+  return K;
+}
+
 // Upper-triangle index of a symmetric B x B matrix stored packed.
 template <int B>
 __device__ __forceinline__ constexpr int sx(int p, int q) {
@@ -644,6 +660,7 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *_
     sq = min(sq, 60);
   }
   const double sc = ldexp(tp, -sq);
+  const int K = taylor_degree(ldexp(nrm, -sq));
   double X[NP], P[NP], Q[NP], R[NP], I[NP];
 #pragma unroll
   for (int p = 0; p < B; ++p)
@@ -654,9 +671,10 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *_
       R[sx<B>(p, q)] = (p == q) ? 1.0 : 0.0;
       I[sx<B>(p, q)] = -P[sx<B>(p, q)];  // k = 1 term: -i X
     }
-  // terms k = 2..: P_k = P_{k-1} X / k; (-i)^k cycles -1, +i, +1, -i
+  // terms k = 2..K: P_k = P_{k-1} X / k; (-i)^k cycles -1, +i, +1, -i
 #pragma unroll
   for (int kt = 2; kt <= kTaylorTerms; ++kt) {
+    if (kt > K) break;
     sym_mul<B>(P, X, Q, 1.0 / kt);
 #pragma unroll
     for (int j = 0; j < NP; ++j) {
@@ -1139,6 +1157,7 @@ struct ScratchArena {
   char *base = nullptr;
   size_t cap = 0, used = 0;
   const char *label = "static device scratch of the allocation-free entry point";
+  bool aux_streams = false;  // the Job may create its own streams (not on the allocation-free path)
 };
 static thread_local ScratchArena *g_arena = nullptr;
 // Set by job_bytes: the Job constructor records its memory plan here and returns before
@@ -1193,9 +1212,10 @@ struct JobImpl {
   int Cb = 0, nbatch = 0, nwarps_total = 0;
   std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices (size <= kMaxBlock)
   std::vector<int> big_blocks;                   // blocks larger than kMaxBlock
-  std::vector<int> big_pairs_h;                  // Q/R pairs with a block larger than kMaxBlock
-  DevBuf<int> big_pairs;
-  size_t big_smem_step = 0, big_smem_mat = 0, big_smem_qr = 0;
+  std::vector<BigPair> big_pairs;                // Q/R pairs with a block larger than kMaxBlock
+  std::vector<size_t> big_rp_off;                // each big pair's row pointers in big_rp
+  DevBuf<int> big_rp, big_ci;                    // non-zeros of M_ab by row, all big pairs
+  DevBuf<double2> big_cv;
   DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status, srp, seo;
   std::vector<DevBuf<int>> blist;
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
@@ -1219,8 +1239,16 @@ struct JobImpl {
   };
   std::vector<Mark> marks;
   int evnext = 0;
+  // streams on which the large blocks of one stage run side by side (fork/join on the
+  // context stream), so that their one-CTA-per-crystallite launches fill the SMs together
+  std::vector<cudaStream_t> aux;
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> join_ev;
   ~JobImpl() {
     for (auto &e : evpool) cudaEventDestroy(e);
+    for (auto &e : join_ev) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (auto &a : aux) cudaStreamDestroy(a);
   }
   double cos_rotb = 1, sin_rotb = 0;
   DevSys base{};
@@ -1390,11 +1418,18 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     g_sizing->cpad = cpad_all;
     return;
   }
-  size_t budget = ctx.hbm_budget ? ctx.hbm_budget : (size_t(16) << 30);
+  size_t budget = ctx.hbm_budget;
+  if (!budget) {  // default: 60% of the device memory free when the job is created
+    size_t fr = 0, tot = 0;
+    CUDA_OK(cudaMemGetInfo(&fr, &tot));
+    budget = size_t(0.6 * double(fr));
+  }
   long cb = long(budget / std::max<size_t>(per_c, 1));
   cb = (cb / 32) * 32;
   if (cb < 32) throw Error(4, "job does not fit the device memory budget (one warp of crystallites)");
-  J.Cb = int(std::min(cb, cpad_all));
+  // as few batches as the budget allows, of equal size (no small remainder batch)
+  const long nb_min = (cpad_all + cb - 1) / cb;
+  J.Cb = int(((long(J.Ceff) + nb_min - 1) / nb_min + 31) / 32 * 32);
   J.nbatch = int((cpad_all + J.Cb - 1) / J.Cb);
   J.nwarps_total = J.nbatch * (J.Cb / 32);
   // block lists by size
@@ -1403,29 +1438,76 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     if (L.size[k] <= kMaxBlock) J.blocks_by_size[L.size[k]].push_back(k);
     else J.big_blocks.push_back(k);
   }
+  std::vector<int> big_rp_h, big_ci_h;
+  std::vector<double2> big_cv_h;
   if (!J.big_blocks.empty()) {
     if (J.nint > kMaxInt) throw Error(5, "more than " + std::to_string(kMaxInt) + " anisotropic interactions");
-    int bmax = 0;
-    for (int k : J.big_blocks) bmax = std::max(bmax, L.size[k]);
-    J.big_smem_step = sizeof(double) * 5 * size_t(bmax) * bmax;
-    J.big_smem_mat = sizeof(double2) * 2 * size_t(bmax) * bmax;
+    const size_t csz = J.mixed ? sizeof(float2) : sizeof(double2);
+    size_t smem_step = 0, smem_mat = 0, smem_qr[2] = {0, 0};
+    for (int k : J.big_blocks) {
+      smem_step = std::max(smem_step, big_step_smem(L.size[k]));
+      smem_mat = std::max(smem_mat, sizeof(double2) * 2 * size_t(L.size[k]) * L.size[k]);
+    }
+    // Q/R pairs with a big block: M_ab's non-zeros by row, and the W_b column chunk that
+    // keeps W_a, W_b and X within half the shared memory (two CTAs per SM) where it can
     for (int pr = 0; pr < J.npq + J.npr; ++pr) {
-      int a = pr < J.npq ? qa[pr] : ra[pr - J.npq], b = pr < J.npq ? qb[pr] : rb[pr - J.npq];
-      if (L.size[a] > kMaxBlock || L.size[b] > kMaxBlock) {
-        J.big_pairs_h.push_back(pr);
-        J.big_smem_qr = std::max(J.big_smem_qr, sizeof(double2) * size_t(L.size[a]) * (L.size[a] + L.size[b]));
+      const bool isq = pr < J.npq;
+      const int a = isq ? qa[pr] : ra[pr - J.npq], b = isq ? qb[pr] : rb[pr - J.npq];
+      const int ba = L.size[a], bb = L.size[b];
+      if (ba <= kMaxBlock && bb <= kMaxBlock) continue;
+      const double2 *M = isq ? Dblk.data() + doff[pr] : Rhoblk.data() + rhooff[pr - J.npq];
+      J.big_rp_off.push_back(big_rp_h.size());
+      for (int l = 0; l < ba; ++l) {
+        big_rp_h.push_back(int(big_ci_h.size()));
+        for (int m = 0; m < bb; ++m) {
+          const double2 v = M[l * bb + m];
+          if (v.x != 0.0 || v.y != 0.0) big_ci_h.push_back(m), big_cv_h.push_back(v);
+        }
+      }
+      big_rp_h.push_back(int(big_ci_h.size()));
+      int nch = 1, w = bb;
+      for (;;) {
+        w = (bb + nch - 1) / nch;
+        if (csz * (size_t(ba) * ba + size_t(bb + ba) * w) <= (size_t(113) << 10) || w <= 8) break;
+        ++nch;
+      }
+      BigPair P{a, b, isq ? qoff[pr] : roff[pr - J.npq], isq ? J.nq : J.nr, isq ? 1 : 0, w, nullptr, nullptr, nullptr};
+      J.big_pairs.push_back(P);
+      const size_t sm = J.mixed ? big_qr_smem<float2>(ba, bb, w) : big_qr_smem<double2>(ba, bb, w);
+      smem_qr[big_nt(ba, w) - 1] = std::max(smem_qr[big_nt(ba, w) - 1], sm);
+    }
+    if (!g_sizing) {
+      auto attr = [](const void *f, size_t bytes) {
+        if (bytes) CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes)));
+      };
+      attr((const void *)k_big_step, smem_step);
+      attr((const void *)k_big_dyson<1>, smem_mat);
+      attr((const void *)k_big_dyson<2>, smem_mat);
+      attr((const void *)k_big_eigframe<1, double2>, smem_mat);
+      attr((const void *)k_big_eigframe<2, double2>, smem_mat);
+      attr((const void *)k_big_eigframe<1, float2>, smem_mat);
+      attr((const void *)k_big_eigframe<2, float2>, smem_mat);
+      attr((const void *)k_big_floquet, smem_mat);
+      if (J.mixed) {
+        attr((const void *)k_big_qr<1, float2>, smem_qr[0]);
+        attr((const void *)k_big_qr<2, float2>, smem_qr[1]);
+      } else {
+        attr((const void *)k_big_qr<1, double2>, smem_qr[0]);
+        attr((const void *)k_big_qr<2, double2>, smem_qr[1]);
       }
     }
-    CUDA_OK(cudaFuncSetAttribute(k_big_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_step)));
-    CUDA_OK(cudaFuncSetAttribute(k_big_dyson, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
-    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(J.big_smem_mat)));
-    CUDA_OK(cudaFuncSetAttribute(k_big_eigframe<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 int(J.big_smem_mat)));
-    CUDA_OK(cudaFuncSetAttribute(k_big_floquet, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_mat)));
-    if (J.big_smem_qr)
-      for (auto f : {k_big_qr<double2>, k_big_qr<float2>})
-        CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(J.big_smem_qr)));
+  }
+  if (!g_sizing && !J.big_blocks.empty() && (!g_arena || g_arena->aux_streams)) {
+    const int naux = int(std::min<size_t>(4, std::max(J.big_blocks.size(), J.big_pairs.size())));
+    CUDA_OK(cudaEventCreateWithFlags(&J.fork_ev, cudaEventDisableTiming));
+    for (int a = 0; a < naux; ++a) {
+      cudaStream_t x;
+      cudaEvent_t e;
+      CUDA_OK(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+      J.aux.push_back(x);
+      CUDA_OK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      J.join_ev.push_back(e);
+    }
   }
   J.blist.resize(kMaxBlock + 1);
   cudaStream_t st = ctx.stream;
@@ -1439,7 +1521,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.ra.upload(ra, st), J.rb.upload(rb, st), J.roff.upload(roff, st), J.rhooff.upload(rhooff, st);
   J.eq.upload(eq, st), J.erev.upload(erev, st), J.er.upload(er, st), J.erg.upload(erg, st), J.esg.upload(esg, st);
   J.srp.upload(srp, st), J.seo.upload(seo, st);
-  J.big_pairs.upload(J.big_pairs_h, st);
+  J.big_rp.upload(big_rp_h, st), J.big_ci.upload(big_ci_h, st), J.big_cv.upload(big_cv_h, st);
+  for (size_t t = 0; t < J.big_pairs.size(); ++t) {
+    J.big_pairs[t].rp = J.big_rp.p + J.big_rp_off[t];
+    J.big_pairs[t].ci = J.big_ci.p;
+    J.big_pairs[t].cv = J.big_cv.p;
+  }
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
@@ -1589,7 +1676,25 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
   ++J.launches;
 }
 
+// Work enqueued on the auxiliary streams after fork() waits for everything before it on
+// the context stream; join() makes the context stream wait for all of it.
+static void fork(JobImpl &J) {
+  if (J.aux.empty()) return;
+  CUDA_OK(cudaEventRecord(J.fork_ev, J.ctx->stream));
+  for (auto a : J.aux) CUDA_OK(cudaStreamWaitEvent(a, J.fork_ev, 0));
+}
+static void join(JobImpl &J) {
+  for (size_t a = 0; a < J.aux.size(); ++a) {
+    CUDA_OK(cudaEventRecord(J.join_ev[a], J.aux[a]));
+    CUDA_OK(cudaStreamWaitEvent(J.ctx->stream, J.join_ev[a], 0));
+  }
+}
+static cudaStream_t aux_stream(JobImpl &J, size_t idx) {
+  return J.aux.empty() ? J.ctx->stream : J.aux[idx % J.aux.size()];
+}
+
 static void launch_stage(JobImpl &J, DevSys &s, int stage) {
+  if (!J.big_blocks.empty()) fork(J);
   launch_block_kernels<1>(J, s, stage);
   launch_block_kernels<2>(J, s, stage);
   launch_block_kernels<3>(J, s, stage);
@@ -1598,24 +1703,36 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
   launch_block_kernels<6>(J, s, stage);
   launch_block_kernels<7>(J, s, stage);
   launch_block_kernels<8>(J, s, stage);
-  // blocks larger than kMaxBlock: one CTA per crystallite (per step for the exponential)
-  cudaStream_t st = J.ctx->stream;
-  for (int k : J.big_blocks) {
+  // blocks larger than kMaxBlock: one CTA per crystallite (per step for the exponential),
+  // each block on its own auxiliary stream
+  for (size_t kb = 0; kb < J.big_blocks.size(); ++kb) {
+    const int k = J.big_blocks[kb];
     const int b = J.L.size[k];
+    cudaStream_t st = aux_stream(J, kb);
     const size_t smat = sizeof(double2) * 2 * size_t(b) * b;
+    const size_t sw = (s.mixed ? sizeof(float2) : sizeof(double2)) * 2 * size_t(b) * b;
+    const unsigned th = big_threads(b, b), th_step = unsigned((big_sym_tiles(b) + 31) / 32 * 32);
+    const bool nt1 = big_nt(b, b) == 1;
     switch (stage) {
-      case 0:
-        k_big_step<<<unsigned(s.C) * unsigned(s.n), kBigThreads, sizeof(double) * 5 * size_t(b) * b, st>>>(s, k);
+      case 0: k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k); break;
+      case 1:
+        if (nt1) k_big_dyson<1><<<unsigned(s.C), th, smat, st>>>(s, k);
+        else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);
         break;
-      case 1: k_big_dyson<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
       case 2: k_big_floquet<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
       case 3:
-        if (s.mixed) k_big_eigframe<float2><<<unsigned(s.C), kBigThreads, smat, st>>>(s, k);
-        else k_big_eigframe<double2><<<unsigned(s.C), kBigThreads, smat, st>>>(s, k);
+        if (s.mixed) {
+          if (nt1) k_big_eigframe<1, float2><<<unsigned(s.C), th, sw, st>>>(s, k);
+          else k_big_eigframe<2, float2><<<unsigned(s.C), th, sw, st>>>(s, k);
+        } else {
+          if (nt1) k_big_eigframe<1, double2><<<unsigned(s.C), th, sw, st>>>(s, k);
+          else k_big_eigframe<2, double2><<<unsigned(s.C), th, sw, st>>>(s, k);
+        }
         break;
     }
     ++J.launches;
   }
+  if (!J.big_blocks.empty()) join(J);
 }
 
 static void mark_begin(JobImpl &J, int stage);
@@ -1650,20 +1767,32 @@ void Job::run() {
     }
     long Cp = s.Cpad;
     mark_begin(J, 4);
+    const int qr_before = J.launches;
     if (!J.is_static && J.npq + J.npr > 0) {
+      if (!J.big_pairs.empty()) fork(J);
       if (s.mixed) k_qr<float2><<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
       else k_qr<double2><<<grid_for(Cp * (J.npq + J.npr) * J.n), kThreads, 0, st>>>(s);
       ++J.launches;
-      if (!J.big_pairs_h.empty()) {
-        unsigned grid = unsigned(J.big_pairs_h.size()) * unsigned(s.C) * unsigned(J.n);
-        if (s.mixed)
-          k_big_qr<float2><<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
-        else
-          k_big_qr<double2><<<grid, kBigThreads, J.big_smem_qr, st>>>(s, J.big_pairs.p, int(J.big_pairs_h.size()));
+      for (size_t t = 0; t < J.big_pairs.size(); ++t) {
+        const BigPair &P = J.big_pairs[t];
+        cudaStream_t st = aux_stream(J, t);
+        const int ba = J.L.size[P.a], bb = J.L.size[P.b];
+        const unsigned grid = unsigned(s.C) * unsigned(J.n), th = big_threads(ba, P.wchunk);
+        const bool nt1 = big_nt(ba, P.wchunk) == 1;
+        if (s.mixed) {
+          const size_t sm = big_qr_smem<float2>(ba, bb, P.wchunk);
+          if (nt1) k_big_qr<1, float2><<<grid, th, sm, st>>>(s, P);
+          else k_big_qr<2, float2><<<grid, th, sm, st>>>(s, P);
+        } else {
+          const size_t sm = big_qr_smem<double2>(ba, bb, P.wchunk);
+          if (nt1) k_big_qr<1, double2><<<grid, th, sm, st>>>(s, P);
+          else k_big_qr<2, double2><<<grid, th, sm, st>>>(s, P);
+        }
         ++J.launches;
       }
+      if (!J.big_pairs.empty()) join(J);
     }
-    mark_end(J, 4, !J.is_static && J.npq + J.npr > 0 ? 1 : 0);
+    mark_end(J, 4, J.launches - qr_before);
     mark_begin(J, 5);
     if (J.is_static && J.ne > 0) {
       k_static_elems<<<grid_for(Cp * J.npq), kThreads, 0, st>>>(s);
@@ -1959,6 +2088,7 @@ std::unique_ptr<Job> job_in_region(Context &ctx, void *base, size_t bytes, const
   arena.base = static_cast<char *>(base);
   arena.cap = bytes;
   arena.label = "device region given to the job";
+  arena.aux_streams = true;
   size_t fixed = fixed_bytes(pw, p);
   if (fixed >= bytes) throw Error(4, "job does not fit a device region of " + std::to_string(bytes >> 20) + " MiB");
   ctx.hbm_budget = bytes - fixed;

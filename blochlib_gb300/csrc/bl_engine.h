@@ -23,6 +23,7 @@ struct FidParams {
 struct Context {
   int device = 0;
   size_t hbm_budget = 0;  // bytes the engine may hold for one job's work buffers
+                          // (0: 60% of the device memory free when the job is created)
   cudaStream_t stream = nullptr;
   ~Context();
 };

@@ -65,7 +65,9 @@ const char *bl_last_error(void);
 /* Library version string. */
 const char *bl_version(void);
 
-/* Context: one CUDA device and stream; hbm_budget bytes for work buffers (0 = 16 GiB). */
+/* Context: one CUDA device and stream; hbm_budget bytes for one job's work buffers (0 = 60%
+ * of the device memory free when the job is created).  A job whose crystallites do not fit
+ * runs them in equal batches. */
 bl_status bl_ctx_create(int device, size_t hbm_budget, bl_ctx **out);
 void bl_ctx_destroy(bl_ctx *ctx);
 
