@@ -118,10 +118,15 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def workload(name):
+def workload(args):
+    """The single-job workload: c0/c1/c2, or one seeded c3/c4 system (--system), with
+    optional overrides of the steps per rotor period (--period-steps)."""
     from blochlib_gb300 import workloads as W
-    idx = {"c0": 0, "c1": 1, "c2": 2}[name]
-    return W.config(idx)
+    idx = {"c0": 0, "c1": 1, "c2": 2, "c3": 3, "c4": 4}[args.config]
+    cfg = W.config(idx, args.system or 0)
+    if args.period_steps:
+        cfg = dict(cfg, sw=args.period_steps * cfg["wr"])
+    return cfg
 
 
 def make_job(bl, cfg, ctx, step_method=None, fave_method=None, precision=0):
@@ -190,7 +195,7 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    cfg = workload(args.config)
+    cfg = workload(args)
     binary, kind = _ref_binary()
     vals = []
     # each step is a bounded sample; the whole run stays within about two minutes
@@ -376,6 +381,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"])
     ap.add_argument("--systems", type=int, default=128, help="c3: number of seeded systems in the batch")
+    ap.add_argument("--system", type=int, default=None,
+                    help="c3/c4: time this one seeded system as a single job instead of the batching/serving form")
+    ap.add_argument("--period-steps", type=int, default=0, help="override the steps per rotor period (sw = n wr)")
     ap.add_argument("--lanes", type=int, default=16, help="c3/c4: serving lanes (CUDA streams)")
     ap.add_argument("--pool-gib", type=int, default=128, help="c3/c4: serving memory pool (GiB)")
     ap.add_argument("--rate", type=float, default=200.0, help="c4: offered requests per second")
@@ -395,16 +403,16 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.config == "c3":
+    if args.config == "c3" and args.system is None:
         return run_batch(args)
-    if args.config == "c4":
+    if args.config == "c4" and args.system is None:
         return run_serving(args)
     args.warmup = max(args.warmup, 3)
     prec = args.precision or ("mixed" if args.config == "c2" else "fp64")
     import blochlib_gb300 as bl
     d = Dist()
     ctx = bl.Context(d.local)
-    cfg = workload(args.config)
+    cfg = workload(args)
     if args.crystallites:
         cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
     s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if prec == "mixed" else 0)

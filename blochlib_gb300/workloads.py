@@ -14,9 +14,11 @@ for couplings and shifts, degrees for Euler and rotor angles, radians in powder 
   c2  8 x 1H (dim 256): coordinates in a 5 A cube with 1.5 A minimum separation, all 28
       dipoles, CSA as c1; 30 kHz MAS, 200 steps, 4096 points, ZCW 1154.
   c3  512 systems of 2..7 1H (dims 4..128), dipoles + CSA as c2, weak J U(0,200) Hz,
-      MAS U(5,35) kHz, U{64..256} steps, 1024 points, powders from
-      {144, 320, 678, 1154} (the reference ships repulsion sets for the first three; here
-      they are stand-in 3-angle ZCW-type lattices of the same size).
+      MAS U(5,35) kHz, U{64..256} steps, 1024 points, powders drawn from {144, 320, 678,
+      1154}: the reference's repulsion sets crystals/rep144, rep320, rep678 (677 points,
+      gamma = 0) and the 3-angle ZCW 1154.
+  c4  the serving stream: c3-like jobs plus large jobs of 9..10 1H (dims 512..1024) drawn
+      like c3 on the reference's 100-point repulsion set crystals/rep100 (config(4, i)).
 
 Dipole sign: BlochLib's 'D del' enters H as del*(3cos^2-1)/2*(2IzSz - IxSx - IySy), so
 the physical homonuclear coupling is del = -b with b = 120.07 kHz / r^3 (r in A).
@@ -50,15 +52,20 @@ def zcw3(N, a=None, b=None, g=None):
     return alpha, beta, gamma, w
 
 
-def lattice3(N, seed):
-    """Stand-in 3-angle set of N points (golden-ratio lattice, gamma from a second
-    irrational step), equal weights; used where the reference has no 3-angle ZCW file."""
-    j = np.arange(N, dtype=np.float64) + 0.5
-    phi1 = (1 + 5 ** 0.5) / 2
-    alpha = 2 * np.pi * ((j / phi1) % 1.0)
-    beta = np.arccos(1 - 2 * j / N)
-    gamma = 2 * np.pi * ((j * 2 ** 0.5) % 1.0)
-    return alpha, beta, gamma, np.full(N, 1.0 / N)
+_REP = None
+
+
+def rep(N):
+    """The reference's repulsion powder set crystals/rep<N> (N in 100, 144, 320, 678; rep678
+    holds 677 points) as (phi, theta, gamma, weight); stored in data/rep_powders.npz by
+    data/make_powders.py."""
+    global _REP
+    if _REP is None:
+        from pathlib import Path
+        with np.load(Path(__file__).resolve().parent / "data" / "rep_powders.npz") as z:
+            _REP = {k: z[k] for k in z.files}
+    a = _REP[f"rep{N}"]
+    return tuple(np.array(a[i]) for i in range(4))
 
 
 def _euler(rng):
@@ -103,7 +110,7 @@ def _csa_lines(rng, nspin, hz_per_ppm=400.0, max_ppm=10.0):
 
 def config(index, system=0):
     """Workload dict: spin lines, rho/det expressions, params and powder arrays."""
-    rng = np.random.default_rng(SEED0 + index + (system if index == 3 else 0))
+    rng = np.random.default_rng(SEED0 + index + (system if index in (3, 4) else 0))
     if index == 0:
         a, b, g = rng.uniform(0, 360, 3)
         iso = rng.uniform(-50, 50) * 100.0
@@ -126,8 +133,8 @@ def config(index, system=0):
         lines = ["numspin 8"] + [f"T 1H {k}" for k in range(8)] + _csa_lines(rng, 8) + _dipole_lines(xyz)
         return dict(name="c2", lines=lines, rho="Fx", det="Fp", npts=4096, wr=30e3, sw=200 * 30e3,
                     rotb=MAGIC_ANGLE, powder=zcw3(1154))
-    if index == 3:
-        nspin = int(rng.integers(2, 8))
+    if index in (3, 4):
+        nspin = int(rng.integers(2, 8)) if index == 3 else int(rng.integers(9, 11))
         xyz = _proton_cluster(rng, nspin, 5.0, min_sep=1.5)
         lines = ["numspin %d" % nspin] + [f"T 1H {k}" for k in range(nspin)] + _csa_lines(rng, nspin) + _dipole_lines(xyz)
         for i in range(nspin):
@@ -135,9 +142,12 @@ def config(index, system=0):
                 lines.append(f"J {rng.uniform(0, 200):.10g} {i} {j}")
         wr = float(rng.uniform(5e3, 35e3))
         n = int(rng.integers(64, 257))
-        npow = int(rng.choice([144, 320, 678, 1154]))
-        pw = zcw3(1154) if npow == 1154 else lattice3(npow, SEED0 + system)
-        return dict(name=f"c3.{system}", lines=lines, rho="Fx", det="Fp", npts=1024, wr=wr, sw=n * wr,
+        if index == 3:
+            npow = int(rng.choice([144, 320, 678, 1154]))
+            pw = zcw3(1154) if npow == 1154 else rep(npow)
+        else:
+            pw = rep(100)
+        return dict(name=f"c{index}.{system}", lines=lines, rho="Fx", det="Fp", npts=1024, wr=wr, sw=n * wr,
                     rotb=MAGIC_ANGLE, powder=pw)
     raise ValueError(index)
 
