@@ -94,10 +94,10 @@ STEP_EIGH, STEP_TAYLOR = 0, 1
 
 
 def _step_method(m):
-    """Step exponential: 'eigh' (0, Jacobi eigen-decomposition) or 'taylor' (1);
-    default from BL_STEP_METHOD, else eigh."""
+    """Step exponential: 'eigh' (0, Jacobi eigen-decomposition) or 'taylor' (1, faster);
+    default from BL_STEP_METHOD, else taylor."""
     if m is None:
-        m = os.environ.get("BL_STEP_METHOD", "eigh")
+        m = os.environ.get("BL_STEP_METHOD", "taylor")
     if isinstance(m, str):
         m = {"eigh": STEP_EIGH, "taylor": STEP_TAYLOR}[m]
     return int(m)

@@ -7,7 +7,7 @@
 //   SolidSys::Fx() ... Imi(k)          src/QMspins/spinsys.h:143-162
 //   Rotations (Cartesian)              src/QMspins/space_ten.h:60-111, space_ten.cc:578-805
 //   powder(powder::zcw, t, p, g)       src/QMspins/driver/powder.cc:94-113, 248-280
-//   powder::read(file)                 src/QMspins/driver/powder.cc:333-389
+//   powder(file)                       src/QMspins/driver/powder.cc:333-389
 //   oneFID<SolidSys>(sys, npts, sw, wr, rotb, startT), FID(powder, ro, det)
 //                                      src/QMspins/driver/oneFID.h:103-108, 200-208
 //   plotterFID(fid, file, dt)          src/utils/plotter.cc:49-135
@@ -154,7 +154,7 @@ class oneFID {
   oneFID(Func_T &sys, int npts, double sw = 20000, double wr = 0, double rotb = 0, double startT = 0)
       : sys_(&sys), npts_(npts), sw_(sw), wr_(wr), rotb_(rotb), startT_(startT) {}
   std::vector<complex> FID(powder &pw, const matrix &ro, const matrix &det) {
-    bl_fid_params p = {npts_, sw_, wr_, rotb_, startT_, 0, 0, 0};
+    bl_fid_params p = {npts_, sw_, wr_, rotb_, startT_, 0, /*Taylor step*/ 1, 0};
     std::vector<complex> fid(static_cast<size_t>(npts_));
     double sw_used = sw_;
     check(bl_powder_fid(Context::get(), sys_->handle(), pw.handle(), ro.data(), det.data(), &p,
