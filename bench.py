@@ -310,16 +310,15 @@ def run_batch(args):
 
 
 def run_serving(args):
-    """c4: Poisson request stream (seeded) of c3-like jobs plus 10% large (8 x 1H, dim 256, 100
-    crystallites; 9-10 spin jobs exceed the engine's block limit), for a fixed window; the
-    backlog left at the end is cancelled and reported.  Mixed and FP64 on the same stream."""
+    """c4: Poisson request stream (seeded) of c3-like jobs plus 10% large jobs (9-10 x 1H,
+    dims 512-1024, on the 100-point repulsion set), for a fixed window; the backlog left at
+    the end is cancelled and reported.  Mixed and FP64 on the same stream."""
     import blochlib_gb300 as bl
     from blochlib_gb300 import workloads as W
     rank, world, local = dist_env()
     rng = np.random.default_rng(W.SEED0 + 4)
     small = [_job_inputs(bl, W.config(3, 1000 + i)) for i in range(48)]
-    c2 = W.config(2)
-    large = [_job_inputs(bl, dict(c2, powder=W.subset(c2["powder"], 100, 100 * i))) for i in range(4)]
+    large = [_job_inputs(bl, W.config(4, i)) for i in range(4)]
     n_req = int(args.rate * args.duration)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
     picks = [(large[rng.integers(len(large))] if rng.uniform() < 0.1 else small[rng.integers(len(small))])
@@ -367,7 +366,7 @@ def run_serving(args):
         "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["total_s"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic seeded Poisson stream (workloads.py)",
         "config": {"workload": f"c4 serving form: Poisson {args.rate}/s for {args.duration} s, 90% c3-like, 10% "
-                               "8 x 1H dim 256 on 100 crystallites", "lanes": args.lanes, "pool_gib": args.pool_gib,
+                               "9-10 x 1H (dims 512-1024) on rep100", "lanes": args.lanes, "pool_gib": args.pool_gib,
                    "drain_s": args.drain},
         "latency_ms": forms["mixed"]["latency_ms"], "precision_forms": forms}))
     return 0

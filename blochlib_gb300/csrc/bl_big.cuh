@@ -379,23 +379,27 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_qr(DevSys s, BigPa
   }
 }
 
-// One CTA per crystallite: unitary eigen-decomposition of the big block of A_n by the
-// Cayley transform K = i (I+W)^{-1}(I-W), W = e^{ia} A_n, and a parallel (round-robin)
-// complex Jacobi on K; a second pass moves -1 into the widest spectral gap when the first
-// is ill conditioned.  Shared memory: two complex b x b matrices.
-__global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
-  extern __shared__ double2 bsc[];
-  __shared__ double2 rot[kMaxBigBlock / 2 + 1][2];  // (c, 0), (s e^{i ph}) per pair
-  __shared__ int rpair[kMaxBigBlock / 2 + 1][2];
-  __shared__ double2 fv[kMaxBigBlock];
-  __shared__ double2 lam[kMaxBigBlock];
-  __shared__ double red[kBigThreads];
+// One CTA per crystallite: unitary eigen-decomposition of a block of A_n by the Cayley
+// transform K = i (I+W)^{-1}(I-W), W = e^{ia} A_n, and a parallel (round-robin) complex
+// Jacobi on K; a second pass moves -1 into the widest spectral gap when the first is ill
+// conditioned.  Work arrays of floquet_cta: Mm, Xk (b x b each), rot and rpair ((b/2+1) x 2),
+// fv and lam (b each), red (max(b, blockDim.x)); in shared memory for blocks up to
+// kMaxBigBlock, Mm and Xk in global memory above.
+struct FloqWork {
+  double2 *Mm, *Xk, *rot, *fv, *lam;
+  int *rpair;
+  double *red;
+};
+
+__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk) {
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
-  const int c = blockIdx.x;
   const int b = s.bs[k], bp = s.bpoff[k], bo = s.boff[k], bb = b * b;
-  double2 *Mm = bsc, *Xk = Mm + bb;
+  double2 *Mm = wk.Mm, *Xk = wk.Xk, *fv = wk.fv, *lam = wk.lam;
+  double *red = wk.red;
+  auto rot = [&](int t, int q) -> double2 & { return wk.rot[2 * t + q]; };
+  auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
   const double2 *U = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;  // U(r,q) = U[at(bp + r*b + q, c)]
   auto Ug = [&](int r, int q) { return U[at(bp + r * b + q, c, s.Cpad)]; };
   if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
@@ -516,8 +520,8 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
             int tmp = p;
             p = q, q = tmp;
           }
-          rpair[t][0] = p, rpair[t][1] = q;
-          rot[t][0] = cmk(1, 0), rot[t][1] = cmk(0, 0);
+          rpair(t, 0) = p, rpair(t, 1) = q;
+          rot(t, 0) = cmk(1, 0), rot(t, 1) = cmk(0, 0);
           if (q < b) {
             const double2 hpq = Xk[p * b + q];
             const double ab = hypot(hpq.x, hpq.y);
@@ -528,8 +532,8 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
               if (fabs(theta) > 1e100) tt = 0.5 / theta;
               else tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
               const double cc = rsqrt(fma(tt, tt, 1.0));
-              rot[t][0] = cmk(cc, 0.0);
-              rot[t][1] = cscale(ph, tt * cc);
+              rot(t, 0) = cmk(cc, 0.0);
+              rot(t, 1) = cscale(ph, tt * cc);
             }
           }
         }
@@ -538,10 +542,10 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
         for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
           const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
           double2 *Mx = rem2 < b ? Xk : Mm;
-          const int p = rpair[t][0], q = rpair[t][1];
+          const int p = rpair(t, 0), q = rpair(t, 1);
           if (q >= b) continue;
-          const double cc = rot[t][0].x;
-          const double2 sp = rot[t][1], spc = cconj(sp);
+          const double cc = rot(t, 0).x;
+          const double2 sp = rot(t, 1), spc = cconj(sp);
           const double2 xkp = Mx[kk * b + p], xkq = Mx[kk * b + q];
           Mx[kk * b + p] = csub(cscale(xkp, cc), cmul(spc, xkq));
           Mx[kk * b + q] = cadd(cmul(sp, xkp), cscale(xkq, cc));
@@ -550,18 +554,18 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
         // rows p, q of K:  K <- G^H K
         for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
           const int t = e / b, kk = e % b;
-          const int p = rpair[t][0], q = rpair[t][1];
+          const int p = rpair(t, 0), q = rpair(t, 1);
           if (q >= b) continue;
-          const double cc = rot[t][0].x;
-          const double2 sp = rot[t][1], spc = cconj(sp);
+          const double cc = rot(t, 0).x;
+          const double2 sp = rot(t, 1), spc = cconj(sp);
           const double2 xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
           Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
           Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
         }
         __syncthreads();
         for (int t = threadIdx.x; t < np; t += blockDim.x) {
-          const int p = rpair[t][0], q = rpair[t][1];
-          if (q >= b || (rot[t][1].x == 0.0 && rot[t][1].y == 0.0)) continue;
+          const int p = rpair(t, 0), q = rpair(t, 1);
+          if (q >= b || (rot(t, 1).x == 0.0 && rot(t, 1).y == 0.0)) continue;
           Xk[p * b + q] = cmk(0, 0), Xk[q * b + p] = cmk(0, 0);
           Xk[p * b + p].y = 0.0, Xk[q * b + q].y = 0.0;
         }
@@ -610,4 +614,16 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   for (int e = threadIdx.x; e < bb; e += blockDim.x) s.VF[at(bp + e, c, s.Cpad)] = Mm[e];
   for (int r = threadIdx.x; r < b; r += blockDim.x)
     s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
+}
+
+// One CTA per crystallite: unitary eigen-decomposition of a large block of A_n.
+__global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
+  extern __shared__ double2 bsc[];
+  __shared__ double2 rot[(kMaxBigBlock / 2 + 1) * 2];  // (c, 0), (s e^{i ph}) per pair
+  __shared__ int rpair[(kMaxBigBlock / 2 + 1) * 2];
+  __shared__ double2 fv[kMaxBigBlock];
+  __shared__ double2 lam[kMaxBigBlock];
+  __shared__ double red[kBigThreads];
+  const int b = s.bs[k];
+  floquet_cta(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red});
 }

@@ -1053,6 +1053,7 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
 }
 
 #include "bl_big.cuh"
+#include "bl_huge.cuh"
 
 constexpr int kFidJT = 4, kFidPT = 4;
 
@@ -1165,6 +1166,7 @@ static thread_local ScratchArena *g_arena = nullptr;
 struct JobSizing {
   size_t per_c = 0;
   long cpad = 0;
+  size_t extra = 0;  // bytes independent of the batch size (huge-block workspace)
 };
 static thread_local JobSizing *g_sizing = nullptr;
 
@@ -1211,9 +1213,17 @@ struct JobImpl {
   int nint = 0, nq = 0, nr = 0, ne = 0, npq = 0, npr = 0;
   int Cb = 0, nbatch = 0, nwarps_total = 0;
   std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices (size <= kMaxBlock)
-  std::vector<int> big_blocks;                   // blocks larger than kMaxBlock
-  std::vector<BigPair> big_pairs;                // Q/R pairs with a block larger than kMaxBlock
-  std::vector<size_t> big_rp_off;                // each big pair's row pointers in big_rp
+  std::vector<int> big_blocks;                   // blocks kMaxBlock < b <= kMaxBigBlock
+  std::vector<BigPair> big_pairs;                // Q/R pairs whose largest block is one of those
+  std::vector<int> huge_blocks;                  // blocks larger than kMaxBigBlock
+  std::vector<int> huge_sq;                      // per huge block: squarings that bound every step's
+  std::vector<BigPair> huge_pairs;               // Q/R pairs with a huge block
+  size_t huge_ws_bytes = 0;                      // workspace of the huge-block products
+  int huge_items = 0;                            // largest chunk of exponential items
+  DevBuf<double2> huge_ws;
+  DevBuf<double> hfk, hsc;
+  DevBuf<int> hsq, hsqmax;
+  std::vector<size_t> big_rp_off, huge_rp_off;   // each pair's row pointers in big_rp
   DevBuf<int> big_rp, big_ci;                    // non-zeros of M_ab by row, all big pairs
   DevBuf<double2> big_cv;
   DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status, srp, seo;
@@ -1301,9 +1311,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   J.L = sys.layout();
   const BlockLayout &L = J.L;
-  if (L.max_block > kMaxBigBlock)
+  if (L.max_block > kMaxHugeBlock)
     throw Error(5, "Hamiltonian block of size " + std::to_string(L.max_block) + " exceeds this engine's limit of " +
-                       std::to_string(kMaxBigBlock));
+                       std::to_string(kMaxHugeBlock));
   if (J.is_static && L.max_block > kMaxBlock)
     throw Error(5, "static powder FIDs support Hamiltonian blocks up to " + std::to_string(kMaxBlock));
   const int nb = int(L.size.size());
@@ -1413,9 +1423,35 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
                          : sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + wide);
   per_c += sizeof(double) * 11;
   long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
+  // huge blocks: one workspace for their batched products, at least one item of each use
+  // (exponential: 7 real b x b; Floquet: 2 complex b x b; eigenframe, Q/R: one complex
+  // matrix), else 1 GiB
+  size_t huge_fixed = 0;
+  {
+    size_t need = 0;
+    int bmin = 0;
+    for (int k = 0; k < nb; ++k) {
+      const size_t b = size_t(L.size[k]);
+      if (L.size[k] <= kMaxBigBlock) continue;
+      need = std::max(need, std::max(sizeof(double) * kHugeSlots * b * b, 2 * sizeof(double2) * b * b));
+      bmin = bmin ? std::min(bmin, L.size[k]) : L.size[k];
+    }
+    for (int pr = 0; pr < J.npq + J.npr; ++pr) {
+      const bool isq = pr < J.npq;
+      const int ba = L.size[isq ? qa[pr] : ra[pr - J.npq]], bb = L.size[isq ? qb[pr] : rb[pr - J.npq]];
+      if (std::max(ba, bb) > kMaxBigBlock) need = std::max(need, sizeof(double2) * size_t(ba) * bb);
+    }
+    if (need && !J.is_static) {
+      J.huge_ws_bytes = (std::max(need, size_t(1) << 30) + 255) / 256 * 256;
+      J.huge_items = int(std::min<size_t>(kHugeMaxItems, J.huge_ws_bytes / (sizeof(double) * kHugeSlots *
+                                                                            size_t(bmin) * size_t(bmin))));
+      huge_fixed = J.huge_ws_bytes + size_t(J.huge_items) * (sizeof(double) * (J.nint + 1) + sizeof(int)) + 4096;
+    }
+  }
   if (g_sizing) {
     g_sizing->per_c = per_c;
     g_sizing->cpad = cpad_all;
+    g_sizing->extra = huge_fixed;
     return;
   }
   size_t budget = ctx.hbm_budget;
@@ -1424,6 +1460,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     CUDA_OK(cudaMemGetInfo(&fr, &tot));
     budget = size_t(0.6 * double(fr));
   }
+  budget = budget > huge_fixed ? budget - huge_fixed : 0;
   long cb = long(budget / std::max<size_t>(per_c, 1));
   cb = (cb / 32) * 32;
   if (cb < 32) throw Error(4, "job does not fit the device memory budget (one warp of crystallites)");
@@ -1436,12 +1473,41 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.blocks_by_size.assign(kMaxBlock + 1, {});
   for (int k = 0; k < nb; ++k) {
     if (L.size[k] <= kMaxBlock) J.blocks_by_size[L.size[k]].push_back(k);
-    else J.big_blocks.push_back(k);
+    else if (L.size[k] <= kMaxBigBlock) J.big_blocks.push_back(k);
+    else J.huge_blocks.push_back(k);
+  }
+  // per huge block: squarings enough for every step, from a rotation-free bound on
+  // ||2 pi tau H||_inf (|a_k| <= ||PAS'_k||_F); the kernels skip items that need fewer
+  for (int k : J.huge_blocks) {
+    const int b = L.size[k], bp = L.poff[k];
+    double nrm = 0;
+    for (int r = 0; r < b; ++r) {
+      double rs = 0;
+      for (int q = 0; q < b; ++q) {
+        double v = std::fabs(Hc[bp + r * b + q]);
+        for (int kk = 0; kk < J.nint; ++kk) {
+          const double *Pa = pas.data() + 6 * kk;
+          const double fro = std::sqrt(Pa[0] * Pa[0] + Pa[3] * Pa[3] + Pa[5] * Pa[5] +
+                                       2 * (Pa[1] * Pa[1] + Pa[2] * Pa[2] + Pa[4] * Pa[4]));
+          v += std::fabs(isc[kk]) * fro * std::fabs(Tk[size_t(kk) * L.S2 + bp + r * b + q]);
+        }
+        rs += v;
+      }
+      nrm = std::max(nrm, rs);
+    }
+    nrm *= J.tau * kPi2 * (1.0 + 1e-12);  // margin over the device's rounding of the same sum
+    int q = 0;
+    if (nrm > 0.5) {
+      std::frexp(nrm / 0.5, &q);
+      q = std::min(q, 60);
+    }
+    J.huge_sq.push_back(q);
   }
   std::vector<int> big_rp_h, big_ci_h;
   std::vector<double2> big_cv_h;
-  if (!J.big_blocks.empty()) {
-    if (J.nint > kMaxInt) throw Error(5, "more than " + std::to_string(kMaxInt) + " anisotropic interactions");
+  if (!J.big_blocks.empty() || !J.huge_blocks.empty()) {
+    if (!J.big_blocks.empty() && J.nint > kMaxInt)
+      throw Error(5, "more than " + std::to_string(kMaxInt) + " anisotropic interactions");
     const size_t csz = J.mixed ? sizeof(float2) : sizeof(double2);
     size_t smem_step = 0, smem_mat = 0, smem_qr[2] = {0, 0};
     for (int k : J.big_blocks) {
@@ -1456,7 +1522,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       const int ba = L.size[a], bb = L.size[b];
       if (ba <= kMaxBlock && bb <= kMaxBlock) continue;
       const double2 *M = isq ? Dblk.data() + doff[pr] : Rhoblk.data() + rhooff[pr - J.npq];
-      J.big_rp_off.push_back(big_rp_h.size());
+      const size_t rp_off = big_rp_h.size();
       for (int l = 0; l < ba; ++l) {
         big_rp_h.push_back(int(big_ci_h.size()));
         for (int m = 0; m < bb; ++m) {
@@ -1472,7 +1538,13 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         ++nch;
       }
       BigPair P{a, b, isq ? qoff[pr] : roff[pr - J.npq], isq ? J.nq : J.nr, isq ? 1 : 0, w, nullptr, nullptr, nullptr};
+      if (std::max(ba, bb) > kMaxBigBlock) {  // k_huge_mx + k_huge_zgemm
+        J.huge_pairs.push_back(P);
+        J.huge_rp_off.push_back(rp_off);
+        continue;
+      }
       J.big_pairs.push_back(P);
+      J.big_rp_off.push_back(rp_off);
       const size_t sm = J.mixed ? big_qr_smem<float2>(ba, bb, w) : big_qr_smem<double2>(ba, bb, w);
       smem_qr[big_nt(ba, w) - 1] = std::max(smem_qr[big_nt(ba, w) - 1], sm);
     }
@@ -1488,6 +1560,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
       attr((const void *)k_big_eigframe<2, float2>, smem_mat);
       attr((const void *)k_big_floquet, smem_mat);
+      size_t smem_hf = 0;
+      for (int k : J.huge_blocks) smem_hf = std::max(smem_hf, huge_floquet_smem(L.size[k]));
+      if (smem_hf > (size_t(48) << 10)) attr((const void *)k_huge_floquet, smem_hf);
       if (J.mixed) {
         attr((const void *)k_big_qr<1, float2>, smem_qr[0]);
         attr((const void *)k_big_qr<2, float2>, smem_qr[1]);
@@ -1522,11 +1597,11 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   J.eq.upload(eq, st), J.erev.upload(erev, st), J.er.upload(er, st), J.erg.upload(erg, st), J.esg.upload(esg, st);
   J.srp.upload(srp, st), J.seo.upload(seo, st);
   J.big_rp.upload(big_rp_h, st), J.big_ci.upload(big_ci_h, st), J.big_cv.upload(big_cv_h, st);
-  for (size_t t = 0; t < J.big_pairs.size(); ++t) {
-    J.big_pairs[t].rp = J.big_rp.p + J.big_rp_off[t];
-    J.big_pairs[t].ci = J.big_ci.p;
-    J.big_pairs[t].cv = J.big_cv.p;
-  }
+  for (size_t t = 0; t < J.big_pairs.size(); ++t)
+    J.big_pairs[t].rp = J.big_rp.p + J.big_rp_off[t], J.big_pairs[t].ci = J.big_ci.p, J.big_pairs[t].cv = J.big_cv.p;
+  for (size_t t = 0; t < J.huge_pairs.size(); ++t)
+    J.huge_pairs[t].rp = J.big_rp.p + J.huge_rp_off[t], J.huge_pairs[t].ci = J.big_ci.p,
+    J.huge_pairs[t].cv = J.big_cv.p;
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
@@ -1558,6 +1633,13 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.Q.alloc(nQ), J.R.alloc(nR), J.G.alloc(nG), J.Z.alloc(nZ);
   }
   J.partial.alloc(size_t(J.nwarps_total) * p.npts);
+  if (J.huge_ws_bytes) {
+    J.huge_ws.alloc(J.huge_ws_bytes / sizeof(double2));
+    J.hfk.alloc(size_t(J.huge_items) * std::max(J.nint, 1));
+    J.hsc.alloc(size_t(J.huge_items));
+    J.hsq.alloc(size_t(J.huge_items));
+    J.hsqmax.alloc(1);
+  }
   J.fid.alloc(p.npts);
   CUDA_OK(cudaMemsetAsync(J.partial.p, 0, J.partial.n * sizeof(double2), st));
   CUDA_OK(cudaStreamSynchronize(st));
@@ -1693,6 +1775,143 @@ static cudaStream_t aux_stream(JobImpl &J, size_t idx) {
   return J.aux.empty() ? J.ctx->stream : J.aux[idx % J.aux.size()];
 }
 
+
+// ------------------------------------------------------------------ huge blocks (bl_huge.cuh)
+// All on the context stream; every launch covers at most kHugeMaxItems items and the
+// workspace holds one launch's items.
+template <class T>
+static HMat<T> item_mat(T *p, long off, long sstr, int ld, int Cpad) {
+  return HMat<T>{p, off, sstr, long(ld), long(Cpad), 1};
+}
+template <class T>
+static HMat<T> ws_mat(T *p, long j0, long mat, int C, int ld) {
+  return HMat<T>{p, -j0 * mat, long(C) * mat, long(ld), 1, mat};
+}
+static unsigned tiles(int m, int n) { return unsigned(((m + kHT - 1) / kHT) * ((n + kHT - 1) / kHT)); }
+
+// U_i of huge block k for every (crystallite, step): symmetric Paterson-Stockmeyer.
+static void huge_step(JobImpl &J, DevSys &s, size_t kh) {
+  const int k = J.huge_blocks[kh], b = J.L.size[k], bp = J.L.poff[k];
+  const long bb = long(b) * b, total = long(s.C) * J.n;
+  const long per = std::min<long>(J.huge_items, long(J.huge_ws_bytes / (sizeof(double) * kHugeSlots * bb)));
+  cudaStream_t st = J.ctx->stream;
+  double *ws = reinterpret_cast<double *>(J.huge_ws.p);
+  const unsigned ge = unsigned((bb + 255) / 256), tm = unsigned((b + kHT - 1) / kHT), gs = tm * (tm + 1) / 2;
+  for (long j0 = 0; j0 < total; j0 += per) {
+    const int items = int(std::min(per, total - j0));
+    auto sym = [&](int a, int bsl, int o, int akind, double alpha, int round, bool low, double c0, double c1,
+                   double c2, double c3) {
+      SymArgs g{ws, J.hsc.p, J.hsq.p, bb, b, a, bsl, o, akind, alpha, round, low ? 1 : 0, c0, c1, c2, c3};
+      k_huge_sym<<<dim3(gs, unsigned(items)), kHThreads, 0, st>>>(g);
+      ++J.launches;
+    };
+    k_huge_fk<<<unsigned((items + 127) / 128), 128, 0, st>>>(s, j0, items, J.hfk.p);
+    k_huge_hbuild<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, bp, b, J.hfk.p, ws);
+    CUDA_OK(cudaMemsetAsync(J.hsqmax.p, 0, sizeof(int), st));
+    k_huge_norm<<<unsigned(items), 256, 0, st>>>(ws, b, s.tau * kPi2, J.hsc.p, J.hsq.p, J.hsqmax.p);
+    J.launches += 3;
+    sym(0, 0, 1, 1, 1.0, -1, false, 0, 0, 0, 0);  // Y = sc^2 H H
+    sym(1, 1, 2, 0, 1.0, -1, false, 0, 0, 0, 0);  // Y^2
+    sym(2, 1, 3, 0, 1.0, -1, false, 0, 0, 0, 0);  // Y^3
+    sym(2, 2, 4, 0, 1.0, -1, false, 0, 0, 0, 0);  // Y^4
+    // cos X = C(Y), coefficients (-1)^j/(2j)!;  sin X = X S(Y), (-1)^j/(2j+1)!
+    k_huge_low<<<dim3(ge, unsigned(items)), 256, 0, st>>>(ws, b, 1.0 / 40320, -1.0 / 3628800, 1.0 / 479001600,
+                                                          -1.0 / 87178291200.0);
+    sym(4, 5, 6, 0, 1.0, -1, true, 1.0, -1.0 / 2, 1.0 / 24, -1.0 / 720);  // R = cos X
+    k_huge_low<<<dim3(ge, unsigned(items)), 256, 0, st>>>(ws, b, 1.0 / 362880, -1.0 / 39916800,
+                                                          1.0 / 6227020800.0, -1.0 / 1307674368000.0);
+    sym(4, 5, 3, 0, 1.0, -1, true, 1.0, -1.0 / 6, 1.0 / 120, -1.0 / 5040);  // S(Y) over Y^3
+    sym(0, 3, 1, 2, 1.0, -1, false, 0, 0, 0, 0);                            // I = -sc H S
+    J.launches += 2;
+    // squarings: the host bound for the block; each item skips the rounds it does not need
+    for (int t = 0; t < J.huge_sq[kh]; ++t) {
+      sym(6, 6, 2, 0, 1.0, t, false, 0, 0, 0, 0);
+      sym(1, 1, 4, 0, 1.0, t, false, 0, 0, 0, 0);
+      sym(6, 1, 5, 0, 2.0, t, false, 0, 0, 0, 0);
+      k_huge_sqcomb<<<dim3(ge, unsigned(items)), 256, 0, st>>>(ws, b, J.hsq.p, t);
+      ++J.launches;
+    }
+    k_huge_store_u<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, ws, bp, b, j0);
+    ++J.launches;
+  }
+}
+
+// A_{i+1} = U_i A_i for huge block k, one product launch per step.
+static void huge_dyson(JobImpl &J, DevSys &s, size_t kh) {
+  const int k = J.huge_blocks[kh], b = J.L.size[k], bp = J.L.poff[k];
+  const long bb = long(b) * b;
+  cudaStream_t st = J.ctx->stream;
+  k_huge_copy_u0<<<dim3(unsigned((bb + 255) / 256), unsigned(s.C)), 256, 0, st>>>(s, bp, b);
+  ++J.launches;
+  const auto U = item_mat<const double2>(s.U, bp, s.S2, b, s.Cpad);
+  const auto Ain = item_mat<const double2>(s.A, long(bp) - s.S2, s.S2, b, s.Cpad);
+  const auto Aout = item_mat<double2>(s.A, bp, s.S2, b, s.Cpad);
+  for (int i = 1; i < J.n; ++i) {
+    k_huge_zgemm<double2, false, double2, double2, double2>
+        <<<dim3(tiles(b, b), unsigned(s.C)), kHThreads, 0, st>>>(U, Ain, Aout, b, b, b, s.C, long(i) * s.C, 1.0);
+    ++J.launches;
+  }
+}
+
+static void huge_floquet(JobImpl &J, DevSys &s, size_t kh) {
+  const int k = J.huge_blocks[kh], b = J.L.size[k];
+  const int per = int(std::min<size_t>(size_t(s.C), J.huge_ws_bytes / (2 * sizeof(double2) * size_t(b) * b)));
+  for (int c0 = 0; c0 < s.C; c0 += per) {
+    k_huge_floquet<<<unsigned(std::min(per, s.C - c0)), kBigThreads, huge_floquet_smem(b), J.ctx->stream>>>(
+        s, k, J.huge_ws.p, c0);
+    ++J.launches;
+  }
+}
+
+// W_i = A_{i+1} V_F for huge block k: straight into W in the mixed form; through the
+// workspace and back over A in FP64 (a product may not overwrite its own operand).
+static void huge_eigframe(JobImpl &J, DevSys &s, size_t kh) {
+  const int k = J.huge_blocks[kh], b = J.L.size[k], bp = J.L.poff[k];
+  const long bb = long(b) * b, total = long(s.C) * J.n;
+  cudaStream_t st = J.ctx->stream;
+  const auto A = item_mat<const double2>(s.A, bp, s.S2, b, s.Cpad);
+  const auto V = item_mat<const double2>(s.VF, bp, 0, b, s.Cpad);
+  if (s.mixed) {
+    const auto W = item_mat<float2>(s.Wf, bp, s.S2, b, s.Cpad);
+    for (long j0 = 0; j0 < total; j0 += kHugeMaxItems) {
+      const int items = int(std::min<long>(kHugeMaxItems, total - j0));
+      k_huge_zgemm<float2, false, double2, double2, float2>
+          <<<dim3(tiles(b, b), unsigned(items)), kHThreads, 0, st>>>(A, V, W, b, b, b, s.C, j0, 1.0);
+      ++J.launches;
+    }
+    return;
+  }
+  const long per = std::min<long>(kHugeMaxItems, long(J.huge_ws_bytes / (sizeof(double2) * bb)));
+  for (long j0 = 0; j0 < total; j0 += per) {
+    const int items = int(std::min(per, total - j0));
+    const auto O = ws_mat<double2>(J.huge_ws.p, j0, bb, s.C, b);
+    k_huge_zgemm<double2, false, double2, double2, double2>
+        <<<dim3(tiles(b, b), unsigned(items)), kHThreads, 0, st>>>(A, V, O, b, b, b, s.C, j0, 1.0);
+    k_huge_copy_back<<<dim3(unsigned((bb + 255) / 256), unsigned(items)), 256, 0, st>>>(s, J.huge_ws.p, bp, b, j0);
+    J.launches += 2;
+  }
+}
+
+// Q^{ab} (or R) = W_a^H (M_ab W_b) for a pair with a huge block, every (crystallite, step).
+template <class C>
+static void huge_qr(JobImpl &J, DevSys &s, const BigPair &P, C *Wbuf, C *out) {
+  const int ba = J.L.size[P.a], bb = J.L.size[P.b], pa = J.L.poff[P.a];
+  const long ne = long(ba) * bb, total = long(s.C) * J.n;
+  const long per = std::min<long>(kHugeMaxItems, long(J.huge_ws_bytes / (sizeof(C) * ne)));
+  cudaStream_t st = J.ctx->stream;
+  C *ws = reinterpret_cast<C *>(J.huge_ws.p);
+  const auto Wa = item_mat<const C>(Wbuf, pa, s.S2, ba, s.Cpad);
+  const auto O = item_mat<C>(out, P.off, P.nitems, bb, s.Cpad);
+  for (long j0 = 0; j0 < total; j0 += per) {
+    const int items = int(std::min(per, total - j0));
+    k_huge_mx<C><<<dim3(unsigned((ne + 255) / 256), unsigned(items)), 256, 0, st>>>(s, P, j0, ws);
+    const auto X = ws_mat<const C>(ws, j0, ne, s.C, bb);
+    k_huge_zgemm<C, true, C, C, C><<<dim3(tiles(ba, bb), unsigned(items)), kHThreads, 0, st>>>(Wa, X, O, ba, bb, ba,
+                                                                                             s.C, j0, 1.0);
+    J.launches += 2;
+  }
+}
+
 static void launch_stage(JobImpl &J, DevSys &s, int stage) {
   if (!J.big_blocks.empty()) fork(J);
   launch_block_kernels<1>(J, s, stage);
@@ -1731,6 +1950,16 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         break;
     }
     ++J.launches;
+  }
+  // blocks larger than kMaxBigBlock: batched products on the context stream, alongside the
+  // large blocks on the auxiliary streams
+  for (size_t kh = 0; kh < J.huge_blocks.size(); ++kh) {
+    switch (stage) {
+      case 0: huge_step(J, s, kh); break;
+      case 1: huge_dyson(J, s, kh); break;
+      case 2: huge_floquet(J, s, kh); break;
+      case 3: huge_eigframe(J, s, kh); break;
+    }
   }
   if (!J.big_blocks.empty()) join(J);
 }
@@ -1789,6 +2018,10 @@ void Job::run() {
           else k_big_qr<2, double2><<<grid, th, sm, st>>>(s, P);
         }
         ++J.launches;
+      }
+      for (const BigPair &P : J.huge_pairs) {
+        if (s.mixed) huge_qr<float2>(J, s, P, s.Wf, P.isq ? s.Qf : s.Rf);
+        else huge_qr<double2>(J, s, P, s.A, P.isq ? s.Q : s.R);
       }
       if (!J.big_pairs.empty()) join(J);
     }

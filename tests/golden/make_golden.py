@@ -104,12 +104,25 @@ def big_cases():
     yield "c2_sub1", W.job_text(c2), powder_rows(c2["powder"], spread(1154, 1))
 
 
+def huge_cases():
+    """9 like spins (dim 512; blocks 1,9,36,84,126,126,84,36,9,1): blocks above 74 take the
+    batched-product path; one crystallite, few steps, so that the dense reference is quick."""
+    c0 = W.config(0)
+    for seed, name, rho, nstep in [(21, "huge_9h", "Fx", 12), (22, "huge_9h_nonsym", "Fx+Fz", 10)]:
+        rng = np.random.default_rng(W.SEED0 + seed)
+        xyz = W._proton_cluster(rng, 9, 6.0, min_sep=1.5)
+        lines = ["numspin 9"] + [f"T 1H {k}" for k in range(9)] + W._csa_lines(rng, 9) + W._dipole_lines(xyz) + \
+            ["J 75 0 1", "J 40 3 4"]
+        cfg = dict(lines=lines, rho=rho, det="Fp", npts=96, wr=25000.0, sw=nstep * 25000.0, rotb=W.MAGIC_ANGLE)
+        yield name, W.job_text(cfg), powder_rows(c0["powder"], spread(1154, 1) + 300)
+
+
 def main():
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
-    if "--big" in sys.argv:
+    if "--big" in sys.argv or "--huge" in sys.argv:
         man = json.loads((OUT / "manifest.json").read_text())
-        for name, job, rows in big_cases():
+        for name, job, rows in (huge_cases() if "--huge" in sys.argv else big_cases()):
             sw64, f64 = run_ref(BIN64, job, rows)
             np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,
                                 sw=np.array(sw64))

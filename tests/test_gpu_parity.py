@@ -130,8 +130,9 @@ def test_c1_full_size_properties():
 def test_unsupported_inputs_return_status():
     cfg = W.config(0)
     rows = np.stack(cfg["powder"], axis=1)[:4]
-    # 9 like spins: the M = 1/2 sector is a block of 126 > 74
-    big = "\n".join(f"spin: {l}" for l in ["numspin 9"] + [f"D -5000 {i} {i + 1}" for i in range(8)])
+    # 13 spins 1/2: dimension 8192 > 4096 (the largest block a SolidSys of dimension <= 4096
+    # can have is 924, within the engine's 1024)
+    big = "\n".join(f"spin: {l}" for l in ["numspin 13"] + [f"D -5000 {i} {i + 1}" for i in range(12)])
     big += "\nnpts: 16\nsw: 100000\nwr: 10000\nrotb: 54.7356\nrho: Fx\ndet: Fp\n"
     with pytest.raises(bl.BlochError) as e:
         gpu_fid(big, rows)

@@ -5,7 +5,7 @@ import pytest
 from helpers import golden_cases, load_golden, oracle_fid, rel
 
 # the dense oracle is too slow for dim 256 (c2); those fixtures pin the GPU path directly
-ORACLE_CASES = [c for c in golden_cases() if not c.startswith("c2_")]
+ORACLE_CASES = [c for c in golden_cases() if not c.startswith(("c2_", "huge_"))]
 
 
 @pytest.mark.parametrize("case", ORACLE_CASES)
