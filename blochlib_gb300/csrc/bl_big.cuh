@@ -391,7 +391,9 @@ struct FloqWork {
   double *red;
 };
 
-__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk) {
+// sweeps0 < kMaxSweeps: the first pass only locates the spectrum (that many sweeps); the
+// second pass, with -1 in the widest gap of those eigenphases, always follows.
+__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps) {
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
@@ -480,7 +482,8 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk) {
     const int bq = b + (b & 1);  // players in the round-robin (one dummy when b is odd)
     const int np = bq / 2;
     bool conv = false;
-    for (int sweep = 0; sweep < kMaxSweeps && !conv; ++sweep) {
+    const int max_sweeps = pass == 0 ? sweeps0 : kMaxSweeps;
+    for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
       double off = 0, dg = 0;
       for (int e = threadIdx.x; e < bb; e += blockDim.x) {
         const int r = e / b, q = e % b;
@@ -572,7 +575,7 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk) {
         __syncthreads();
       }
     }
-    if (!conv) atomicOr(s.status, kNoConvergeFloquet);
+    if (!conv && max_sweeps == kMaxSweeps) atomicOr(s.status, kNoConvergeFloquet);
     // Rayleigh quotients lam_r = v_r^H U v_r
     for (int r = threadIdx.x; r < b; r += blockDim.x) {
       double2 acc = cmk(0, 0);
@@ -591,7 +594,7 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk) {
         const double2 w = cmul(ea, lam[r]);
         mind = fmin(mind, (1.0 + w.x) * (1.0 + w.x) + w.y * w.y);
       }
-      done_s = mind >= 0.0625;
+      done_s = conv && mind >= 0.0625;
       if (!done_s) {
         // widest gap of the eigenphases: sort them (insertion sort into red[])
         for (int r = 0; r < b; ++r) {

@@ -1853,13 +1853,32 @@ static void huge_dyson(JobImpl &J, DevSys &s, size_t kh) {
   }
 }
 
-static void huge_floquet(JobImpl &J, DevSys &s, size_t kh) {
-  const int k = J.huge_blocks[kh], b = J.L.size[k];
-  const int per = int(std::min<size_t>(size_t(s.C), J.huge_ws_bytes / (2 * sizeof(double2) * size_t(b) * b)));
-  for (int c0 = 0; c0 < s.C; c0 += per) {
-    k_huge_floquet<<<unsigned(std::min(per, s.C - c0)), kBigThreads, huge_floquet_smem(b), J.ctx->stream>>>(
-        s, k, J.huge_ws.p, c0);
-    ++J.launches;
+// Floquet of all huge blocks: one launch per group of kMaxHugeLaunch blocks and chunk of
+// crystallites, each (crystallite, block) with its own part of the workspace.
+static void huge_floquet_all(JobImpl &J, DevSys &s) {
+  const size_t nh = J.huge_blocks.size();
+  for (size_t g0 = 0; g0 < nh; g0 += kMaxHugeLaunch) {
+    HugeFloq hf{};
+    hf.n = int(std::min<size_t>(kMaxHugeLaunch, nh - g0));
+    size_t per_c = 0, smem = 0;
+    for (int t = 0; t < hf.n; ++t) {
+      const size_t b = size_t(J.L.size[J.huge_blocks[g0 + t]]);
+      per_c += 2 * b * b;
+      smem = std::max(smem, huge_floquet_smem(int(b)));
+    }
+    const int per = int(std::min<size_t>(size_t(s.C), J.huge_ws_bytes / (sizeof(double2) * per_c)));
+    long off = 0;
+    for (int t = 0; t < hf.n; ++t) {
+      const long b = J.L.size[J.huge_blocks[g0 + t]];
+      hf.k[t] = J.huge_blocks[g0 + t];
+      hf.ws[t] = off;
+      off += long(per) * 2 * b * b;
+    }
+    for (int c0 = 0; c0 < s.C; c0 += per) {
+      k_huge_floquet<<<dim3(unsigned(std::min(per, s.C - c0)), unsigned(hf.n)), kHugeFloqThreads, smem,
+                       J.ctx->stream>>>(s, hf, J.huge_ws.p, c0);
+      ++J.launches;
+    }
   }
 }
 
@@ -1957,7 +1976,9 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
     switch (stage) {
       case 0: huge_step(J, s, kh); break;
       case 1: huge_dyson(J, s, kh); break;
-      case 2: huge_floquet(J, s, kh); break;
+      case 2:
+        if (kh == 0) huge_floquet_all(J, s);
+        break;
       case 3: huge_eigframe(J, s, kh); break;
     }
   }

@@ -298,20 +298,32 @@ __global__ void k_huge_mx(DevSys s, BigPair P, long j0, C *ws) {
   ws[long(j) * ne + e] = x;
 }
 
+constexpr int kHugeFloqThreads = 1024;
+constexpr int kHugeFloqSweeps0 = 4;  // first pass: locate the spectrum only
+constexpr int kMaxHugeLaunch = 16;   // huge blocks per Floquet launch
+
 __host__ __device__ constexpr size_t huge_floquet_smem(int b) {
-  return sizeof(double2) * (2 * size_t(b / 2 + 1) + 2 * size_t(b)) + sizeof(double) * size_t(b > 256 ? b : 256) +
-         sizeof(int) * 2 * size_t(b / 2 + 1);
+  return sizeof(double2) * (2 * size_t(b / 2 + 1) + 2 * size_t(b)) +
+         sizeof(double) * size_t(b > kHugeFloqThreads ? b : kHugeFloqThreads) + sizeof(int) * 2 * size_t(b / 2 + 1);
 }
 
-// One CTA per crystallite c0 + blockIdx.x: Floquet eigen-decomposition of a huge block, its
-// two b x b matrices in the workspace (2 b^2 per CTA), the small arrays in shared memory.
-__global__ void __launch_bounds__(kBigThreads) k_huge_floquet(DevSys s, int k, double2 *ws, int c0) {
+// Huge blocks of one Floquet launch and each one's workspace (2 b^2 per crystallite).
+struct HugeFloq {
+  int n;
+  int k[kMaxHugeLaunch];
+  long ws[kMaxHugeLaunch];
+};
+
+// One CTA per (crystallite c0 + blockIdx.x, huge block blockIdx.y): Floquet eigen-
+// decomposition with its two b x b matrices in the workspace, the small arrays in shared
+// memory; all huge blocks of the system in one launch.
+__global__ void __launch_bounds__(kHugeFloqThreads) k_huge_floquet(DevSys s, HugeFloq hf, double2 *ws, int c0) {
   extern __shared__ __align__(16) unsigned char fsm[];
-  const int b = s.bs[k], c = c0 + blockIdx.x;
+  const int k = hf.k[blockIdx.y], b = s.bs[k], c = c0 + blockIdx.x;
   const int np1 = b / 2 + 1;
   double2 *rot = reinterpret_cast<double2 *>(fsm), *fv = rot + 2 * np1, *lam = fv + b;
   double *red = reinterpret_cast<double *>(lam + b);
-  int *rpair = reinterpret_cast<int *>(red + (b > kBigThreads ? b : kBigThreads));
-  double2 *Mm = ws + size_t(blockIdx.x) * 2 * b * b;
-  floquet_cta(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red});
+  int *rpair = reinterpret_cast<int *>(red + (b > kHugeFloqThreads ? b : kHugeFloqThreads));
+  double2 *Mm = ws + hf.ws[blockIdx.y] + size_t(blockIdx.x) * 2 * b * b;
+  floquet_cta(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red}, kHugeFloqSweeps0);
 }
