@@ -14,7 +14,9 @@ struct bl_ctx {
   bl::Context c;
 };
 struct bl_system {
-  bl::SpinSystem s;
+  // shared, so that a serving request keeps the system alive without copying its operators
+  std::shared_ptr<const bl::SpinSystem> sp;
+  const bl::SpinSystem &s() const { return *sp; }
 };
 struct bl_powder {
   bl::Powder p;
@@ -92,24 +94,24 @@ void *bl_ctx_stream(bl_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr;
 bl_status bl_system_create(const char *spin_text, bl_system **out) {
   if (!spin_text || !out) return fail(BL_ERR_INVALID, "null argument");
   *out = nullptr;
-  return guarded([&] { *out = new bl_system{bl::SpinSystem::from_text(spin_text)}; });
+  return guarded([&] { *out = new bl_system{std::make_shared<const bl::SpinSystem>(bl::SpinSystem::from_text(spin_text))}; });
 }
 
 void bl_system_destroy(bl_system *sys) { delete sys; }
-int bl_system_dim(const bl_system *sys) { return sys ? sys->s.dim() : 0; }
-int bl_system_spins(const bl_system *sys) { return sys ? sys->s.spins() : 0; }
+int bl_system_dim(const bl_system *sys) { return sys ? sys->s().dim() : 0; }
+int bl_system_spins(const bl_system *sys) { return sys ? sys->s().spins() : 0; }
 
 bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out) {
   if (!sys || !expr || !out) return fail(BL_ERR_INVALID, "null argument");
   return guarded([&] {
-    bl::CMatrix M = sys->s.op(expr);
+    bl::CMatrix M = sys->s().op(expr);
     for (size_t i = 0; i < M.a.size(); ++i) out[2 * i] = M.a[i].real(), out[2 * i + 1] = M.a[i].imag();
   });
 }
 
 bl_status bl_system_blocks(const bl_system *sys, int *sizes, int cap, int *nblocks) {
   if (!sys || !nblocks) return fail(BL_ERR_INVALID, "null argument");
-  const auto &L = sys->s.layout();
+  const auto &L = sys->s().layout();
   *nblocks = int(L.size.size());
   for (int k = 0; k < *nblocks && k < cap && sizes; ++k) sizes[k] = L.size[k];
   return BL_OK;
@@ -161,9 +163,9 @@ bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
   if (!ctx || !sys || !pw || !ro || !det || !params || !out) return fail(BL_ERR_INVALID, "null argument");
   *out = nullptr;
   return guarded([&] {
-    int N = sys->s.dim();
+    int N = sys->s().dim();
     std::unique_ptr<bl_job> j(new bl_job);
-    j->j.reset(new bl::Job(ctx->c, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
+    j->j.reset(new bl::Job(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
     *out = j.release();
   });
 }
@@ -263,8 +265,8 @@ bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powd
                                 const double *det, const bl_fid_params *params, double *fid_out, double *sw_out) {
   if (!ctx || !sys || !pw || !ro || !det || !params || !fid_out) return fail(BL_ERR_INVALID, "null argument");
   return guarded([&] {
-    int N = sys->s.dim();
-    bl::powder_fid_noalloc(ctx->c, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out,
+    int N = sys->s().dim();
+    bl::powder_fid_noalloc(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out,
                            sw_out);
   });
 }
@@ -306,8 +308,8 @@ bl_status bl_job_bytes(int device, const bl_system *sys, const bl_powder *pw, co
                        const bl_fid_params *params, size_t *min_bytes, size_t *full_bytes) {
   if (!sys || !pw || !ro || !det || !params) return fail(BL_ERR_INVALID, "null argument");
   return guarded([&] {
-    int N = sys->s.dim();
-    bl::job_bytes(device, sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params), min_bytes, full_bytes);
+    int N = sys->s().dim();
+    bl::job_bytes(device, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params), min_bytes, full_bytes);
   });
 }
 
@@ -327,9 +329,9 @@ bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder
                            const double *det, const bl_fid_params *params, long long *ticket) {
   if (!srv || !sys || !pw || !ro || !det || !params || !ticket) return fail(BL_ERR_INVALID, "null argument");
   return guarded([&] {
-    int N = sys->s.dim();
+    int N = sys->s().dim();
     if (params->npts <= 0) throw bl::Error(BL_ERR_INVALID, "npts must be positive");
-    *ticket = srv->s->submit(sys->s, pw->p, load_op(ro, N), load_op(det, N), to_params(params));
+    *ticket = srv->s->submit(sys->sp, pw->p, load_op(ro, N), load_op(det, N), to_params(params));
   });
 }
 

@@ -1334,16 +1334,18 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         for (int q = 0; q < L.size[k]; ++q)
           dst[L.poff[k] + r * L.size[k] + q] = M[size_t(L.perm[L.off[k] + r]) * N + L.perm[L.off[k] + q]];
   };
-  pack(sys.h_const(), Hc.data());
+  if (!g_sizing) pack(sys.h_const(), Hc.data());  // planning needs only the counts
   const auto &ints = sys.interactions();
   for (size_t kk = 0; kk < ints.size(); ++kk) {
     if (ints[kk].kind == 'J') continue;
     const auto &I = ints[kk];
     pas.insert(pas.end(), {I.pas[0][0], I.pas[0][1], I.pas[0][2], I.pas[1][1], I.pas[1][2], I.pas[2][2]});
     isc.push_back(I.op_scale);
-    size_t o = Tk.size();
-    Tk.resize(o + L.S2);
-    pack(sys.h_ops()[kk], Tk.data() + o);
+    if (!g_sizing) {
+      size_t o = Tk.size();
+      Tk.resize(o + L.S2);
+      pack(sys.h_ops()[kk], Tk.data() + o);
+    }
     ++J.nint;
   }
   // Q pairs (blocks of D) and R pairs (blocks of rho when rho != (D + D^H)/2)

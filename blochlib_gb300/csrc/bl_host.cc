@@ -203,9 +203,9 @@ SpinSystem::SpinSystem(const std::vector<std::string> &lines) {
   build();
 }
 
-CMatrix SpinSystem::single(char which, int spin) const {
-  if (spin < 0 || spin >= nspin_) throw Error(1, "spin index out of range");
-  int hs = dims_[spin];
+namespace {
+// Single-spin operator of a spin with hs levels (m from +I down), hs x hs.
+CMatrix small_op(char which, int hs) {
   CMatrix m(hs);
   double q = (hs - 1.0) / 2.0, q1 = q * (q + 1.0);
   if (which == 'z') {
@@ -224,6 +224,48 @@ CMatrix SpinSystem::single(char which, int spin) const {
       else throw Error(1, "unknown single-spin operator");
     }
   }
+  return m;
+}
+}  // namespace
+
+// For the two spins s1 != s2: every element (row, col) of the full space where a product of
+// single-spin operators of these spins can be non-zero, with the real parts of the xx, yy and
+// zz products there, f(row, col, xx, yy, zz).  A product of operators on different spins has
+// one term per element (the Kronecker digits of s1 and s2 change, all others agree), so the
+// values equal the dense products exactly.
+template <class F>
+void SpinSystem::pair_terms(int s1, int s2, F f) const {
+  const int h1 = dims_[s1], h2 = dims_[s2];
+  long R1 = 1, R2 = 1;
+  for (int i = s1 + 1; i < nspin_; ++i) R1 *= dims_[i];
+  for (int i = s2 + 1; i < nspin_; ++i) R2 *= dims_[i];
+  const CMatrix ax = small_op('x', h1), ay = small_op('y', h1), az = small_op('z', h1);
+  const CMatrix bx = small_op('x', h2), by = small_op('y', h2), bz = small_op('z', h2);
+  for (long row = 0; row < N_; ++row) {
+    const int d1 = int((row / R1) % h1), d2 = int((row / R2) % h2);
+    for (int c1 = 0; c1 < h1; ++c1)
+      for (int c2 = 0; c2 < h2; ++c2) {
+        const cplx xx = ax(d1, c1) * bx(d2, c2), yy = ay(d1, c1) * by(d2, c2), zz = az(d1, c1) * bz(d2, c2);
+        if (xx == cplx(0, 0) && yy == cplx(0, 0) && zz == cplx(0, 0)) continue;
+        f(row, row + (c1 - d1) * R1 + (c2 - d2) * R2, xx.real(), yy.real(), zz.real());
+      }
+  }
+}
+
+// Diagonal of Iz of one spin in the full space.
+std::vector<double> SpinSystem::iz_diag(int s) const {
+  long R = 1;
+  for (int i = s + 1; i < nspin_; ++i) R *= dims_[i];
+  const double q = (dims_[s] - 1.0) / 2.0;
+  std::vector<double> z(N_);
+  for (long row = 0; row < N_; ++row) z[row] = q - double((row / R) % dims_[s]);
+  return z;
+}
+
+CMatrix SpinSystem::single(char which, int spin) const {
+  if (spin < 0 || spin >= nspin_) throw Error(1, "spin index out of range");
+  int hs = dims_[spin];
+  CMatrix m = small_op(which, hs);
   // Kronecker expansion, spin 0 most significant (multispinop.cc:51-74)
   int left = 1, right = 1;
   for (int i = 0; i < spin; ++i) left *= dims_[i];
@@ -300,42 +342,40 @@ void SpinSystem::build() {
     std::vector<double> T(NN, 0.0);
     if (it.kind == 'C') {
       // a*Iz + (1/sqrt3 Iz)(-sqrt3 iso)   (csa.cc:289-329, spin_ten.cc:211-236)
-      CMatrix Iz = single('z', it.s1);
+      const std::vector<double> Iz = iz_diag(it.s1);
       for (int k = 0; k < N_; ++k) {
-        double z = Iz(k, k).real();
+        double z = Iz[k];
         T[size_t(k) * N_ + k] = z;
         if (it.iso != 0) hc_[size_t(k) * N_ + k] += (inv_r3 * z) * (-r3 * it.iso);
       }
     } else if (it.kind == 'D') {
       // homonuclear sqrt(1/6)(2IzIz - IxIx - IyIy); heteronuclear sqrt(4/6) IzIz (spin_ten.cc:431-452)
-      CMatrix zz = mul(single('z', it.s1), single('z', it.s2));
       if (iso_[it.s1] == iso_[it.s2]) {
-        CMatrix xx = mul(single('x', it.s1), single('x', it.s2));
-        CMatrix yy = mul(single('y', it.s1), single('y', it.s2));
         double f = std::pow(1. / 6., 0.5);
-        for (size_t i = 0; i < NN; ++i) T[i] = f * (2.0 * zz.a[i].real() - xx.a[i].real() - yy.a[i].real());
+        pair_terms(it.s1, it.s2, [&](long r, long c, double xx, double yy, double zz) {
+          T[size_t(r) * N_ + c] = f * (2.0 * zz - xx - yy);
+        });
       } else {
         double f = std::pow(4. / 6., 0.5);
-        for (size_t i = 0; i < NN; ++i) T[i] = f * zz.a[i].real();
+        pair_terms(it.s1, it.s2, [&](long r, long c, double, double, double zz) {
+          T[size_t(r) * N_ + c] = f * zz;
+        });
       }
     } else if (it.kind == 'J') {
       // iso*sqrt3 * (1/sqrt3)(IzIz [+IxIx+IyIy])   (j.cc:129-137, spin_ten.cc:455-465)
-      CMatrix zz = mul(single('z', it.s1), single('z', it.s2));
-      CMatrix xx, yy;
-      if (it.strong) xx = mul(single('x', it.s1), single('x', it.s2)), yy = mul(single('y', it.s1), single('y', it.s2));
-      for (size_t i = 0; i < NN; ++i) {
-        double v = zz.a[i].real();
-        if (it.strong) v = v + xx.a[i].real() + yy.a[i].real();
-        hc_[i] += (inv_r3 * v) * (it.iso * std::sqrt(3.));
-      }
+      pair_terms(it.s1, it.s2, [&](long r, long c, double xx, double yy, double zz) {
+        double v = zz;
+        if (it.strong) v = v + xx + yy;
+        hc_[size_t(r) * N_ + c] += (inv_r3 * v) * (it.iso * std::sqrt(3.));
+      });
     } else if (it.kind == 'Q') {
       // first order: Qp * a * 3 Iz^2, Qp = Q / (4 I (2I-1))   (qua.cc:219-267, spin_ten.cc:285-300)
       double spin = isotope_spin(iso_[it.s1]);
       if (spin < 1.0) throw Error(2, "a quadrupole needs a spin >= 1");
       it.op_scale = it.del / (4.0 * spin * (2.0 * spin - 1.0));
-      CMatrix Iz = single('z', it.s1);
+      const std::vector<double> Iz = iz_diag(it.s1);
       for (int k = 0; k < N_; ++k) {
-        double z = Iz(k, k).real();
+        double z = Iz[k];
         T[size_t(k) * N_ + k] = 3.0 * (z * z);
       }
     }
@@ -348,13 +388,15 @@ void SpinSystem::build() {
     while (parent[x] != x) x = parent[x] = parent[parent[x]];
     return x;
   };
-  auto scan = [&](const std::vector<double> &M) {
-    for (int r = 0; r < N_; ++r)
-      for (int c = r + 1; c < N_; ++c)
-        if (M[size_t(r) * N_ + c] != 0.0 || M[size_t(c) * N_ + r] != 0.0) {
+  auto scan = [&](const std::vector<double> &M) {  // row by row: both triangles
+    for (int r = 0; r < N_; ++r) {
+      const double *row = M.data() + size_t(r) * N_;
+      for (int c = 0; c < N_; ++c)
+        if (c != r && row[c] != 0.0) {
           int a = find(r), b = find(c);
           if (a != b) parent[std::max(a, b)] = std::min(a, b);
         }
+    }
   };
   scan(hc_);
   for (auto &T : hops_) scan(T);

@@ -75,6 +75,9 @@ class SpinSystem {
   // Fx Fy Fz Fp Fm Fe Ix Iy Iz Ip Im.
   CMatrix op(const std::string &expr) const;
   CMatrix single(char which, int spin) const;  // x y z p m e
+  template <class F>
+  void pair_terms(int s1, int s2, F f) const;  // two-spin operator products, element by element
+  std::vector<double> iz_diag(int s) const;    // diagonal of Iz of spin s
 
   // Constant part of H (isotropic CSA, J couplings) and the operator multiplying each
   // orientation-dependent interaction (index matches interactions(); zero for J).

@@ -65,6 +65,7 @@ Server::Server(int device, int lanes, size_t pool_bytes)
     lanes_.push_back(std::move(s));
   }
   worker_ = std::thread([this] { loop(); });
+  planner_ = std::thread([this] { plan(); });
 }
 
 Server::~Server() {
@@ -73,6 +74,8 @@ Server::~Server() {
     stop_ = true;
   }
   cv_.notify_all();
+  plan_cv_.notify_all();
+  if (planner_.joinable()) planner_.join();
   if (worker_.joinable()) worker_.join();
   cudaSetDevice(device_);
   for (auto &s : lanes_) {
@@ -89,22 +92,56 @@ size_t Server::grant(const ServeRequest &r) const {
   return round_up(std::min(r.full_bytes, std::max(r.min_bytes, share)));
 }
 
-int64_t Server::submit(const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+int64_t Server::submit(std::shared_ptr<const SpinSystem> sys, const Powder &pw, CMatrix ro, CMatrix det,
                        const FidParams &p) {
-  auto r = std::make_shared<ServeRequest>(sys, pw, ro, det, p);
+  auto r = std::make_shared<ServeRequest>(std::move(sys), pw, std::move(ro), std::move(det), p);
   r->t_submit = std::chrono::steady_clock::now();
-  job_bytes(device_, sys, pw, ro, det, p, &r->min_bytes, &r->full_bytes);
-  if (round_up(r->min_bytes) > pool_bytes_)
-    throw Error(4, "job needs " + std::to_string(r->min_bytes >> 20) + " MiB for one warp of crystallites; the pool has " +
-                       std::to_string(pool_bytes_ >> 20) + " MiB");
   {
     std::lock_guard<std::mutex> lk(mu_);
     r->id = next_id_++;
     all_[r->id] = r;
-    queue_.push_back(r);
+    unplanned_.push_back(r);
   }
-  cv_.notify_one();
+  plan_cv_.notify_one();
   return r->id;
+}
+
+// Planner thread: sizes queued requests in submission order and passes them to admission.
+void Server::plan() {
+  for (;;) {
+    std::shared_ptr<ServeRequest> r;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      plan_cv_.wait(lk, [&] { return stop_ || !unplanned_.empty(); });
+      if (stop_) return;
+      r = unplanned_.front();
+      unplanned_.pop_front();
+      if (r->state != 0) continue;  // cancelled while waiting
+    }
+    std::string err;
+    try {
+      job_bytes(device_, *r->sys, r->pw, r->ro, r->det, r->p, &r->min_bytes, &r->full_bytes);
+      if (round_up(r->min_bytes) > pool_bytes_)
+        err = "job needs " + std::to_string(r->min_bytes >> 20) + " MiB for one warp of crystallites; the pool has " +
+              std::to_string(pool_bytes_ >> 20) + " MiB";
+    } catch (const std::exception &e) {
+      err = e.what();
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!err.empty()) {
+        if (r->state == 0) {
+          r->err = err;
+          r->state = 3;
+          r->t_done = std::chrono::steady_clock::now();
+          ++n_done_;
+        }
+      } else {
+        queue_.push_back(r);
+      }
+    }
+    cv_.notify_one();
+  }
 }
 
 int Server::poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err) {
@@ -210,7 +247,7 @@ void Server::loop() {
       try {
         s.off = off;
         s.bytes = bytes;
-        s.job = job_in_region(s.ctx, static_cast<char *>(pool_) + off, bytes, r->sys, r->pw, r->ro, r->det, r->p);
+        s.job = job_in_region(s.ctx, static_cast<char *>(pool_) + off, bytes, *r->sys, r->pw, r->ro, r->det, r->p);
         s.job->run();
         cuda_ok(cudaEventRecord(static_cast<cudaEvent_t>(s.event), s.ctx.stream), "cudaEventRecord");
         s.req = r;

@@ -7,9 +7,10 @@
 // job (spin system + powder + rho/detect + parameters) and the workers are CUDA streams
 // ("lanes") sharing one pool of device memory:
 //   * one device allocation at start (the pool) and `lanes` non-blocking streams;
-//   * each request is sized when it is submitted (job_bytes: the bytes for one warp of
-//     crystallites per batch and for all crystallites at once); a request whose one-warp
-//     size exceeds the pool is refused at submission;
+//   * submit() only queues a request; a planner thread sizes requests in submission order
+//     (job_bytes: the bytes for one warp of crystallites per batch and for all crystallites
+//     at once) and fails those whose one-warp size exceeds the pool, so that submitting
+//     never waits on host-side planning;
 //   * admission is first come first served: the head of the queue is admitted when a lane
 //     is idle and the pool holds a free range of its grant, grant = its full size capped at
 //     pool/lanes but never below its one-warp size.  The job is built inside that range (no
@@ -40,7 +41,7 @@ namespace bl {
 
 struct ServeRequest {
   int64_t id = 0;
-  SpinSystem sys;
+  std::shared_ptr<const SpinSystem> sys;  // shared with the caller's handle, never copied
   Powder pw;
   CMatrix ro, det;
   FidParams p;
@@ -50,8 +51,8 @@ struct ServeRequest {
   std::vector<double> fid;
   double sw = 0;
   std::string err;
-  ServeRequest(const SpinSystem &s, const Powder &w, const CMatrix &r, const CMatrix &d, const FidParams &q)
-      : sys(s), pw(w), ro(r), det(d), p(q) {}
+  ServeRequest(std::shared_ptr<const SpinSystem> s, const Powder &w, CMatrix r, CMatrix d, const FidParams &q)
+      : sys(std::move(s)), pw(w), ro(std::move(r)), det(std::move(d)), p(q) {}
 };
 
 // First-fit ranges of the pool, free neighbours merged on release.
@@ -70,8 +71,8 @@ class Server {
  public:
   Server(int device, int lanes, size_t pool_bytes);
   ~Server();
-  // sizes the job (throws Error 4 when one warp of it exceeds the pool) and queues it
-  int64_t submit(const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det, const FidParams &p);
+  // queues the job (the planner fails it later if one warp of it exceeds the pool)
+  int64_t submit(std::shared_ptr<const SpinSystem> sys, const Powder &pw, CMatrix ro, CMatrix det, const FidParams &p);
   // state of a ticket; when done and fid_out is given, copies the FID and forgets the ticket
   int poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err);
   bool cancel(int64_t id);
@@ -89,6 +90,7 @@ class Server {
     void *event = nullptr;  // cudaEvent_t
   };
   void loop();
+  void plan();
   size_t grant(const ServeRequest &r) const;
   int device_;
   size_t pool_bytes_;
@@ -97,7 +99,9 @@ class Server {
   std::vector<std::unique_ptr<Lane>> lanes_;
   mutable std::mutex mu_;
   std::condition_variable cv_;
-  std::deque<std::shared_ptr<ServeRequest>> queue_;
+  std::deque<std::shared_ptr<ServeRequest>> queue_, unplanned_;
+  std::condition_variable plan_cv_;
+  std::thread planner_;
   std::unordered_map<int64_t, std::shared_ptr<ServeRequest>> all_;
   int64_t next_id_ = 1, n_done_ = 0;
   double flops_done_ = 0;

@@ -154,13 +154,14 @@ bl_status bl_job_bytes(int device, const bl_system *sys, const bl_powder *pw, co
  * counterpart in the reference beyond its MPI crystallite farm (src/QMspins/driver/
  * oneFID.h:230-286, examples/solid-2.0/src/sequencerun.cc:435-526), which hands work to
  * whichever worker finishes first; here whole jobs go to CUDA streams ("lanes") sharing one
- * pool of device memory allocated at creation.  A submitted job is sized (bl_job_bytes) and
- * refused with BL_ERR_NOMEM if 32 of its crystallites do not fit the pool; otherwise it is
- * queued and admitted first come first served when a lane is idle and the pool has a free
- * range of its grant (its full size, capped at pool_bytes/lanes but never below its
- * 32-crystallite size).  The job is built inside that range (no further allocation;
- * crystallites batched to fit) and runs on the lane's stream, overlapping the other lanes.
- * Inputs are copied at submission.
+ * pool of device memory allocated at creation.  Submitting only queues a job (the spin system
+ * is shared with the caller's handle, the other inputs are copied); a planner thread sizes
+ * jobs in submission order (bl_job_bytes) and fails those whose 32 crystallites do not fit
+ * the pool (ticket state 3).  A sized job is admitted first come first served when a lane is
+ * idle and the pool has a free range of its grant (its full size, capped at pool_bytes/lanes
+ * but never below its 32-crystallite size).  The job is built inside that range (no further
+ * allocation; crystallites batched to fit) and runs on the lane's stream, overlapping the
+ * other lanes.
  * Ticket states: 0 queued, 1 running, 2 done, 3 failed, 4 cancelled; -1 unknown ticket. */
 typedef struct bl_server bl_server;
 bl_status bl_server_create(int device, int lanes, size_t pool_bytes, bl_server **out);

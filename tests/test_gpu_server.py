@@ -66,9 +66,10 @@ def test_cancel_queued_and_reject_oversized():
     st, fid, _, _ = srv.result(tickets[-1])
     assert st == srv.CANCELLED and fid is None
     big = _job(dict(W.config(1), sw=2000 * 20e3), 64)  # one warp needs > 64 MiB
+    tb = srv.submit(**big)  # queued; the planner fails it
     with pytest.raises(bl.BlochError) as e:
-        srv.submit(**big)
-    assert e.value.status == 4
+        _wait(srv, [tb])
+    assert "MiB" in str(e.value)
     srv.close()
 
 
