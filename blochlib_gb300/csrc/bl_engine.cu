@@ -110,7 +110,8 @@ __device__ __forceinline__ double2 todbl(C v) { return make_double2(double(v.x),
 // ------------------------------------------------------------------ job description
 struct DevSys {
   int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
-  int M, logM, fave_method;  // FFT length (pow2 >= 2n) for the Fave correlation; 0 direct, 1 FFT
+  int M, logM, fave_method;  // FFT length for the Fave correlation; 0 direct, 1 FFT
+  int fave_twist;            // 1: M == n, circular correlation of the twisted sequences
   int is_static;             // static powder FID (oneFID.h:292-336): dt = 1/sw, n = p-period
   double dt;
   const int *srp, *seo;      // per D pair (a,b): the rho pair (b,a) and first element, or -1
@@ -980,11 +981,21 @@ __device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw) {
 // Then G_p = Lin_p + z Lin_{p-n} (the same G as k_fave).  When r = conj(q) (rho = (D+D^H)/2
 // and D has no block pair (b,a) for this element) the product is |FFT(q)|^2 and the second
 // forward transform is skipped.
+// Twisted form (fave_twist, n a power of two, M = n): with zeta^n = z, u_i = zeta^-i q_i and
+// v_i = zeta^i r_i, the circular correlation C_p = sum_i v_i u_{(i+p) mod n} equals
+// zeta^-p G_p (the wrapped terms carry zeta^n = z), so G_p = zeta^p C_p from transforms of
+// length n instead of 2n.  zeta = e^{i tau w}; in the autocorrelation case r = conj(q) needs
+// |zeta| = 1, and zeta = e^{i tau Re w} is used there: exact when the chop has zeroed Im w,
+// otherwise G_p carries z e^{-n tau Im w} in place of z on its wrapped part (relative error
+// at most n tau |Im w|).
 template <int CG, class C>
 __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   extern __shared__ __align__(16) unsigned char fsm_raw[];
   const int M = s.M, logM = s.logM, n = s.n;
   C *X = reinterpret_cast<C *>(fsm_raw), *Y = X + size_t(M) * CG;
+  // twist tables per column: zeta^b (b < 8), zeta^8a (a < M/8), and those of zeta^-1
+  double2 *tp1 = reinterpret_cast<double2 *>(Y + size_t(M) * CG), *tp8 = tp1 + 8 * CG;
+  double2 *tm1 = tp8 + (M / 8) * CG, *tm8 = tm1 + 8 * CG;
   __shared__ C zc[CG];
   const int groups = s.Cpad / CG;
   const int e = blockIdx.x / groups;
@@ -1004,6 +1015,32 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     if (j == s.J) zc[cc] = cvt<C>(cexp(cmk(-nt * w.y, nt * w.x)));
     else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x)));
   }
+  const bool twist = s.fave_twist;
+  if (twist) {
+    // one thread per column: zeta^b by products, zeta^8a by products restarted from cexp
+    // every 16 entries; zeta^-k the same from -log zeta (the conjugate when |zeta| = 1)
+    for (int cc = threadIdx.x; cc < CG; cc += blockDim.x) {
+      const int c = c0 + cc;
+      double2 zl = cmk(0, 0);
+      if (c < s.C) {
+        double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
+        double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+        zl = autoc ? cmk(0.0, s.tau * w.x) : cmk(-s.tau * w.y, s.tau * w.x);
+      }
+      for (int sgn = 0; sgn < 2; ++sgn) {
+        const double2 l = sgn ? cmk(-zl.x, -zl.y) : zl;
+        double2 *t1 = sgn ? tm1 : tp1, *t8 = sgn ? tm8 : tp8;
+        const double2 z1 = cexp(l);
+        t1[cc] = cmk(1, 0);
+        for (int b = 1; b < 8; ++b) t1[b * CG + cc] = cmul(t1[(b - 1) * CG + cc], z1);
+        const double2 z8 = cmul(t1[7 * CG + cc], z1);
+        t8[cc] = cmk(1, 0);
+        for (int a = 1; a < M / 8; ++a)
+          t8[a * CG + cc] = (a % 16 == 0) ? cexp(cmk(8.0 * a * l.x, 8.0 * a * l.y)) : cmul(t8[(a - 1) * CG + cc], z8);
+      }
+    }
+    __syncthreads();
+  }
   // load q (and conj r) zero-padded, bit-reversed
   for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
     const int cc = idx % CG, i = idx / CG, c = c0 + cc;
@@ -1011,11 +1048,16 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     C q = mkc<C>(0, 0), y = mkc<C>(0, 0);
     if (i < n && c < s.C) {
       q = Qb[i * qstride + at(eq, c, s.Cpad)];
+      C r;
       if (!autoc) {
-        C r;
         if (s.rosym) r = cadd(cconj(q), Qb[i * qstride + at(erev, c, s.Cpad)]);
         else r = Rb[i * rstride + at(er, c, s.Cpad)];
         y = cconj(r);
+      }
+      if (twist) {  // u_i = zeta^-i q_i, conj(v_i) = conj(zeta^i r_i)
+        const int a = i >> 3, b = i & 7;
+        q = cvt<C>(cmul(cmul(tm8[a * CG + cc], tm1[b * CG + cc]), todbl(q)));
+        if (!autoc) y = cconj(cvt<C>(cmul(cmul(tp8[a * CG + cc], tp1[b * CG + cc]), todbl(r))));
       }
     }
     X[ri * CG + cc] = q;
@@ -1044,12 +1086,19 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     if (c >= s.C) continue;
     C lp = cscale(cconj(Y[p * CG + cc]), invM);
     C g = lp;
-    if (p > 0) {
+    if (twist) {  // G_p = zeta^p C_p
+      g = cvt<C>(cmul(cmul(tp8[(p >> 3) * CG + cc], tp1[(p & 7) * CG + cc]), todbl(lp)));
+    } else if (p > 0) {
       C lm = cscale(cconj(Y[(M + p - n) * CG + cc]), invM);
       g = cfma(zc[cc], lm, lp);
     }
     Gb[at(p * s.ne + e, c, s.Cpad)] = g;
   }
+}
+
+// Shared memory of k_fave_fft's twist tables (four per column, 8 or M/8 entries).
+static size_t fave_twist_bytes(const DevSys &s, int cg) {
+  return s.fave_twist ? sizeof(double2) * size_t(cg) * 2 * (8 + s.M / 8) : 0;
 }
 
 #include "bl_big.cuh"
@@ -1666,14 +1715,17 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   {
     // Fave correlation: direct 8 n^2 per element; FFT: 5 M log2 M per length-M transform
     // (two when r = conj(q), three otherwise), 8 M for the spectrum product, 8 n for G
+    // (length n with 6 flop per twisted point when n is a power of two, else length >= 2n)
+    const bool twist = !J.mixed && J.n >= 8 && (J.n & (J.n - 1)) == 0;
     int lm = 1;
-    while ((1 << lm) < 2 * J.n) ++lm;
+    while ((1 << lm) < (twist ? J.n : 2 * J.n)) ++lm;
     double M = double(1 << lm), fftf = 5.0 * M * lm;
     bool fft = p.fave_method != 1 && M <= 4096;
     double per = 0;
     for (int e = 0; e < J.ne; ++e) {
       bool autoc = J.rosym && erev[e] < 0;
-      per += fft ? (autoc ? 2 : 3) * fftf + 8.0 * M + 8.0 * J.n : 8.0 * J.n * J.n;
+      per += fft ? (autoc ? 2 : 3) * fftf + 8.0 * M + 8.0 * J.n + (twist ? (autoc ? 12.0 : 18.0) * J.n : 0.0)
+                 : 8.0 * J.n * J.n;
     }
     J.stage_fl[5] = J.is_static ? Ce * (16.0 * pairs + 8.0 * J.n * J.ne) : Ce * per;
   }
@@ -1685,8 +1737,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   DevSys &s = J.base;
   s.n = J.n, s.npts = p.npts, s.N = N, s.nb = nb, s.S2 = L.S2, s.nint = J.nint, s.nq = J.nq, s.nr = J.nr;
   s.ne = J.ne, s.J = J.J, s.rosym = J.rosym, s.step_method = p.step_method;
+  // FFT length: n itself when it is a power of two (twisted circular correlation; FP64 form
+  // only, its twist factors are FP64 work), else the power of two >= 2n (zero-padded linear
+  // correlation, the single-precision transforms of the mixed form)
+  s.fave_twist = (!J.mixed && J.n >= 8 && (J.n & (J.n - 1)) == 0) ? 1 : 0;
   s.logM = 1;
-  while ((1 << s.logM) < 2 * J.n) ++s.logM;
+  while ((1 << s.logM) < (s.fave_twist ? J.n : 2 * J.n)) ++s.logM;
   s.M = 1 << s.logM;
   // FFT correlation up to M = 4096 (its shared-memory tile is M * max(1, 2048/M) * 32 B)
   if (p.fave_method == 2 && s.M > 4096) throw Error(5, "FFT Fave supports at most 2048 steps per period");
@@ -1706,7 +1762,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     g_upload_counter = nullptr;
     s.tw = J.tw.p;
     s.twf = J.twf.p;
-    size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * std::max(1, std::min(8, 2048 / s.M));
+    const int cgm = std::max(1, std::min(8, 2048 / s.M));
+    size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * cgm + fave_twist_bytes(s, cgm);
     for (auto f : {k_fave_fft<8, double2>, k_fave_fft<4, double2>, k_fave_fft<2, double2>, k_fave_fft<1, double2>,
                    k_fave_fft<8, float2>, k_fave_fft<4, float2>, k_fave_fft<2, float2>, k_fave_fft<1, float2>})
       CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
@@ -2056,23 +2113,24 @@ void Job::run() {
     } else if (J.ne > 0) {
       if (s.fave_method == 1) {
         int cg = std::max(1, std::min(8, 2048 / s.M));
-        size_t shm = sizeof(double2) * size_t(s.M) * cg * 2;
+        const size_t shm = sizeof(double2) * size_t(s.M) * cg * 2 + fave_twist_bytes(s, cg);
+        const size_t shmf = sizeof(float2) * size_t(s.M) * cg * 2 + fave_twist_bytes(s, cg);
         unsigned grid = unsigned(J.ne) * unsigned(Cp / cg);
         switch (cg) {
           case 8:
-            if (s.mixed) k_fave_fft<8, float2><<<grid, 128, shm / 2, st>>>(s);
+            if (s.mixed) k_fave_fft<8, float2><<<grid, 128, shmf, st>>>(s);
             else k_fave_fft<8, double2><<<grid, 128, shm, st>>>(s);
             break;
           case 4:
-            if (s.mixed) k_fave_fft<4, float2><<<grid, 128, shm / 2, st>>>(s);
+            if (s.mixed) k_fave_fft<4, float2><<<grid, 128, shmf, st>>>(s);
             else k_fave_fft<4, double2><<<grid, 128, shm, st>>>(s);
             break;
           case 2:
-            if (s.mixed) k_fave_fft<2, float2><<<grid, 128, shm / 2, st>>>(s);
+            if (s.mixed) k_fave_fft<2, float2><<<grid, 128, shmf, st>>>(s);
             else k_fave_fft<2, double2><<<grid, 128, shm, st>>>(s);
             break;
           default:
-            if (s.mixed) k_fave_fft<1, float2><<<grid, 128, shm / 2, st>>>(s);
+            if (s.mixed) k_fave_fft<1, float2><<<grid, 128, shmf, st>>>(s);
             else k_fave_fft<1, double2><<<grid, 128, shm, st>>>(s);
             break;
         }

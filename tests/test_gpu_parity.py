@@ -219,3 +219,17 @@ def test_c2_subset_batches_consistently():
     small = bl.Context(0, hbm_budget=6 << 30)  # ~160 MB per crystallite: forces two batches
     two = gpu_fid(job, rows, ctx=small)
     np.testing.assert_array_equal(one, two)
+
+
+@pytest.mark.parametrize("seed,nsteps", [(0, 16), (1, 32), (2, 64), (3, 256), (6, 32), (10, 128)])
+def test_twisted_fave_matches_oracle(seed, nsteps):
+    """A power-of-two step count takes the twisted length-n correlation: all four rho/detect
+    combinations of random_system (symmetric rho with and without mirrored block pairs,
+    non-symmetric rho), against the oracle and against the direct correlation."""
+    job, rows = random_system(seed)
+    lines, kv = parse_job(job)
+    job = job.replace(f"sw: {kv['sw']}", f"sw: {nsteps * float(kv['wr'])!r}")
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, fave_method="fft")
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+    assert rel(fid, gpu_fid(job, rows, fave_method="direct")) <= TOL
