@@ -628,6 +628,41 @@ __device__ __forceinline__ void sym_mul(const double *X, const double *Y, double
     }
 }
 
+// cos X = sum_j c_j Y^j, sin X = X sum_j s_j Y^j (Y = X^2): c_j = (-1)^j/(2j)!, s_j = (-1)^j/(2j+1)!
+__device__ __forceinline__ constexpr double cos_coef(int j) {
+  return j == 0 ? 1.0 : j == 1 ? -1.0 / 2 : j == 2 ? 1.0 / 24 : j == 3 ? -1.0 / 720 : j == 4 ? 1.0 / 40320
+       : j == 5 ? -1.0 / 3628800 : j == 6 ? 1.0 / 479001600 : -1.0 / 87178291200.0;
+}
+__device__ __forceinline__ constexpr double sin_coef(int j) {
+  return j == 0 ? 1.0 : j == 1 ? -1.0 / 6 : j == 2 ? 1.0 / 120 : j == 3 ? -1.0 / 5040 : j == 4 ? 1.0 / 362880
+       : j == 5 ? -1.0 / 39916800 : j == 6 ? 1.0 / 6227020800.0 : -1.0 / 1307674368000.0;
+}
+
+// acc = sum_{j <= d} coef_j Y^j (d <= 7) for this thread's d: pairs L_m = coef_2m I +
+// coef_2m+1 Y (zero beyond d); acc = L_top, then acc = acc Y2 + L_m for m = top-1 .. 0
+// (Paterson-Stockmeyer with Y2 = Y^2: d/2 symmetric products).
+template <int B, bool SIN>
+__device__ __forceinline__ void ps_poly(int d, const double *Y, const double *Y2, double *acc, double *tmp) {
+  constexpr int NP = B * (B + 1) / 2;
+  const int top = d / 2;
+#pragma unroll
+  for (int m = 3; m >= 0; --m) {
+    if (m > top) continue;
+    const double a0 = SIN ? sin_coef(2 * m) : cos_coef(2 * m);
+    const double a1 = (2 * m + 1 <= d) ? (SIN ? sin_coef(2 * m + 1) : cos_coef(2 * m + 1)) : 0.0;
+    if (m < top) sym_mul<B>(acc, Y2, tmp, 1.0);
+#pragma unroll
+    for (int p = 0; p < B; ++p)
+#pragma unroll
+      for (int q = p; q < B; ++q) {
+        const int j = sx<B>(p, q);
+        const double l = fma(a1, Y[j], p == q ? a0 : 0.0);
+        acc[j] = (m < top) ? tmp[j] + l : l;
+      }
+  }
+  (void)NP;
+}
+
 // One thread per (crystallite, block k, step i): U_i = exp(-i 2pi tau H_i) by a Taylor
 // series of the scaled real symmetric block plus repeated squaring.  Real and imaginary
 // parts of U are polynomials in H, hence symmetric and commuting, so every product is a
@@ -662,39 +697,35 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *_
   }
   const double sc = ldexp(tp, -sq);
   const int K = taylor_degree(ldexp(nrm, -sq));
-  double X[NP], P[NP], Q[NP], R[NP], I[NP];
+  // The degree-K Taylor polynomial of exp(-iX) as cos X - i sin X with cos X = C(Y) of degree
+  // K/2 and sin X = X S(Y) of degree (K-1)/2 in Y = X^2, each by Paterson-Stockmeyer in Y^2
+  // (K = 11: 7 symmetric products instead of 10).  X waits in this thread's slice of shared
+  // memory, so that five packed arrays are live in registers.
+  __shared__ double Xs[NP * kThreads];
+  double Y[NP], Y2[NP], R[NP], S[NP], T[NP];
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
-    for (int q = p; q < B; ++q) {
-      X[sx<B>(p, q)] = sc * h[p][q];
-      P[sx<B>(p, q)] = X[sx<B>(p, q)];
-      R[sx<B>(p, q)] = (p == q) ? 1.0 : 0.0;
-      I[sx<B>(p, q)] = -P[sx<B>(p, q)];  // k = 1 term: -i X
-    }
-  // terms k = 2..K: P_k = P_{k-1} X / k; (-i)^k cycles -1, +i, +1, -i
+    for (int q = p; q < B; ++q) T[sx<B>(p, q)] = sc * h[p][q];
 #pragma unroll
-  for (int kt = 2; kt <= kTaylorTerms; ++kt) {
-    if (kt > K) break;
-    sym_mul<B>(P, X, Q, 1.0 / kt);
+  for (int j = 0; j < NP; ++j) Xs[j * blockDim.x + threadIdx.x] = T[j];
+  sym_mul<B>(T, T, Y, 1.0);
+  sym_mul<B>(Y, Y, Y2, 1.0);
+  ps_poly<B, false>(K / 2, Y, Y2, R, T);        // R = cos X
+  ps_poly<B, true>((K - 1) / 2, Y, Y2, S, T);   // S(Y)
 #pragma unroll
-    for (int j = 0; j < NP; ++j) {
-      P[j] = Q[j];
-      if ((kt & 3) == 2) R[j] -= Q[j];
-      else if ((kt & 3) == 3) I[j] += Q[j];
-      else if ((kt & 3) == 0) R[j] += Q[j];
-      else I[j] -= Q[j];
-    }
-  }
+  for (int j = 0; j < NP; ++j) T[j] = Xs[j * blockDim.x + threadIdx.x];
+  double *I = Y2;
+  sym_mul<B>(T, S, I, -1.0);  // I = -sin X = -X S(Y)
   // (R + iI)^2 = (R R - I I) + i 2 R I
   for (int t = 0; t < sq; ++t) {
-    sym_mul<B>(R, R, P, 1.0);
-    sym_mul<B>(I, I, Q, 1.0);
-    sym_mul<B>(R, I, X, 2.0);
+    sym_mul<B>(R, R, Y, 1.0);
+    sym_mul<B>(I, I, S, 1.0);
+    sym_mul<B>(R, I, T, 2.0);
 #pragma unroll
     for (int j = 0; j < NP; ++j) {
-      R[j] = P[j] - Q[j];
-      I[j] = X[j];
+      R[j] = Y[j] - S[j];
+      I[j] = T[j];
     }
   }
   double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
