@@ -799,6 +799,259 @@ __global__ void __launch_bounds__(kThreads) k_floquet(DevSys s, const int *__res
   }
 }
 
+
+// ------------------------------------------------------------------ Floquet, lanes per matrix
+// The FP64 pipe costs a warp instruction whatever its active lanes, so one thread per
+// (crystallite, block) leaves most SM sub-partitions idle when there are few blocks.  Here B
+// lanes work on one matrix (lane r owns row r), 32/B matrices per warp: the same Cayley
+// transform with partial pivoting and back substitution as unitary_eig, then a parallel
+// (round-robin) complex Jacobi on K as in floquet_cta, and the Rayleigh quotients.  Every
+// index into a lane's row is a compile-time constant (the rounds and pairs are unrolled);
+// rows move between lanes by shuffles within the group.
+template <int B>
+struct LaneGroup {
+  unsigned mask;
+  int base;
+  __device__ __forceinline__ double shfl(double v, int src) const { return __shfl_sync(mask, v, base + src); }
+  __device__ __forceinline__ double2 shfl(double2 v, int src) const { return cmk(shfl(v.x, src), shfl(v.y, src)); }
+  __device__ __forceinline__ int shfl(int v, int src) const { return __shfl_sync(mask, v, base + src); }
+};
+
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int *__restrict__ blist, int nblist) {
+  constexpr int GPW = 32 / B;             // matrices per warp
+  constexpr int BQ = B + (B & 1), NP = BQ / 2;  // round-robin players (one dummy when B is odd)
+  const int lane = threadIdx.x & 31;
+  const long warp = (long(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int gi = lane / B, r = lane % B;
+  if (gi >= GPW) return;
+  const long item = warp * GPW + gi;
+  if (item >= long(nblist) * s.Cpad) return;
+  const int c = int(item % s.Cpad), k = blist[item / s.Cpad];
+  if (c >= s.C) return;  // the whole group leaves together
+  const LaneGroup<B> g{((1u << B) - 1u) << (gi * B), gi * B};
+  const int bp = s.bpoff[k], bo = s.boff[k];
+  const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
+  double2 U[B], V[B], K[B], lam[B];
+#pragma unroll
+  for (int q = 0; q < B; ++q) U[q] = An[at(bp + r * B + q, c, s.Cpad)];
+  int st = 0;
+  double a = 0.5;
+  for (int pass = 0; pass < 2; ++pass) {
+    double sa, ca;
+    sincos(a, &sa, &ca);
+    const double2 ea = cmk(ca, sa);
+    double2 M[B], X[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      const double2 w = cmul(ea, U[q]);
+      const double id = (q == r) ? 1.0 : 0.0;
+      M[q] = cmk(id + w.x, w.y);
+      X[q] = cmk(id - w.x, -w.y);
+    }
+    // Gaussian elimination with partial pivoting (first largest |M[i][k]|, i >= k): M X' = X
+#pragma unroll
+    for (int kc = 0; kc < B; ++kc) {
+      const double m2 = (r >= kc) ? M[kc].x * M[kc].x + M[kc].y * M[kc].y : -1.0;
+      int piv = kc;
+      double best = g.shfl(m2, kc);
+#pragma unroll
+      for (int i = kc + 1; i < B; ++i) {
+        const double v = g.shfl(m2, i);
+        if (v > best) best = v, piv = i;
+      }
+      if (best == 0.0) st |= kSingularCayley;
+      const int src = (r == kc) ? piv : (r == piv ? kc : r);
+#pragma unroll
+      for (int q = 0; q < B; ++q) M[q] = g.shfl(M[q], src), X[q] = g.shfl(X[q], src);
+      double2 Mk[B], Xk[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) Mk[q] = g.shfl(M[q], kc), Xk[q] = g.shfl(X[q], kc);
+      if (r > kc) {
+        const double2 f = cmul(M[kc], cdiv(cmk(1, 0), Mk[kc]));
+#pragma unroll
+        for (int q = kc; q < B; ++q) M[q] = csub(M[q], cmul(f, Mk[q]));
+#pragma unroll
+        for (int q = 0; q < B; ++q) X[q] = csub(X[q], cmul(f, Xk[q]));
+      }
+    }
+    // back substitution, row kc on lane kc from the final rows below it
+#pragma unroll
+    for (int kc = B - 1; kc >= 0; --kc) {
+      double2 acc[B];
+#pragma unroll
+      for (int q = 0; q < B; ++q) acc[q] = X[q];
+#pragma unroll
+      for (int i = kc + 1; i < B; ++i) {
+        const double2 mki = M[i];  // M[kc][i] on lane kc
+#pragma unroll
+        for (int q = 0; q < B; ++q) {
+          const double2 xiq = g.shfl(X[q], i);
+          acc[q] = csub(acc[q], cmul(mki, xiq));
+        }
+      }
+      if (r == kc) {
+        const double2 inv = cdiv(cmk(1, 0), M[kc]);
+#pragma unroll
+        for (int q = 0; q < B; ++q) X[q] = cmul(acc[q], inv);
+      }
+    }
+    // K = Hermitian part of i X (row r needs column r of X: X[q][r] from lane q), V = I
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      double2 xqr = cmk(0, 0);
+#pragma unroll
+      for (int t = 0; t < B; ++t) {
+        const double2 v = g.shfl(X[t], q);
+        if (t == r) xqr = v;
+      }
+      const double2 krq = cmk(-X[q].y, X[q].x), kqr = cmk(-xqr.y, xqr.x);
+      K[q] = cscale(cadd(krq, cconj(kqr)), 0.5);
+      V[q] = cmk(q == r ? 1.0 : 0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < B; ++q)
+      if (q == r) K[q].y = 0.0;
+    bool conv = false;
+    for (int sweep = 0; sweep < kMaxSweeps && !conv; ++sweep) {
+      double off = 0, dg = 0;
+#pragma unroll
+      for (int q = 0; q < B; ++q) {
+        if (q > r) off += K[q].x * K[q].x + K[q].y * K[q].y;
+        if (q == r) dg += K[q].x * K[q].x;
+      }
+      double offs = 0, dgs = 0;
+#pragma unroll
+      for (int t = 0; t < B; ++t) offs += g.shfl(off, t), dgs += g.shfl(dg, t);
+      if (offs <= 1e-34 * dgs || offs == 0.0) {
+        conv = true;
+        break;
+      }
+#pragma unroll
+      for (int round = 0; round < BQ - 1; ++round) {
+        // this lane's pair (mp, mq) of the round, or none
+        int mp = r, mq = r;
+        bool paired = false;
+#pragma unroll
+        for (int t = 0; t < NP; ++t) {
+          const int j1 = t, j2 = BQ - 1 - t;
+          int p = j1 == 0 ? 0 : 1 + (j1 - 1 + round) % (BQ - 1);
+          int q = j2 == 0 ? 0 : 1 + (j2 - 1 + round) % (BQ - 1);
+          if (p > q) { const int x = p; p = q; q = x; }
+          if (q < B && (r == p || r == q)) mp = p, mq = q, paired = true;
+        }
+        // the pair's rotation, computed identically by both of its lanes from K[p][q]
+        // (lane p's entry q), K[p][p] and K[q][q]
+        double2 own_q = cmk(0, 0), own_d = cmk(0, 0);
+#pragma unroll
+        for (int q2 = 0; q2 < B; ++q2) {
+          if (q2 == mq) own_q = K[q2];
+          if (q2 == r) own_d = K[q2];
+        }
+        const double2 hpq = g.shfl(own_q, mp);
+        const double kpp = g.shfl(own_d.x, mp), kqq = g.shfl(own_d.x, mq);
+        double cs = 1.0;
+        double2 sp = cmk(0, 0);
+        if (paired) {
+          const double ab = hypot(hpq.x, hpq.y);
+          if (ab != 0.0) {
+            const double2 ph = cmk(hpq.x / ab, hpq.y / ab);
+            const double theta = 0.5 * (kqq - kpp) / ab;
+            double tt;
+            if (fabs(theta) > 1e100) tt = 0.5 / theta;
+            else tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
+            cs = rsqrt(fma(tt, tt, 1.0));
+            sp = cscale(ph, tt * cs);
+          }
+        }
+        // columns p, q of K and V for every pair: K <- K G, V <- V G, G = [[c, sp], [-conj(sp), c]]
+#pragma unroll
+        for (int t = 0; t < NP; ++t) {
+          const int j1 = t, j2 = BQ - 1 - t;
+          int p = j1 == 0 ? 0 : 1 + (j1 - 1 + round) % (BQ - 1);
+          int q = j2 == 0 ? 0 : 1 + (j2 - 1 + round) % (BQ - 1);
+          if (p > q) { const int x = p; p = q; q = x; }
+          if (q >= B) continue;
+          const double cst = g.shfl(cs, p);
+          const double2 spt = g.shfl(sp, p), spc = cconj(spt);
+          const double2 kp = K[p], kq = K[q];
+          K[p] = csub(cscale(kp, cst), cmul(spc, kq));
+          K[q] = cadd(cmul(spt, kp), cscale(kq, cst));
+          const double2 vp = V[p], vq = V[q];
+          V[p] = csub(cscale(vp, cst), cmul(spc, vq));
+          V[q] = cadd(cmul(spt, vp), cscale(vq, cst));
+        }
+        // rows p, q of K: K <- G^H K, as row = alpha row_p + beta row_q in every lane
+        // (lane p: cs, -sp; lane q: conj(sp), cs; a lane without a pair keeps its row)
+        const bool isp = paired && r == mp;
+        const double2 al = !paired ? cmk(1, 0) : (isp ? cmk(cs, 0) : cconj(sp));
+        const double2 be = !paired ? cmk(0, 0) : (isp ? cmk(-sp.x, -sp.y) : cmk(cs, 0));
+#pragma unroll
+        for (int q2 = 0; q2 < B; ++q2) {
+          const double2 kpk = g.shfl(K[q2], mp), kqk = g.shfl(K[q2], mq);
+          if (paired) K[q2] = cadd(cmul(al, kpk), cmul(be, kqk));
+        }
+        if (paired && !(sp.x == 0.0 && sp.y == 0.0)) {
+          const int other = isp ? mq : mp;
+#pragma unroll
+          for (int q2 = 0; q2 < B; ++q2) {
+            if (q2 == other) K[q2] = cmk(0, 0);
+            if (q2 == r) K[q2].y = 0.0;
+          }
+        }
+      }
+    }
+    if (!conv) st |= kNoConvergeFloquet;
+    // Rayleigh quotients lam_r = v_r^H U v_r (columns of V), in every lane
+    double2 uv[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) uv[q] = cmk(0, 0);
+#pragma unroll
+    for (int l = 0; l < B; ++l)
+#pragma unroll
+      for (int q = 0; q < B; ++q) uv[q] = cfma(U[l], g.shfl(V[q], l), uv[q]);  // (U V)[r][q], l ascending
+#pragma unroll
+    for (int q = 0; q < B; ++q) lam[q] = cmk(0, 0);
+#pragma unroll
+    for (int kk = 0; kk < B; ++kk)
+#pragma unroll
+      for (int q = 0; q < B; ++q) lam[q] = cfmaconj(g.shfl(V[q], kk), g.shfl(uv[q], kk), lam[q]);
+    if (pass == 1) break;
+    double mind = 4.0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      const double2 w = cmul(ea, lam[q]);
+      mind = fmin(mind, (1.0 + w.x) * (1.0 + w.x) + w.y * w.y);
+    }
+    if (mind >= 0.0625) break;
+    // widest gap of the eigenphases (every lane, same values): -1 into its middle
+    double th[B];
+#pragma unroll
+    for (int q = 0; q < B; ++q) th[q] = atan2(lam[q].y, lam[q].x);
+#pragma unroll
+    for (int i = 1; i < B; ++i)
+#pragma unroll
+      for (int j = i; j > 0; --j)
+        if (th[j - 1] > th[j]) { const double x = th[j]; th[j] = th[j - 1]; th[j - 1] = x; }
+    double best = -1, mid = 0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) {
+      const double lo = th[q], hi = (q + 1 < B) ? th[q + 1] : th[0] + kPi2;
+      if (hi - lo > best) best = hi - lo, mid = 0.5 * (lo + hi);
+    }
+    a = kPi - mid;
+  }
+  if (st && r == 0) atomicOr(s.status, st);
+#pragma unroll
+  for (int q = 0; q < B; ++q) s.VF[at(bp + r * B + q, c, s.Cpad)] = V[q];
+  double2 lr = cmk(0, 0);
+#pragma unroll
+  for (int q = 0; q < B; ++q)
+    if (q == r) lr = lam[q];
+  // principal-branch log: (ln|lam|, atan2)   (complex.h:1058-1061)
+  s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lr.x, lr.y)), atan2(lr.y, lr.x));
+}
+
 // One thread per (crystallite, block, step): W_i = A_{i+1} V_F (in place over A in FP64;
 // into the single-precision W array in the mixed form).
 template <int B, class C>
@@ -1839,7 +2092,14 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
       else k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
       break;
     case 1: k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl); break;
-    case 2: k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl); break;
+    case 2:
+      if (B == 1) {
+        k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl);
+      } else {  // B lanes per matrix, 32/B matrices per warp
+        const long warps = (Cp * nl + (32 / B) - 1) / (32 / B);
+        k_floquet_lanes<B><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
+      }
+      break;
     case 3:
       if (s.mixed) k_eigframe<B, float2><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
       else k_eigframe<B, double2><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
