@@ -65,6 +65,11 @@ _SIGS = {
     "bl_job_describe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "bl_job_destroy": (None, [ctypes.c_void_p]),
     "bl_plotter_fid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_double]),
+    "bl_mat5_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_mat5_put": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                   ctypes.c_int]),
+    "bl_mat5_put_string": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_char_p]),
+    "bl_mat5_close": (None, [ctypes.c_void_p]),
     "bl_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
     "bl_job_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "bl_job_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -497,6 +502,49 @@ def rotationMatrix3D(a, b, g=None):
     else:
         _check(load().bl_rotation3(float(a), float(b), float(g), _ptr(R)))
     return R.reshape(3, 3)
+
+
+class matstream:
+    """MAT-file level 5 output, as the reference's Matlab5 / matstream (bl_mat5_*):
+    put(name, value) appends a scalar (1 x 1), a 1-D array (column vector, the reference's
+    put(name, Vector)), a 2-D array, real or complex, or a string."""
+
+    def __init__(self, path):
+        h = ctypes.c_void_p()
+        _check(load().bl_mat5_open(str(path).encode(), ctypes.byref(h)))
+        self._h = h
+
+    def put(self, name, value):
+        if isinstance(value, str):
+            _check(load().bl_mat5_put_string(self._h, name.encode(), value.encode()))
+            return
+        a = np.asarray(value)
+        if a.ndim == 0:
+            a = a.reshape(1, 1)
+        elif a.ndim == 1:
+            a = a.reshape(-1, 1)
+        elif a.ndim != 2:
+            raise ValueError("matstream.put takes scalars, vectors, matrices or strings")
+        cplx = np.iscomplexobj(a)
+        d = np.ascontiguousarray(a, dtype=np.complex128 if cplx else np.float64)
+        _check(load().bl_mat5_put(self._h, name.encode(), _ptr(d), d.shape[0], d.shape[1], int(cplx)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().bl_mat5_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def plotterFID(fid, datasave="fid", dt=1.0):

@@ -271,6 +271,39 @@ bl_status bl_powder_fid_noalloc(bl_ctx *ctx, const bl_system *sys, const bl_powd
   });
 }
 
+struct bl_mat5 {
+  bl::Mat5Writer w;
+  explicit bl_mat5(const char *path) : w(path) {}
+};
+
+bl_status bl_mat5_open(const char *path, bl_mat5 **out) {
+  if (!path || !out) return fail(BL_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] { *out = new bl_mat5(path); });
+}
+
+bl_status bl_mat5_put(bl_mat5 *m, const char *name, const double *data, int rows, int cols, int is_complex) {
+  if (!m || !name || (!data && rows * cols > 0) || rows < 0 || cols < 0) return fail(BL_ERR_INVALID, "bad arguments");
+  return guarded([&] {
+    const size_t n = size_t(rows) * size_t(cols);
+    std::vector<double> re(n), im(is_complex ? n : 0);
+    for (int r = 0; r < rows; ++r)  // row-major in, column-major (MATLAB order) out
+      for (int c = 0; c < cols; ++c) {
+        const size_t src = size_t(r) * cols + c, dst = size_t(c) * rows + r;
+        re[dst] = is_complex ? data[2 * src] : data[src];
+        if (is_complex) im[dst] = data[2 * src + 1];
+      }
+    m->w.put_matrix(name, re.data(), is_complex ? im.data() : nullptr, rows, cols);
+  });
+}
+
+bl_status bl_mat5_put_string(bl_mat5 *m, const char *name, const char *text) {
+  if (!m || !name || !text) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] { m->w.put_string(name, text); });
+}
+
+void bl_mat5_close(bl_mat5 *m) { delete m; }
+
 bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt) {
   if (!fid || !path || npts <= 0) return fail(BL_ERR_INVALID, "bad arguments");
   return guarded([&] { bl::write_fid_text(path, reinterpret_cast<const bl::cplx *>(fid), npts, dt); });

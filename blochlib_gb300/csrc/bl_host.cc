@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <map>
 #include <numeric>
@@ -542,6 +543,84 @@ void write_fid_text(const std::string &path, const cplx *fid, int npts, double d
     minw += dw;
     t += dt;
   }
+}
+
+// ---------------------------------------------------------------- MAT-5 files
+namespace {
+constexpr uint32_t miINT8 = 1, miUINT16 = 4, miINT32 = 5, miUINT32 = 6, miDOUBLE = 9, miMATRIX = 14;
+constexpr uint32_t mxCHAR_CLASS = 4, mxDOUBLE_CLASS = 6, kComplexFlag = 0x0800;
+size_t padded8(size_t n) { return (n + 7) / 8 * 8; }
+}  // namespace
+
+void Mat5Writer::bytes(const void *p, size_t n) { f_.write(static_cast<const char *>(p), std::streamsize(n)); }
+void Mat5Writer::u32(uint32_t v) {  // little endian, whatever the host
+  const unsigned char b[4] = {static_cast<unsigned char>(v), static_cast<unsigned char>(v >> 8),
+                              static_cast<unsigned char>(v >> 16), static_cast<unsigned char>(v >> 24)};
+  bytes(b, 4);
+}
+void Mat5Writer::pad8(size_t n) {
+  static const char z[8] = {0};
+  if (padded8(n) != n) bytes(z, padded8(n) - n);
+}
+void Mat5Writer::name_element(const std::string &name) {
+  u32(miINT8), u32(uint32_t(name.size()));
+  bytes(name.data(), name.size());
+  pad8(name.size());
+}
+
+Mat5Writer::Mat5Writer(const std::string &path) : f_(path, std::ios::binary | std::ios::trunc) {
+  if (!f_) throw Error(1, "cannot write '" + path + "'");
+  std::string txt = "MATLAB 5.0 MAT-file, written by blochlib_gb300";
+  txt.resize(116, ' ');
+  bytes(txt.data(), 116);
+  const char subsys[8] = {0};
+  bytes(subsys, 8);
+  const unsigned char ver_endian[4] = {0x00, 0x01, 'I', 'M'};  // version 0x0100, "MI" read as int16
+  bytes(ver_endian, 4);
+}
+
+void Mat5Writer::put_matrix(const std::string &name, const double *re, const double *im, int rows, int cols) {
+  if (rows < 0 || cols < 0 || name.empty()) throw Error(1, "bad MAT-5 variable");
+  const size_t n = size_t(rows) * size_t(cols), data = 8 * n;
+  const size_t body = 16 + 16 + 8 + padded8(name.size()) + 8 + data + (im ? 8 + data : 0);
+  u32(miMATRIX), u32(uint32_t(body));
+  u32(miUINT32), u32(8), u32(mxDOUBLE_CLASS | (im ? kComplexFlag : 0)), u32(0);  // array flags
+  u32(miINT32), u32(8), u32(uint32_t(rows)), u32(uint32_t(cols));                 // dimensions
+  name_element(name);
+  u32(miDOUBLE), u32(uint32_t(data));
+  for (size_t i = 0; i < n; ++i) {
+    uint64_t v;
+    std::memcpy(&v, re + i, 8);
+    u32(uint32_t(v)), u32(uint32_t(v >> 32));
+  }
+  if (im) {
+    u32(miDOUBLE), u32(uint32_t(data));
+    for (size_t i = 0; i < n; ++i) {
+      uint64_t v;
+      std::memcpy(&v, im + i, 8);
+      u32(uint32_t(v)), u32(uint32_t(v >> 32));
+    }
+  }
+  f_.flush();
+  if (!f_) throw Error(1, "MAT-5 write failed for '" + name + "'");
+}
+
+void Mat5Writer::put_string(const std::string &name, const std::string &text) {
+  if (name.empty()) throw Error(1, "bad MAT-5 variable");
+  const size_t n = text.size(), data = 2 * n;
+  const size_t body = 16 + 16 + 8 + padded8(name.size()) + 8 + padded8(data);
+  u32(miMATRIX), u32(uint32_t(body));
+  u32(miUINT32), u32(8), u32(mxCHAR_CLASS), u32(0);
+  u32(miINT32), u32(8), u32(1), u32(uint32_t(n));
+  name_element(name);
+  u32(miUINT16), u32(uint32_t(data));
+  for (unsigned char ch : text) {
+    const unsigned char b[2] = {ch, 0};
+    bytes(b, 2);
+  }
+  pad8(data);
+  f_.flush();
+  if (!f_) throw Error(1, "MAT-5 write failed for '" + name + "'");
 }
 
 }  // namespace bl

@@ -12,9 +12,12 @@
 //   Hamiltonian(t1,t2,wr)             src/QMspins/sys.cc:749-770
 //   powder generation / file reader   src/QMspins/driver/powder.cc:179-311, 333-389
 //   plotterFID text output            src/utils/plotter.cc:49-135
+//   Matlab5 / matstream MAT-5 files   src/utils/matlab5.h:603-792
 #pragma once
 
 #include <complex>
+#include <cstdint>
+#include <fstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -115,5 +118,23 @@ Powder powder_read(const std::string &path);        // powder.cc:333-389 (no ren
 
 // plotterFID-style 7-column text output (src/utils/plotter.cc:49-135)
 void write_fid_text(const std::string &path, const cplx *fid, int npts, double dt);
+
+// MAT-file level 5 writer, the file format of the reference's Matlab5 / matstream
+// (src/utils/matlab5.h:603-792): a 128-byte header, then one uncompressed miMATRIX element per
+// variable (double matrices, real or complex, and character strings), little endian.
+class Mat5Writer {
+ public:
+  explicit Mat5Writer(const std::string &path);
+  // rows x cols in MATLAB (column-major) order; im may be null for a real matrix
+  void put_matrix(const std::string &name, const double *re, const double *im, int rows, int cols);
+  void put_string(const std::string &name, const std::string &text);
+
+ private:
+  std::ofstream f_;
+  void bytes(const void *p, size_t n);
+  void u32(uint32_t v);
+  void pad8(size_t n);
+  void name_element(const std::string &name);
+};
 
 }  // namespace bl

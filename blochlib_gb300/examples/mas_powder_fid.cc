@@ -31,6 +31,9 @@ int main(int argc, char **argv) {
     oneFID<SolidSys> myfid(mysys, npts, sw, wr, beta);
     std::vector<complex> fid = myfid.FID(zcw, roeq, detect);
     plotterFID(fid, argv[7], 1.0 / myfid.sw());
+    matstream matout(std::string(argv[7]) + ".mat");  // as solid-2.0 saves its FIDs
+    matout.put("vdat", fid);
+    matout.put("sw1", myfid.sw());
     std::printf("%d crystallites, dim %d, sw %.6g Hz, fid[0] = %.15g %+.15gi\n", zcw.size(), mysys.HS(),
                 myfid.sw(), fid[0].real(), fid[0].imag());
   } catch (const bl_error &e) {

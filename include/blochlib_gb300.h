@@ -21,6 +21,7 @@
  *                         keep inputs resident on the GPU between calls (no reference twin;
  *                         oneFID::FID recomputes from host data every call)
  *   bl_plotter_fid        plotterFID(fid, file, dt)                  src/utils/plotter.cc:49-135
+ *   bl_mat5_*             Matlab5 / matstream put(name, data)        src/utils/matlab5.h:603-792
  *   bl_rotation3/2        rotationMatrix3D(a,b,g) / (phi,theta)      src/QMspins/space_ten.cc:578-652
  */
 #ifndef BLOCHLIB_GB300_H
@@ -185,6 +186,17 @@ bl_status bl_rotation2(double phi, double theta, double *R9);
 
 /* plotterFID-style text file: t, f, Re S, Im S, Re fid, Im fid, |S| (7 columns). */
 bl_status bl_plotter_fid(const double *fid, int npts, const char *path, double dt);
+
+/* MAT-file level 5 output, as the reference's Matlab5 / matstream (src/utils/matlab5.h:603-792,
+ * e.g. matout.put("vdat", fid) in examples/solid-2.0/src/sequencerun_funcs.cc:786-868): open
+ * truncates the file and writes the header; each put appends one variable.  bl_mat5_put takes
+ * a rows x cols double matrix in row-major order, interleaved (re, im) when is_complex; a
+ * vector is rows x 1 (the reference's put(name, Vector)), a scalar 1 x 1. */
+typedef struct bl_mat5 bl_mat5;
+bl_status bl_mat5_open(const char *path, bl_mat5 **out);
+bl_status bl_mat5_put(bl_mat5 *m, const char *name, const double *data, int rows, int cols, int is_complex);
+bl_status bl_mat5_put_string(bl_mat5 *m, const char *name, const char *text);
+void bl_mat5_close(bl_mat5 *m);
 
 #ifdef __cplusplus
 }

@@ -11,6 +11,7 @@
 //   oneFID<SolidSys>(sys, npts, sw, wr, rotb, startT), FID(powder, ro, det)
 //                                      src/QMspins/driver/oneFID.h:103-108, 200-208
 //   plotterFID(fid, file, dt)          src/utils/plotter.cc:49-135
+//   matstream / Matlab5 put(name, x)   src/utils/matlab5.h:603-792
 #ifndef BLOCHLIB_GB300_HPP
 #define BLOCHLIB_GB300_HPP
 
@@ -183,6 +184,35 @@ inline std::string plotterFID(const std::vector<complex> &fid, const std::string
   check(bl_plotter_fid(reinterpret_cast<const double *>(fid.data()), int(fid.size()), datasave.c_str(), dt));
   return datasave;
 }
+
+// MAT-5 output (src/utils/matlab5.h:603-792, `typedef Matlab5 matstream`): put(name, x)
+// appends a scalar, a vector (column), a matrix or a string.
+class matstream {
+ public:
+  explicit matstream(const std::string &fname) { check(bl_mat5_open(fname.c_str(), &h_)); }
+  ~matstream() { bl_mat5_close(h_); }
+  matstream(const matstream &) = delete;
+  matstream &operator=(const matstream &) = delete;
+  void put(const std::string &name, double x) { check(bl_mat5_put(h_, name.c_str(), &x, 1, 1, 0)); }
+  void put(const std::string &name, complex x) {
+    check(bl_mat5_put(h_, name.c_str(), reinterpret_cast<const double *>(&x), 1, 1, 1));
+  }
+  void put(const std::string &name, const std::vector<double> &v) {
+    check(bl_mat5_put(h_, name.c_str(), v.data(), int(v.size()), 1, 0));
+  }
+  void put(const std::string &name, const std::vector<complex> &v) {
+    check(bl_mat5_put(h_, name.c_str(), reinterpret_cast<const double *>(v.data()), int(v.size()), 1, 1));
+  }
+  void put(const std::string &name, const matrix &m) { check(bl_mat5_put(h_, name.c_str(), m.data(), m.n, m.n, 1)); }
+  void put(const std::string &name, const std::string &text) {
+    check(bl_mat5_put_string(h_, name.c_str(), text.c_str()));
+  }
+  void put(const std::string &name, const char *text) { put(name, std::string(text)); }
+
+ private:
+  bl_mat5 *h_ = nullptr;
+};
+typedef matstream Matlab5;
 
 }  // namespace blochlib_gb300
 

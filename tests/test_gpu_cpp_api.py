@@ -1,5 +1,6 @@
 """The C++ host API (include/blochlib_gb300.hpp) end to end: the example program runs a
-BlochLib-style powder FID and its plotterFID output matches the Python path."""
+BlochLib-style powder FID; its plotterFID text matches the Python path to the text's
+precision and its MAT-5 output (matstream) bit for bit."""
 import subprocess
 
 import numpy as np
@@ -25,3 +26,7 @@ def test_cpp_example_matches_python_path(tmp_path):
     s = bl.SolidSys(spinl)
     fid = bl.oneFID(s, npts, sw, wr, beta).FID(bl.powder(bl.powder.zcw, t, p), s.Fx() + s.Fz(), s.Fp())
     np.testing.assert_allclose(d[:npts, 4] + 1j * d[:npts, 5], fid, rtol=2e-5, atol=2e-5 * np.abs(fid).max())
+    sio = pytest.importorskip("scipy.io")
+    m = sio.loadmat(str(out) + ".mat")
+    np.testing.assert_array_equal(m["vdat"][:, 0], fid)
+    assert m["sw1"][0, 0] == sw

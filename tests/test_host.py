@@ -161,3 +161,26 @@ def test_job_bytes_plans_on_the_host():
     assert _sized(c1, 64, precision=1)[1] < hi64
     small, big = _sized(W.config(3, 5), 64), _sized(W.config(3, 0), 64)  # 3 vs 7 protons
     assert big[0] > small[0]
+
+
+def test_mat5_files_read_back(tmp_path):
+    """matstream writes MAT-file level 5 (the reference's Matlab5 format): complex and real
+    vectors, matrices, scalars and strings come back exactly through scipy.io.loadmat."""
+    sio = pytest.importorskip("scipy.io")
+    rng = np.random.default_rng(5)
+    fid = rng.normal(size=100) + 1j * rng.normal(size=100)
+    m = rng.normal(size=(3, 4)) + 1j * rng.normal(size=(3, 4))
+    r = rng.normal(size=(2, 5))
+    path = tmp_path / "out.mat"
+    with bl.matstream(path) as ms:
+        ms.put("vdat", fid)
+        ms.put("sw1", 123456.5)
+        ms.put("mx", m)
+        ms.put("rx", r)
+        ms.put("note", "powder FID, 3722 crystallites")
+    d = sio.loadmat(str(path))
+    np.testing.assert_array_equal(d["vdat"], fid.reshape(-1, 1))
+    assert d["sw1"].shape == (1, 1) and d["sw1"][0, 0] == 123456.5
+    np.testing.assert_array_equal(d["mx"], m)
+    np.testing.assert_array_equal(d["rx"], r)
+    assert str(d["note"][0]) == "powder FID, 3722 crystallites"
