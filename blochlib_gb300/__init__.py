@@ -65,6 +65,7 @@ _SIGS = {
     "bl_job_describe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "bl_job_destroy": (None, [ctypes.c_void_p]),
     "bl_plotter_fid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_double]),
+    "bl_system_set_bfield": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "bl_mat5_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     "bl_mat5_put": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int]),
@@ -218,6 +219,11 @@ class SolidSys:
                 load().bl_system_destroy(self._h)
         except Exception:
             pass
+
+    def setBfield(self, bfield):
+        """SolidSys::setBfield: with |B| > 1e-12 quadrupoles add their second-order term
+        (or use it alone when their Q line's order column is 2)."""
+        _check(load().bl_system_set_bfield(self._h, float(bfield)))
 
     def dim(self):
         return load().bl_system_dim(self._h)

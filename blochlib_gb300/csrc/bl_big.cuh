@@ -167,16 +167,9 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
     double tmid = (t2 - t1) / 2.0 + t1;
     double sp, cp;
     sincos(tmid * s.wr * kPi2, &sp, &cp);
-    double rr0 = sp * s.sin_rotb, rr1 = -cp * s.sin_rotb, rr2 = s.cos_rotb, r[3];
-    for (int j = 0; j < 3; ++j)
-      r[j] = rr0 * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr1 * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
-             rr2 * s.Rp[at(2 * 3 + j, c, s.Cpad)];
-    for (int kk = 0; kk < s.nint; ++kk) {
-      const double *Pa = s.pas + 6 * kk;
-      double a = r[0] * (Pa[0] * r[0] + Pa[1] * r[1] + Pa[2] * r[2]) +
-                 r[1] * (Pa[1] * r[0] + Pa[3] * r[1] + Pa[4] * r[2]) + r[2] * (Pa[2] * r[0] + Pa[4] * r[1] + Pa[5] * r[2]);
-      fk[kk] = s.iscale[kk] * a;
-    }
+    double m[3][3];
+    orient_rows(s, c, sp, cp, m);
+    for (int kk = 0; kk < s.nint; ++kk) fk[kk] = term_coef(s, kk, m);
   }
   __syncthreads();
   double *X = bsm;

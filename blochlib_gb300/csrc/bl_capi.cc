@@ -98,6 +98,15 @@ bl_status bl_system_create(const char *spin_text, bl_system **out) {
 }
 
 void bl_system_destroy(bl_system *sys) { delete sys; }
+
+bl_status bl_system_set_bfield(bl_system *sys, double bfield) {
+  if (!sys) return fail(BL_ERR_INVALID, "null system");
+  return guarded([&] {  // a new system object: requests already holding the old one keep it
+    auto copy = std::make_shared<bl::SpinSystem>(*sys->sp);
+    copy->set_bfield(bfield);
+    sys->sp = copy;
+  });
+}
 int bl_system_dim(const bl_system *sys) { return sys ? sys->s().dim() : 0; }
 int bl_system_spins(const bl_system *sys) { return sys ? sys->s().spins() : 0; }
 

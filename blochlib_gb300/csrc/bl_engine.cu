@@ -121,6 +121,8 @@ struct DevSys {
   const int *bs, *boff, *bpoff;
   // per interaction: crystal tensor (xx xy xz yy yz zz), scale, packed operator
   const double *pas, *iscale, *Tk, *Hc;
+  const int *ikind;  // per term: 0 first order, 1 / 2 second-order quadrupolar (c4 / c2)
+  int has2;
   // Q pairs (D blocks) and R pairs (rho blocks)
   int npq, npr;
   const int *qa, *qb, *qoff, *doff;
@@ -413,26 +415,57 @@ __device__ int unitary_eig(const double2 (&U)[B][B], double2 (&lam)[B], double2 
 // ------------------------------------------------------------------ kernels
 __device__ __forceinline__ size_t at(int item, int c, int Cpad) { return size_t(item) * Cpad + c; }
 
+// Rows of M = R_rotor(phi, beta) R_powder for crystallite c, phi the rotor phase (sin sp,
+// cos cp): row 2 always, rows 0 and 1 only when second-order quadrupolar terms need them.
+__device__ __forceinline__ void orient_rows(const DevSys &s, int c, double sp, double cp, double (&m)[3][3]) {
+  const double rr[3][3] = {{cp, sp, 0.0}, {-s.cos_rotb * sp, cp * s.cos_rotb, s.sin_rotb},
+                           {sp * s.sin_rotb, -cp * s.sin_rotb, s.cos_rotb}};
+#pragma unroll
+  for (int i = 2; i >= 0; --i) {
+    if (i < 2 && !s.has2) break;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      m[i][j] = rr[i][0] * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr[i][1] * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
+                rr[i][2] * s.Rp[at(2 * 3 + j, c, s.Cpad)];
+  }
+}
+
+// u PAS' v for the packed symmetric crystal tensor of term kk
+__device__ __forceinline__ double pas_form(const double *P, const double *u, const double *v) {
+  return u[0] * (P[0] * v[0] + P[1] * v[1] + P[2] * v[2]) + u[1] * (P[1] * v[0] + P[3] * v[1] + P[4] * v[2]) +
+         u[2] * (P[2] * v[0] + P[4] * v[1] + P[5] * v[2]);
+}
+
+// Coefficient of term kk: scale (M PAS' M^T)_22 (kind 0); second-order quadrupolar
+// scale ((r00-r11)^2/4 + r01^2) (kind 1) and scale (r02^2 + r12^2) (kind 2), r = M PAS' M^T.
+__device__ __forceinline__ double term_coef(const DevSys &s, int kk, const double (&m)[3][3]) {
+  const double *P = s.pas + 6 * kk;
+  const int kind = s.has2 ? s.ikind[kk] : 0;
+  double a;
+  if (kind == 0) {
+    a = pas_form(P, m[2], m[2]);
+  } else if (kind == 1) {
+    const double r00 = pas_form(P, m[0], m[0]), r11 = pas_form(P, m[1], m[1]), r01 = pas_form(P, m[0], m[1]);
+    a = (r00 - r11) * (r00 - r11) / 4.0 + r01 * r01;
+  } else {
+    const double r02 = pas_form(P, m[0], m[2]), r12 = pas_form(P, m[1], m[2]);
+    a = r02 * r02 + r12 * r12;
+  }
+  return s.iscale[kk] * a;
+}
+
 // H_i block at the midpoint of step i (sys.cc:749-770): rotor phase 2 pi wr t_mid,
 // a = (M PAS M^T)_22 with M = R_rotor R_powder, H = Hc + sum_k scale_k a_k T_k.
 template <int B>
 __device__ __forceinline__ void build_h_at(const DevSys &s, int c, double sp, double cp, int bp, double (&h)[B][B]) {
-  // row 2 of R_rotor(phi, beta) times R_powder, phi the rotor phase (sin sp, cos cp)
-  double rr0 = sp * s.sin_rotb, rr1 = -cp * s.sin_rotb, rr2 = s.cos_rotb;
-  double r[3];
-#pragma unroll
-  for (int j = 0; j < 3; ++j)
-    r[j] = rr0 * s.Rp[at(0 * 3 + j, c, s.Cpad)] + rr1 * s.Rp[at(1 * 3 + j, c, s.Cpad)] +
-           rr2 * s.Rp[at(2 * 3 + j, c, s.Cpad)];
+  double m[3][3];
+  orient_rows(s, c, sp, cp, m);
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
     for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
   for (int kk = 0; kk < s.nint; ++kk) {
-    const double *P = s.pas + 6 * kk;
-    double a = r[0] * (P[0] * r[0] + P[1] * r[1] + P[2] * r[2]) + r[1] * (P[1] * r[0] + P[3] * r[1] + P[4] * r[2]) +
-               r[2] * (P[2] * r[0] + P[4] * r[1] + P[5] * r[2]);
-    double f = s.iscale[kk] * a;
+    const double f = term_coef(s, kk, m);
     const double *T = s.Tk + size_t(kk) * s.S2 + bp;
 #pragma unroll
     for (int p = 0; p < B; ++p)
@@ -1562,6 +1595,8 @@ struct JobImpl {
   DevBuf<int> bs, boff, bpoff, qa, qb, qoff, doff, ra, rb, roff, rhooff, eq, erev, er, erg, esg, status, srp, seo;
   std::vector<DevBuf<int>> blist;
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
+  DevBuf<int> ikind;
+  int has2 = 0;  // second-order quadrupolar terms present
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
@@ -1668,19 +1703,38 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
           dst[L.poff[k] + r * L.size[k] + q] = M[size_t(L.perm[L.off[k] + r]) * N + L.perm[L.off[k] + q]];
   };
   if (!g_sizing) pack(sys.h_const(), Hc.data());  // planning needs only the counts
+  // orientation-dependent terms: kind 0 = scale (M PAS' M^T)_22 T; a quadrupole in a field
+  // adds kind 1 = s2 ((r00-r11)^2/4 + r01^2) c4 and kind 2 = -s2 (r02^2 + r12^2) c2 with
+  // s2 = Qp^2/(B nu_rel), r = M PAS' M^T (qua.cc:219-267: order 1 or |B| <= 1e-12 first order
+  // only, order 2 second order only, otherwise both)
   const auto &ints = sys.interactions();
-  for (size_t kk = 0; kk < ints.size(); ++kk) {
-    if (ints[kk].kind == 'J') continue;
-    const auto &I = ints[kk];
+  const double Bf = sys.bfield();
+  std::vector<int> ikind;
+  auto add_term = [&](const Interaction &I, int kind, double scale, const std::vector<double> &op) {
     pas.insert(pas.end(), {I.pas[0][0], I.pas[0][1], I.pas[0][2], I.pas[1][1], I.pas[1][2], I.pas[2][2]});
-    isc.push_back(I.op_scale);
+    isc.push_back(scale);
+    ikind.push_back(kind);
     if (!g_sizing) {
       size_t o = Tk.size();
       Tk.resize(o + L.S2);
-      pack(sys.h_ops()[kk], Tk.data() + o);
+      pack(op, Tk.data() + o);
     }
     ++J.nint;
+  };
+  for (size_t kk = 0; kk < ints.size(); ++kk) {
+    const auto &I = ints[kk];
+    if (I.kind == 'J') continue;
+    const bool quad = I.kind == 'Q';
+    const bool first_only = !quad || I.order == 1 || std::fabs(Bf) <= 1e-12;
+    const bool second_only = !first_only && I.order == 2;
+    if (!second_only) add_term(I, 0, I.op_scale, sys.h_ops()[kk]);
+    if (!first_only) {
+      const double s2 = I.op_scale * I.op_scale / (Bf * isotope_rel_freq(sys.isotopes()[I.s1]));
+      add_term(I, 1, s2, sys.h_ops_q4()[kk]);
+      add_term(I, 2, -s2, sys.h_ops_q2()[kk]);
+    }
   }
+  J.has2 = std::any_of(ikind.begin(), ikind.end(), [](int k) { return k != 0; }) ? 1 : 0;
   // Q pairs (blocks of D) and R pairs (blocks of rho when rho != (D + D^H)/2)
   std::vector<int> qa, qb, qoff, doff, ra, rb, roff, rhooff;
   std::vector<double2> Dblk, Rhoblk;
@@ -1824,7 +1878,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
           const double *Pa = pas.data() + 6 * kk;
           const double fro = std::sqrt(Pa[0] * Pa[0] + Pa[3] * Pa[3] + Pa[5] * Pa[5] +
                                        2 * (Pa[1] * Pa[1] + Pa[2] * Pa[2] + Pa[4] * Pa[4]));
-          v += std::fabs(isc[kk]) * fro * std::fabs(Tk[size_t(kk) * L.S2 + bp + r * b + q]);
+          // |r_ij| <= ||PAS'||_F: first order |a| <= fro, second order |a| <= 2 fro^2
+          const double amax = ikind[kk] == 0 ? fro : 2.0 * fro * fro;
+          v += std::fabs(isc[kk]) * amax * std::fabs(Tk[size_t(kk) * L.S2 + bp + r * b + q]);
         }
         rs += v;
       }
@@ -1938,6 +1994,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.huge_pairs[t].rp = J.big_rp.p + J.huge_rp_off[t], J.huge_pairs[t].ci = J.big_ci.p,
     J.huge_pairs[t].cv = J.big_cv.p;
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
+  J.ikind.upload(ikind, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
   // per-crystallite inputs, all batches, transposed to [item][c] per batch at run time
@@ -2057,6 +2114,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.scale = J.is_static ? 1.0 : double(1. / double(J.n / (J.rosym ? 2 : 1)));
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
   s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
+  s.ikind = J.ikind.p, s.has2 = J.has2;
   s.npq = J.npq, s.npr = J.npr;
   s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
   s.ra = J.ra.p, s.rb = J.rb.p, s.roff = J.roff.p, s.rhooff = J.rhooff.p;

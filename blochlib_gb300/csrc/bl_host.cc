@@ -73,6 +73,22 @@ CMatrix mul(const CMatrix &x, const CMatrix &y) {
 }
 }  // namespace
 
+double isotope_rel_freq(const std::string &iso) {
+  // Larmor frequencies in MHz at 400.13 MHz for 1H, as tabulated by the reference
+  // (src/bloch/Isotope.cc:154-263); only quadrupolar nuclei need them here
+  static const std::map<std::string, double> t = {
+      {"2H", 61.424},   {"6Li", 58.883},  {"7Li", 155.503}, {"9Be", 56.226},   {"10B", 42.99},   {"11B", 128.33},
+      {"14N", 28.913},  {"17O", 54.242},  {"21Ne", 31.586}, {"23Na", 105.842}, {"25Mg", 24.496}, {"27Al", 104.262},
+      {"33S", 30.714},  {"35Cl", 39.205}, {"37Cl", 32.635}, {"39K", 18.67},    {"43Ca", 26.925}, {"45Sc", 97.2},
+      {"47Ti", 22.563}, {"49Ti", 22.557}, {"51V", 105.246}, {"53Cr", 22.615},  {"55Mn", 99.012}, {"59Co", 94.939},
+      {"61Ni", 35.756}, {"63Cu", 106.146}, {"65Cu", 113.705}, {"67Zn", 25.036}, {"69Ga", 96.035}, {"71Ga", 122.028},
+      {"79Br", 100.249}, {"81Br", 108.063}, {"87Rb", 130.927}, {"93Nb", 97.936}, {"95Mo", 26.076},
+      {"115In", 87.68}, {"127I", 80.062}, {"131Xe", 32.811}, {"133Cs", 52.481}};
+  auto it = t.find(iso);
+  if (it == t.end()) throw Error(2, "no relative frequency for isotope '" + iso + "'");
+  return it->second / 400.13;
+}
+
 double isotope_spin(const std::string &iso) {
   // nuclear spin quantum numbers of common NMR isotopes (physical constants)
   static const std::map<std::string, double> t = {
@@ -194,6 +210,7 @@ SpinSystem::SpinSystem(const std::vector<std::string> &lines) {
       it.kind = 'Q';
       it.del = num(1), it.eta = num(2), it.s1 = std::atoi(t[3].c_str());
       it.alpha = num(4), it.beta = num(5), it.gamma = num(6);
+      it.order = t.size() >= 8 ? int(num(7)) : 0;  // qua.cc:557-560
       check_spin(it.s1);
       crystal_tensor(it, (it.eta - 1.0) / 2.0, -(it.eta + 1.0) / 2.0, 1.0);
       qua.push_back(it);
@@ -338,6 +355,8 @@ void SpinSystem::build() {
   size_t NN = size_t(N_) * N_;
   hc_.assign(NN, 0.0);
   hops_.clear();
+  hq4_.assign(ints_.size(), {});
+  hq2_.assign(ints_.size(), {});
   const double inv_r3 = 1.0 / std::pow(3., 0.5), r3 = std::pow(3., 0.5);
   for (auto &it : ints_) {
     std::vector<double> T(NN, 0.0);
@@ -375,9 +394,15 @@ void SpinSystem::build() {
       if (spin < 1.0) throw Error(2, "a quadrupole needs a spin >= 1");
       it.op_scale = it.del / (4.0 * spin * (2.0 * spin - 1.0));
       const std::vector<double> Iz = iz_diag(it.s1);
+      const size_t ki = size_t(&it - ints_.data());
+      hq4_[ki].assign(NN, 0.0), hq2_[ki].assign(NN, 0.0);
+      const double q = spin;
       for (int k = 0; k < N_; ++k) {
         double z = Iz[k];
         T[size_t(k) * N_ + k] = 3.0 * (z * z);
+        // T_QuadTotal: Iz 2 (-8 Iz^2 - 1 + 4 I(I+1)) (rank 2), Iz 2 (-2 Iz^2 - 1 + 2 I(I+1)) (rank 4)
+        hq2_[ki][size_t(k) * N_ + k] = (z * 2.0) * ((-8.0 * (z * z) - 1.0) + 4.0 * q * (q + 1));
+        hq4_[ki][size_t(k) * N_ + k] = (z * 2.0) * ((-2.0 * (z * z) - 1.0) + 2.0 * q * (q + 1));
       }
     }
     hops_.push_back(T);

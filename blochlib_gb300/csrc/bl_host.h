@@ -47,6 +47,7 @@ struct Interaction {
   double iso = 0, del = 0, eta = 0;
   double alpha = 0, beta = 0, gamma = 0;  // PAS Euler angles, degrees
   int s1 = 0, s2 = 0, strong = 0;
+  int order = 0;  // quadrupole: 1 first order, 2 second order only, else both (with a field)
   double pas[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // crystal-frame tensor
   double op_scale = 0;  // H term = op_scale * (R pas R^T)_22 * T
 };
@@ -86,6 +87,14 @@ class SpinSystem {
   // orientation-dependent interaction (index matches interactions(); zero for J).
   const std::vector<double> &h_const() const { return hc_; }  // N*N real, row-major
   const std::vector<std::vector<double>> &h_ops() const { return hops_; }
+  // second-order quadrupolar spin operators of each quadrupole (empty for other kinds):
+  // T_QuadTotal(rank 4) and (rank 2) of spin_ten.cc:364-375, both diagonal
+  const std::vector<std::vector<double>> &h_ops_q4() const { return hq4_; }
+  const std::vector<std::vector<double>> &h_ops_q2() const { return hq2_; }
+  // SolidSys::setBfield (sys.cc:206-210): with a field, quadrupoles add their second-order
+  // term Qp^2 / (B nu_rel) (c4 ((r00-r11)^2/4 + r01^2) - c2 (r02^2 + r12^2)) (qua.cc:219-267)
+  double bfield() const { return bfield_; }
+  void set_bfield(double b) { bfield_ = b; }
   const BlockLayout &layout() const { return layout_; }
 
   // Reference-order dense H at rotor phase 'alpha_rot' for powder rotation Rp (for tests).
@@ -98,11 +107,14 @@ class SpinSystem {
   std::vector<int> dims_;
   std::vector<Interaction> ints_;
   std::vector<double> hc_;
-  std::vector<std::vector<double>> hops_;
+  std::vector<std::vector<double>> hops_, hq4_, hq2_;
+  double bfield_ = 0;
   BlockLayout layout_;
 };
 
 double isotope_spin(const std::string &iso);
+// Larmor frequency relative to 1H (src/bloch/Isotope.cc:378), quadrupolar isotopes
+double isotope_rel_freq(const std::string &iso);
 
 // Cartesian rotations of the reference (src/QMspins/space_ten.cc:578-652)
 void rotation3(double a, double b, double g, double R[3][3]);

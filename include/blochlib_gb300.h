@@ -77,6 +77,12 @@ bl_status bl_system_create(const char *spin_text, bl_system **out);
 void bl_system_destroy(bl_system *sys);
 int bl_system_dim(const bl_system *sys);
 int bl_system_spins(const bl_system *sys);
+/* SolidSys::setBfield (src/QMspins/sys.cc:206-210): with |B| > 1e-12 each quadrupole adds its
+ * second-order term Qp^2/(B nu_rel) (c4 ((r00-r11)^2/4 + r01^2) - c2 (r02^2 + r12^2)), or
+ * replaces its first-order term when its Q line's 8th column (order) is 2; order 1 keeps
+ * first order only (src/QMspins/qua.cc:219-267).  Default 0.  Jobs created before the call
+ * keep the field they were created with. */
+bl_status bl_system_set_bfield(bl_system *sys, double bfield);
 /* Operator expression, e.g. "Fx", "Ip 0", "0.5*Fx + Iz 1"; out = 2*N*N doubles. */
 bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out);
 /* Block structure of the Hamiltonian: writes up to cap block sizes, returns the count

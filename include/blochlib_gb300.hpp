@@ -85,6 +85,8 @@ class SolidSys {
   ~SolidSys() { bl_system_destroy(h_); }
   int HS() const { return bl_system_dim(h_); }
   int spins() const { return bl_system_spins(h_); }
+  // sys.cc:206-210: second-order quadrupolar terms (qua.cc:219-267) with a field
+  void setBfield(double Bf) { check(bl_system_set_bfield(h_, Bf)); }
   matrix op(const std::string &expr) const {
     matrix m(HS());
     check(bl_system_operator(h_, expr.c_str(), reinterpret_cast<double *>(m.a.data())));

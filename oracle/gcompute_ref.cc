@@ -238,6 +238,21 @@ void unitary_eig(const CMat &U, std::vector<cplx> &lam, CMat &V) {
 
 // ---------------------------------------------------------------- spin system
 
+// Larmor frequency relative to 1H (src/bloch/Isotope.cc:154-263, 378), quadrupolar nuclei
+double isotope_rel_freq(const std::string &iso) {
+  static const std::map<std::string, double> t = {
+      {"2H", 61.424},   {"6Li", 58.883},  {"7Li", 155.503}, {"9Be", 56.226},   {"10B", 42.99},   {"11B", 128.33},
+      {"14N", 28.913},  {"17O", 54.242},  {"21Ne", 31.586}, {"23Na", 105.842}, {"25Mg", 24.496}, {"27Al", 104.262},
+      {"33S", 30.714},  {"35Cl", 39.205}, {"37Cl", 32.635}, {"39K", 18.67},    {"43Ca", 26.925}, {"45Sc", 97.2},
+      {"47Ti", 22.563}, {"49Ti", 22.557}, {"51V", 105.246}, {"53Cr", 22.615},  {"55Mn", 99.012}, {"59Co", 94.939},
+      {"61Ni", 35.756}, {"63Cu", 106.146}, {"65Cu", 113.705}, {"67Zn", 25.036}, {"69Ga", 96.035}, {"71Ga", 122.028},
+      {"79Br", 100.249}, {"81Br", 108.063}, {"87Rb", 130.927}, {"93Nb", 97.936}, {"95Mo", 26.076},
+      {"115In", 87.68}, {"127I", 80.062}, {"131Xe", 32.811}, {"133Cs", 52.481}};
+  auto it = t.find(iso);
+  if (it == t.end()) throw std::runtime_error("no relative frequency for isotope " + iso);
+  return it->second / 400.13;
+}
+
 double isotope_spin(const std::string &iso) {
   // nuclear spin quantum numbers of common NMR isotopes (physical data)
   static const std::map<std::string, double> t = {
@@ -262,6 +277,7 @@ struct Interaction {
   char kind;  // 'C' CSA, 'D' dipole, 'J' scalar, 'Q' quadrupole
   double iso = 0, del = 0, eta = 0, a = 0, b = 0, g = 0;
   int s1 = 0, s2 = 0, strong = 0;
+  int order = 0;  // quadrupole order column (qua.cc:557-560)
   double PAS[3][3];
 };
 
@@ -272,6 +288,7 @@ struct System {
   int N = 1;
   std::vector<CMat> Ix, Iy, Iz, Ip, Im;
   std::vector<Interaction> ints;
+  double bfield = 0;  // SolidSys::setBfield (sys.cc:206-210)
 };
 
 std::vector<std::string> tokens(const std::string &s) {
@@ -422,6 +439,7 @@ System parse_system(const std::vector<std::string> &lines) {
       it.kind = 'Q';
       it.del = num(1), it.eta = num(2), it.s1 = std::atoi(t[3].c_str());
       it.a = num(4), it.b = num(5), it.g = num(6);
+      it.order = t.size() >= 8 ? int(num(7)) : 0;
       set_pas(it, (it.eta - 1.0) / 2.0, -(it.eta + 1.0) / 2.0, 1.0);
       qua.push_back(it);
     }
@@ -471,10 +489,34 @@ CMat hamiltonian(const System &S, const double Rp[3][3], double alpha, double ro
       T = scale(T, inv_r3);
       H = add(H, T, it.iso * std::sqrt(3.));
     } else if (it.kind == 'Q') {
+      // Qua::get_H (qua.cc:219-267): first order Qp a 3Iz^2; with a field (|B| > 1e-12) and
+      // order != 1 the second-order term Qp^2/(B nu_rel) (c4 ((r00-r11)^2/4 + r01^2) -
+      // c2 (r02^2 + r12^2)), r = M PAS M^T, c2/c4 = T_QuadTotal (spin_ten.cc:364-375); order 2
+      // keeps the second-order term alone
       double spin = isotope_spin(S.iso[it.s1]);
       double Qp = it.del / (4.0 * spin * (2.0 * spin - 1.0));
-      CMat T = scale(mul(S.Iz[it.s1], S.Iz[it.s1]), 3.0);
-      H = add(H, T, Qp * a);
+      const bool first_only = it.order == 1 || std::fabs(S.bfield) <= 1e-12;
+      const bool second_only = !first_only && it.order == 2;
+      if (!second_only) {
+        CMat T = scale(mul(S.Iz[it.s1], S.Iz[it.s1]), 3.0);
+        H = add(H, T, Qp * a);
+      }
+      if (!first_only) {
+        double T[3][3], Mt[3][3], Rm[3][3];
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) Mt[i][j] = M[j][i];
+        mat3mul(M, it.PAS, T);
+        mat3mul(T, Mt, Rm);
+        const double s2 = Qp * Qp / (S.bfield * isotope_rel_freq(S.iso[it.s1]));
+        const double A4 = (Rm[0][0] - Rm[1][1]) * (Rm[0][0] - Rm[1][1]) / 4.0 + Rm[0][1] * Rm[0][1];
+        const double A2 = Rm[0][2] * Rm[0][2] + Rm[1][2] * Rm[1][2];
+        for (int k = 0; k < S.N; ++k) {
+          const double z = S.Iz[it.s1](k, k).real();
+          const double c2 = (z * 2.0) * ((-8.0 * (z * z) - 1.0) + 4.0 * spin * (spin + 1));
+          const double c4 = (z * 2.0) * ((-2.0 * (z * z) - 1.0) + 2.0 * spin * (spin + 1));
+          H(k, k) += s2 * (c4 * A4 - c2 * A2);
+        }
+      }
     }
   }
   return H;
@@ -650,6 +692,7 @@ struct Job {
   std::string powder;
   Params P;
   std::string rho, det;
+  double bfield = 0;
 };
 
 Job parse_job(const std::string &text) {
@@ -671,6 +714,7 @@ Job parse_job(const std::string &text) {
     else if (key == "start") J.P.startT = std::atof(val.c_str());
     else if (key == "rho") J.rho = val;
     else if (key == "det") J.det = val;
+    else if (key == "bfield") J.bfield = std::atof(val.c_str());
   }
   return J;
 }
@@ -738,6 +782,7 @@ std::vector<cplx> single_static_fid(const System &S, const Params &P, double the
 
 int run(const Job &J, const double *pw, int C, double *out, double *sw_out) {
   System S = parse_system(J.spin);
+  S.bfield = J.bfield;
   CMat ro = op_expr(S, J.rho), det = op_expr(S, J.det);
   std::vector<cplx> acc(J.P.npts, cplx(0, 0));
   double sw = J.P.sw;

@@ -17,6 +17,8 @@
 //   powder_zcw: <theta_steps> <phi_steps>      (instead of 'powder:'; powder.cc:248-280)
 //   dump_powder: <path>   (writes the powder as C rows of theta phi gamma weight doubles)
 //   npts: <int>   sw: <Hz>   wr: <Hz>   rotb: <degrees>   start: <s>
+//   bfield: <value passed to SolidSys::setBfield>  (sys.cc:206-210; 0 when absent: a system
+//           read from text leaves its field unset, so the harness always sets it)
 //   rho: <operator expression>   det: <operator expression>
 // An operator expression is a '+'-separated sum of terms "[coef*]NAME [spin]" with NAME
 // one of Fx Fy Fz Fp Fm Fe Ix Iy Iz Ip Im (single-spin names take a spin index).
@@ -100,7 +102,7 @@ int main(int argc, char **argv) {
   Vector<std::string> spin_lines;
   std::string powder_file, rho_s, det_s, dump_file;
   int npts = 0, zcw_t = 0, zcw_p = 0;
-  double sw = 0, wr = 0, rotb = 0, start = 0;
+  double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0;
   std::string line;
   while (std::getline(in, line)) {
     std::string l = trim(line);
@@ -117,10 +119,12 @@ int main(int argc, char **argv) {
     else if (key == "sw") sw = std::atof(val.c_str());
     else if (key == "wr") wr = std::atof(val.c_str());
     else if (key == "rotb") rotb = std::atof(val.c_str());
+    else if (key == "bfield") bfield = std::atof(val.c_str());
     else if (key == "rho") rho_s = val;
     else if (key == "det") det_s = val;
   }
   SolidSys sys(spin_lines);
+  sys.setBfield(bfield);
   powder pw;
   if (zcw_t > 0) pw = powder(powder::zcw, zcw_t, zcw_p);
   else pw.read(powder_file);

@@ -117,12 +117,41 @@ def huge_cases():
         yield name, W.job_text(cfg), powder_rows(c0["powder"], spread(1154, 1) + 300)
 
 
+def quad2_cases():
+    """Second-order quadrupolar terms (SolidSys::setBfield): 2H with two 1H (both orders),
+    27Al with 1H (Q line order 2: second order only), and a static case.  The fields are small
+    so that the second-order term is large against the FP64 parity bar."""
+    c0 = W.config(0)
+    base = ["T 2H 0", "T 1H 1", "T 1H 2", "C 300 2500 0.4 1 10 40 70", "D -9000 1 2 20 50 0",
+            "D 3000 0 1 60 80 0", "D 2000 0 2 100 30 0"]
+    mas = dict(npts=256, wr=20000.0, sw=40 * 20000.0, rotb=W.MAGIC_ANGLE, rho="Fx", det="Fp")
+    cfg = dict(mas, lines=["numspin 3"] + base + ["Q 160000 0.3 0 30 60 90"])
+    yield "quad2_2h1h", W.job_text(cfg) + "bfield: 200000\n", powder_rows(c0["powder"], spread(1154, 5))
+    al = ["numspin 2", "T 27Al 0", "T 1H 1", "C 800 1500 0.2 1 0 30 0", "D 4000 0 1 20 70 0",
+          "Q 2500000 0.5 0 15 45 75 2"]
+    cfg = dict(mas, lines=al, rho="Ix 0", det="Ip 0", wr=25000.0, sw=32 * 25000.0)
+    yield "quad2_only_27al", W.job_text(cfg) + "bfield: 5000000\n", powder_rows(c0["powder"], spread(1154, 4))
+    cfg = dict(mas, lines=["numspin 3"] + base + ["Q 160000 0.3 0 30 60 90"], wr=0.0, sw=400000.0, npts=200)
+    yield "static_quad2", W.job_text(cfg) + "bfield: 200000\n", powder_rows(c0["powder"], spread(1154, 4))
+    # 2H with n protons: n = 4 (dim 48, largest Fz block 14: per-crystallite CTA path) and
+    # n = 7 (dim 384, largest block 91: batched-product path; kept out of the dense oracle)
+    for n, name, nstep, ncry in [(4, "quad2_big_2h4h", 24, 3), (7, "huge_quad2_2h7h", 10, 1)]:
+        rng = np.random.default_rng(W.SEED0 + 40 + n)
+        xyz = W._proton_cluster(rng, n + 1, 5.0, min_sep=1.5)
+        dips = [l for l in W._dipole_lines(xyz)]
+        lines = [f"numspin {n + 1}", "T 2H 0"] + [f"T 1H {k}" for k in range(1, n + 1)] + \
+            W._csa_lines(rng, n + 1)[1:] + dips + ["Q 140000 0.6 0 20 70 10"]
+        cfg = dict(lines=lines, rho="Fx", det="Fp", npts=96, wr=25000.0, sw=nstep * 25000.0, rotb=W.MAGIC_ANGLE)
+        yield name, W.job_text(cfg) + "bfield: 250000\n", powder_rows(c0["powder"], (spread(1154, ncry) + 200) % 1154)
+
+
 def main():
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
-    if "--big" in sys.argv or "--huge" in sys.argv:
+    if "--big" in sys.argv or "--huge" in sys.argv or "--quad2" in sys.argv:
         man = json.loads((OUT / "manifest.json").read_text())
-        for name, job, rows in (huge_cases() if "--huge" in sys.argv else big_cases()):
+        extra = huge_cases() if "--huge" in sys.argv else (quad2_cases() if "--quad2" in sys.argv else big_cases())
+        for name, job, rows in extra:
             sw64, f64 = run_ref(BIN64, job, rows)
             np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,
                                 sw=np.array(sw64))

@@ -54,6 +54,8 @@ def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_me
     import blochlib_gb300 as bl
     lines, kv = parse_job(job_text)
     sys_ = bl.SolidSys(lines)
+    if "bfield" in kv:
+        sys_.setBfield(float(kv["bfield"]))
     rows = np.asarray(rows, dtype=np.float64)
     pw = bl.powder.from_arrays(theta=rows[:, 1], phi=rows[:, 0], gamma=rows[:, 2], weight=rows[:, 3])
     drv = bl.oneFID(sys_, int(kv["npts"]), float(kv["sw"]), float(kv["wr"]), float(kv["rotb"]),

@@ -233,3 +233,52 @@ def test_twisted_fave_matches_oracle(seed, nsteps):
     fid = gpu_fid(job, rows, fave_method="fft")
     assert rel(fid, ref) <= TOL, rel(fid, ref)
     assert rel(fid, gpu_fid(job, rows, fave_method="direct")) <= TOL
+
+
+def quad2_system(seed):
+    """A quadrupolar nucleus (spin 1 to 5/2) with one or two spin-1/2 partners, its Q line of
+    order 0 (both terms), 1 (first order) or 2 (second order only) and a field chosen so the
+    second-order coefficient Qp^2 / (B nu_rel) lands between 1 and 30 kHz."""
+    rng = np.random.default_rng(1000 + seed)
+    q = ["2H", "14N", "7Li", "23Na", "27Al", "17O"][seed % 6]
+    rel_freq = {"2H": 61.424, "14N": 28.913, "7Li": 155.503, "23Na": 105.842, "27Al": 104.262,
+                "17O": 54.242}[q] / 400.13
+    others = [str(rng.choice(["1H", "13C"])) for _ in range(int(rng.integers(1, 3)))]
+    iso = [q] + others
+    n = len(iso)
+    lines = [f"numspin {n}"] + [f"T {iso[k]} {k}" for k in range(n)]
+    for k in range(n):
+        a = rng.uniform(0, 360, 3)
+        lines.append(f"C {rng.uniform(-2e3, 2e3):.9g} {rng.uniform(-6e3, 6e3):.9g} {rng.uniform(0, 1):.9g} {k} "
+                     f"{a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    for i in range(n):
+        for j in range(i + 1, n):
+            a = rng.uniform(0, 360, 3)
+            lines.append(f"D {rng.uniform(-1e4, 1e4):.9g} {i} {j} {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    qp = float(rng.uniform(5e4, 4e5))
+    order = seed % 3
+    a = rng.uniform(0, 360, 3)
+    lines.append(f"Q {qp:.9g} {rng.uniform(0, 1):.9g} 0 {a[0]:.9g} {a[1]:.9g} {a[2]:.9g} {order}")
+    bfield = qp * qp / (rel_freq * float(rng.uniform(1e3, 3e4)))
+    rho, det = [("Fx", "Fp"), ("Ix 0", "Ip 0"), ("Fx+Fz", "Fp")][seed % 3]
+    wr = float(rng.uniform(8e3, 30e3)) if seed % 4 else 0.0
+    n_steps = int(rng.integers(12, 50))
+    job = "\n".join(f"spin: {l}" for l in lines) + (
+        f"\nnpts: {int(rng.integers(50, 200))}\nsw: {(n_steps * wr if wr else 3e5)!r}\nwr: {wr!r}\n"
+        f"rotb: {rng.uniform(30, 70)!r}\nrho: {rho}\ndet: {det}\nbfield: {bfield!r}\n")
+    c = int(rng.integers(1, 24))
+    rows = np.stack([rng.uniform(0, 2 * np.pi, c), np.arccos(rng.uniform(-1, 1, c)), rng.uniform(0, 2 * np.pi, c),
+                     rng.uniform(0.1, 1, c)], axis=1)
+    return job, rows
+
+
+@pytest.mark.parametrize("method", ["eigh", "taylor"])
+@pytest.mark.parametrize("seed", range(12))
+def test_second_order_quadrupole_matches_oracle(seed, method):
+    """SolidSys::setBfield: second-order quadrupolar terms for every Q order, quadrupolar
+    spins 1 to 5/2, spinning and static, against the oracle."""
+    job, rows = quad2_system(seed)
+    ref, sw = oracle_fid(job, rows)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
+    assert sw_g == sw
+    assert rel(fid, ref) <= TOL, rel(fid, ref)

@@ -13,8 +13,10 @@ def test_oracle_matches_reference_fp64(case):
     job, rows, fid64, fid32, sw = load_golden(case)
     fid, sw_o = oracle_fid(job, rows)
     assert sw_o == sw
-    # the oracle restates the reference with its QL iteration in double
-    assert rel(fid, fid64) <= 1e-12, rel(fid, fid64)
+    # the oracle restates the reference with its QL iteration in double; it sums H terms in
+    # another order, so roundoff through the per-step eigendecompositions differs: ~1e-13 at
+    # dim <= 12, up to ~3e-12 at dim 48 (quad2_big_2h4h)
+    assert rel(fid, fid64) <= 1e-11, rel(fid, fid64)
 
 
 @pytest.mark.parametrize("case", [c for c in golden_cases() if np.any(load_golden(c)[3])])
