@@ -15,12 +15,13 @@ All compute runs in the CUDA library; there is no CPU fallback.  Loading fails l
 when the library is missing or cannot initialise a GPU.
 """
 import ctypes
+import math
 import os
 from pathlib import Path
 
 import numpy as np
 
-__all__ = ["SolidSys", "powder", "oneFID", "plotterFID", "Context", "Job", "BlochError", "library_path", "load"]
+__all__ = ["SolidSys", "powder", "oneFID", "PropReduce", "plotterFID", "Context", "Job", "BlochError", "library_path", "load"]
 
 _HERE = Path(__file__).resolve().parent
 _LIB = None
@@ -56,6 +57,8 @@ _SIGS = {
     "bl_powder_destroy": (None, [ctypes.c_void_p]),
     "bl_powder_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
+    "bl_p2p_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
+    "bl_p2p_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
     "bl_job_run": (ctypes.c_int, [ctypes.c_void_p]),
     "bl_job_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "bl_job_sync": (ctypes.c_int, [ctypes.c_void_p]),
@@ -125,6 +128,29 @@ class FidParams(ctypes.Structure):
     _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
                 ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
                 ("step_method", ctypes.c_int), ("fave_method", ctypes.c_int)]
+
+
+class P2PParams(ctypes.Structure):
+    _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
+                ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
+                ("step_method", ctypes.c_int), ("base", ctypes.c_int), ("factor", ctypes.c_int),
+                ("maxtstep", ctypes.c_double)]
+
+
+class PropReduce:
+    """PropReduce(base, factor) (examples/qmsims/MMMQMAS/propreduce.cc:16-60): a rotor period
+    cut into `base` chunks, one dwell spanning `factor` of them, both divided by their gcd.
+    sequences()[k] lists the chunks (in time order) that dwell k mod base covers."""
+
+    def __init__(self, base, factor):
+        if int(base) <= 0 or int(factor) <= 0:
+            raise ValueError("base and factor must be positive")
+        g = math.gcd(int(base), int(factor))
+        self.base, self.factor = int(base) // g, int(factor) // g
+
+    def sequences(self):
+        b, f = self.base, self.factor
+        return [[(k * f + m) % b for m in range(f)] for k in range(b)]
 
 
 def load():
@@ -324,6 +350,23 @@ class Job:
         self._h = h
         self.npts = int(npts)
 
+    @classmethod
+    def p2p(cls, sys, pw, ro, det, npts, wr, rotb, base, factor, maxtstep=0.0, sw=0.0, start_t=0.0, precision=0,
+            ctx=None, step_method=None):
+        """Resident point-to-point job (bl_p2p_job_create); see oneFID.p2pFID."""
+        self = cls.__new__(cls)
+        self.ctx = ctx or default_context()
+        n = sys.dim()
+        self._ro, self._det = _cmat(ro, n), _cmat(det, n)
+        self.params = P2PParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
+                                _step_method(step_method), int(base), int(factor), float(maxtstep))
+        h = ctypes.c_void_p()
+        _check(load().bl_p2p_job_create(self.ctx._h, sys._h, pw._h, _ptr(self._ro), _ptr(self._det),
+                                        ctypes.byref(self.params), ctypes.byref(h)))
+        self._h = h
+        self.npts = int(npts)
+        return self
+
     def run(self):
         _check(load().bl_job_run(self._h))
 
@@ -418,6 +461,26 @@ class oneFID:
                            _step_method(self.step_method), _fave_method(self.fave_method))
         _check(load().bl_powder_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
                                     _ptr(out), _ptr(sw_out)))
+        self.sw = float(sw_out[0])
+        self.fid_ = out
+        return out
+
+    def p2pFID(self, pw, ro, det, base=1, factor=1, maxtstep=0.0):
+        """Point-to-point powder FID (bl_p2p_fid): points every factor/base rotor periods
+        (PropReduce(base, factor)), fid[p] = sum_c w_c Tr(rho_c(t_p) det) / Tr(det det^H);
+        steps of at most maxtstep inside each chunk.  Static (wr == 0 or rotor angle 0): one
+        step of 1/sw per point.  Updates self.sw to base*wr/factor."""
+        if isinstance(base, PropReduce):
+            base, factor = base.base, base.factor
+        ctx = self.ctx or default_context()
+        n = self.sys.dim()
+        ro, det = _cmat(ro, n), _cmat(det, n)
+        out = np.zeros(self.npts, dtype=np.complex128)
+        sw_out = np.zeros(1)
+        params = P2PParams(self.npts, self.sw, self.wr, self.rotb, self.startT, int(self.precision),
+                           _step_method(self.step_method), int(base), int(factor), float(maxtstep))
+        _check(load().bl_p2p_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
+                                 _ptr(out), _ptr(sw_out)))
         self.sw = float(sw_out[0])
         self.fid_ = out
         return out

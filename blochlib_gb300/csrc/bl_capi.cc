@@ -62,6 +62,16 @@ bl::FidParams to_params(const bl_fid_params *p) {
   f.fave_method = p->fave_method;
   return f;
 }
+
+bl::FidParams to_params(const bl_p2p_params *p) {
+  bl::FidParams f;
+  f.npts = p->npts, f.sw = p->sw, f.wr = p->wr, f.rotb_deg = p->rotb_deg, f.start_t = p->start_t;
+  f.precision = p->precision;
+  f.step_method = p->step_method;
+  if (p->base <= 0 || p->factor <= 0) throw bl::Error(BL_ERR_INVALID, "point-to-point base and factor must be positive");
+  f.p2p_base = p->base, f.p2p_factor = p->factor, f.maxtstep = p->maxtstep;
+  return f;
+}
 }  // namespace
 
 extern "C" {
@@ -177,6 +187,33 @@ bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
     j->j.reset(new bl::Job(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
     *out = j.release();
   });
+}
+
+bl_status bl_p2p_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                            const double *det, const bl_p2p_params *params, bl_job **out) {
+  if (!ctx || !sys || !pw || !ro || !det || !params || !out) return fail(BL_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] {
+    int N = sys->s().dim();
+    std::unique_ptr<bl_job> j(new bl_job);
+    j->j.reset(new bl::Job(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
+    *out = j.release();
+  });
+}
+
+bl_status bl_p2p_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
+                     const bl_p2p_params *params, double *fid_out, double *sw_out) {
+  if (!fid_out) return fail(BL_ERR_INVALID, "null output");
+  bl_job *job = nullptr;
+  bl_status st = bl_p2p_job_create(ctx, sys, pw, ro, det, params, &job);
+  if (st != BL_OK) return st;
+  st = bl_job_run(job);
+  if (st == BL_OK) st = bl_job_read(job, fid_out);
+  if (st == BL_OK && sw_out) *sw_out = job->j->sw_out();
+  std::string keep = g_err;
+  bl_job_destroy(job);
+  g_err = keep;
+  return st;
 }
 
 bl_status bl_job_run(bl_job *job) {

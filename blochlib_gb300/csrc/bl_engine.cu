@@ -22,6 +22,7 @@
 //   k_eigframe   (c, block, step)   W_i = A_{i+1} V_F  (in place)
 //   k_qr         (c, step, pair)    Q_i = W^H D W (and R_i = W^H rho W when needed)
 //   k_fave       (c, element, p)    G_p = sum_i q_{(i+p)%n} r_i (with the period twist)
+//   k_p2p_elems  (c, element)       point-to-point FID terms from Q/R and the Floquet phases
 //   k_fid        (c, j, p)          fid[jn+p] = sum_e z_e^j G_p(e); weighted warp sum
 //   k_reduce     (k)                compensated sum of warp partials (fixed order)
 #include <cuda_runtime.h>
@@ -42,6 +43,7 @@ namespace {
 
 constexpr int kMaxBlock = 8;      // largest Hamiltonian block handled by this engine
 constexpr int kMaxSweeps = 40;    // bound on Jacobi sweeps; exceeding it sets a status bit
+constexpr int kMaxP2PSteps = 16384;  // steps per rotor period of a point-to-point FID
 constexpr int kThreads = 128;
 constexpr double kPi = 3.14159265358979323846;
 constexpr double kPi2 = 2.0 * kPi;
@@ -113,6 +115,8 @@ struct DevSys {
   int M, logM, fave_method;  // FFT length for the Fave correlation; 0 direct, 1 FFT
   int fave_twist;            // 1: M == n, circular correlation of the twisted sequences
   int is_static;             // static powder FID (oneFID.h:292-336): dt = 1/sw, n = p-period
+  int gper;                  // period of the FID split fid[j*gper + p] (n, or the p2p base)
+  int p2p, pb, pf, psub;     // point-to-point FID: base, factor, steps per chunk
   double dt;
   const int *srp, *seo;      // per D pair (a,b): the rho pair (b,a) and first element, or -1
   const double2 *tw;         // exp(-2 pi i k / M), k < M/2
@@ -1430,7 +1434,7 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
   int c = int(tid % s.Cpad);
   long rest = tid / s.Cpad;
-  int npt = (s.n + kFidPT - 1) / kFidPT, njt = (s.J + kFidJT - 1) / kFidJT;
+  int npt = (s.gper + kFidPT - 1) / kFidPT, njt = (s.J + kFidJT - 1) / kFidJT;
   if (rest >= long(npt) * njt) return;  // warp-uniform: whole warp leaves together
   int pt = int(rest % npt), jt = int(rest / npt);
   int p0 = pt * kFidPT, j0 = jt * kFidJT;
@@ -1459,7 +1463,7 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
           zj[a] = (j0 + a < s.J) ? Zb[at((j0 + a) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
         for (int b = 0; b < kFidPT; ++b)
-          gp[b] = (p0 + b < s.n) ? Gb[at((p0 + b) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
+          gp[b] = (p0 + b < s.gper) ? Gb[at((p0 + b) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
         for (int a = 0; a < kFidJT; ++a)
 #pragma unroll
@@ -1487,9 +1491,60 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
         v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
         v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
       }
-      int k = (j0 + a) * s.n + p0 + b;
-      if (lane == 0 && p0 + b < s.n && k < s.npts) s.partial[size_t(wglob) * s.npts + k] = v;
+      int k = (j0 + a) * s.gper + p0 + b;
+      if (lane == 0 && p0 + b < s.gper && k < s.npts) s.partial[size_t(wglob) * s.npts + k] = v;
     }
+}
+
+// Point-to-point FID terms, one thread per (crystallite, element (r,s)).
+// With W_i = A_{i+1} V (A_n = Omega = V diag(lam) V^H), Q_i = W_i^H D W_i and R_{n-1} =
+// W_{n-1}^H rho W_{n-1} = diag(lam)^H (V^H rho V) diag(lam), the density matrix after
+// m_tot chunks, G = A_{j'} Omega^{q'} with m_tot = q' b + j' (1 <= j' <= b), gives
+//   Tr(D G rho G^H) = sum_rs Q_i(r,s) R_{n-1}(s,r) e^{i m (th_s - th_r)},
+//   i = j' sub - 1, m = q' + 1   (m_tot = 0: i = n - 1, m = 0).
+// Point p = j b + k has m_tot = p f: its i depends on k only and m grows by f per j, so
+// G[k] = Q_{i_k}(r,s) R(s,r) e^{i m_k d} and Z[j] = e^{i j f d} (d = th_s - th_r) feed
+// k_fid's fid[j b + k] = sum_e Z[j] G[k].  The chunk products are never formed: the
+// reference's PropReduce (examples/qmsims/MMMQMAS/propreduce.cc:455-521) builds every
+// dwell propagator from shared sub-products; here the Floquet powers replace them.
+template <class C>
+__global__ void __launch_bounds__(kThreads) k_p2p_elems(DevSys s) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= s.ne) return;
+  const int e = int(rest);
+  if (c >= s.C) return;
+  const C *Q = Bufs<C>::Q(s), *R = Bufs<C>::R(s);
+  const int qlast = (s.n - 1) * s.nq;
+  double2 rsr;  // R_{n-1}(s,r)
+  if (s.rosym) {  // rho = (D + D^H)/2: R = (Q(s,r) + conj(Q(r,s)))/2
+    double2 v = cconj(todbl(Q[at(qlast + s.eq[e], c, s.Cpad)]));
+    if (s.erev[e] >= 0) v = cadd(v, todbl(Q[at(qlast + s.erev[e], c, s.Cpad)]));
+    rsr = cscale(v, 0.5);
+  } else {
+    rsr = todbl(R[at((s.n - 1) * s.nr + s.er[e], c, s.Cpad)]);
+  }
+  const double d = s.L[at(s.esg[e], c, s.Cpad)].y - s.L[at(s.erg[e], c, s.Cpad)].y;
+  for (int k = 0; k < s.pb; ++k) {
+    const long mt = long(k) * s.pf;
+    int i = s.n - 1;
+    long m = 0;
+    if (mt > 0) {
+      const long jp = (mt - 1) % s.pb + 1, qp = (mt - jp) / s.pb;
+      i = int(jp) * s.psub - 1;
+      m = qp + 1;
+    }
+    double sn, cs;
+    sincos(double(m) * d, &sn, &cs);
+    const double2 g = cmul(cmul(todbl(Q[at(i * s.nq + s.eq[e], c, s.Cpad)]), rsr), cmk(cs, sn));
+    Bufs<C>::G(s)[at(k * s.ne + e, c, s.Cpad)] = cvt<C>(g);
+  }
+  for (int j = 0; j < s.J; ++j) {
+    double sn, cs;
+    sincos(double(j) * double(s.pf) * d, &sn, &cs);
+    Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = mkc<C>(cs, sn);
+  }
 }
 
 // Compensated (Kahan) sum of the warp partials in fixed order: deterministic.
@@ -1597,6 +1652,7 @@ struct JobImpl {
   DevBuf<double> pas, iscale, Tk, Hc, Rp_all, t0_all, w_all;
   DevBuf<int> ikind;
   int has2 = 0;  // second-order quadrupolar terms present
+  int p2p = 0, pb = 1, pf = 1, psub = 1;  // point-to-point FID: base, factor, steps per chunk
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
@@ -1656,7 +1712,39 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   // oneFID::FID dispatch (oneFID.h:206): no spinning or rotor angle 0 -> static powder FID
   J.is_static = (p.wr == 0.0 || p.rotb_deg == 0.0) ? 1 : 0;
   double tmin = p.start_t;
-  if (J.is_static) {
+  J.p2p = p.p2p_base > 0 ? 1 : 0;
+  if (J.p2p) {
+    if (p.p2p_factor <= 0) throw Error(1, "the point-to-point factor must be positive");
+    // PropReduce::setParams (examples/qmsims/MMMQMAS/propreduce.cc:16-33): base and factor
+    // divided by their greatest common divisor
+    int u = p.p2p_base, v = p.p2p_factor;
+    while (v) {
+      const int t = u % v;
+      u = v, v = t;
+    }
+    J.pb = p.p2p_base / u, J.pf = p.p2p_factor / u;
+    J.gammaloop = 1;
+    if (J.is_static) {  // time-independent H: one step of 1/sw per point
+      if (!(p.sw > 0)) throw Error(1, "sw must be positive");
+      J.pb = J.pf = J.psub = J.n = 1;
+      J.tau = 1.0 / p.sw;
+      J.sw_out = p.sw;
+    } else {
+      // chunk of 1/(wr base); steps of at most maxtstep in it, as Propogation::propogator
+      // splits a pulse (examples/solid-2.0/src/propogation.cc:246-253)
+      const double chunk = 1.0 / (p.wr * J.pb);
+      double sub = p.maxtstep > 0 ? std::ceil(chunk / p.maxtstep) : 1.0;
+      if (!(sub >= 1.0)) sub = 1.0;
+      if (double(J.pb) * sub > double(kMaxP2PSteps))
+        throw Error(5, "point-to-point FID needs more than " + std::to_string(kMaxP2PSteps) +
+                           " steps per rotor period (base x ceil(chunk/maxtstep))");
+      J.psub = int(sub);
+      J.n = J.pb * J.psub;
+      J.tau = chunk / J.psub;
+      J.sw_out = p.wr * J.pb / J.pf;
+    }
+    J.is_static = 0;  // spinning machinery: steps, Dyson, Floquet, Q/R, then the p2p terms
+  } else if (J.is_static) {
     // oneFID::singleStaticFID (oneFID.h:292-336): dt = 1/sw as given; the FID index k is
     // split as k = j*ns + p for the reconstruction kernel
     if (!(p.sw > 0)) throw Error(1, "sw must be positive");
@@ -1786,7 +1874,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       }
   }
   J.ne = int(eq.size());
-  J.J = (p.npts + J.n - 1) / J.n;
+  J.J = (p.npts + (J.p2p ? J.pb : J.n) - 1) / (J.p2p ? J.pb : J.n);
   // crystallites, expanded by the gamma loop (compute.h:294-306: fid summed over q)
   J.C = pw.size();
   J.Ceff = J.C * J.gammaloop;
@@ -1797,7 +1885,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     for (int q = 0; q < J.gammaloop; ++q) {
       for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) J.h_Rp.push_back(R[a][b]);
-      J.h_t0.push_back(tmin + kPi2 * double(q) / double(J.gammaloop * J.n) / p.wr);
+      J.h_t0.push_back(q == 0 ? tmin : tmin + kPi2 * double(q) / double(J.gammaloop * J.n) / p.wr);
       J.h_w.push_back(pw.weight[c]);
     }
   }
@@ -2069,6 +2157,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
                  : 8.0 * J.n * J.n;
     }
     J.stage_fl[5] = J.is_static ? Ce * (16.0 * pairs + 8.0 * J.n * J.ne) : Ce * per;
+    if (J.p2p) J.stage_fl[5] = Ce * 16.0 * J.pb * J.ne;  // two complex products per (k, element)
   }
   J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
   J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total;                // compensated powder sum
@@ -2081,37 +2170,50 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   // FFT length: n itself when it is a power of two (twisted circular correlation; FP64 form
   // only, its twist factors are FP64 work), else the power of two >= 2n (zero-padded linear
   // correlation, the single-precision transforms of the mixed form)
-  s.fave_twist = (!J.mixed && J.n >= 8 && (J.n & (J.n - 1)) == 0) ? 1 : 0;
-  s.logM = 1;
-  while ((1 << s.logM) < (s.fave_twist ? J.n : 2 * J.n)) ++s.logM;
-  s.M = 1 << s.logM;
-  // FFT correlation up to M = 4096 (its shared-memory tile is M * max(1, 2048/M) * 32 B)
-  if (p.fave_method == 2 && s.M > 4096) throw Error(5, "FFT Fave supports at most 2048 steps per period");
-  s.fave_method = (p.fave_method != 1 && s.M <= 4096) ? 1 : 0;
-  if (J.mixed && !s.fave_method) throw Error(5, "the mixed form needs the FFT correlation (at most 2048 steps)");
-  {
-    std::vector<double2> tw(s.M / 2);
-    for (int k = 0; k < s.M / 2; ++k) {
-      double a = kPi2 * double(k) / double(s.M);
-      tw[k] = make_double2(std::cos(a), -std::sin(a));
+  if (!J.p2p) {
+    s.fave_twist = (!J.mixed && J.n >= 8 && (J.n & (J.n - 1)) == 0) ? 1 : 0;
+    s.logM = 1;
+    while ((1 << s.logM) < (s.fave_twist ? J.n : 2 * J.n)) ++s.logM;
+    s.M = 1 << s.logM;
+    // FFT correlation up to M = 4096 (its shared-memory tile is M * max(1, 2048/M) * 32 B)
+    if (p.fave_method == 2 && s.M > 4096) throw Error(5, "FFT Fave supports at most 2048 steps per period");
+    s.fave_method = (p.fave_method != 1 && s.M <= 4096) ? 1 : 0;
+    if (J.mixed && !s.fave_method) throw Error(5, "the mixed form needs the FFT correlation (at most 2048 steps)");
+    {
+      std::vector<double2> tw(s.M / 2);
+      for (int k = 0; k < s.M / 2; ++k) {
+        double a = kPi2 * double(k) / double(s.M);
+        tw[k] = make_double2(std::cos(a), -std::sin(a));
+      }
+      std::vector<float2> twf(tw.size());
+      for (size_t k = 0; k < tw.size(); ++k) twf[k] = make_float2(float(tw[k].x), float(tw[k].y));
+      g_upload_counter = &J.h2d;
+      J.tw.upload(tw, st);
+      J.twf.upload(twf, st);
+      g_upload_counter = nullptr;
+      s.tw = J.tw.p;
+      s.twf = J.twf.p;
+      const int cgm = std::max(1, std::min(8, 2048 / s.M));
+      size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * cgm + fave_twist_bytes(s, cgm);
+      for (auto f : {k_fave_fft<8, double2>, k_fave_fft<4, double2>, k_fave_fft<2, double2>, k_fave_fft<1, double2>,
+                     k_fave_fft<8, float2>, k_fave_fft<4, float2>, k_fave_fft<2, float2>, k_fave_fft<1, float2>})
+        CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
     }
-    std::vector<float2> twf(tw.size());
-    for (size_t k = 0; k < tw.size(); ++k) twf[k] = make_float2(float(tw[k].x), float(tw[k].y));
-    g_upload_counter = &J.h2d;
-    J.tw.upload(tw, st);
-    J.twf.upload(twf, st);
-    g_upload_counter = nullptr;
-    s.tw = J.tw.p;
-    s.twf = J.twf.p;
-    const int cgm = std::max(1, std::min(8, 2048 / s.M));
-    size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * cgm + fave_twist_bytes(s, cgm);
-    for (auto f : {k_fave_fft<8, double2>, k_fave_fft<4, double2>, k_fave_fft<2, double2>, k_fave_fft<1, double2>,
-                   k_fave_fft<8, float2>, k_fave_fft<4, float2>, k_fave_fft<2, float2>, k_fave_fft<1, float2>})
-      CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
+  } else {  // no Fave: the point-to-point terms come from Q/R and the Floquet phases
+    s.fave_twist = 0, s.logM = 0, s.M = 0, s.fave_method = 0;
+    s.tw = nullptr, s.twf = nullptr;
   }
   s.tau = J.tau, s.wr = p.wr, s.sin_rotb = J.sin_rotb, s.cos_rotb = J.cos_rotb;
   s.is_static = J.is_static, s.dt = J.dt, s.srp = J.srp.p, s.seo = J.seo.p;
   s.scale = J.is_static ? 1.0 : double(1. / double(J.n / (J.rosym ? 2 : 1)));
+  s.gper = J.n, s.p2p = J.p2p, s.pb = J.pb, s.pf = J.pf, s.psub = J.psub;
+  if (J.p2p) {  // fid = sum_c w_c Tr(rho_c det) / Tr(det det^H)  (sequencerun_funcs.cc:624-645)
+    double dd = 0;
+    for (const auto &v : det.a) dd += std::norm(v);
+    if (!(dd > 0)) throw Error(1, "the detection operator is zero");
+    s.scale = 1.0 / dd;
+    s.gper = J.pb;
+  }
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
   s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
   s.ikind = J.ikind.p, s.has2 = J.has2;
@@ -2459,6 +2561,10 @@ void Job::run() {
     if (J.is_static && J.ne > 0) {
       k_static_elems<<<grid_for(Cp * J.npq), kThreads, 0, st>>>(s);
       ++J.launches;
+    } else if (J.p2p && J.ne > 0) {
+      if (s.mixed) k_p2p_elems<float2><<<grid_for(Cp * J.ne), kThreads, 0, st>>>(s);
+      else k_p2p_elems<double2><<<grid_for(Cp * J.ne), kThreads, 0, st>>>(s);
+      ++J.launches;
     } else if (J.ne > 0) {
       if (s.fave_method == 1) {
         int cg = std::max(1, std::min(8, 2048 / s.M));
@@ -2492,7 +2598,7 @@ void Job::run() {
     mark_end(J, 5, J.ne > 0 ? 1 : 0);
     // k_fid writes every (warp, k) of this batch, so partials need no clearing; it exits
     // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
-    int npt = (J.n + kFidPT - 1) / kFidPT, njt = (J.J + kFidJT - 1) / kFidJT;
+    int npt = (s.gper + kFidPT - 1) / kFidPT, njt = (J.J + kFidJT - 1) / kFidJT;
     mark_begin(J, 6);
     if (s.mixed) k_fid<float2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
     else k_fid<double2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);

@@ -18,6 +18,12 @@ struct FidParams {
                       // single-precision eigenframe, Q/R, Fave and FID terms)
   int step_method = 0;  // step exponential: 0 Jacobi eigen-decomposition, 1 Taylor + squaring
   int fave_method = 0;  // Fave correlation: 0 auto (FFT when n <= 2048), 1 direct, 2 FFT
+  // Point-to-point FID (p2p_base > 0): points every p2p_factor/p2p_base rotor periods,
+  // fid[p] = sum_c w_c Tr(rho_c(t_p) det) / Tr(det det^H); each rotor period is cut into
+  // p2p_base chunks of ceil(chunk / maxtstep) steps (one step when maxtstep <= 0).  Static
+  // (wr == 0 or rotor angle 0): one step of 1/sw per point.
+  int p2p_base = 0, p2p_factor = 0;
+  double maxtstep = 0;
 };
 
 struct Context {

@@ -20,6 +20,14 @@
  *   bl_job_*              the same call split into upload / run / read, for callers that
  *                         keep inputs resident on the GPU between calls (no reference twin;
  *                         oneFID::FID recomputes from host data every call)
+ *   bl_p2p_fid            point-to-point FID at dwell = factor/base rotor periods: the dwell
+ *                         propagators of PropReduce(base, factor)::generateProps
+ *                         (examples/qmsims/MMMQMAS/propreduce.cc:16-60, 455-521; chunk products
+ *                         as in mmmqmas.cc:290-341), rho stepped point by point and
+ *                         Tr(rho det)/Tr(det det^H) collected per point as the solid-2.0
+ *                         point-to-point collector does (examples/solid-2.0/src/
+ *                         sequencerun_funcs.cc:624-645; steps of at most maxtstep per chunk,
+ *                         propogation.cc:246-296)
  *   bl_plotter_fid        plotterFID(fid, file, dt)                  src/utils/plotter.cc:49-135
  *   bl_mat5_*             Matlab5 / matstream put(name, data)        src/utils/matlab5.h:603-792
  *   bl_rotation3/2        rotationMatrix3D(a,b,g) / (phi,theta)      src/QMspins/space_ten.cc:578-652
@@ -51,10 +59,11 @@ typedef struct bl_job bl_job;
 typedef struct {
   int npts;        /* FID points */
   double sw;       /* sweep width, Hz (rounded to n*wr, n = floor(sw/wr+0.5)) */
-  double wr;       /* rotor speed, Hz (0 = static; not implemented) */
+  double wr;       /* rotor speed, Hz (0 = static powder FID, as is rotor angle 0) */
   double rotb_deg; /* rotor angle, degrees */
   double start_t;  /* start time, s */
-  int precision;   /* 0 = FP64 */
+  int precision;   /* 0 = FP64; 1 = mixed (FP64 propagators, single-precision eigenframe, Q/R,
+                      Fave and FID terms; <= 1e-6 relative to FP64) */
   int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
                       1 = Taylor series with scaling and squaring; both FP64 */
   int fave_method; /* correlation over the rotor period: 0 = automatic (FFT for n <= 2048),
@@ -102,6 +111,31 @@ void bl_powder_destroy(bl_powder *pw);
 /* Powder FID: fid_out = 2*npts doubles; *sw_out = the sweep width actually used. */
 bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
                         const double *det, const bl_fid_params *params, double *fid_out, double *sw_out);
+
+/* Point-to-point powder FID.  A rotor period is cut into 'base' chunks (each of
+ * ceil(chunk/maxtstep) steps exp(-i 2pi tau H(t)), one when maxtstep <= 0); point p sits at
+ * start_t + p*factor/(base*wr) and
+ *   fid[p] = sum_c w_c Tr(U_c(t_p) rho U_c(t_p)^H det) / Tr(det det^H).
+ * base and factor are divided by their gcd.  Static (wr == 0 or rotor angle 0): one step of
+ * 1/sw per point.  *sw_out = base*wr/factor (sw when static). */
+typedef struct {
+  int npts;        /* FID points */
+  double sw;       /* static only: sweep width, Hz (dwell 1/sw) */
+  double wr;       /* rotor speed, Hz */
+  double rotb_deg; /* rotor angle, degrees */
+  double start_t;  /* time of point 0, s */
+  int precision;   /* 0 = FP64, 1 = mixed (as bl_fid_params) */
+  int step_method; /* 0 = eigen-decomposition, 1 = Taylor (as bl_fid_params) */
+  int base;        /* chunks per rotor period (PropReduce 'base') */
+  int factor;      /* chunks per dwell (PropReduce 'factor') */
+  double maxtstep; /* longest step inside a chunk, s (<= 0: one step per chunk) */
+} bl_p2p_params;
+
+bl_status bl_p2p_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                     const double *det, const bl_p2p_params *params, double *fid_out, double *sw_out);
+/* The same as a resident job (run with bl_job_run / bl_job_read, free with bl_job_destroy). */
+bl_status bl_p2p_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
+                            const double *det, const bl_p2p_params *params, bl_job **out);
 
 /* Resident job: inputs uploaded once, each run recomputes the FID on the device. */
 bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,

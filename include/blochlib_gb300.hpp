@@ -151,6 +151,25 @@ class powder {
   bl_powder *h_ = nullptr;
 };
 
+// PropReduce(base, factor) (examples/qmsims/MMMQMAS/propreduce.cc:16-60): a rotor period in
+// 'base' chunks, a dwell of 'factor' chunks, both divided by their gcd.  The dwell propagators
+// it would assemble are never formed here: oneFID::p2pFID takes the pair.
+class PropReduce {
+ public:
+  int base = 1, factor = 1;
+  PropReduce() {}
+  PropReduce(int bas, int fac) { setParams(bas, fac); }
+  void setParams(int bas, int fac) {
+    if (bas <= 0 || fac <= 0) throw std::invalid_argument("PropReduce: base and factor must be positive");
+    int u = bas, v = fac;
+    while (v) {
+      int t = u % v;
+      u = v, v = t;
+    }
+    base = bas / u, factor = fac / u;
+  }
+};
+
 template <class Func_T = SolidSys>
 class oneFID {
  public:
@@ -163,6 +182,19 @@ class oneFID {
     check(bl_powder_fid(Context::get(), sys_->handle(), pw.handle(), ro.data(), det.data(), &p,
                         reinterpret_cast<double *>(fid.data()), &sw_used));
     sw_ = sw_used;  // as the reference, sw becomes n * wr (oneFID.h:429)
+    fid_ = fid;
+    return fid;
+  }
+  // Point-to-point FID every red.factor/red.base rotor periods, steps of at most maxtstep
+  // (bl_p2p_fid); sw becomes base*wr/factor.
+  std::vector<complex> p2pFID(powder &pw, const matrix &ro, const matrix &det, const PropReduce &red,
+                              double maxtstep = 0) {
+    bl_p2p_params p = {npts_, sw_, wr_, rotb_, startT_, 0, /*Taylor step*/ 1, red.base, red.factor, maxtstep};
+    std::vector<complex> fid(static_cast<size_t>(npts_));
+    double sw_used = sw_;
+    check(bl_p2p_fid(Context::get(), sys_->handle(), pw.handle(), ro.data(), det.data(), &p,
+                     reinterpret_cast<double *>(fid.data()), &sw_used));
+    sw_ = sw_used;
     fid_ = fid;
     return fid;
   }

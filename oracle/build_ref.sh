@@ -8,8 +8,11 @@
 #   ref_fid64  the same sources with that iteration in double (the FP64 oracle)
 #
 # Source: $BLOCHLIB_REF/src (default /root/reference/src) is copied to oracle/_ref/src
-# and build-fixed by patch_ref.py.  Where the reference tree is absent but a scratch
-# copy already sits in oracle/_ref/src, that copy is built as is.
+# and build-fixed by patch_ref.py; the propagator-reduction class of the MMMQMAS example
+# (examples/qmsims/MMMQMAS/propreduce.{h,cc}) is copied unchanged to oracle/_ref/mmmqmas,
+# beside a one-line blochlib.h that includes only QMspins/sys.h (the umbrella header pulls
+# in unrelated, unpatched parts of the tree).  Where the reference tree is absent but a
+# scratch copy already sits in oracle/_ref, that copy is built as is.
 #   usage: build_ref.sh [f32|f64|all]   (default all)
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
@@ -24,6 +27,14 @@ if [ -d "$ref/src" ]; then
     python3 "$here/patch_ref.py" "$here/_ref/src"
     touch "$here/_ref/src/.patched"
   fi
+  mkdir -p "$here/_ref/mmmqmas"
+  for f in propreduce.h propreduce.cc; do
+    if [ ! -f "$here/_ref/mmmqmas/$f" ] || [ "$ref/examples/qmsims/MMMQMAS/$f" -nt "$here/_ref/mmmqmas/$f" ]; then
+      cp "$ref/examples/qmsims/MMMQMAS/$f" "$here/_ref/mmmqmas/$f"
+      chmod u+w "$here/_ref/mmmqmas/$f"
+    fi
+  done
+  printf '#include "QMspins/sys.h"\n' > "$here/_ref/mmmqmas/blochlib.h"
 elif [ ! -f "$here/_ref/src/.patched" ]; then
   echo "build_ref.sh: reference sources not found (set BLOCHLIB_REF)" >&2
   exit 3

@@ -23,6 +23,9 @@
 //   powder loop                    src/QMspins/driver/oneFID.h:200-208, 339-431
 //   static powder FID              src/QMspins/driver/oneFID.h:220-336
 //   powder file reader             src/QMspins/driver/powder.cc:333-389
+//   point-to-point FID             examples/qmsims/MMMQMAS/propreduce.cc:16-60, 455-521,
+//                                  mmmqmas.cc:290-370; examples/solid-2.0/src/
+//                                  sequencerun_funcs.cc:624-645, propogation.cc:246-296
 //
 // Eigen-solvers are this file's own: cyclic complex Jacobi for Hermitian matrices, and
 // for the unitary period propagator a Cayley transform K = i(I-W)(I+W)^-1 of the
@@ -693,6 +696,8 @@ struct Job {
   Params P;
   std::string rho, det;
   double bfield = 0;
+  int p2p_base = 0, p2p_factor = 0;  // point-to-point FID when p2p_base > 0
+  double maxtstep = 0;
 };
 
 Job parse_job(const std::string &text) {
@@ -715,6 +720,8 @@ Job parse_job(const std::string &text) {
     else if (key == "rho") J.rho = val;
     else if (key == "det") J.det = val;
     else if (key == "bfield") J.bfield = std::atof(val.c_str());
+    else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &J.p2p_base, &J.p2p_factor);
+    else if (key == "maxtstep") J.maxtstep = std::atof(val.c_str());
   }
   return J;
 }
@@ -780,6 +787,69 @@ std::vector<cplx> single_static_fid(const System &S, const Params &P, double the
   return fid;
 }
 
+// Point-to-point FID of one crystallite, propagated point by point.  A rotor period is cut
+// into b chunks (b, f = base, factor over their gcd, as PropReduce::setParams,
+// examples/qmsims/MMMQMAS/propreduce.cc:16-33), each the product of ceil(chunk/maxtstep)
+// steps exp(-i 2 pi tau H(t)) (propogation.cc:246-296 splitting, compute.h:257-274 step);
+// dwell k is the product of chunks (k f + m) mod b, m < f, later chunks on the left (what
+// PropReduce::generateProps assembles, propreduce.cc:455-521); rho_{p+1} = W rho_p W^H and
+// fid[p] = Tr(rho_p det) / Tr(det det^H) (sequencerun_funcs.cc:624-645).  Static (wr == 0 or
+// rotor angle 0): W = exp(-i 2 pi H / sw).
+std::vector<cplx> single_p2p_fid(const System &S, const Job &J, double theta, double phi, double gamma,
+                                 const CMat &ro, const CMat &det, double &sw_out) {
+  const Params &P = J.P;
+  int u = J.p2p_base, v = J.p2p_factor;
+  if (u <= 0 || v <= 0) throw std::runtime_error("p2p base and factor must be positive");
+  while (v) {
+    int t = u % v;
+    u = v, v = t;
+  }
+  int b = J.p2p_base / u, f = J.p2p_factor / u;
+  double Rp[3][3];
+  rot3(phi, theta, gamma, Rp);
+  const double rotb = P.rotb * kDeg2Rad;
+  std::vector<CMat> W;
+  if (P.wr == 0.0 || P.rotb == 0.0) {
+    CMat H = hamiltonian(S, Rp, 0.0, rotb);
+    W.push_back(step_prop(H, 1.0 / P.sw));
+    b = f = 1;
+    sw_out = P.sw;
+  } else {
+    const double chunk = 1.0 / (P.wr * b);
+    int sub = J.maxtstep > 0 ? int(std::ceil(chunk / J.maxtstep)) : 1;
+    if (sub < 1) sub = 1;
+    const double tau = chunk / sub;
+    std::vector<CMat> U(b);
+    for (int k = 0; k < b; ++k) {
+      U[k] = identity(S.N);
+      for (int j = 0; j < sub; ++j) {
+        double t1 = P.startT + double(k * sub + j) * tau;
+        double tmid = t1 + tau / 2.0;
+        U[k] = mul(step_prop(hamiltonian(S, Rp, tmid * P.wr * kPi2, rotb), tau), U[k]);
+      }
+    }
+    for (int k = 0; k < b; ++k) {
+      CMat w = identity(S.N);
+      for (int m = 0; m < f; ++m) w = mul(U[(k * f + m) % b], w);
+      W.push_back(w);
+    }
+    sw_out = P.wr * b / f;
+  }
+  double dd = 0;
+  for (const auto &x : det.a) dd += std::norm(x);
+  std::vector<cplx> fid(P.npts);
+  CMat rho = ro;
+  for (int p = 0; p < P.npts; ++p) {
+    cplx tr = 0;
+    for (int r = 0; r < S.N; ++r)
+      for (int c = 0; c < S.N; ++c) tr += rho(r, c) * det(c, r);
+    fid[p] = tr / dd;
+    const CMat &w = W[p % b];
+    rho = mul(w, mul(rho, adj(w)));
+  }
+  return fid;
+}
+
 int run(const Job &J, const double *pw, int C, double *out, double *sw_out) {
   System S = parse_system(J.spin);
   S.bfield = J.bfield;
@@ -789,8 +859,9 @@ int run(const Job &J, const double *pw, int C, double *out, double *sw_out) {
   const bool stat = J.P.wr == 0.0 || J.P.rotb == 0.0;  // oneFID::FID dispatch (oneFID.h:206)
   for (int c = 0; c < C; ++c) {
     double phi = pw[4 * c + 0], theta = pw[4 * c + 1], gamma = pw[4 * c + 2], w = pw[4 * c + 3];
-    std::vector<cplx> f = stat ? single_static_fid(S, J.P, theta, phi, gamma, ro, det)
-                               : single_fid(S, J.P, theta, phi, gamma, ro, det, sw);
+    std::vector<cplx> f = J.p2p_base > 0 ? single_p2p_fid(S, J, theta, phi, gamma, ro, det, sw)
+                          : stat          ? single_static_fid(S, J.P, theta, phi, gamma, ro, det)
+                                          : single_fid(S, J.P, theta, phi, gamma, ro, det, sw);
     for (int k = 0; k < J.P.npts; ++k) acc[k] += w * f[k];
   }
   for (int k = 0; k < J.P.npts; ++k) {

@@ -8,7 +8,8 @@ QL ?= float
 BIN ?= _ref/ref_fid
 CXX ?= g++
 OPT ?= -O2
-CXXFLAGS = -std=gnu++98 -fpermissive -w $(OPT) -include ref_prelude.h -DBL_QL_REAL=$(QL) -I$(SRC)
+RED ?= _ref/mmmqmas
+CXXFLAGS = -std=gnu++98 -fpermissive -w $(OPT) -include ref_prelude.h -DBL_QL_REAL=$(QL) -I$(SRC) -I$(RED)
 
 TUS = version.cc container/complex.cc container/range.cc \
   utils/blassert.cc utils/params.cc utils/endians.cc utils/matlab5.cc utils/utils.cc \
@@ -24,12 +25,16 @@ TUS = version.cc container/complex.cc container/range.cc \
   QMspins/space_ten.cc QMspins/spin_ten.cc QMspins/sys.cc QMspins/j.cc QMspins/csa.cc \
   QMspins/dip.cc QMspins/qua.cc QMspins/driver/powder.cc QMspins/driver/ham_gen.cc
 
-OBJS = $(patsubst %.cc,$(OBJ)/%.o,$(TUS)) $(OBJ)/ref_harness.o
+OBJS = $(patsubst %.cc,$(OBJ)/%.o,$(TUS)) $(OBJ)/propreduce.o $(OBJ)/ref_harness.o
 
 $(BIN): $(OBJS)
 	$(CXX) -o $@ $(OBJS) -lm
 
-$(OBJ)/ref_harness.o: ref_harness.cc
+$(OBJ)/ref_harness.o: ref_harness.cc $(RED)/propreduce.h
+	@mkdir -p $(dir $@)
+	$(CXX) $(CXXFLAGS) -c $< -o $@
+
+$(OBJ)/propreduce.o: $(RED)/propreduce.cc $(RED)/propreduce.h
 	@mkdir -p $(dir $@)
 	$(CXX) $(CXXFLAGS) -c $< -o $@
 

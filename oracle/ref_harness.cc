@@ -20,6 +20,9 @@
 //   bfield: <value passed to SolidSys::setBfield>  (sys.cc:206-210; 0 when absent: a system
 //           read from text leaves its field unset, so the harness always sets it)
 //   rho: <operator expression>   det: <operator expression>
+//   p2p: <base> <factor>   maxtstep: <s>   (point-to-point FID instead of oneFID::FID: see
+//           p2p_fid below; a rotor period in 'base' chunks of ceil(chunk/maxtstep) steps,
+//           a point every 'factor' chunks)
 // An operator expression is a '+'-separated sum of terms "[coef*]NAME [spin]" with NAME
 // one of Fx Fy Fz Fp Fm Fe Ix Iy Iz Ip Im (single-spin names take a spin index).
 //
@@ -27,6 +30,7 @@
 #include "mpi/mpi_controller.h"
 #include "QMspins/sys.h"
 #include "QMspins/driver/oneFID.h"
+#include "propreduce.h"  // examples/qmsims/MMMQMAS (scratch copy, built by oracle/ref.mk)
 
 #include <cstdio>
 #include <fstream>
@@ -92,6 +96,79 @@ static matrix op_expr(SolidSys &sys, const std::string &expr) {
   return acc;
 }
 
+// Point-to-point powder FID assembled from the reference's own pieces: chunk propagators as
+// products of Mexp(SolidSys::Hamiltonian(t1,t2,wr), -i tau 2pi) with later steps on the left
+// (compute.h:257-274 convention; chunk loop of mmmqmas.cc:315-330), the forward and back
+// products that PropReduce documents (propreduce.h:88-97), the dwell propagators from
+// PropReduce::reduce + generateProps (propreduce.cc:455-521) where reduce terminates (base <
+// factor; otherwise the direct products of the same chunks), rho stepped as A rho A^H
+// and trace(rho, det)/trace(det, adjoint(det)) summed per point with the powder weight
+// (sequencerun_funcs.cc:624-645).  Static (wr == 0 or rotor angle 0): one Mexp of 1/sw.
+static Vector<complex> p2p_fid(SolidSys &sys, powder &pw, matrix &ro, matrix &det, int npts, double sw, double wr,
+                               double rotb, double start, int base, int factor, double maxtstep, double &sw_out) {
+  PropReduce red(base, factor);  // divides base and factor by their gcd (propreduce.cc:16-33)
+  const int b = red.base, f = red.factor;
+  // PropReduce::reduce terminates only for base < factor: setParams sizes BackRed to base-1
+  // but fills min(base, factor)-1 entries, and an empty entry matches every sequence in
+  // iteration(), so backReduce's while loop never ends when base > factor.  There (and for
+  // base == 1) the dwell products are formed directly, in the same order.
+  const bool use_red = b > 1 && b < f;
+  if (use_red) red.reduce();
+  const bool stat = wr == 0.0 || rotb == 0.0;
+  Vector<complex> fid(npts, complex(0, 0));
+  complex nrm = trace(det, adjoint(det));
+  powder::iterator it(pw);
+  while (it) {
+    sys.setRotorAngles(0.0, rotb * DEG2RAD);
+    sys.setPowderAngles(it.theta(), it.phi(), it.gamma());
+    Vector<matrix> W;
+    int nb = b;
+    if (stat) {
+      double dt = 1.0 / sw;
+      nb = 1;
+      W.resize(1);
+      W[0] = Mexp(sys.Hamiltonian(0.0, dt, 0.0), -complexi * dt * PI2);
+      sw_out = sw;
+    } else {
+      const double chunk = 1.0 / (wr * b);
+      int sub = maxtstep > 0 ? int(std::ceil(chunk / maxtstep)) : 1;
+      if (sub < 1) sub = 1;
+      const double tau = chunk / sub;
+      Vector<matrix> U(b);
+      for (int k = 0; k < b; ++k) {
+        U[k] = sys.Fe();
+        for (int j = 0; j < sub; ++j) {
+          double t1 = start + double(k * sub + j) * tau;
+          U[k] = Mexp(sys.Hamiltonian(t1, t1 + tau, wr), -complexi * tau * PI2) * U[k];
+        }
+      }
+      W.resize(b);
+      if (!use_red) {
+        for (int k = 0; k < b; ++k) {
+          W[k] = U[(k * f) % b];
+          for (int m = 1; m < f; ++m) W[k] = U[(k * f + m) % b] * W[k];
+        }
+      } else {
+        Vector<matrix> Fow(b - 1), Back(red.maxBackReduce());
+        Fow[0] = U[1] * U[0];  // "0*1", "0*1*2", ...
+        for (int i = 2; i < b; ++i) Fow[i - 1] = U[i] * Fow[i - 2];
+        if (Back.size() > 0) Back[0] = U[b - 1] * U[b - 2];  // "b-2 b-1", "b-3 b-2 b-1", ...
+        for (int i = 1; i < Back.size(); ++i) Back[i] = Back[i - 1] * U[b - 2 - i];
+        red.generateProps(U, Fow, Back, W);
+      }
+      sw_out = wr * b / f;
+    }
+    matrix r = ro;
+    for (int p = 0; p < npts; ++p) {
+      fid[p] += it.weight() * trace(r, det) / nrm;
+      r = W[p % nb] * r * adjoint(W[p % nb]);  // prop (A rho A^H); the member form does not
+                                               // compile (its own adjoint() hides the free one)
+    }
+    ++it;
+  }
+  return fid;
+}
+
 int main(int argc, char **argv) {
   if (argc < 3) {
     std::cerr << "usage: ref_harness <job file> <output file>\n";
@@ -102,7 +179,8 @@ int main(int argc, char **argv) {
   Vector<std::string> spin_lines;
   std::string powder_file, rho_s, det_s, dump_file;
   int npts = 0, zcw_t = 0, zcw_p = 0;
-  double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0;
+  double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0, maxtstep = 0;
+  int p2p_base = 0, p2p_factor = 0;
   std::string line;
   while (std::getline(in, line)) {
     std::string l = trim(line);
@@ -122,6 +200,8 @@ int main(int argc, char **argv) {
     else if (key == "bfield") bfield = std::atof(val.c_str());
     else if (key == "rho") rho_s = val;
     else if (key == "det") det_s = val;
+    else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &p2p_base, &p2p_factor);
+    else if (key == "maxtstep") maxtstep = std::atof(val.c_str());
   }
   SolidSys sys(spin_lines);
   sys.setBfield(bfield);
@@ -140,11 +220,17 @@ int main(int argc, char **argv) {
   }
   matrix ro = op_expr(sys, rho_s);
   matrix det = op_expr(sys, det_s);
-  oneFID<SolidSys> driver(sys, npts, sw, wr, rotb, start);
-  Vector<complex> fid = driver.FID(pw, ro, det);
+  Vector<complex> fid;
+  double sw_out = sw;
+  if (p2p_base > 0) {
+    fid = p2p_fid(sys, pw, ro, det, npts, sw, wr, rotb, start, p2p_base, p2p_factor, maxtstep, sw_out);
+  } else {
+    oneFID<SolidSys> driver(sys, npts, sw, wr, rotb, start);
+    fid = driver.FID(pw, ro, det);
+    sw_out = driver.sw();
+  }
   FILE *f = std::fopen(argv[2], "wb");
   if (!f) { std::cerr << "ref_harness: cannot write " << argv[2] << "\n"; return 2; }
-  double sw_out = driver.sw();
   std::fwrite(&sw_out, sizeof(double), 1, f);
   for (int i = 0; i < fid.size(); ++i) {
     double re = Re(fid[i]), im = Im(fid[i]);

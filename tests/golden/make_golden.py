@@ -39,7 +39,7 @@ def run_ref(binary, job_text, rows):
         job = Path(td) / "job.txt"
         job.write_text(job_text + f"powder: {pw}\n")
         out = Path(td) / "out.bin"
-        subprocess.run([str(binary), str(job), str(out)], check=True)
+        subprocess.run([str(binary), str(job), str(out)], check=True, timeout=1800)
         a = np.fromfile(out, dtype=np.float64)
     return float(a[0]), a[1:].view(np.complex128).copy()
 
@@ -145,12 +145,49 @@ def quad2_cases():
         yield name, W.job_text(cfg) + "bfield: 250000\n", powder_rows(c0["powder"], (spread(1154, ncry) + 200) % 1154)
 
 
+def p2p_cases():
+    """Point-to-point FIDs (ref_harness 'p2p: base factor'): dwell = factor/base rotor periods,
+    chunks of ceil(chunk/maxtstep) steps.  base < factor runs the reference's own
+    PropReduce::reduce + generateProps; the others form the same dwell products directly."""
+    c0, c1 = W.config(0), W.config(1)
+    het = ["numspin 3", "T 13C 0", "T 1H 1", "T 1H 2", "C 900 7000 0.6 0 33 44 55", "D 9000 0 1 10 20 30",
+           "D 7000 0 2 40 50 60", "D -20000 1 2 70 80 0"]
+    js = ["numspin 3", "T 1H 0", "T 1H 1", "T 1H 2", "C 120 3000 0.4 0 10 20 30", "C -80 2500 0.7 1 40 50 60",
+          "C 0 1800 0.1 2 70 80 90", "D -15000 0 1 0 30 0", "D -9000 1 2 50 60 0", "D -6000 0 2 120 100 0",
+          "J 140 0 1 1", "J 70 1 2"]
+    q2 = ["numspin 2", "T 2H 0", "T 1H 1", "C 300 2500 0.4 1 10 40 70", "D 3000 0 1 60 80 0",
+          "Q 160000 0.3 0 30 60 90"]
+    mas = dict(rotb=W.MAGIC_ANGLE, sw=0.0)
+    cases = [
+        ("p2p_het_9_7", dict(mas, lines=het, rho="Ix 0", det="Ip 0", npts=160, wr=10000.0), "9 7", 3e-6, 6, ""),
+        ("p2p_jstrong_7_9_nonsym", dict(mas, lines=js, rho="Fx+Fz", det="Fp", npts=128, wr=15000.0), "7 9", 2e-6,
+         5, ""),
+        ("p2p_quad2_5_3", dict(mas, lines=q2, rho="Fx", det="Fp", npts=128, wr=20000.0), "5 3", 2e-6, 5,
+         "bfield: 200000\n"),
+        ("p2p_c1_sync_1_1", dict(c1, npts=96), "1 1", 5e-6, 4, ""),
+        ("p2p_het_2_3_start", dict(mas, lines=het, rho="Ix 0", det="Ip 0", npts=100, wr=12000.0), "2 3", 0.0, 4,
+         "start: 1.3e-05\n"),
+        ("p2p_static", dict(lines=het, rho="Ix 0", det="Ip 0", npts=128, wr=0.0, sw=100000.0,
+                            rotb=W.MAGIC_ANGLE), "1 1", 0.0, 6, ""),
+    ]
+    for name, cfg, bf, mt, ncry, extra in cases:
+        yield name, W.job_text(cfg) + f"p2p: {bf}\nmaxtstep: {mt!r}\n" + extra, \
+            powder_rows(c0["powder"], (spread(1154, ncry) + 77) % 1154)
+    # large blocks (5 like spins, blocks up to 10): base 4, factor 1
+    rng = np.random.default_rng(W.SEED0 + 11)
+    xyz = W._proton_cluster(rng, 5, 5.0, min_sep=1.5)
+    lines = ["numspin 5"] + [f"T 1H {k}" for k in range(5)] + W._csa_lines(rng, 5) + W._dipole_lines(xyz)
+    cfg = dict(lines=lines, rho="Fx", det="Fp", npts=64, wr=25000.0, sw=0.0, rotb=W.MAGIC_ANGLE)
+    yield "p2p_big_5h_4_1", W.job_text(cfg) + "p2p: 4 1\nmaxtstep: 2e-06\n", powder_rows(c0["powder"], spread(1154, 2))
+
+
 def main():
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
-    if "--big" in sys.argv or "--huge" in sys.argv or "--quad2" in sys.argv:
+    if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p")):
         man = json.loads((OUT / "manifest.json").read_text())
-        extra = huge_cases() if "--huge" in sys.argv else (quad2_cases() if "--quad2" in sys.argv else big_cases())
+        extra = (huge_cases() if "--huge" in sys.argv else quad2_cases() if "--quad2" in sys.argv
+                 else p2p_cases() if "--p2p" in sys.argv else big_cases())
         for name, job, rows in extra:
             sw64, f64 = run_ref(BIN64, job, rows)
             np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,

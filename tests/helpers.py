@@ -61,7 +61,11 @@ def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_me
     drv = bl.oneFID(sys_, int(kv["npts"]), float(kv["sw"]), float(kv["wr"]), float(kv["rotb"]),
                     float(kv.get("start", 0.0)), precision=precision, ctx=ctx, step_method=step_method,
                     fave_method=fave_method)
-    fid = drv.FID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]))
+    if "p2p" in kv:  # point-to-point FID (bl_p2p_fid)
+        base, factor = (int(x) for x in kv["p2p"].split())
+        fid = drv.p2pFID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]), base, factor, float(kv.get("maxtstep", 0.0)))
+    else:
+        fid = drv.FID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]))
     return (fid, drv.sw) if return_sw else fid
 
 
