@@ -126,7 +126,35 @@ def workload(args):
     cfg = W.config(idx, args.system or 0)
     if args.period_steps:
         cfg = dict(cfg, sw=args.period_steps * cfg["wr"])
+    if args.p2p:  # point-to-point FID: a point every factor/base rotor periods
+        cfg = dict(cfg, p2p=(args.p2p[0], args.p2p[1], args.maxtstep))
     return cfg
+
+
+def job_text(cfg):
+    """The workload in the reference harness's job format (with its p2p line if any)."""
+    from blochlib_gb300 import workloads as W
+    t = W.job_text(cfg)
+    if "p2p" in cfg:
+        b, f, mt = cfg["p2p"]
+        t += f"p2p: {b} {f}\nmaxtstep: {mt!r}\n"
+    return t
+
+
+def describe(cfg, dim):
+    if "p2p" in cfg:
+        b, f, mt = cfg["p2p"]
+        return (f"point-to-point every {f}/{b} rotor periods, chunks of ceil(1/(wr*{b})/{mt:g} s) steps"
+                if mt > 0 else f"point-to-point every {f}/{b} rotor periods, one step per chunk")
+    return f"n={int(round(cfg['sw'] / cfg['wr']))} steps/period"
+
+
+def drive_fid(bl, cfg, drv, pw, ro, det):
+    """The reference-facing call: oneFID::FID, or p2pFID for a point-to-point workload."""
+    if "p2p" in cfg:
+        b, f, mt = cfg["p2p"]
+        return drv.p2pFID(pw, ro, det, b, f, mt)
+    return drv.FID(pw, ro, det)
 
 
 def make_job(bl, cfg, ctx, step_method=None, fave_method=None, precision=0):
@@ -134,8 +162,13 @@ def make_job(bl, cfg, ctx, step_method=None, fave_method=None, precision=0):
     phi, theta, gamma, w = cfg["powder"]
     pw = bl.powder.from_arrays(theta, phi, gamma, w)
     ro, det = s.op(cfg["rho"]), s.op(cfg["det"])
-    job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=step_method,
-                 fave_method=fave_method, precision=precision)
+    if "p2p" in cfg:
+        b, f, mt = cfg["p2p"]
+        job = bl.Job.p2p(s, pw, ro, det, cfg["npts"], cfg["wr"], cfg["rotb"], b, f, maxtstep=mt, sw=cfg["sw"],
+                         ctx=ctx, step_method=step_method, precision=precision)
+    else:
+        job = bl.Job(s, pw, ro, det, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx,
+                     step_method=step_method, fave_method=fave_method, precision=precision)
     return s, pw, ro, det, job
 
 
@@ -163,7 +196,7 @@ def _cpu_run(binary, cfg, ranges, tmp):
             for j in range(a, a + k):
                 f.write(f"{phi[j]:.17g} {theta[j]:.17g} {gamma[j]:.17g} {w[j]:.17g}\n")
         jf = Path(tmp) / f"job{i}.txt"
-        jf.write_text(W.job_text(cfg) + f"powder: {pf}\n")
+        jf.write_text(job_text(cfg) + f"powder: {pf}\n")
         procs.append(subprocess.Popen([str(binary), str(jf), str(Path(tmp) / f"out{i}.bin")],
                                       stdout=subprocess.DEVNULL, stderr=subprocess.PIPE))
     for p in procs:
@@ -210,7 +243,7 @@ def run_reference(args):
            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workloads.py)",
            "config": {"workload": f"{cfg['name']}: {cfg['lines'][0]}, dim {2 ** int(cfg['lines'][0].split()[1])}, "
-                                  f"{len(cfg['powder'][0])} crystallites, n={int(round(cfg['sw'] / cfg['wr']))}, "
+                                  f"{len(cfg['powder'][0])} crystallites, {describe(cfg, 0)}, "
                                   f"npts={cfg['npts']}"},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": kind,
                             "sample": f"per step: {last['cores']} processes, contiguous crystallite ranges, "
@@ -389,6 +422,9 @@ def main():
     ap.add_argument("--duration", type=float, default=10.0, help="c4: arrival window (s)")
     ap.add_argument("--drain", type=float, default=20.0, help="c4: wait after the window (s)")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--p2p", type=int, nargs=2, default=None, metavar=("BASE", "FACTOR"),
+                    help="point-to-point FID every FACTOR/BASE rotor periods instead of gamma-COMPUTE")
+    ap.add_argument("--maxtstep", type=float, default=0.0, help="--p2p: longest step inside a chunk (s)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--crystallites", type=int, default=0,
@@ -436,6 +472,9 @@ def main():
     fid_main = job.read()
     stages = job.stage_times()
     sflops = job.stage_flops()
+    if "p2p" in cfg:  # stage 5 runs the point-to-point terms instead of the Fave correlation
+        stages = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in stages.items()}
+        sflops = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in sflops.items()}
     dom = max(stages, key=lambda k: stages[k][0])
     dom_ms_per_run = stages[dom][0] / args.steps
     achieved = sflops[dom] / (dom_ms_per_run / 1e3) / 1e12
@@ -465,10 +504,10 @@ def main():
     # e2e through the reference-facing call with host buffers
     drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method,
                     fave_method=args.fave_method, precision=1 if prec == "mixed" else 0)
-    drv.FID(pw, ro, det)
+    drive_fid(bl, cfg, drv, pw, ro, det)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        drv.FID(pw, ro, det)
+        drive_fid(bl, cfg, drv, pw, ro, det)
     e2e_s = (time.perf_counter() - t0) / args.e2e_steps
     h2d, d2h = job.io_bytes()
     h2d += 8 * 4 * len(cfg["powder"][0]) + 2 * ro.nbytes  # the caller's powder arrays and rho/det
@@ -481,7 +520,7 @@ def main():
         "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded spin systems and ZCW powder, workloads.py)",
         "config": {"workload": f"{cfg['name']}: {cfg['lines'][0]} ({' '.join(cfg['lines'][1:2])}...), "
                                f"dim {s.dim()}, {len(cfg['powder'][0])} crystallites, "
-                               f"n={int(round(cfg['sw'] / cfg['wr']))} steps/period, npts={cfg['npts']}, "
+                               f"{describe(cfg, s.dim())}, npts={cfg['npts']}, "
                                f"{'plain FP64' if prec == 'fp64' else 'mixed precision'}",
                    "precision": prec, "step_method": args.step_method,
                    "parallelism": f"replicas x{d.world}",

@@ -1429,50 +1429,50 @@ constexpr int kFidJT = 4, kFidPT = 4;
 
 // One thread per (crystallite, tile of kFidJT j's, tile of kFidPT p's); lanes are
 // 32 consecutive crystallites, reduced with the powder weights by warp shuffles.
-template <class C>
+template <class C, int JT = kFidJT, int PT = kFidPT>
 __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
   int c = int(tid % s.Cpad);
   long rest = tid / s.Cpad;
-  int npt = (s.gper + kFidPT - 1) / kFidPT, njt = (s.J + kFidJT - 1) / kFidJT;
+  int npt = (s.gper + PT - 1) / PT, njt = (s.J + JT - 1) / JT;
   if (rest >= long(npt) * njt) return;  // warp-uniform: whole warp leaves together
   int pt = int(rest % npt), jt = int(rest / npt);
-  int p0 = pt * kFidPT, j0 = jt * kFidJT;
-  C acc[kFidJT][kFidPT];
+  int p0 = pt * PT, j0 = jt * JT;
+  C acc[JT][PT];
 #pragma unroll
-  for (int a = 0; a < kFidJT; ++a)
+  for (int a = 0; a < JT; ++a)
 #pragma unroll
-    for (int b = 0; b < kFidPT; ++b) acc[a][b] = mkc<C>(0, 0);
+    for (int b = 0; b < PT; ++b) acc[a][b] = mkc<C>(0, 0);
   const C *Zb = Bufs<C>::Z(s), *Gb = Bufs<C>::G(s);
   // Partial sums over chunks of kFidChunk elements in C, folded into FP64 accumulators:
   // in single precision this keeps the summation error at ~sqrt(chunk) eps instead of
   // ~sqrt(ne) eps (ne reaches 10^4 for 8 spins); in FP64 it changes nothing.
   constexpr int kFidChunk = 32;
-  double2 acc64[kFidJT][kFidPT];
+  double2 acc64[JT][PT];
 #pragma unroll
-  for (int a = 0; a < kFidJT; ++a)
+  for (int a = 0; a < JT; ++a)
 #pragma unroll
-    for (int b = 0; b < kFidPT; ++b) acc64[a][b] = cmk(0, 0);
+    for (int b = 0; b < PT; ++b) acc64[a][b] = cmk(0, 0);
   if (c < s.C) {
     for (int e0 = 0; e0 < s.ne; e0 += kFidChunk) {
       const int e1 = min(s.ne, e0 + kFidChunk);
       for (int e = e0; e < e1; ++e) {
-        C zj[kFidJT], gp[kFidPT];
+        C zj[JT], gp[PT];
 #pragma unroll
-        for (int a = 0; a < kFidJT; ++a)
+        for (int a = 0; a < JT; ++a)
           zj[a] = (j0 + a < s.J) ? Zb[at((j0 + a) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
-        for (int b = 0; b < kFidPT; ++b)
+        for (int b = 0; b < PT; ++b)
           gp[b] = (p0 + b < s.gper) ? Gb[at((p0 + b) * s.ne + e, c, s.Cpad)] : mkc<C>(0, 0);
 #pragma unroll
-        for (int a = 0; a < kFidJT; ++a)
+        for (int a = 0; a < JT; ++a)
 #pragma unroll
-          for (int b = 0; b < kFidPT; ++b) acc[a][b] = cfma(zj[a], gp[b], acc[a][b]);
+          for (int b = 0; b < PT; ++b) acc[a][b] = cfma(zj[a], gp[b], acc[a][b]);
       }
 #pragma unroll
-      for (int a = 0; a < kFidJT; ++a)
+      for (int a = 0; a < JT; ++a)
 #pragma unroll
-        for (int b = 0; b < kFidPT; ++b) {
+        for (int b = 0; b < PT; ++b) {
           acc64[a][b] = cadd(acc64[a][b], todbl(acc[a][b]));
           acc[a][b] = mkc<C>(0, 0);
         }
@@ -1482,9 +1482,9 @@ __global__ void __launch_bounds__(kThreads) k_fid(DevSys s) {
   int lane = threadIdx.x & 31;
   int wglob = s.warp_base + c / 32;
 #pragma unroll
-  for (int a = 0; a < kFidJT; ++a)
+  for (int a = 0; a < JT; ++a)
 #pragma unroll
-    for (int b = 0; b < kFidPT; ++b) {
+    for (int b = 0; b < PT; ++b) {
       double2 v = cscale(acc64[a][b], wc);  // powder weight and the warp sum in FP64
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -1540,10 +1540,15 @@ __global__ void __launch_bounds__(kThreads) k_p2p_elems(DevSys s) {
     const double2 g = cmul(cmul(todbl(Q[at(i * s.nq + s.eq[e], c, s.Cpad)]), rsr), cmk(cs, sn));
     Bufs<C>::G(s)[at(k * s.ne + e, c, s.Cpad)] = cvt<C>(g);
   }
+  // Z[j] = e^{i j f d}: a running product, re-anchored by an exact sincos every 64 powers
+  // (its rounding then stays near 64 eps; arguments reach ~10^4 rad)
+  double2 z1;
+  sincos(double(s.pf) * d, &z1.y, &z1.x);
+  double2 zj = cmk(1, 0);
   for (int j = 0; j < s.J; ++j) {
-    double sn, cs;
-    sincos(double(j) * double(s.pf) * d, &sn, &cs);
-    Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = mkc<C>(cs, sn);
+    if ((j & 63) == 0 && j) sincos(double(j) * double(s.pf) * d, &zj.y, &zj.x);
+    Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(zj);
+    zj = cmul(zj, z1);
   }
 }
 
@@ -2498,6 +2503,31 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
 static void mark_begin(JobImpl &J, int stage);
 static void mark_end(JobImpl &J, int stage, int nlaunch);
 
+// k_fid with a (j, p) register tile of about 16 accumulators whose p-width wastes the least of
+// the period gper (a point-to-point period of 9 takes 3-wide tiles instead of 4-wide)
+template <int JT, int PT, class C>
+static void launch_fid_tile(const DevSys &s, long Cp, int Jn, cudaStream_t st) {
+  const int npt = (s.gper + PT - 1) / PT, njt = (Jn + JT - 1) / JT;
+  k_fid<C, JT, PT><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
+}
+template <class C>
+static void launch_fid(const DevSys &s, long Cp, int Jn, cudaStream_t st) {
+  int pt = kFidPT;
+  if (s.gper % kFidPT != 0 && s.gper < 64) {
+    int waste = 1 << 30;
+    for (int w = kFidPT; w >= 1; --w) {
+      const int ws = (s.gper + w - 1) / w * w - s.gper;
+      if (ws < waste) waste = ws, pt = w;
+    }
+  }
+  switch (pt) {
+    case 1: launch_fid_tile<16, 1, C>(s, Cp, Jn, st); break;
+    case 2: launch_fid_tile<8, 2, C>(s, Cp, Jn, st); break;
+    case 3: launch_fid_tile<5, 3, C>(s, Cp, Jn, st); break;
+    default: launch_fid_tile<kFidJT, kFidPT, C>(s, Cp, Jn, st); break;
+  }
+}
+
 void Job::run() {
   JobImpl &J = *d_;
   CUDA_OK(cudaSetDevice(J.ctx->device));
@@ -2598,10 +2628,9 @@ void Job::run() {
     mark_end(J, 5, J.ne > 0 ? 1 : 0);
     // k_fid writes every (warp, k) of this batch, so partials need no clearing; it exits
     // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
-    int npt = (s.gper + kFidPT - 1) / kFidPT, njt = (J.J + kFidJT - 1) / kFidJT;
     mark_begin(J, 6);
-    if (s.mixed) k_fid<float2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
-    else k_fid<double2><<<grid_for(Cp * npt * njt), kThreads, 0, st>>>(s);
+    if (s.mixed) launch_fid<float2>(s, Cp, J.J, st);
+    else launch_fid<double2>(s, Cp, J.J, st);
     ++J.launches;
     mark_end(J, 6, 1);
   }
