@@ -21,7 +21,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["SolidSys", "powder", "oneFID", "PropReduce", "plotterFID", "Context", "Job", "BlochError", "library_path", "load"]
+__all__ = ["SolidSys", "powder", "oneFID", "PropReduce", "HamiltonianGen", "plotterFID", "Context", "Job", "BlochError", "library_path", "load"]
 
 _HERE = Path(__file__).resolve().parent
 _LIB = None
@@ -58,6 +58,8 @@ _SIGS = {
     "bl_powder_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
     "bl_p2p_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
+    "bl_hamgen": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "bl_p2p_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
     "bl_job_run": (ctypes.c_int, [ctypes.c_void_p]),
     "bl_job_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -135,6 +137,27 @@ class P2PParams(ctypes.Structure):
                 ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
                 ("step_method", ctypes.c_int), ("base", ctypes.c_int), ("factor", ctypes.c_int),
                 ("maxtstep", ctypes.c_double)]
+
+
+class HamiltonianGen:
+    """HamiltonianGen (src/QMspins/driver/ham_gen.h): operator expressions such as
+    "Ix_0 + complexi*Iy_1" or "T2m1_0,1*A21" evaluated to N x N matrices (host side, no GPU)."""
+
+    def __init__(self):
+        self.vars = {}
+
+    def addVar(self, name, value):
+        self.vars[str(name)] = complex(value)
+
+    def Hamiltonian(self, sys, expr, theta=0.0, phi=0.0, gamma=0.0):
+        n = sys.dim()
+        out = np.zeros((n, n), dtype=np.complex128)
+        names = (ctypes.c_char_p * max(1, len(self.vars)))(*[k.encode() for k in self.vars])
+        vals = np.array([[v.real, v.imag] for v in self.vars.values()], dtype=np.float64).reshape(-1)
+        _check(load().bl_hamgen(sys._h, str(expr).encode(), float(theta), float(phi), float(gamma),
+                                ctypes.cast(names, ctypes.c_void_p), _ptr(vals) if len(vals) else None,
+                                len(self.vars), _ptr(out)))
+        return out
 
 
 class PropReduce:

@@ -57,6 +57,7 @@ def build_library(verbose=False, force=False):
         (CSRC / "bl_engine.cu", [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                  "-Xptxas", "-v" if verbose else "-O3"]),
         (CSRC / "bl_host.cc", ["g++", "-O2", "-std=c++17", "-fPIC"]),
+        (CSRC / "bl_hamgen.cc", ["g++", "-O2", "-std=c++17", "-fPIC"]),
         (CSRC / "bl_capi.cc", ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{cuda / 'include'}"]),
         (CSRC / "bl_server.cc", ["g++", "-O2", "-std=c++17", "-fPIC", f"-I{cuda / 'include'}"]),
     ]

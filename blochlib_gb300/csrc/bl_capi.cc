@@ -7,6 +7,7 @@
 
 #include "../../include/blochlib_gb300.h"
 #include "bl_engine.h"
+#include "bl_hamgen.h"
 #include "bl_host.h"
 #include "bl_server.h"
 
@@ -115,6 +116,19 @@ bl_status bl_system_set_bfield(bl_system *sys, double bfield) {
     auto copy = std::make_shared<bl::SpinSystem>(*sys->sp);
     copy->set_bfield(bfield);
     sys->sp = copy;
+  });
+}
+bl_status bl_hamgen(const bl_system *sys, const char *expr, double theta, double phi, double gamma,
+                    const char *const *names, const double *values, int nvars, double *out) {
+  if (!sys || !expr || !out || nvars < 0 || (nvars > 0 && (!names || !values))) return fail(BL_ERR_INVALID, "bad arguments");
+  return guarded([&] {
+    bl::HamiltonianGen gen;
+    for (int k = 0; k < nvars; ++k) {
+      if (!names[k]) throw bl::Error(BL_ERR_INVALID, "null variable name");
+      gen.add_var(names[k], bl::cplx(values[2 * k], values[2 * k + 1]));
+    }
+    const bl::CMatrix m = gen.evaluate(sys->s(), expr, theta, phi, gamma);
+    for (size_t i = 0; i < m.a.size(); ++i) out[2 * i] = m.a[i].real(), out[2 * i + 1] = m.a[i].imag();
   });
 }
 int bl_system_dim(const bl_system *sys) { return sys ? sys->s().dim() : 0; }

@@ -28,6 +28,9 @@
  *                         point-to-point collector does (examples/solid-2.0/src/
  *                         sequencerun_funcs.cc:624-645; steps of at most maxtstep per chunk,
  *                         propogation.cc:246-296)
+ *   bl_hamgen             HamiltonianGen::Hamiltonian(sys, expr, theta, phi, gamma)
+ *                                                                    src/QMspins/driver/ham_gen.h:295-299,
+ *                                                                    ham_gen.cc:428-1212
  *   bl_plotter_fid        plotterFID(fid, file, dt)                  src/utils/plotter.cc:49-135
  *   bl_mat5_*             Matlab5 / matstream put(name, data)        src/utils/matlab5.h:603-792
  *   bl_rotation3/2        rotationMatrix3D(a,b,g) / (phi,theta)      src/QMspins/space_ten.cc:578-652
@@ -97,6 +100,14 @@ bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out
 /* Block structure of the Hamiltonian: writes up to cap block sizes, returns the count
  * through *nblocks. */
 bl_status bl_system_blocks(const bl_system *sys, int *sizes, int cap, int *nblocks);
+
+/* HamiltonianGen expression ("Ix_0 + complexi*Iy_1", "T2m1_0,1*A21", "2*Iz" ...) evaluated
+ * for the system at powder angles (theta, phi; gamma is unused, as in the reference) into
+ * out (N x N complex).  nvars extra variables: names[k] = values[2k] + i values[2k+1].
+ * Grammar, functions and operator set: those of the reference's HamiltonianGen, quirks
+ * included (M^2 is M*M*M; "2*-3" is 2*3); a syntax error or a numeric result fails. */
+bl_status bl_hamgen(const bl_system *sys, const char *expr, double theta, double phi, double gamma,
+                    const char *const *names, const double *values, int nvars, double *out);
 
 /* Powder sets. */
 bl_status bl_powder_zcw(int theta_steps, int phi_steps, int gamma_steps, bl_powder **out);

@@ -18,6 +18,7 @@
 #include <complex>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "blochlib_gb300.h"
@@ -149,6 +150,27 @@ class powder {
 
  private:
   bl_powder *h_ = nullptr;
+};
+
+// HamiltonianGen (src/QMspins/driver/ham_gen.h): "Ix_0 + complexi*Iy_1", "T2m1_0,1*A21", ...
+// evaluated for a system at powder angles (theta, phi); see bl_hamgen for the grammar.
+class HamiltonianGen {
+ public:
+  void addVar(const std::string &name, complex v) { vars_.push_back({name, v}); }
+  matrix Hamiltonian(const SolidSys &sys, const std::string &expr, double theta = 0, double phi = 0,
+                     double gamma = 0) const {
+    std::vector<const char *> names;
+    std::vector<double> vals;
+    for (const auto &v : vars_) names.push_back(v.first.c_str()), vals.push_back(v.second.real()),
+        vals.push_back(v.second.imag());
+    matrix m(sys.HS());
+    check(bl_hamgen(sys.handle(), expr.c_str(), theta, phi, gamma, names.data(), vals.data(), int(vars_.size()),
+                    reinterpret_cast<double *>(m.a.data())));
+    return m;
+  }
+
+ private:
+  std::vector<std::pair<std::string, complex>> vars_;
 };
 
 // PropReduce(base, factor) (examples/qmsims/MMMQMAS/propreduce.cc:16-60): a rotor period in

@@ -20,6 +20,9 @@
 //   bfield: <value passed to SolidSys::setBfield>  (sys.cc:206-210; 0 when absent: a system
 //           read from text leaves its field unset, so the harness always sets it)
 //   rho: <operator expression>   det: <operator expression>
+//   hamgen: <expression>   (repeatable; instead of a FID, writes the matrix the reference's
+//           HamiltonianGen (QMspins/driver/ham_gen.cc) evaluates for each expression, at the
+//           angles of 'hamgen_angles: <theta> <phi> <gamma>' (radians, default 0 0 0))
 //   p2p: <base> <factor>   maxtstep: <s>   (point-to-point FID instead of oneFID::FID: see
 //           p2p_fid below; a rotor period in 'base' chunks of ceil(chunk/maxtstep) steps,
 //           a point every 'factor' chunks)
@@ -31,6 +34,7 @@
 #include "QMspins/sys.h"
 #include "QMspins/driver/oneFID.h"
 #include "propreduce.h"  // examples/qmsims/MMMQMAS (scratch copy, built by oracle/ref.mk)
+#include "QMspins/driver/ham_gen.h"
 
 #include <cstdio>
 #include <fstream>
@@ -181,6 +185,8 @@ int main(int argc, char **argv) {
   int npts = 0, zcw_t = 0, zcw_p = 0;
   double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0, maxtstep = 0;
   int p2p_base = 0, p2p_factor = 0;
+  std::vector<std::string> hamgen;
+  double hg_theta = 0, hg_phi = 0, hg_gamma = 0;
   std::string line;
   while (std::getline(in, line)) {
     std::string l = trim(line);
@@ -202,9 +208,29 @@ int main(int argc, char **argv) {
     else if (key == "det") det_s = val;
     else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &p2p_base, &p2p_factor);
     else if (key == "maxtstep") maxtstep = std::atof(val.c_str());
+    else if (key == "hamgen") hamgen.push_back(val);
+    else if (key == "hamgen_angles") std::sscanf(val.c_str(), "%lf %lf %lf", &hg_theta, &hg_phi, &hg_gamma);
   }
   SolidSys sys(spin_lines);
   sys.setBfield(bfield);
+  if (!hamgen.empty()) {  // output: per expression, N then N*N (re, im) row-major
+    FILE *f = std::fopen(argv[2], "wb");
+    if (!f) { std::cerr << "ref_harness: cannot write " << argv[2] << "\n"; return 2; }
+    for (size_t k = 0; k < hamgen.size(); ++k) {
+      HamiltonianGen gen;
+      matrix m = gen.Hamiltonian(sys, hamgen[k], hg_theta, hg_phi, hg_gamma);
+      double nd = m.rows();
+      std::fwrite(&nd, sizeof(double), 1, f);
+      for (int r = 0; r < m.rows(); ++r)
+        for (int c = 0; c < m.cols(); ++c) {
+          double re = Re(m(r, c)), im = Im(m(r, c));
+          std::fwrite(&re, sizeof(double), 1, f);
+          std::fwrite(&im, sizeof(double), 1, f);
+        }
+    }
+    std::fclose(f);
+    return 0;
+  }
   powder pw;
   if (zcw_t > 0) pw = powder(powder::zcw, zcw_t, zcw_p);
   else pw.read(powder_file);

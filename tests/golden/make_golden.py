@@ -181,7 +181,82 @@ def p2p_cases():
     yield "p2p_big_5h_4_1", W.job_text(cfg) + "p2p: 4 1\nmaxtstep: 2e-06\n", powder_rows(c0["powder"], spread(1154, 2))
 
 
+HAMGEN_SYSTEMS = {
+    "h_c_d": ["numspin 3", "T 1H 0", "T 13C 1", "T 2H 2"],
+    "hh": ["numspin 2", "T 1H 0", "T 1H 1"],
+}
+HAMGEN_EXPRS = [
+    # spin operators: totals, single spins, every Cartesian name
+    "Ix", "Iy", "Iz", "Ip", "Im", "Ie", "Ix_0", "Iy_1", "Iz_2", "Ip_2", "Im_1", "Ie_2",
+    # arithmetic, variables, precedence
+    "Ix_0 + Iz_1", "Ix_0 - Iz_1", "2*Ix_0", "Ix_0*2", "Ix_0/2", "2/Iz_0", "Ix_0/Iz_0", "complexi*Iy_1",
+    "Ix_0 + complexi*Iy_0", "pi*Iz_1", "deg2rad*90*Ix_2", "e*Ie_0", "Pi*PI/pi*rad2deg*Iz_0", "Iz_0*Iz_1",
+    "Ip_0*Im_1 + Im_0*Ip_1", "(Ix_0+Iy_1)*(Ix_0-Iy_1)", "((Ix_0+Iz_1)*2 - Iy_2)/3", "-Ix_0", "+Ix_1",
+    "Ix_0 + 1", "1 - Iz_0", "Iz_0 - 1", "1 + 2 + Iz_0", "6/2*Iz_0", "2*3*4*Iz_0", "1.5e1*Iz_0", "2e-1*Iz_0",
+    ".5*Iz_0", "2.5E0*Iz_0",
+    # quirks of the reference's parser and evaluator
+    "Iz_1^2", "Ix_2^3", "Iz_0^0", "Iz_0^-1", "Iz_0^2.7", "-2^2*Iz_0", "2*-3*Iz_0", "2^3^2*Iz_0",
+    "Ix_0 Iz_1", "Ixy", "Ix_0 = Iz_0", "Ix_0 & Iz_0", "frac(2)*Iz_0", "round(2.5)*Iz_0", "trunc(3.3)*Iz_0",
+    # spin tensors
+    "T00_1", "T10_0", "T11_0", "T1m1_2", "T20_0,1", "T21_0,2", "T2m1_1,2", "T22_2", "T2m2_0,2", "T20_2",
+    # spatial tensors of the powder angles
+    "A20*Iz_0", "A21*T2m1_0,1 + A2m1*T21_0,1", "A10*Iz_1", "A11*Ix_0", "A1m1*Iy_0", "A22*T2m2_0,1",
+    "A2m2*T22_0,1", "A00*Ix_0",
+    # functions on matrices (element by element)
+    "exp(Iz_0)", "sqrt(Iz_0)", "abs(Iy_0)", "real(Iy_0)", "imag(Iy_0)", "ceil(Iz_0)", "floor(Iz_0)",
+    "cos(Ix_0)", "sin(Ix_0)", "tan(Iz_0)", "sinh(Iz_0)", "cosh(Iz_0)", "tanh(Iz_0)", "ln(Ix_0+2)",
+    "log(Ix_0+2)", "acos(Iz_0)", "asin(Iz_0)", "atan(Iz_0)", "-(Ix_0)", "exp(complexi*Iz_0)",
+    # functions and logic on numbers
+    "sqrt(2)*Iz_0", "exp(1)*Ix_0", "ln(2)*Iz_0", "log(100)*Iz_0", "cos(pi/3)*Ix_0", "sin(pi/6)*Iy_0",
+    "tan(1)*Iz_0", "acos(0.5)*Iz_0", "asin(0.5)*Iz_0", "atan(1)*Iz_0", "sinh(1)*Iz_0", "cosh(1)*Iz_0",
+    "tanh(0.5)*Iz_0", "abs(-3)*Iz_0", "int(2.7)*Iz_0", "ceil(2.1)*Iz_0", "floor(2.9)*Iz_0", "2^3*Iz_0",
+    "(2>1)*Iz_0", "(1>2)*Iz_0 + Ix_0", "(2<=2)*Iz_0", "(3>=4)*Iz_0 + Ix_0", "(3==3)*Iz_0",
+    "(3!=3)*Iz_0 + Ix_0", "(1&&0)*Iz_0 + Ix_0", "(1||0)*Iz_0", "(7%3)*Iz_0", "!0*Iz_0", "(-3>2)*Iz_0",
+    "real(complexi)*Iz_0 + Ix_0", "imag(complexi)*Iz_0", "sqrt(-4)*Iz_0", "ln(-1)*Iz_0", "log(complexi)*Iz_0",
+    "(2+complexi)^(1-complexi)*Iz_0", "acos(2)*Iz_0", "atan(complexi/2)*Iz_0",
+    # user variables (added with addVar)
+    "w1*Ix_0 + w2*Iy_0",
+]
+HAMGEN_VARS = {"w1": complex(2.5, 0.0), "w2": complex(0.0, -1.25)}
+HAMGEN_ANGLES = [(0.7, 1.1, 0.3), (2.0, -0.4, 0.0)]
+
+
+def hamgen_fixtures():
+    """Matrices of the reference's HamiltonianGen (ref_harness 'hamgen:'), one process per
+    expression (a reference exception then loses only that expression).  User variables are
+    substituted textually for the reference, which has no job key for them."""
+    out = {}
+    for sname, lines in HAMGEN_SYSTEMS.items():
+        for ai, ang in enumerate(HAMGEN_ANGLES):
+            for ei, ex in enumerate(HAMGEN_EXPRS):
+                if sname == "hh" and any(t in ex for t in ("_2", "T22_2", "T20_2")):
+                    continue
+                rex = ex
+                for k, v in HAMGEN_VARS.items():  # no "*-": the reference drops that sign
+                    rex = rex.replace(k, f"({v.real!r}{'+' if v.imag >= 0 else '-'}complexi*{abs(v.imag)!r})")
+                job = "".join(f"spin: {l}\n" for l in lines) + f"hamgen_angles: {ang[0]!r} {ang[1]!r} {ang[2]!r}\n"
+                job += f"hamgen: {rex}\n"
+                with tempfile.TemporaryDirectory() as td:
+                    (Path(td) / "j.txt").write_text(job)
+                    r = subprocess.run([str(BIN64), str(Path(td) / "j.txt"), str(Path(td) / "o.bin")],
+                                       capture_output=True, timeout=60)
+                    if r.returncode != 0:
+                        print("reference failed:", sname, ex, r.stderr.decode()[-200:])
+                        continue
+                    a = np.fromfile(Path(td) / "o.bin")
+                n = int(a[0])
+                out[f"{sname}|{ai}|{ei}"] = a[1:1 + 2 * n * n].view(np.complex128).reshape(n, n)
+    np.savez_compressed(OUT / "hamgen.npz", **out,
+                        _exprs=np.array(HAMGEN_EXPRS), _angles=np.array(HAMGEN_ANGLES),
+                        _systems=np.array(json.dumps(HAMGEN_SYSTEMS)), _vars=np.array(json.dumps(
+                            {k: [v.real, v.imag] for k, v in HAMGEN_VARS.items()})))
+    print("hamgen fixtures:", len(out))
+
+
 def main():
+    if "--hamgen" in sys.argv:
+        hamgen_fixtures()
+        return
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
     if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p")):
