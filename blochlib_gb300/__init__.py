@@ -71,6 +71,8 @@ _SIGS = {
     "bl_job_destroy": (None, [ctypes.c_void_p]),
     "bl_plotter_fid": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_double]),
     "bl_system_set_bfield": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "bl_system_add_rf": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double]),
     "bl_mat5_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
     "bl_mat5_put": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                    ctypes.c_int]),
@@ -273,6 +275,11 @@ class SolidSys:
         """SolidSys::setBfield: with |B| > 1e-12 quadrupoles add their second-order term
         (or use it alone when their Q line's order column is 2)."""
         _check(load().bl_system_set_bfield(self._h, float(bfield)))
+
+    def addRf(self, iso, amp, phase=0.0, offset=0.0):
+        """Continuous rf on every `iso` spin during the FID (solid-2.0 PulseData::Pulse):
+        amp (Ix cos phase + Iy sin phase) + offset Iz, Hz and degrees."""
+        _check(load().bl_system_add_rf(self._h, str(iso).encode(), float(amp), float(phase), float(offset)))
 
     def dim(self):
         return load().bl_system_dim(self._h)

@@ -131,6 +131,14 @@ bl_status bl_hamgen(const bl_system *sys, const char *expr, double theta, double
     for (size_t i = 0; i < m.a.size(); ++i) out[2 * i] = m.a[i].real(), out[2 * i + 1] = m.a[i].imag();
   });
 }
+bl_status bl_system_add_rf(bl_system *sys, const char *iso, double amp_hz, double phase_deg, double offset_hz) {
+  if (!sys || !iso) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    auto copy = std::make_shared<bl::SpinSystem>(*sys->sp);
+    copy->add_rf(bl::RfField{iso, amp_hz, phase_deg, offset_hz});
+    sys->sp = copy;
+  });
+}
 int bl_system_dim(const bl_system *sys) { return sys ? sys->s().dim() : 0; }
 int bl_system_spins(const bl_system *sys) { return sys ? sys->s().spins() : 0; }
 

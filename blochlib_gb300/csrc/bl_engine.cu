@@ -1700,7 +1700,7 @@ static bool any_nonzero(const CMatrix &M, const BlockLayout &L, int a, int b) {
   return false;
 }
 
-Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro_in, const CMatrix &det_in,
          const FidParams &p)
     : d_(new JobImpl) {
   JobImpl &J = *d_;
@@ -1713,7 +1713,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   if (p.npts <= 0) throw Error(1, "npts must be positive");
   if (pw.size() <= 0) throw Error(1, "empty powder");
   const int N = sys.dim();
-  if (ro.n != N || det.n != N) throw Error(1, "rho/detect dimension does not match the spin system");
+  if (ro_in.n != N || det_in.n != N) throw Error(1, "rho/detect dimension does not match the spin system");
   // oneFID::FID dispatch (oneFID.h:206): no spinning or rotor angle 0 -> static powder FID
   J.is_static = (p.wr == 0.0 || p.rotb_deg == 0.0) ? 1 : 0;
   double tmin = p.start_t;
@@ -1778,14 +1778,16 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   if (J.is_static && L.max_block > kMaxBlock)
     throw Error(5, "static powder FIDs support Hamiltonian blocks up to " + std::to_string(kMaxBlock));
   const int nb = int(L.size.size());
-  // rosym: exact test ro == 0.5*(det + det^H)   (compute.h:75-83)
+  // rosym: exact test ro == 0.5*(det + det^H) on the caller's matrices   (compute.h:75-83)
   J.rosym = 1;
   for (int r = 0; r < N && J.rosym; ++r)
     for (int s = 0; s < N; ++s)
-      if (ro(r, s) != 0.5 * (det(r, s) + std::conj(det(s, r)))) {
+      if (ro_in(r, s) != 0.5 * (det_in(r, s) + std::conj(det_in(s, r)))) {
         J.rosym = 0;
         break;
       }
+  // rf phases: the engine propagates the real H' = R^H H R, so rho and det enter as R^H X R
+  const CMatrix ro = sys.to_frame(ro_in), det = sys.to_frame(det_in);
   if (J.is_static) J.rosym = 0;  // the static FID always transforms rho itself
   // Hamiltonian terms, packed per block
   std::vector<double> pas, isc, Tk, Hc(L.S2, 0.0);

@@ -407,6 +407,67 @@ void SpinSystem::build() {
     }
     hops_.push_back(T);
   }
+  // rf fields (PulseData::Pulse, pulsedata.cc:110-125): per isotope the sum of its fields
+  // amp e^{i phase}; the real axis goes into hc_, a phase off it into the frame
+  frame_.clear();
+  if (!rf_.empty()) {
+    std::map<std::string, std::pair<cplx, double>> chan;  // iso -> (sum amp e^{i phase}, offsets)
+    for (const RfField &f : rf_) {
+      if (f.amp == 0.0) continue;
+      const double r = std::fmod(f.phase_deg, 360.0);
+      cplx e;
+      if (std::fmod(f.phase_deg, 180.0) == 0.0) e = (r == 0.0) ? 1.0 : -1.0;  // x or -x: exact
+      else e = cplx(std::cos(f.phase_deg * 3.14159265358979323846 / 180.0),
+                    std::sin(f.phase_deg * 3.14159265358979323846 / 180.0));
+      chan[f.iso].first += f.amp * e;
+      chan[f.iso].second += f.offset;
+    }
+    std::vector<double> frame_phase(N_, 0.0);
+    bool any_phase = false;
+    for (auto &kv : chan) {
+      const cplx c = kv.second.first;
+      double ax = c.real();
+      std::vector<double> m(N_, 0.0);  // Fz of the isotope, diagonal
+      bool present = false;
+      for (int s = 0; s < nspin_; ++s) {
+        if (iso_[s] != kv.first) continue;
+        present = true;
+        const std::vector<double> z = iz_diag(s);
+        for (int k = 0; k < N_; ++k) m[k] += z[k];
+      }
+      if (!present) continue;
+      if (c.imag() != 0.0) {
+        // the rest of H must commute with Fz of this isotope for the frame to be exact
+        auto commutes = [&](const std::vector<double> &M) {
+          for (int r = 0; r < N_; ++r)
+            for (int q = 0; q < N_; ++q)
+              if (M[size_t(r) * N_ + q] != 0.0 && m[r] != m[q]) return false;
+          return true;
+        };
+        bool ok = commutes(hc_);
+        for (const auto &T : hops_) ok = ok && commutes(T);
+        if (!ok)
+          throw Error(5, "an rf phase off the x axis on " + kv.first +
+                             " needs a Hamiltonian that commutes with its Fz (a strong J coupling to another "
+                             "isotope does not)");
+        ax = std::abs(c);
+        const double ph = std::atan2(c.imag(), c.real());
+        for (int k = 0; k < N_; ++k) frame_phase[k] -= ph * m[k];
+        any_phase = true;
+      }
+      for (int s = 0; s < nspin_; ++s) {
+        if (iso_[s] != kv.first) continue;
+        const CMatrix x = single('x', s);
+        const std::vector<double> z = iz_diag(s);
+        for (size_t i = 0; i < hc_.size(); ++i) hc_[i] += ax * x.a[i].real();
+        for (int k = 0; k < N_; ++k) hc_[size_t(k) * N_ + k] += kv.second.second * z[k];
+      }
+    }
+    if (any_phase) {
+      frame_.resize(N_);
+      for (int k = 0; k < N_; ++k) frame_[k] = cplx(std::cos(frame_phase[k]), std::sin(frame_phase[k]));
+    }
+  }
   // Block structure: connected components of the union non-zero pattern.
   std::vector<int> parent(N_);
   std::iota(parent.begin(), parent.end(), 0);
@@ -444,6 +505,25 @@ void SpinSystem::build() {
       L.perm.push_back(s);
     }
   }
+}
+
+void SpinSystem::add_rf(const RfField &f) {
+  rf_.push_back(f);
+  try {
+    build();
+  } catch (...) {
+    rf_.pop_back();
+    build();
+    throw;
+  }
+}
+
+CMatrix SpinSystem::to_frame(const CMatrix &X) const {
+  if (frame_.empty()) return X;
+  CMatrix Y = X;
+  for (int r = 0; r < N_; ++r)
+    for (int c = 0; c < N_; ++c) Y(r, c) = std::conj(frame_[r]) * X(r, c) * frame_[c];
+  return Y;
 }
 
 std::vector<double> SpinSystem::hamiltonian(const double Rp[3][3], double alpha_rot, double rotb_rad) const {

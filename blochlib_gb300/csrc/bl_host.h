@@ -65,6 +65,15 @@ struct BlockLayout {
   int max_block = 0;
 };
 
+// Continuous rf on every spin of one isotope during the whole FID: the pulse Hamiltonian of
+// solid-2.0's PulseData::Pulse (examples/solid-2.0/src/pulsedata.cc:110-125),
+// amp (Ix cos phase + Iy sin phase) + offset Iz per spin, in Hz and degrees; a field with
+// amp == 0 adds nothing (its offset included), as there.
+struct RfField {
+  std::string iso;
+  double amp = 0, phase_deg = 0, offset = 0;
+};
+
 class SpinSystem {
  public:
   explicit SpinSystem(const std::vector<std::string> &lines);
@@ -95,6 +104,15 @@ class SpinSystem {
   // term Qp^2 / (B nu_rel) (c4 ((r00-r11)^2/4 + r01^2) - c2 (r02^2 + r12^2)) (qua.cc:219-267)
   double bfield() const { return bfield_; }
   void set_bfield(double b) { bfield_ = b; }
+  // rf fields (rebuilds the operators and the block layout).  The x part of each isotope's
+  // summed field is a real constant term of h_const(); a phase off the x axis is carried by
+  // the frame R = diag(frame()) = exp(-i phase Fz_iso): the engine propagates the real H'
+  // with rho and det taken as R^H X R, exact when the rest of H commutes with Fz_iso (every
+  // SolidSys term but a strong J coupling to another isotope; add_rf refuses otherwise).
+  void add_rf(const RfField &f);
+  const std::vector<RfField> &rf() const { return rf_; }
+  const std::vector<cplx> &frame() const { return frame_; }  // empty: no phase frame
+  CMatrix to_frame(const CMatrix &X) const;                  // R^H X R
   const BlockLayout &layout() const { return layout_; }
 
   // Reference-order dense H at rotor phase 'alpha_rot' for powder rotation Rp (for tests).
@@ -109,6 +127,8 @@ class SpinSystem {
   std::vector<double> hc_;
   std::vector<std::vector<double>> hops_, hq4_, hq2_;
   double bfield_ = 0;
+  std::vector<RfField> rf_;
+  std::vector<cplx> frame_;
   BlockLayout layout_;
 };
 

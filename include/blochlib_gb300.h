@@ -95,6 +95,14 @@ int bl_system_spins(const bl_system *sys);
  * first order only (src/QMspins/qua.cc:219-267).  Default 0.  Jobs created before the call
  * keep the field they were created with. */
 bl_status bl_system_set_bfield(bl_system *sys, double bfield);
+/* Continuous rf on every spin of isotope 'iso' during the FID, the pulse Hamiltonian of
+ * solid-2.0's PulseData::Pulse (examples/solid-2.0/src/pulsedata.cc:110-125):
+ * amp (Ix cos phase + Iy sin phase) + offset Iz per spin (Hz, degrees; amp == 0 adds
+ * nothing).  Repeatable; fields on one isotope add.  Both FID forms and the static branch
+ * see it (H stays periodic with the rotor).  A phase off the x axis needs a Hamiltonian that
+ * commutes with the isotope's Fz (a strong J coupling to another isotope does not):
+ * BL_ERR_UNSUPPORTED otherwise.  Copy-on-write, as bl_system_set_bfield. */
+bl_status bl_system_add_rf(bl_system *sys, const char *iso, double amp_hz, double phase_deg, double offset_hz);
 /* Operator expression, e.g. "Fx", "Ip 0", "0.5*Fx + Iz 1"; out = 2*N*N doubles. */
 bl_status bl_system_operator(const bl_system *sys, const char *expr, double *out);
 /* Block structure of the Hamiltonian: writes up to cap block sizes, returns the count

@@ -88,6 +88,10 @@ class SolidSys {
   int spins() const { return bl_system_spins(h_); }
   // sys.cc:206-210: second-order quadrupolar terms (qua.cc:219-267) with a field
   void setBfield(double Bf) { check(bl_system_set_bfield(h_, Bf)); }
+  // continuous rf during the FID (solid-2.0 PulseData::Pulse, pulsedata.cc:110-125)
+  void addRf(const std::string &iso, double amp, double phase_deg = 0, double offset = 0) {
+    check(bl_system_add_rf(h_, iso.c_str(), amp, phase_deg, offset));
+  }
   matrix op(const std::string &expr) const {
     matrix m(HS());
     check(bl_system_operator(h_, expr.c_str(), reinterpret_cast<double *>(m.a.data())));

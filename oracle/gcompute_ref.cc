@@ -292,6 +292,11 @@ struct System {
   std::vector<CMat> Ix, Iy, Iz, Ip, Im;
   std::vector<Interaction> ints;
   double bfield = 0;  // SolidSys::setBfield (sys.cc:206-210)
+  struct Rf {
+    std::string iso;
+    double amp, phase_deg, offset;
+  };
+  std::vector<Rf> rf;  // continuous rf during the FID (solid-2.0 PulseData::Pulse)
 };
 
 std::vector<std::string> tokens(const std::string &s) {
@@ -522,6 +527,17 @@ CMat hamiltonian(const System &S, const double Rp[3][3], double alpha, double ro
       }
     }
   }
+  // rf: amp (Ix cos phase + Iy sin phase) + offset Iz on every spin of the isotope, nothing
+  // when amp == 0 (examples/solid-2.0/src/pulsedata.cc:110-125; phase in degrees, 215)
+  for (const auto &f : S.rf) {
+    if (f.amp == 0.0) continue;
+    const double ph = f.phase_deg * kDeg2Rad;
+    for (int sp = 0; sp < S.nspin; ++sp) {
+      if (S.iso[sp] != f.iso) continue;
+      for (size_t e = 0; e < H.a.size(); ++e)
+        H.a[e] += f.amp * (S.Ix[sp].a[e] * std::cos(ph) + S.Iy[sp].a[e] * std::sin(ph)) + f.offset * S.Iz[sp].a[e];
+    }
+  }
   return H;
 }
 
@@ -698,6 +714,7 @@ struct Job {
   double bfield = 0;
   int p2p_base = 0, p2p_factor = 0;  // point-to-point FID when p2p_base > 0
   double maxtstep = 0;
+  std::vector<System::Rf> rf;
 };
 
 Job parse_job(const std::string &text) {
@@ -722,6 +739,12 @@ Job parse_job(const std::string &text) {
     else if (key == "bfield") J.bfield = std::atof(val.c_str());
     else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &J.p2p_base, &J.p2p_factor);
     else if (key == "maxtstep") J.maxtstep = std::atof(val.c_str());
+    else if (key == "rf") {
+      auto t = tokens(val);
+      if (t.size() < 2) throw std::runtime_error("rf: <iso> <amp> [phase_deg] [offset]");
+      J.rf.push_back({t[0], std::atof(t[1].c_str()), t.size() > 2 ? std::atof(t[2].c_str()) : 0.0,
+                      t.size() > 3 ? std::atof(t[3].c_str()) : 0.0});
+    }
   }
   return J;
 }
@@ -853,6 +876,7 @@ std::vector<cplx> single_p2p_fid(const System &S, const Job &J, double theta, do
 int run(const Job &J, const double *pw, int C, double *out, double *sw_out) {
   System S = parse_system(J.spin);
   S.bfield = J.bfield;
+  S.rf = J.rf;
   CMat ro = op_expr(S, J.rho), det = op_expr(S, J.det);
   std::vector<cplx> acc(J.P.npts, cplx(0, 0));
   double sw = J.P.sw;

@@ -23,6 +23,8 @@
 //   hamgen: <expression>   (repeatable; instead of a FID, writes the matrix the reference's
 //           HamiltonianGen (QMspins/driver/ham_gen.cc) evaluates for each expression, at the
 //           angles of 'hamgen_angles: <theta> <phi> <gamma>' (radians, default 0 0 0))
+//   rf: <iso> <amp Hz> [phase deg] [offset Hz]   (repeatable: continuous rf during the FID,
+//           added to SolidSys::Hamiltonian by RfSys below, as solid-2.0's PulseData::Pulse)
 //   p2p: <base> <factor>   maxtstep: <s>   (point-to-point FID instead of oneFID::FID: see
 //           p2p_fid below; a rotor period in 'base' chunks of ceil(chunk/maxtstep) steps,
 //           a point every 'factor' chunks)
@@ -100,6 +102,43 @@ static matrix op_expr(SolidSys &sys, const std::string &expr) {
   return acc;
 }
 
+struct RfSpec {
+  std::string iso;
+  double amp, phase_deg, offset;
+};
+
+// SolidSys with continuous rf: the Func_T that oneFID and compute are templated on (they call
+// setRotorAngles, setPowderAngles, Hamiltonian, Fe, Fz: oneFID.h:299-301, compute.h:206,
+// 265, 403), with the rf term built as PulseData::Pulse builds it
+// (examples/solid-2.0/src/pulsedata.cc:110-125; phase in degrees, pulsedata.cc:215).
+class RfSys {
+ public:
+  RfSys(SolidSys &s, const std::vector<RfSpec> &rf) : s_(&s) {
+    matrix tm = s.F0();
+    for (size_t j = 0; j < rf.size(); ++j) {
+      if (rf[j].amp == 0) continue;
+      const double ph = rf[j].phase_deg * DEG2RAD;
+      for (int i = 0; i < s.size(); ++i)
+        if (s.symbol(i) == rf[j].iso)
+          tm += rf[j].amp * (s.Ix(i) * cos(ph) + s.Iy(i) * sin(ph)) + rf[j].offset * s.Iz(i);
+    }
+    P_ = tm;
+  }
+  void setRotorAngles(double a, double b) { s_->setRotorAngles(a, b); }
+  void setPowderAngles(double t, double p, double g) { s_->setPowderAngles(t, p, g); }
+  hmatrix &Hamiltonian(double t1, double t2, double wr = 0.0) {
+    H_ = s_->Hamiltonian(t1, t2, wr);
+    H_ += P_;
+    return H_;
+  }
+  rimatrix &Fe() { return s_->Fe(); }
+  rdmatrix &Fz() { return s_->Fz(); }
+
+ private:
+  SolidSys *s_;
+  hmatrix P_, H_;
+};
+
 // Point-to-point powder FID assembled from the reference's own pieces: chunk propagators as
 // products of Mexp(SolidSys::Hamiltonian(t1,t2,wr), -i tau 2pi) with later steps on the left
 // (compute.h:257-274 convention; chunk loop of mmmqmas.cc:315-330), the forward and back
@@ -108,8 +147,9 @@ static matrix op_expr(SolidSys &sys, const std::string &expr) {
 // factor; otherwise the direct products of the same chunks), rho stepped as A rho A^H
 // and trace(rho, det)/trace(det, adjoint(det)) summed per point with the powder weight
 // (sequencerun_funcs.cc:624-645).  Static (wr == 0 or rotor angle 0): one Mexp of 1/sw.
-static Vector<complex> p2p_fid(SolidSys &sys, powder &pw, matrix &ro, matrix &det, int npts, double sw, double wr,
-                               double rotb, double start, int base, int factor, double maxtstep, double &sw_out) {
+static Vector<complex> p2p_fid(SolidSys &sys, RfSys &hs, powder &pw, matrix &ro, matrix &det, int npts, double sw,
+                               double wr, double rotb, double start, int base, int factor, double maxtstep,
+                               double &sw_out) {
   PropReduce red(base, factor);  // divides base and factor by their gcd (propreduce.cc:16-33)
   const int b = red.base, f = red.factor;
   // PropReduce::reduce terminates only for base < factor: setParams sizes BackRed to base-1
@@ -131,7 +171,7 @@ static Vector<complex> p2p_fid(SolidSys &sys, powder &pw, matrix &ro, matrix &de
       double dt = 1.0 / sw;
       nb = 1;
       W.resize(1);
-      W[0] = Mexp(sys.Hamiltonian(0.0, dt, 0.0), -complexi * dt * PI2);
+      W[0] = Mexp(hs.Hamiltonian(0.0, dt, 0.0), -complexi * dt * PI2);
       sw_out = sw;
     } else {
       const double chunk = 1.0 / (wr * b);
@@ -143,7 +183,7 @@ static Vector<complex> p2p_fid(SolidSys &sys, powder &pw, matrix &ro, matrix &de
         U[k] = sys.Fe();
         for (int j = 0; j < sub; ++j) {
           double t1 = start + double(k * sub + j) * tau;
-          U[k] = Mexp(sys.Hamiltonian(t1, t1 + tau, wr), -complexi * tau * PI2) * U[k];
+          U[k] = Mexp(hs.Hamiltonian(t1, t1 + tau, wr), -complexi * tau * PI2) * U[k];
         }
       }
       W.resize(b);
@@ -184,6 +224,7 @@ int main(int argc, char **argv) {
   std::string powder_file, rho_s, det_s, dump_file;
   int npts = 0, zcw_t = 0, zcw_p = 0;
   double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0, maxtstep = 0;
+  std::vector<RfSpec> rf;
   int p2p_base = 0, p2p_factor = 0;
   std::vector<std::string> hamgen;
   double hg_theta = 0, hg_phi = 0, hg_gamma = 0;
@@ -209,6 +250,13 @@ int main(int argc, char **argv) {
     else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &p2p_base, &p2p_factor);
     else if (key == "maxtstep") maxtstep = std::atof(val.c_str());
     else if (key == "hamgen") hamgen.push_back(val);
+    else if (key == "rf") {
+      RfSpec r = {"", 0, 0, 0};
+      char iso[32] = {0};
+      std::sscanf(val.c_str(), "%31s %lf %lf %lf", iso, &r.amp, &r.phase_deg, &r.offset);
+      r.iso = iso;
+      rf.push_back(r);
+    }
     else if (key == "hamgen_angles") std::sscanf(val.c_str(), "%lf %lf %lf", &hg_theta, &hg_phi, &hg_gamma);
   }
   SolidSys sys(spin_lines);
@@ -248,8 +296,13 @@ int main(int argc, char **argv) {
   matrix det = op_expr(sys, det_s);
   Vector<complex> fid;
   double sw_out = sw;
+  RfSys hs(sys, rf);
   if (p2p_base > 0) {
-    fid = p2p_fid(sys, pw, ro, det, npts, sw, wr, rotb, start, p2p_base, p2p_factor, maxtstep, sw_out);
+    fid = p2p_fid(sys, hs, pw, ro, det, npts, sw, wr, rotb, start, p2p_base, p2p_factor, maxtstep, sw_out);
+  } else if (!rf.empty()) {
+    oneFID<RfSys> driver(hs, npts, sw, wr, rotb, start);
+    fid = driver.FID(pw, ro, det);
+    sw_out = driver.sw();
   } else {
     oneFID<SolidSys> driver(sys, npts, sw, wr, rotb, start);
     fid = driver.FID(pw, ro, det);

@@ -253,16 +253,55 @@ def hamgen_fixtures():
     print("hamgen fixtures:", len(out))
 
 
+def rf_cases():
+    """Continuous rf during the FID (ref_harness 'rf:': SolidSys wrapped in a Func_T that adds
+    solid-2.0's PulseData::Pulse term), for oneFID::FID (spinning and static) and the
+    point-to-point form."""
+    c0 = W.config(0)
+    ch = ["numspin 2", "T 13C 0", "T 1H 1", "C 1500 6000 0.5 0 10 70 30", "D 8000 0 1 20 30 40"]
+    het3 = ["numspin 3", "T 13C 0", "T 1H 1", "T 1H 2", "C 900 7000 0.6 0 33 44 55", "D 9000 0 1 10 20 30",
+            "D 7000 0 2 40 50 60", "D -20000 1 2 70 80 0", "J 100 1 2 1"]
+    q2 = ["numspin 2", "T 2H 0", "T 1H 1", "C 300 2500 0.4 1 10 40 70", "D 3000 0 1 60 80 0",
+          "Q 160000 0.3 0 30 60 90"]
+    mas = dict(rotb=W.MAGIC_ANGLE)
+    cases = [
+        ("rf_decouple_x", dict(mas, lines=ch, rho="Ix 0", det="Ip 0", npts=256, wr=10000.0, sw=400000.0),
+         "rf: 1H 80000 0 0\n", 6),
+        ("rf_decouple_y_offset", dict(mas, lines=ch, rho="Ix 0", det="Ip 0", npts=256, wr=10000.0, sw=400000.0),
+         "rf: 1H 60000 90 2000\n", 6),
+        ("rf_het3_30deg_strongj", dict(mas, lines=het3, rho="Fx", det="Fp", npts=256, wr=12000.0, sw=12000.0 * 32),
+         "rf: 1H 50000 30 0\n", 5),
+        ("rf_lock_13c_two_fields", dict(mas, lines=ch, rho="Ix 0", det="Ip 0", npts=256, wr=10000.0, sw=400000.0),
+         "rf: 13C 20000 0 500\nrf: 13C 15000 90 0\nrf: 1H 0 45 3000\n", 6),
+        ("static_rf_120deg", dict(mas, lines=ch, rho="Ix 0", det="Ip 0", npts=200, wr=0.0, sw=200000.0),
+         "rf: 1H 70000 120 0\n", 6),
+        ("p2p_rf_5_3", dict(mas, lines=het3, rho="Fx", det="Fp", npts=100, wr=12000.0, sw=0.0),
+         "rf: 1H 50000 60 1000\np2p: 5 3\nmaxtstep: 3e-06\n", 4),
+        ("rf_quad2_45deg", dict(mas, lines=q2, rho="Fx", det="Fp", npts=256, wr=20000.0, sw=20000.0 * 40),
+         "rf: 2H 30000 45 0\nbfield: 200000\n", 5),
+    ]
+    for name, cfg, extra, ncry in cases:
+        yield name, W.job_text(cfg) + extra, powder_rows(c0["powder"], (spread(1154, ncry) + 33) % 1154)
+    # rf on like spins joins every Fz sector: 5 1H (one block of 32, the CTA kernels) and
+    # 7 1H (one block of 128, the batched products)
+    for n, name, nstep, ncry in [(5, "rf_lock_5h_big", 24, 2), (7, "huge_rf_lock_7h", 8, 1)]:
+        rng = np.random.default_rng(W.SEED0 + 60 + n)
+        xyz = W._proton_cluster(rng, n, 5.0, min_sep=1.5)
+        lines = [f"numspin {n}"] + [f"T 1H {k}" for k in range(n)] + W._csa_lines(rng, n) + W._dipole_lines(xyz)
+        cfg = dict(lines=lines, rho="Fx", det="Fp", npts=96, wr=25000.0, sw=nstep * 25000.0, rotb=W.MAGIC_ANGLE)
+        yield name, W.job_text(cfg) + "rf: 1H 40000 0 0\n", powder_rows(c0["powder"], (spread(1154, ncry) + 500) % 1154)
+
+
 def main():
     if "--hamgen" in sys.argv:
         hamgen_fixtures()
         return
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
-    if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p")):
+    if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p", "--rf")):
         man = json.loads((OUT / "manifest.json").read_text())
         extra = (huge_cases() if "--huge" in sys.argv else quad2_cases() if "--quad2" in sys.argv
-                 else p2p_cases() if "--p2p" in sys.argv else big_cases())
+                 else p2p_cases() if "--p2p" in sys.argv else rf_cases() if "--rf" in sys.argv else big_cases())
         for name, job, rows in extra:
             sw64, f64 = run_ref(BIN64, job, rows)
             np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,

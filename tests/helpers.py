@@ -56,6 +56,10 @@ def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_me
     sys_ = bl.SolidSys(lines)
     if "bfield" in kv:
         sys_.setBfield(float(kv["bfield"]))
+    for line in str(job_text).splitlines():  # continuous rf fields, in order
+        if line.startswith("rf:"):
+            t = line[3:].split()
+            sys_.addRf(t[0], float(t[1]), float(t[2]) if len(t) > 2 else 0.0, float(t[3]) if len(t) > 3 else 0.0)
     rows = np.asarray(rows, dtype=np.float64)
     pw = bl.powder.from_arrays(theta=rows[:, 1], phi=rows[:, 0], gamma=rows[:, 2], weight=rows[:, 3])
     drv = bl.oneFID(sys_, int(kv["npts"]), float(kv["sw"]), float(kv["wr"]), float(kv["rotb"]),
