@@ -149,7 +149,8 @@ __host__ __device__ constexpr size_t big_step_smem(int b) {
 }
 
 // One CTA per (crystallite, step): U_i of a large block, exp(-iX) with X = 2pi tau H_i / 2^sq
-// (||X||_inf <= 1/2) by its degree-15 Taylor polynomial, then sq squarings.
+// (||X||_inf <= 1/2) by its Taylor polynomial, then sq squarings.  Blocks above kBigPSMax
+// sum the series term by term up to the degree taylor_degree gives for the step's norm.
 // Blocks up to kBigPSMax evaluate the polynomial as cos X = C(Y), sin X = X S(Y), Y = X^2,
 // C and S of degree 7 in Y by Paterson-Stockmeyer with Y^4 (Y, Y^2, Y^3, Y^4, C, S, X S:
 // 7 real products); larger blocks accumulate the terms one product at a time (14).  All
@@ -159,7 +160,7 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
   extern __shared__ double bsm[];
   __shared__ double fk[kMaxInt];
   __shared__ double red[kMaxBigBlock];
-  __shared__ double scl[2];
+  __shared__ double scl[3];
   const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
   if (threadIdx.x == 0) {
@@ -200,10 +201,11 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
     }
     scl[0] = ldexp(tp, -sq);
     scl[1] = double(sq);
+    scl[2] = double(taylor_degree(ldexp(nrm, -sq), s.mixed != 0));  // terms the series needs
   }
   __syncthreads();
   const double sc = scl[0];
-  const int sq = int(scl[1]);
+  const int sq = int(scl[1]), nterms = int(scl[2]);
   double *R, *I, *F0, *F1, *F2;  // result R + iI and three free b x b buffers for squaring
   if (b <= kBigPSMax) {
     double *Y = X + bb, *Y2 = Y + bb, *Y3 = Y2 + bb, *Y4 = Y3 + bb, *T = Y4 + bb;
@@ -248,7 +250,7 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
       I[e] = -x;
     }
     __syncthreads();
-    for (int kt = 2; kt <= kTaylorTerms; ++kt) {
+    for (int kt = 2; kt <= nterms; ++kt) {  // the degree the step's norm needs (<= 15)
       cta_mm_sym(P, X, Q, b, 1.0 / kt);
       __syncthreads();
       const int m4 = kt & 3;
