@@ -1271,10 +1271,11 @@ __global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
 
 // In-place radix-2 decimation-in-time FFT (negative exponent) of CG interleaved sequences
 // of length M = 2^logM held in shared memory as X[i * CG + cc], input in bit-reversed
-// order, output in natural order.  tw[k] = exp(-2 pi i k / M), k < M/2.  Y (optional) is
-// transformed alongside X.  Ends with a barrier.
+// order, output in natural order.  tw[k] = exp(-2 pi i k / (M twm)), k < M twm / 2 (twm = 2:
+// a half-length transform on the table of the full length).  Y (optional) is transformed
+// alongside X.  Ends with a barrier.
 template <int CG, class C>
-__device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw) {
+__device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw, int twm = 1) {
   const int nb = (M / 2) * CG;
   for (int st = 0; st < logM; ++st) {
     const int h = 1 << st, tstride = M >> (st + 1);
@@ -1289,8 +1290,17 @@ __device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw) {
           a = Y[i0], d = Y[i1];
           Y[i0] = cadd(a, d), Y[i1] = csub(a, d);
         }
+      } else if (st == 1) {  // twiddles 1 and -i: no multiplication
+        C a = X[i0], d = X[i1];
+        C t = pos ? mkc<C>(d.y, -d.x) : d;
+        X[i0] = cadd(a, t), X[i1] = csub(a, t);
+        if (Y) {
+          a = Y[i0], d = Y[i1];
+          t = pos ? mkc<C>(d.y, -d.x) : d;
+          Y[i0] = cadd(a, t), Y[i1] = csub(a, t);
+        }
       } else {
-        const C w = tw[pos * tstride];
+        const C w = tw[pos * tstride * twm];
         C a = X[i0], t = cmul(w, X[i1]);
         X[i0] = cadd(a, t), X[i1] = csub(a, t);
         if (Y) {
@@ -1335,13 +1345,21 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   const double nt = double(n) * s.tau;
   // per crystallite of the group: w_rs = chop((l_r - l_s)/(i n tau), 1e-10), z = e^{i n tau w},
   // and the powers z^j of the FID reconstruction (always computed in FP64)
-  for (int idx = threadIdx.x; idx < CG * (s.J + 1); idx += blockDim.x) {
-    const int cc = idx % CG, j = idx / CG, c = c0 + cc;
+  // (four powers per thread: one cexp and three products, error a few ulp)
+  constexpr int kZrun = 4;
+  const int nzr = (s.J + 1 + kZrun - 1) / kZrun;
+  for (int idx = threadIdx.x; idx < CG * nzr; idx += blockDim.x) {
+    const int cc = idx % CG, j0 = (idx / CG) * kZrun, c = c0 + cc;
     if (c >= s.C) continue;
     double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
     double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
-    if (j == s.J) zc[cc] = cvt<C>(cexp(cmk(-nt * w.y, nt * w.x)));
-    else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(cexp(cmk(-double(j) * nt * w.y, double(j) * nt * w.x)));
+    const double2 z1 = cexp(cmk(-nt * w.y, nt * w.x));
+    double2 zj = cexp(cmk(-double(j0) * nt * w.y, double(j0) * nt * w.x));
+    for (int j = j0; j < min(j0 + kZrun, s.J + 1); ++j) {
+      if (j == s.J) zc[cc] = cvt<C>(z1);
+      else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(zj);
+      zj = cmul(zj, z1);
+    }
   }
   const bool twist = s.fave_twist;
   if (twist) {
@@ -1355,9 +1373,16 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
         double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
         zl = autoc ? cmk(0.0, s.tau * w.x) : cmk(-s.tau * w.y, s.tau * w.x);
       }
+      // |zeta| = 1 in the autocorrelation case: zeta^-k is conj(zeta^k) (bit for bit, as the
+      // products of conjugates are the conjugated products)
       for (int sgn = 0; sgn < 2; ++sgn) {
         const double2 l = sgn ? cmk(-zl.x, -zl.y) : zl;
         double2 *t1 = sgn ? tm1 : tp1, *t8 = sgn ? tm8 : tp8;
+        if (sgn && autoc) {
+          for (int b = 0; b < 8; ++b) t1[b * CG + cc] = cconj(tp1[b * CG + cc]);
+          for (int a = 0; a < M / 8; ++a) t8[a * CG + cc] = cconj(tp8[a * CG + cc]);
+          continue;
+        }
         const double2 z1 = cexp(l);
         t1[cc] = cmk(1, 0);
         for (int b = 1; b < 8; ++b) t1[b * CG + cc] = cmul(t1[(b - 1) * CG + cc], z1);
@@ -1393,31 +1418,75 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   }
   __syncthreads();
   fft_dit<CG, C>(X, autoc ? nullptr : Y, M, logM, Bufs<C>::tw(s));
-  // conj of the cross spectrum, in place in X (same index read and written)
-  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
-    C x = X[idx];
-    if (autoc) X[idx] = mkc<C>(x.x * x.x + x.y * x.y, 0.0);
-    else X[idx] = cconj(cmul(x, cconj(Y[idx])));
+  // Inverse transform by a forward one: conj(FFT(x))/M.  Autocorrelation: the spectrum
+  // S = |FFT q|^2 is real, so its transform takes one of half length on z_k = S_2k + i S_2k+1
+  // (each column on its own, so a crystallite's result does not depend on its neighbours):
+  // with Z = FFT_{M/2}(z), E_p = (Z_p + conj Z_-p)/2, O_p = (Z_p - conj Z_-p)/(2i),
+  // FFT(S)_p = E_p + w^p O_p and FFT(S)_{p+M/2} = E_p - w^p O_p, w = exp(-2 pi i / M).
+  const int Mh = M / 2;
+  const bool half = autoc && M >= 4;
+  const C *twb = Bufs<C>::tw(s);
+  if (half) {
+    for (int idx = threadIdx.x; idx < Mh * CG; idx += blockDim.x) {
+      const int cc = idx % CG, k = idx / CG;
+      const C xe = X[(2 * k) * CG + cc], xo = X[(2 * k + 1) * CG + cc];
+      Y[int(__brev(unsigned(k)) >> (33 - logM)) * CG + cc] =
+          mkc<C>(xe.x * xe.x + xe.y * xe.y, xo.x * xo.x + xo.y * xo.y);
+    }
+    __syncthreads();
+    fft_dit<CG, C>(Y, nullptr, Mh, logM - 1, twb, 2);
+  } else {
+    // conj of the cross spectrum, in place in X (same index read and written)
+    for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+      C x = X[idx];
+      if (autoc) X[idx] = mkc<C>(x.x * x.x + x.y * x.y, 0.0);
+      else X[idx] = cconj(cmul(x, cconj(Y[idx])));
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+      const int cc = idx % CG, f = idx / CG;
+      Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
+    }
+    __syncthreads();
+    fft_dit<CG, C>(Y, nullptr, M, logM, Bufs<C>::tw(s));
   }
-  __syncthreads();
-  // bit-reverse into Y, forward transform: conj(result)/M is the inverse transform
-  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
-    const int cc = idx % CG, f = idx / CG;
-    Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
-  }
-  __syncthreads();
-  fft_dit<CG, C>(Y, nullptr, M, logM, Bufs<C>::tw(s));
+  // transform of column cc at frequency p
+  auto spec = [&](int p, int cc) -> C {
+    if (!half) return Y[p * CG + cc];
+    const int q = p & (Mh - 1);
+    const C zp = Y[q * CG + cc], zm = cconj(Y[((Mh - q) & (Mh - 1)) * CG + cc]);
+    const C ev = cscale(cadd(zp, zm), 0.5), d = csub(zp, zm);
+    const C wo = cmul(twb[q], mkc<C>(0.5 * d.y, -0.5 * d.x));
+    return p < Mh ? cadd(ev, wo) : csub(ev, wo);
+  };
   const double invM = 1.0 / double(M);
   C *Gb = Bufs<C>::G(s);
+  if (half && twist) {  // n == M: frequencies q and q + M/2 share E_q and w^q O_q
+    for (int idx = threadIdx.x; idx < Mh * CG; idx += blockDim.x) {
+      const int cc = idx % CG, q = idx / CG, c = c0 + cc;
+      if (c >= s.C) continue;
+      const C zp = Y[q * CG + cc], zm = cconj(Y[((Mh - q) & (Mh - 1)) * CG + cc]);
+      const C ev = cscale(cadd(zp, zm), 0.5), d = csub(zp, zm);
+      const C wo = cmul(twb[q], mkc<C>(0.5 * d.y, -0.5 * d.x));
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const int p = q + hh * Mh;
+        const C lp = cscale(cconj(hh ? csub(ev, wo) : cadd(ev, wo)), invM);
+        const C g = cvt<C>(cmul(cmul(tp8[(p >> 3) * CG + cc], tp1[(p & 7) * CG + cc]), todbl(lp)));
+        Gb[at(p * s.ne + e, c, s.Cpad)] = g;
+      }
+    }
+    return;
+  }
   for (int idx = threadIdx.x; idx < n * CG; idx += blockDim.x) {
     const int cc = idx % CG, p = idx / CG, c = c0 + cc;
     if (c >= s.C) continue;
-    C lp = cscale(cconj(Y[p * CG + cc]), invM);
+    C lp = cscale(cconj(spec(p, cc)), invM);
     C g = lp;
     if (twist) {  // G_p = zeta^p C_p
       g = cvt<C>(cmul(cmul(tp8[(p >> 3) * CG + cc], tp1[(p & 7) * CG + cc]), todbl(lp)));
     } else if (p > 0) {
-      C lm = cscale(cconj(Y[(M + p - n) * CG + cc]), invM);
+      C lm = cscale(cconj(spec(M + p - n, cc)), invM);
       g = cfma(zc[cc], lm, lp);
     }
     Gb[at(p * s.ne + e, c, s.Cpad)] = g;
