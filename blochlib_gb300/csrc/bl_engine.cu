@@ -125,6 +125,7 @@ struct DevSys {
   const int *bs, *boff, *bpoff;
   // per interaction: crystal tensor (xx xy xz yy yz zz), scale, packed operator
   const double *pas, *iscale, *Tk, *Hc;
+  const double *fk;  // per (step, term, crystallite): the term coefficients of k_coef, or null
   const int *ikind;  // per term: 0 first order, 1 / 2 second-order quadrupolar (c4 / c2)
   int has2;
   // Q pairs (D blocks) and R pairs (rho blocks)
@@ -481,8 +482,41 @@ __device__ __forceinline__ void build_h_at(const DevSys &s, int c, double sp, do
   }
 }
 
+// Term coefficients of step i for every crystallite, once per (crystallite, step): the
+// small-block step kernels of all blocks read them instead of each recomputing them.
+__global__ void __launch_bounds__(kThreads) k_coef(DevSys s, double *fk) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int c = int(tid % s.Cpad), i = int(tid / s.Cpad);
+  if (i >= s.n || c >= s.C) return;
+  double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
+  double tmid = (t2 - t1) / 2.0 + t1;
+  double sp, cp;
+  sincos(tmid * s.wr * kPi2, &sp, &cp);
+  double m[3][3];
+  orient_rows(s, c, sp, cp, m);
+  for (int kk = 0; kk < s.nint; ++kk) fk[at(i * s.nint + kk, c, s.Cpad)] = term_coef(s, kk, m);
+}
+
 template <int B>
 __device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, double (&h)[B][B]) {
+  if (s.fk) {  // coefficients from k_coef
+#pragma unroll
+    for (int p = 0; p < B; ++p)
+#pragma unroll
+      for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
+    for (int kk = 0; kk < s.nint; ++kk) {
+      const double f = s.fk[at(i * s.nint + kk, c, s.Cpad)];
+      const double *T = s.Tk + size_t(kk) * s.S2 + bp;
+#pragma unroll
+      for (int p = 0; p < B; ++p)
+#pragma unroll
+        for (int q = 0; q < B; ++q) {
+          const double t = T[p * B + q];
+          if (t != 0.0) h[p][q] = fma(f, t, h[p][q]);
+        }
+    }
+    return;
+  }
   double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
   double tmid = (t2 - t1) / 2.0 + t1;
   double sp, cp;
@@ -1734,6 +1768,7 @@ struct JobImpl {
   DevBuf<int> ikind;
   int has2 = 0;  // second-order quadrupolar terms present
   int p2p = 0, pb = 1, pf = 1, psub = 1;  // point-to-point FID: base, factor, steps per chunk
+  DevBuf<double> fkc;                      // k_coef's term coefficients (small blocks)
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
@@ -1982,6 +2017,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   size_t per_c = J.mixed ? sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N) + sizeof(float2) * (nsteps * L.S2 + wide)
                          : sizeof(double2) * (nsteps * L.S2 * 2 + L.S2 + N + wide);
   per_c += sizeof(double) * 11;
+  // term coefficients per (step, term), computed once for all small blocks (k_coef)
+  const bool use_fk = !J.is_static && J.nint > 0;
+  if (use_fk) per_c += sizeof(double) * size_t(J.n) * size_t(J.nint);
   long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
   // huge blocks: one workspace for their batched products, at least one item of each use
   // (exponential: 7 real b x b; Floquet: 2 complex b x b; eigenframe, Q/R: one complex
@@ -2204,6 +2242,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.hsqmax.alloc(1);
   }
   J.fid.alloc(p.npts);
+  if (use_fk) J.fkc.alloc(size_t(J.n) * J.nint * Cb);
   CUDA_OK(cudaMemsetAsync(J.partial.p, 0, J.partial.n * sizeof(double2), st));
   CUDA_OK(cudaStreamSynchronize(st));
   // algorithmic flop count (one complex MAC = 8 flop; eigh counted as 32 b^3, the
@@ -2299,6 +2338,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
   s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
+  s.fk = use_fk ? J.fkc.p : nullptr;
   s.ikind = J.ikind.p, s.has2 = J.has2;
   s.npq = J.npq, s.npr = J.npr;
   s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
@@ -2525,6 +2565,10 @@ static void huge_qr(JobImpl &J, DevSys &s, const BigPair &P, C *Wbuf, C *out) {
 }
 
 static void launch_stage(JobImpl &J, DevSys &s, int stage) {
+  if (stage == 0 && s.fk) {  // the small blocks' term coefficients, before the streams fork
+    k_coef<<<grid_for(long(s.Cpad) * s.n), kThreads, 0, J.ctx->stream>>>(s, J.fkc.p);
+    ++J.launches;
+  }
   if (!J.big_blocks.empty()) fork(J);
   launch_block_kernels<1>(J, s, stage);
   launch_block_kernels<2>(J, s, stage);
