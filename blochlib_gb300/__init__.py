@@ -134,11 +134,24 @@ class FidParams(ctypes.Structure):
                 ("step_method", ctypes.c_int), ("fave_method", ctypes.c_int)]
 
 
+class RfChunk(ctypes.Structure):
+    _fields_ = [("chunk", ctypes.c_int), ("iso", ctypes.c_char_p), ("amp_hz", ctypes.c_double),
+                ("phase_deg", ctypes.c_double), ("offset_hz", ctypes.c_double)]
+
+
 class P2PParams(ctypes.Structure):
     _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
                 ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
                 ("step_method", ctypes.c_int), ("base", ctypes.c_int), ("factor", ctypes.c_int),
-                ("maxtstep", ctypes.c_double)]
+                ("maxtstep", ctypes.c_double), ("rf", ctypes.c_void_p), ("nrf", ctypes.c_int)]
+
+
+def _rf_schedule(rf_chunks):
+    """(chunk, iso, amp Hz[, phase deg[, offset Hz]]) tuples -> a ctypes array (kept by the caller)."""
+    rows = [tuple(r) + (0.0,) * (5 - len(r)) for r in (rf_chunks or [])]
+    arr = (RfChunk * max(1, len(rows)))(*[RfChunk(int(a), str(b).encode(), float(c), float(d), float(e))
+                                          for a, b, c, d, e in rows])
+    return arr, len(rows)
 
 
 class HamiltonianGen:
@@ -382,14 +395,16 @@ class Job:
 
     @classmethod
     def p2p(cls, sys, pw, ro, det, npts, wr, rotb, base, factor, maxtstep=0.0, sw=0.0, start_t=0.0, precision=0,
-            ctx=None, step_method=None):
+            ctx=None, step_method=None, rf_chunks=None):
         """Resident point-to-point job (bl_p2p_job_create); see oneFID.p2pFID."""
         self = cls.__new__(cls)
         self.ctx = ctx or default_context()
         n = sys.dim()
         self._ro, self._det = _cmat(ro, n), _cmat(det, n)
+        self._rf, nrf = _rf_schedule(rf_chunks)
         self.params = P2PParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
-                                _step_method(step_method), int(base), int(factor), float(maxtstep))
+                                _step_method(step_method), int(base), int(factor), float(maxtstep),
+                                ctypes.cast(self._rf, ctypes.c_void_p), nrf)
         h = ctypes.c_void_p()
         _check(load().bl_p2p_job_create(self.ctx._h, sys._h, pw._h, _ptr(self._ro), _ptr(self._det),
                                         ctypes.byref(self.params), ctypes.byref(h)))
@@ -495,11 +510,12 @@ class oneFID:
         self.fid_ = out
         return out
 
-    def p2pFID(self, pw, ro, det, base=1, factor=1, maxtstep=0.0):
+    def p2pFID(self, pw, ro, det, base=1, factor=1, maxtstep=0.0, rf_chunks=None):
         """Point-to-point powder FID (bl_p2p_fid): points every factor/base rotor periods
         (PropReduce(base, factor)), fid[p] = sum_c w_c Tr(rho_c(t_p) det) / Tr(det det^H);
         steps of at most maxtstep inside each chunk.  Static (wr == 0 or rotor angle 0): one
-        step of 1/sw per point.  Updates self.sw to base*wr/factor."""
+        step of 1/sw per point.  rf_chunks: (chunk, iso, amp[, phase[, offset]]) fields on
+        during one chunk of every rotor period.  Updates self.sw to base*wr/factor."""
         if isinstance(base, PropReduce):
             base, factor = base.base, base.factor
         ctx = self.ctx or default_context()
@@ -507,8 +523,10 @@ class oneFID:
         ro, det = _cmat(ro, n), _cmat(det, n)
         out = np.zeros(self.npts, dtype=np.complex128)
         sw_out = np.zeros(1)
+        rf, nrf = _rf_schedule(rf_chunks)
         params = P2PParams(self.npts, self.sw, self.wr, self.rotb, self.startT, int(self.precision),
-                           _step_method(self.step_method), int(base), int(factor), float(maxtstep))
+                           _step_method(self.step_method), int(base), int(factor), float(maxtstep),
+                           ctypes.cast(rf, ctypes.c_void_p), nrf)
         _check(load().bl_p2p_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
                                  _ptr(out), _ptr(sw_out)))
         self.sw = float(sw_out[0])

@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
   }
   __syncthreads();
   double *X = bsm;
+  const double *Hcb = hc_of(s, i) + bp;
   for (int e = threadIdx.x; e < bb; e += blockDim.x) {
-    double h = s.Hc[bp + e];
+    double h = Hcb[e];
     for (int kk = 0; kk < s.nint; ++kk) {
       const double t = s.Tk[size_t(kk) * s.S2 + bp + e];
       if (t != 0.0) h = fma(fk[kk], t, h);
@@ -277,7 +278,14 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
     __syncthreads();
   }
   double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
-  for (int e = threadIdx.x; e < bb; e += blockDim.x) Ub[at(bp + e, c, s.Cpad)] = cmk(R[e], I[e]);
+  const double2 *fr = frame_of(s, i);
+  if (fr) {  // lab frame of a chunk rf phase: U = R U' R^H
+    const int bo = s.boff[k];
+    for (int e = threadIdx.x; e < bb; e += blockDim.x)
+      Ub[at(bp + e, c, s.Cpad)] = cmul(cmul(fr[bo + e / b], cmk(R[e], I[e])), cconj(fr[bo + e % b]));
+  } else {
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) Ub[at(bp + e, c, s.Cpad)] = cmk(R[e], I[e]);
+  }
 }
 
 // One CTA per crystallite: A_{i+1} = U_i A_i for all steps; A lives in shared memory.

@@ -71,6 +71,12 @@ bl::FidParams to_params(const bl_p2p_params *p) {
   f.step_method = p->step_method;
   if (p->base <= 0 || p->factor <= 0) throw bl::Error(BL_ERR_INVALID, "point-to-point base and factor must be positive");
   f.p2p_base = p->base, f.p2p_factor = p->factor, f.maxtstep = p->maxtstep;
+  if (p->nrf < 0 || (p->nrf > 0 && !p->rf)) throw bl::Error(BL_ERR_INVALID, "bad rf schedule");
+  for (int k = 0; k < p->nrf; ++k) {
+    if (!p->rf[k].iso) throw bl::Error(BL_ERR_INVALID, "rf schedule: null isotope");
+    f.rf_chunks.push_back({p->rf[k].chunk, bl::RfField{p->rf[k].iso, p->rf[k].amp_hz, p->rf[k].phase_deg,
+                                                      p->rf[k].offset_hz}});
+  }
   return f;
 }
 }  // namespace

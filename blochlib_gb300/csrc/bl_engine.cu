@@ -126,6 +126,10 @@ struct DevSys {
   // per interaction: crystal tensor (xx xy xz yy yz zz), scale, packed operator
   const double *pas, *iscale, *Tk, *Hc;
   const double *fk;  // per (step, term, crystallite): the term coefficients of k_coef, or null
+  // point-to-point rf schedule: hc_chunks > 0 gives one Hc per chunk of the period (step i in
+  // chunk i / psub); frames (chunk x N, permuted index) rotate each step's U into the lab frame
+  int hc_chunks;
+  const double2 *frames;
   const int *ikind;  // per term: 0 first order, 1 / 2 second-order quadrupolar (c4 / c2)
   int has2;
   // Q pairs (D blocks) and R pairs (rho blocks)
@@ -459,16 +463,40 @@ __device__ __forceinline__ double term_coef(const DevSys &s, int kk, const doubl
   return s.iscale[kk] * a;
 }
 
+// Constant part of H and rf frame of step i: one per chunk under a point-to-point rf
+// schedule (chunk i / psub), else the single Hc and no frame.
+__device__ __forceinline__ const double *hc_of(const DevSys &s, int i) {
+  return s.hc_chunks ? s.Hc + size_t(i / s.psub) * s.S2 : s.Hc;
+}
+__device__ __forceinline__ const double2 *frame_of(const DevSys &s, int i) {
+  return s.frames ? s.frames + size_t(i / s.psub) * s.N : nullptr;
+}
+
+// Stores u = U'(p,q) = U'(q,p) of a step's real-symmetric-H block; with a frame r the lab-frame
+// U = R U' R^H takes r_p u conj(r_q) at (p,q) and r_q u conj(r_p) at (q,p).
+__device__ __forceinline__ void store_u_pair(double2 *Ub, int c, int Cpad, int bp, int bo, int B, int p, int q,
+                                             double2 u, const double2 *fr) {
+  if (!fr) {
+    Ub[at(bp + p * B + q, c, Cpad)] = u;
+    if (q != p) Ub[at(bp + q * B + p, c, Cpad)] = u;
+    return;
+  }
+  const double2 rp = fr[bo + p], rq = fr[bo + q];
+  Ub[at(bp + p * B + q, c, Cpad)] = cmul(cmul(rp, u), cconj(rq));
+  if (q != p) Ub[at(bp + q * B + p, c, Cpad)] = cmul(cmul(rq, u), cconj(rp));
+}
+
 // H_i block at the midpoint of step i (sys.cc:749-770): rotor phase 2 pi wr t_mid,
 // a = (M PAS M^T)_22 with M = R_rotor R_powder, H = Hc + sum_k scale_k a_k T_k.
 template <int B>
-__device__ __forceinline__ void build_h_at(const DevSys &s, int c, double sp, double cp, int bp, double (&h)[B][B]) {
+__device__ __forceinline__ void build_h_at(const DevSys &s, int c, double sp, double cp, const double *Hcb,
+                                           int bp, double (&h)[B][B]) {
   double m[3][3];
   orient_rows(s, c, sp, cp, m);
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
-    for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
+    for (int q = 0; q < B; ++q) h[p][q] = Hcb[p * B + q];
   for (int kk = 0; kk < s.nint; ++kk) {
     const double f = term_coef(s, kk, m);
     const double *T = s.Tk + size_t(kk) * s.S2 + bp;
@@ -499,11 +527,12 @@ __global__ void __launch_bounds__(kThreads) k_coef(DevSys s, double *fk) {
 
 template <int B>
 __device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, double (&h)[B][B]) {
+  const double *Hcb = hc_of(s, i) + bp;
   if (s.fk) {  // coefficients from k_coef
 #pragma unroll
     for (int p = 0; p < B; ++p)
 #pragma unroll
-      for (int q = 0; q < B; ++q) h[p][q] = s.Hc[bp + p * B + q];
+      for (int q = 0; q < B; ++q) h[p][q] = Hcb[p * B + q];
     for (int kk = 0; kk < s.nint; ++kk) {
       const double f = s.fk[at(i * s.nint + kk, c, s.Cpad)];
       const double *T = s.Tk + size_t(kk) * s.S2 + bp;
@@ -521,7 +550,7 @@ __device__ __forceinline__ void build_h(const DevSys &s, int c, int i, int bp, d
   double tmid = (t2 - t1) / 2.0 + t1;
   double sp, cp;
   sincos(tmid * s.wr * kPi2, &sp, &cp);
-  build_h_at<B>(s, c, sp, cp, bp, h);
+  build_h_at<B>(s, c, sp, cp, Hcb, bp, h);
 }
 
 // Static powder FID, step 1 (oneFID.h:301-311): one thread per (crystallite, block): H at
@@ -537,7 +566,7 @@ __global__ void __launch_bounds__(kThreads) k_static_eig(DevSys s, const int *__
   if (c >= s.C) return;
   const int bp = s.bpoff[k], bo = s.boff[k];
   double h[B][B], v[B][B];
-  build_h_at<B>(s, c, 0.0, 1.0, bp, h);
+  build_h_at<B>(s, c, 0.0, 1.0, s.Hc + bp, bp, h);
   if (!jacobi_sym<B>(h, v)) atomicOr(s.status, kNoConvergeStep);
 #pragma unroll
   for (int r = 0; r < B; ++r) {
@@ -645,6 +674,8 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
     e[j] = cmk(chop1(cs, 1e-12), chop1(-sn, 1e-12));
   }
   double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+  const double2 *fr = frame_of(s, i);
+  const int bo = s.boff[k];
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
@@ -656,8 +687,7 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
         u.x = fma(vv, e[j].x, u.x);
         u.y = fma(vv, e[j].y, u.y);
       }
-      Ub[at(bp + p * B + q, c, s.Cpad)] = u;
-      if (q != p) Ub[at(bp + q * B + p, c, s.Cpad)] = u;
+      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr);
     }
 }
 
@@ -807,13 +837,14 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *_
     }
   }
   double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+  const double2 *fr = frame_of(s, i);
+  const int bo = s.boff[k];
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
     for (int q = p; q < B; ++q) {
       double2 u = cmk(R[sx<B>(p, q)], I[sx<B>(p, q)]);
-      Ub[at(bp + p * B + q, c, s.Cpad)] = u;
-      if (q != p) Ub[at(bp + q * B + p, c, s.Cpad)] = u;
+      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr);
     }
 }
 
@@ -1769,6 +1800,7 @@ struct JobImpl {
   int has2 = 0;  // second-order quadrupolar terms present
   int p2p = 0, pb = 1, pf = 1, psub = 1;  // point-to-point FID: base, factor, steps per chunk
   DevBuf<double> fkc;                      // k_coef's term coefficients (small blocks)
+  DevBuf<double2> frames;                  // rf schedule: per chunk frame (permuted index)
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
@@ -1839,6 +1871,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       u = v, v = t;
     }
     J.pb = p.p2p_base / u, J.pf = p.p2p_factor / u;
+    if (!p.rf_chunks.empty()) {  // the schedule is given on the caller's chunks
+      if (J.is_static) throw Error(1, "an rf schedule within the rotor period needs spinning (wr > 0, rotor angle != 0)");
+      J.pb = p.p2p_base, J.pf = p.p2p_factor;
+      for (const auto &rc : p.rf_chunks)
+        if (rc.chunk < 0 || rc.chunk >= J.pb) throw Error(1, "rf schedule: chunk outside 0 .. base-1");
+    }
     J.gammaloop = 1;
     if (J.is_static) {  // time-independent H: one step of 1/sw per point
       if (!(p.sw > 0)) throw Error(1, "sw must be positive");
@@ -1860,6 +1898,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       J.sw_out = p.wr * J.pb / J.pf;
     }
     J.is_static = 0;  // spinning machinery: steps, Dyson, Floquet, Q/R, then the p2p terms
+  } else if (!p.rf_chunks.empty()) {
+    throw Error(1, "an rf schedule within the rotor period needs the point-to-point form");
   } else if (J.is_static) {
     // oneFID::singleStaticFID (oneFID.h:292-336): dt = 1/sw as given; the FID index k is
     // split as k = j*ns + p for the reconstruction kernel
@@ -1881,7 +1921,27 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.tau = (tmax - tmin) / J.n;
     if (!(J.tau > 0)) throw Error(1, "the propagator time step is not positive");
   }
-  J.L = sys.layout();
+  // rf schedule: one system per chunk (the system's own rf plus the chunk's fields) for its
+  // constant H and rf frame; the block layout of a system with every scheduled isotope
+  // irradiated holds all of them
+  const bool sched = !p.rf_chunks.empty();
+  std::vector<SpinSystem> chunk_sys;
+  if (sched) {
+    SpinSystem su = sys;
+    std::vector<std::string> isos;
+    for (const auto &rc : p.rf_chunks)
+      if (rc.field.amp != 0.0 && std::find(isos.begin(), isos.end(), rc.field.iso) == isos.end())
+        isos.push_back(rc.field.iso);
+    for (const auto &iso : isos) su.add_rf(RfField{iso, 1.2345, 0.0, 0.0});
+    J.L = su.layout();
+    for (int kc = 0; kc < J.pb; ++kc) {
+      chunk_sys.push_back(sys);
+      for (const auto &rc : p.rf_chunks)
+        if (rc.chunk == kc) chunk_sys.back().add_rf(rc.field);
+    }
+  } else {
+    J.L = sys.layout();
+  }
   const BlockLayout &L = J.L;
   if (L.max_block > kMaxHugeBlock)
     throw Error(5, "Hamiltonian block of size " + std::to_string(L.max_block) + " exceeds this engine's limit of " +
@@ -1898,17 +1958,24 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         break;
       }
   // rf phases: the engine propagates the real H' = R^H H R, so rho and det enter as R^H X R
-  const CMatrix ro = sys.to_frame(ro_in), det = sys.to_frame(det_in);
+  // (under an rf schedule each step's U is turned back into the lab frame instead)
+  const CMatrix ro = sched ? ro_in : sys.to_frame(ro_in), det = sched ? det_in : sys.to_frame(det_in);
   if (J.is_static) J.rosym = 0;  // the static FID always transforms rho itself
   // Hamiltonian terms, packed per block
-  std::vector<double> pas, isc, Tk, Hc(L.S2, 0.0);
+  const int nhc = sched ? J.pb : 1;
+  std::vector<double> pas, isc, Tk, Hc(size_t(L.S2) * nhc, 0.0);
   auto pack = [&](const std::vector<double> &M, double *dst) {
     for (int k = 0; k < nb; ++k)
       for (int r = 0; r < L.size[k]; ++r)
         for (int q = 0; q < L.size[k]; ++q)
           dst[L.poff[k] + r * L.size[k] + q] = M[size_t(L.perm[L.off[k] + r]) * N + L.perm[L.off[k] + q]];
   };
-  if (!g_sizing) pack(sys.h_const(), Hc.data());  // planning needs only the counts
+  if (!g_sizing) {  // planning needs only the counts
+    if (sched)
+      for (int kc = 0; kc < J.pb; ++kc) pack(chunk_sys[kc].h_const(), Hc.data() + size_t(kc) * L.S2);
+    else
+      pack(sys.h_const(), Hc.data());
+  }
   // orientation-dependent terms: kind 0 = scale (M PAS' M^T)_22 T; a quadrupole in a field
   // adds kind 1 = s2 ((r00-r11)^2/4 + r01^2) c4 and kind 2 = -s2 (r02^2 + r12^2) c2 with
   // s2 = Qp^2/(B nu_rel), r = M PAS' M^T (qua.cc:219-267: order 1 or |B| <= 1e-12 first order
@@ -2082,7 +2149,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     for (int r = 0; r < b; ++r) {
       double rs = 0;
       for (int q = 0; q < b; ++q) {
-        double v = std::fabs(Hc[bp + r * b + q]);
+        double v = 0;  // the largest constant part over the chunks of an rf schedule
+        for (int kc = 0; kc < nhc; ++kc) v = std::max(v, std::fabs(Hc[size_t(kc) * L.S2 + bp + r * b + q]));
         for (int kk = 0; kk < J.nint; ++kk) {
           const double *Pa = pas.data() + 6 * kk;
           const double fro = std::sqrt(Pa[0] * Pa[0] + Pa[3] * Pa[3] + Pa[5] * Pa[5] +
@@ -2203,6 +2271,19 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.huge_pairs[t].rp = J.big_rp.p + J.huge_rp_off[t], J.huge_pairs[t].ci = J.big_ci.p,
     J.huge_pairs[t].cv = J.big_cv.p;
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
+  if (sched) {  // per chunk: the rf frame of each permuted index (1 where a chunk has none)
+    bool any = false;
+    for (const auto &cs : chunk_sys) any = any || !cs.frame().empty();
+    if (any) {
+      std::vector<double2> fr(size_t(J.pb) * N, make_double2(1.0, 0.0));
+      for (int kc = 0; kc < J.pb; ++kc) {
+        const auto &f = chunk_sys[kc].frame();
+        if (f.empty()) continue;
+        for (int x = 0; x < N; ++x) fr[size_t(kc) * N + x] = make_double2(f[L.perm[x]].real(), f[L.perm[x]].imag());
+      }
+      J.frames.upload(fr, st);
+    }
+  }
   J.ikind.upload(ikind, st);
   J.Dblk.upload(Dblk, st), J.Rhoblk.upload(Rhoblk, st);
   J.status.upload(std::vector<int>(1, 0), st);
@@ -2339,6 +2420,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.bs = J.bs.p, s.boff = J.boff.p, s.bpoff = J.bpoff.p;
   s.pas = J.pas.p, s.iscale = J.iscale.p, s.Tk = J.Tk.p, s.Hc = J.Hc.p;
   s.fk = use_fk ? J.fkc.p : nullptr;
+  s.hc_chunks = sched ? J.pb : 0;
+  s.frames = J.frames.n ? J.frames.p : nullptr;
   s.ikind = J.ikind.p, s.has2 = J.has2;
   s.npq = J.npq, s.npr = J.npr;
   s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
@@ -2439,7 +2522,7 @@ static void huge_step(JobImpl &J, DevSys &s, size_t kh) {
       ++J.launches;
     };
     k_huge_fk<<<unsigned((items + 127) / 128), 128, 0, st>>>(s, j0, items, J.hfk.p);
-    k_huge_hbuild<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, bp, b, J.hfk.p, ws);
+    k_huge_hbuild<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, bp, b, J.hfk.p, ws, j0);
     CUDA_OK(cudaMemsetAsync(J.hsqmax.p, 0, sizeof(int), st));
     k_huge_norm<<<unsigned(items), 256, 0, st>>>(ws, b, s.tau * kPi2, J.hsc.p, J.hsq.p, J.hsqmax.p);
     J.launches += 3;
@@ -2464,7 +2547,7 @@ static void huge_step(JobImpl &J, DevSys &s, size_t kh) {
       k_huge_sqcomb<<<dim3(ge, unsigned(items)), 256, 0, st>>>(ws, b, J.hsq.p, t);
       ++J.launches;
     }
-    k_huge_store_u<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, ws, bp, b, j0);
+    k_huge_store_u<<<dim3(ge, unsigned(items)), 256, 0, st>>>(s, ws, bp, J.L.off[k], b, j0);
     ++J.launches;
   }
 }

@@ -24,6 +24,14 @@ struct FidParams {
   // (wr == 0 or rotor angle 0): one step of 1/sw per point.
   int p2p_base = 0, p2p_factor = 0;
   double maxtstep = 0;
+  // rf that changes within the rotor period (point-to-point only): each field is on during
+  // one chunk (0 <= chunk < p2p_base; base and factor are then not reduced by their gcd),
+  // on top of the system's continuous rf; the pattern repeats every rotor period
+  struct RfChunk {
+    int chunk;
+    RfField field;
+  };
+  std::vector<RfChunk> rf_chunks;
 };
 
 struct Context {

@@ -180,11 +180,11 @@ __global__ void k_huge_fk(DevSys s, long j0, int items, double *fk) {
 }
 
 // X = H of block (bp, b): slot 0 of item blockIdx.y.
-__global__ void k_huge_hbuild(DevSys s, int bp, int b, const double *fk, double *ws) {
+__global__ void k_huge_hbuild(DevSys s, int bp, int b, const double *fk, double *ws, long j0) {
   const long bb = long(b) * b, e = long(blockIdx.x) * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (e >= bb) return;
-  double h = s.Hc[bp + e];
+  double h = hc_of(s, int((j0 + j) / s.C))[bp + e];
   const double *f = fk + long(j) * s.nint;
   for (int kk = 0; kk < s.nint; ++kk) {
     const double t = s.Tk[size_t(kk) * s.S2 + bp + e];
@@ -244,14 +244,17 @@ __global__ void k_huge_sqcomb(double *ws, int b, const int *sq, int round) {
 }
 
 // U block (bp, b) of item g = j0 + blockIdx.y = R + i I (slots 6 and 1).
-__global__ void k_huge_store_u(DevSys s, const double *ws, int bp, int b, long j0) {
+__global__ void k_huge_store_u(DevSys s, const double *ws, int bp, int bo, int b, long j0) {
   const long bb = long(b) * b, e = long(blockIdx.x) * blockDim.x + threadIdx.x;
   const int j = blockIdx.y;
   if (e >= bb) return;
   const long g = j0 + j;
   const int c = int(g % s.C), i = int(g / s.C);
   const double *base = ws + long(j) * kHugeSlots * bb;
-  s.U[(size_t(i) * s.S2 + bp + e) * s.Cpad + c] = cmk(base[6 * bb + e], base[bb + e]);
+  double2 u = cmk(base[6 * bb + e], base[bb + e]);
+  const double2 *fr = frame_of(s, i);
+  if (fr) u = cmul(cmul(fr[bo + e / b], u), cconj(fr[bo + e % b]));  // lab frame: U = R U' R^H
+  s.U[(size_t(i) * s.S2 + bp + e) * s.Cpad + c] = u;
 }
 
 // A_1 = U_0 for block (bp, b), crystallite blockIdx.y.

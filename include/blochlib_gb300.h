@@ -136,7 +136,17 @@ bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
  * start_t + p*factor/(base*wr) and
  *   fid[p] = sum_c w_c Tr(U_c(t_p) rho U_c(t_p)^H det) / Tr(det det^H).
  * base and factor are divided by their gcd.  Static (wr == 0 or rotor angle 0): one step of
- * 1/sw per point.  *sw_out = base*wr/factor (sw when static). */
+ * 1/sw per point.  *sw_out = base*wr/factor (sw when static).
+ * rf within the rotor period (windowed or phase-cycled trains, solid-2.0's pulse term per
+ * chunk, propogation.cc:246-296 with pulsedata.cc:110-125): each bl_rf_chunk is on during
+ * one chunk of every period, on top of bl_system_add_rf's continuous fields; base and factor
+ * are then taken as given (no gcd reduction). */
+typedef struct {
+  int chunk;          /* 0 .. base-1 */
+  const char *iso;    /* isotope irradiated */
+  double amp_hz, phase_deg, offset_hz;
+} bl_rf_chunk;
+
 typedef struct {
   int npts;        /* FID points */
   double sw;       /* static only: sweep width, Hz (dwell 1/sw) */
@@ -148,6 +158,8 @@ typedef struct {
   int base;        /* chunks per rotor period (PropReduce 'base') */
   int factor;      /* chunks per dwell (PropReduce 'factor') */
   double maxtstep; /* longest step inside a chunk, s (<= 0: one step per chunk) */
+  const bl_rf_chunk *rf; /* rf schedule (may be NULL) */
+  int nrf;               /* its length */
 } bl_p2p_params;
 
 bl_status bl_p2p_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,

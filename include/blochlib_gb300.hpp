@@ -213,9 +213,18 @@ class oneFID {
   }
   // Point-to-point FID every red.factor/red.base rotor periods, steps of at most maxtstep
   // (bl_p2p_fid); sw becomes base*wr/factor.
+  // rf fields on during one chunk of every rotor period (base and factor then as given)
+  struct RfChunk {
+    int chunk;
+    std::string iso;
+    double amp, phase_deg, offset;
+  };
   std::vector<complex> p2pFID(powder &pw, const matrix &ro, const matrix &det, const PropReduce &red,
-                              double maxtstep = 0) {
-    bl_p2p_params p = {npts_, sw_, wr_, rotb_, startT_, 0, /*Taylor step*/ 1, red.base, red.factor, maxtstep};
+                              double maxtstep = 0, const std::vector<RfChunk> &rf = {}) {
+    std::vector<bl_rf_chunk> sched;
+    for (const auto &r : rf) sched.push_back({r.chunk, r.iso.c_str(), r.amp, r.phase_deg, r.offset});
+    bl_p2p_params p = {npts_, sw_, wr_, rotb_, startT_, 0, /*Taylor step*/ 1, red.base, red.factor, maxtstep,
+                       sched.empty() ? nullptr : sched.data(), int(sched.size())};
     std::vector<complex> fid(static_cast<size_t>(npts_));
     double sw_used = sw_;
     check(bl_p2p_fid(Context::get(), sys_->handle(), pw.handle(), ro.data(), det.data(), &p,

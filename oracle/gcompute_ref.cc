@@ -457,6 +457,20 @@ System parse_system(const std::vector<std::string> &lines) {
 }
 
 // H(t1,t2,wr) at rotor phase alpha (sys.cc:749-770) for crystal orientation Rp.
+// rf: amp (Ix cos phase + Iy sin phase) + offset Iz on every spin of the isotope, nothing
+// when amp == 0 (examples/solid-2.0/src/pulsedata.cc:110-125; phase in degrees, 215)
+void add_rf(const System &S, const std::vector<System::Rf> &fields, CMat &H) {
+  for (const auto &f : fields) {
+    if (f.amp == 0.0) continue;
+    const double ph = f.phase_deg * kDeg2Rad;
+    for (int sp = 0; sp < S.nspin; ++sp) {
+      if (S.iso[sp] != f.iso) continue;
+      for (size_t e = 0; e < H.a.size(); ++e)
+        H.a[e] += f.amp * (S.Ix[sp].a[e] * std::cos(ph) + S.Iy[sp].a[e] * std::sin(ph)) + f.offset * S.Iz[sp].a[e];
+    }
+  }
+}
+
 CMat hamiltonian(const System &S, const double Rp[3][3], double alpha, double rotb) {
   CMat H(S.N);
   double Rr[3][3], M[3][3];
@@ -527,17 +541,7 @@ CMat hamiltonian(const System &S, const double Rp[3][3], double alpha, double ro
       }
     }
   }
-  // rf: amp (Ix cos phase + Iy sin phase) + offset Iz on every spin of the isotope, nothing
-  // when amp == 0 (examples/solid-2.0/src/pulsedata.cc:110-125; phase in degrees, 215)
-  for (const auto &f : S.rf) {
-    if (f.amp == 0.0) continue;
-    const double ph = f.phase_deg * kDeg2Rad;
-    for (int sp = 0; sp < S.nspin; ++sp) {
-      if (S.iso[sp] != f.iso) continue;
-      for (size_t e = 0; e < H.a.size(); ++e)
-        H.a[e] += f.amp * (S.Ix[sp].a[e] * std::cos(ph) + S.Iy[sp].a[e] * std::sin(ph)) + f.offset * S.Iz[sp].a[e];
-    }
-  }
+  add_rf(S, S.rf, H);
   return H;
 }
 
@@ -715,6 +719,7 @@ struct Job {
   int p2p_base = 0, p2p_factor = 0;  // point-to-point FID when p2p_base > 0
   double maxtstep = 0;
   std::vector<System::Rf> rf;
+  std::vector<std::pair<int, System::Rf>> rfc;  // rf on during one chunk of the period (p2p)
 };
 
 Job parse_job(const std::string &text) {
@@ -739,7 +744,13 @@ Job parse_job(const std::string &text) {
     else if (key == "bfield") J.bfield = std::atof(val.c_str());
     else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &J.p2p_base, &J.p2p_factor);
     else if (key == "maxtstep") J.maxtstep = std::atof(val.c_str());
-    else if (key == "rf") {
+    else if (key == "rfc") {
+      auto t = tokens(val);
+      if (t.size() < 3) throw std::runtime_error("rfc: <chunk> <iso> <amp> [phase_deg] [offset]");
+      J.rfc.push_back({std::atoi(t[0].c_str()),
+                       {t[1], std::atof(t[2].c_str()), t.size() > 3 ? std::atof(t[3].c_str()) : 0.0,
+                        t.size() > 4 ? std::atof(t[4].c_str()) : 0.0}});
+    } else if (key == "rf") {
       auto t = tokens(val);
       if (t.size() < 2) throw std::runtime_error("rf: <iso> <amp> [phase_deg] [offset]");
       J.rf.push_back({t[0], std::atof(t[1].c_str()), t.size() > 2 ? std::atof(t[2].c_str()) : 0.0,
@@ -828,6 +839,7 @@ std::vector<cplx> single_p2p_fid(const System &S, const Job &J, double theta, do
     u = v, v = t;
   }
   int b = J.p2p_base / u, f = J.p2p_factor / u;
+  if (!J.rfc.empty()) b = J.p2p_base, f = J.p2p_factor;  // the schedule's own chunks
   double Rp[3][3];
   rot3(phi, theta, gamma, Rp);
   const double rotb = P.rotb * kDeg2Rad;
@@ -848,7 +860,10 @@ std::vector<cplx> single_p2p_fid(const System &S, const Job &J, double theta, do
       for (int j = 0; j < sub; ++j) {
         double t1 = P.startT + double(k * sub + j) * tau;
         double tmid = t1 + tau / 2.0;
-        U[k] = mul(step_prop(hamiltonian(S, Rp, tmid * P.wr * kPi2, rotb), tau), U[k]);
+        CMat H = hamiltonian(S, Rp, tmid * P.wr * kPi2, rotb);
+        for (const auto &rc : J.rfc)
+          if (rc.first == k) add_rf(S, {rc.second}, H);
+        U[k] = mul(step_prop(H, tau), U[k]);
       }
     }
     for (int k = 0; k < b; ++k) {

@@ -25,6 +25,8 @@
 //           angles of 'hamgen_angles: <theta> <phi> <gamma>' (radians, default 0 0 0))
 //   rf: <iso> <amp Hz> [phase deg] [offset Hz]   (repeatable: continuous rf during the FID,
 //           added to SolidSys::Hamiltonian by RfSys below, as solid-2.0's PulseData::Pulse)
+//   rfc: <chunk> <iso> <amp Hz> [phase deg] [offset Hz]   (p2p only, repeatable: rf on during
+//           one chunk of every rotor period; base and factor are then used as given)
 //   p2p: <base> <factor>   maxtstep: <s>   (point-to-point FID instead of oneFID::FID: see
 //           p2p_fid below; a rotor period in 'base' chunks of ceil(chunk/maxtstep) steps,
 //           a point every 'factor' chunks)
@@ -147,16 +149,27 @@ class RfSys {
 // factor; otherwise the direct products of the same chunks), rho stepped as A rho A^H
 // and trace(rho, det)/trace(det, adjoint(det)) summed per point with the powder weight
 // (sequencerun_funcs.cc:624-645).  Static (wr == 0 or rotor angle 0): one Mexp of 1/sw.
-static Vector<complex> p2p_fid(SolidSys &sys, RfSys &hs, powder &pw, matrix &ro, matrix &det, int npts, double sw,
-                               double wr, double rotb, double start, int base, int factor, double maxtstep,
-                               double &sw_out) {
+static Vector<complex> p2p_fid(SolidSys &sys, RfSys &hs, const std::vector<RfSpec> &rf,
+                               const std::vector<std::pair<int, RfSpec> > &rfc, powder &pw, matrix &ro, matrix &det,
+                               int npts, double sw, double wr, double rotb, double start, int base, int factor,
+                               double maxtstep, double &sw_out) {
   PropReduce red(base, factor);  // divides base and factor by their gcd (propreduce.cc:16-33)
-  const int b = red.base, f = red.factor;
+  const int b = rfc.empty() ? red.base : base, f = rfc.empty() ? red.factor : factor;
+  // per chunk: the continuous fields plus the chunk's own (solid-2.0's pulse list, one pulse
+  // per chunk, propogation.cc:246-296)
+  std::vector<RfSys *> hk;
+  if (!rfc.empty())
+    for (int k = 0; k < b; ++k) {
+      std::vector<RfSpec> fk = rf;
+      for (size_t j = 0; j < rfc.size(); ++j)
+        if (rfc[j].first == k) fk.push_back(rfc[j].second);
+      hk.push_back(new RfSys(sys, fk));
+    }
   // PropReduce::reduce terminates only for base < factor: setParams sizes BackRed to base-1
   // but fills min(base, factor)-1 entries, and an empty entry matches every sequence in
   // iteration(), so backReduce's while loop never ends when base > factor.  There (and for
   // base == 1) the dwell products are formed directly, in the same order.
-  const bool use_red = b > 1 && b < f;
+  const bool use_red = b > 1 && b < f && rfc.empty();
   if (use_red) red.reduce();
   const bool stat = wr == 0.0 || rotb == 0.0;
   Vector<complex> fid(npts, complex(0, 0));
@@ -183,7 +196,8 @@ static Vector<complex> p2p_fid(SolidSys &sys, RfSys &hs, powder &pw, matrix &ro,
         U[k] = sys.Fe();
         for (int j = 0; j < sub; ++j) {
           double t1 = start + double(k * sub + j) * tau;
-          U[k] = Mexp(hs.Hamiltonian(t1, t1 + tau, wr), -complexi * tau * PI2) * U[k];
+          RfSys &h = rfc.empty() ? hs : *hk[k];
+          U[k] = Mexp(h.Hamiltonian(t1, t1 + tau, wr), -complexi * tau * PI2) * U[k];
         }
       }
       W.resize(b);
@@ -210,6 +224,7 @@ static Vector<complex> p2p_fid(SolidSys &sys, RfSys &hs, powder &pw, matrix &ro,
     }
     ++it;
   }
+  for (size_t k = 0; k < hk.size(); ++k) delete hk[k];
   return fid;
 }
 
@@ -225,6 +240,7 @@ int main(int argc, char **argv) {
   int npts = 0, zcw_t = 0, zcw_p = 0;
   double sw = 0, wr = 0, rotb = 0, start = 0, bfield = 0, maxtstep = 0;
   std::vector<RfSpec> rf;
+  std::vector<std::pair<int, RfSpec> > rfc;
   int p2p_base = 0, p2p_factor = 0;
   std::vector<std::string> hamgen;
   double hg_theta = 0, hg_phi = 0, hg_gamma = 0;
@@ -250,7 +266,14 @@ int main(int argc, char **argv) {
     else if (key == "p2p") std::sscanf(val.c_str(), "%d %d", &p2p_base, &p2p_factor);
     else if (key == "maxtstep") maxtstep = std::atof(val.c_str());
     else if (key == "hamgen") hamgen.push_back(val);
-    else if (key == "rf") {
+    else if (key == "rfc") {
+      RfSpec r = {"", 0, 0, 0};
+      char iso[32] = {0};
+      int ch = -1;
+      std::sscanf(val.c_str(), "%d %31s %lf %lf %lf", &ch, iso, &r.amp, &r.phase_deg, &r.offset);
+      r.iso = iso;
+      rfc.push_back(std::make_pair(ch, r));
+    } else if (key == "rf") {
       RfSpec r = {"", 0, 0, 0};
       char iso[32] = {0};
       std::sscanf(val.c_str(), "%31s %lf %lf %lf", iso, &r.amp, &r.phase_deg, &r.offset);
@@ -298,7 +321,7 @@ int main(int argc, char **argv) {
   double sw_out = sw;
   RfSys hs(sys, rf);
   if (p2p_base > 0) {
-    fid = p2p_fid(sys, hs, pw, ro, det, npts, sw, wr, rotb, start, p2p_base, p2p_factor, maxtstep, sw_out);
+    fid = p2p_fid(sys, hs, rf, rfc, pw, ro, det, npts, sw, wr, rotb, start, p2p_base, p2p_factor, maxtstep, sw_out);
   } else if (!rf.empty()) {
     oneFID<RfSys> driver(hs, npts, sw, wr, rotb, start);
     fid = driver.FID(pw, ro, det);

@@ -292,16 +292,45 @@ def rf_cases():
         yield name, W.job_text(cfg) + "rf: 1H 40000 0 0\n", powder_rows(c0["powder"], (spread(1154, ncry) + 500) % 1154)
 
 
+def rfc_cases():
+    """rf that changes within the rotor period, point-to-point form (ref_harness 'rfc:': one
+    pulse term per chunk, on top of the continuous fields; base and factor as given)."""
+    c0 = W.config(0)
+    het3 = ["numspin 3", "T 13C 0", "T 1H 1", "T 1H 2", "C 900 7000 0.6 0 33 44 55", "D 9000 0 1 10 20 30",
+            "D 7000 0 2 40 50 60", "D -20000 1 2 70 80 0"]
+    q2 = ["numspin 2", "T 2H 0", "T 1H 1", "C 300 2500 0.4 1 10 40 70", "D 3000 0 1 60 80 0",
+          "Q 160000 0.3 0 30 60 90"]
+    base = dict(lines=het3, rho="Ix 0", det="Ip 0", npts=128, wr=10000.0, sw=0.0, rotb=W.MAGIC_ANGLE)
+    cases = [
+        ("p2p_rfc_window_9_7", base, "p2p: 9 7\nmaxtstep: 3e-06\n" + "".join(f"rfc: {k} 1H 80000 0 0\n" for k in range(5))),
+        ("p2p_rfc_phase_cycle_4_1", base, "p2p: 4 1\nmaxtstep: 5e-06\n" + "".join(f"rfc: {k} 1H 50000 {90 * k} 0\n" for k in range(4))),
+        ("p2p_rfc_cw13c_45deg_5_3", base, "p2p: 5 3\nmaxtstep: 4e-06\nrf: 13C 20000 0 300\n"
+                                           "rfc: 1 1H 60000 45 1000\nrfc: 3 1H 60000 225 1000\n"),
+        ("p2p_rfc_noncoprime_6_4", base, "p2p: 6 4\nmaxtstep: 4e-06\nrfc: 1 1H 70000 30 0\nrfc: 4 1H 70000 30 0\n"),
+        ("p2p_rfc_quad2_4_3", dict(base, lines=q2, rho="Fx", det="Fp", wr=20000.0),
+         "p2p: 4 3\nmaxtstep: 2e-06\nbfield: 200000\nrfc: 0 2H 40000 60 0\nrfc: 2 2H 40000 -60 0\n"),
+    ]
+    for name, cfg, extra in cases:
+        yield name, W.job_text(cfg) + extra, powder_rows(c0["powder"], (spread(1154, 5) + 71) % 1154)
+    rng = np.random.default_rng(W.SEED0 + 77)
+    xyz = W._proton_cluster(rng, 5, 5.0, min_sep=1.5)
+    lines = ["numspin 5"] + [f"T 1H {k}" for k in range(5)] + W._csa_lines(rng, 5) + W._dipole_lines(xyz)
+    cfg = dict(lines=lines, rho="Fx", det="Fp", npts=64, wr=25000.0, sw=0.0, rotb=W.MAGIC_ANGLE)
+    yield ("p2p_rfc_big_5h_3_2", W.job_text(cfg) + "p2p: 3 2\nmaxtstep: 3e-06\nrfc: 0 1H 50000 0 0\nrfc: 2 1H 50000 90 0\n",
+           powder_rows(c0["powder"], spread(1154, 2)))
+
+
 def main():
     if "--hamgen" in sys.argv:
         hamgen_fixtures()
         return
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")
-    if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p", "--rf")):
+    if any(a in sys.argv for a in ("--big", "--huge", "--quad2", "--p2p", "--rf", "--rfc")):
         man = json.loads((OUT / "manifest.json").read_text())
         extra = (huge_cases() if "--huge" in sys.argv else quad2_cases() if "--quad2" in sys.argv
-                 else p2p_cases() if "--p2p" in sys.argv else rf_cases() if "--rf" in sys.argv else big_cases())
+                 else p2p_cases() if "--p2p" in sys.argv else rf_cases() if "--rf" in sys.argv
+                 else rfc_cases() if "--rfc" in sys.argv else big_cases())
         for name, job, rows in extra:
             sw64, f64 = run_ref(BIN64, job, rows)
             np.savez_compressed(OUT / f"{name}.npz", job=np.array(job), powder=rows, fid64=f64, fid32=f64 * 0,

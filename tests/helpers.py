@@ -65,9 +65,16 @@ def gpu_fid(job_text, rows, ctx=None, return_sw=False, step_method=None, fave_me
     drv = bl.oneFID(sys_, int(kv["npts"]), float(kv["sw"]), float(kv["wr"]), float(kv["rotb"]),
                     float(kv.get("start", 0.0)), precision=precision, ctx=ctx, step_method=step_method,
                     fave_method=fave_method)
-    if "p2p" in kv:  # point-to-point FID (bl_p2p_fid)
+    if "p2p" in kv:  # point-to-point FID (bl_p2p_fid), with its rf schedule if any
         base, factor = (int(x) for x in kv["p2p"].split())
-        fid = drv.p2pFID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]), base, factor, float(kv.get("maxtstep", 0.0)))
+        sched = []
+        for line in str(job_text).splitlines():
+            if line.startswith("rfc:"):
+                t = line[4:].split()
+                sched.append((int(t[0]), t[1], float(t[2]), float(t[3]) if len(t) > 3 else 0.0,
+                              float(t[4]) if len(t) > 4 else 0.0))
+        fid = drv.p2pFID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]), base, factor, float(kv.get("maxtstep", 0.0)),
+                         rf_chunks=sched)
     else:
         fid = drv.FID(pw, sys_.op(kv["rho"]), sys_.op(kv["det"]))
     return (fid, drv.sw) if return_sw else fid

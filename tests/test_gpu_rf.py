@@ -84,3 +84,36 @@ def test_rf_joins_blocks():
     s2 = bl.SolidSys(["numspin 2", "T 1H 0", "T 13C 1"])
     s2.addRf("1H", 0.0, 90.0, 5000.0)  # amp 0: nothing at all, the offset included
     assert sorted(s2.blocks()) == [1, 1, 1, 1]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["eigh", "taylor"])
+@pytest.mark.parametrize("seed", range(10))
+def test_rf_schedule_random_systems_match_oracle(seed, method):
+    """rf changing within the rotor period (p2p): random chunk schedules of 1-3 fields with
+    any phase, on top of random continuous fields, against the oracle."""
+    rng = np.random.default_rng(1700 + seed)
+    job, rows = random_system(seed)
+    if seed % 2:
+        job = with_rf(job, rng, nfields=1)
+    lines, kv = parse_job(job)
+    isos = sorted({l.split()[1] for l in lines if l.startswith("T ")})
+    b, f = int(rng.integers(2, 7)), int(rng.integers(1, 7))
+    job += f"p2p: {b} {f}\nmaxtstep: {0.4 / (float(kv['wr']) * b)!r}\n"
+    for _ in range(int(rng.integers(1, 4))):
+        job += (f"rfc: {int(rng.integers(0, b))} {rng.choice(isos)} {rng.uniform(1e4, 9e4):.9g} "
+                f"{rng.uniform(0, 360):.9g} {rng.uniform(-3e3, 3e3):.9g}\n")
+    if strong_hetero_j(job):
+        pytest.skip("off-x phases with a strong heteronuclear J: refused")
+    ref, sw = oracle_fid(job, rows)
+    fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
+    assert sw_g == sw
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
+@pytest.mark.gpu
+def test_rf_schedule_needs_p2p():
+    s = bl.SolidSys(["numspin 2", "T 13C 0", "T 1H 1", "D 5000 0 1 0 30 0"])
+    with pytest.raises(bl.BlochError, match="needs spinning"):  # the static branch takes no schedule
+        bl.Job.p2p(s, bl.powder(bl.powder.zcw, 21, 8), s.op("Ix 0"), s.op("Ip 0"), 16, 0.0, 54.7356, 3, 2,
+                   sw=1e5, rf_chunks=[(0, "1H", 5e4, 0.0, 0.0)])
