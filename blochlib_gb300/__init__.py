@@ -58,6 +58,7 @@ _SIGS = {
     "bl_powder_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
     "bl_p2p_fid": (ctypes.c_int, [ctypes.c_void_p] * 8),
+    "bl_server_submit_p2p": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_longlong)]),
     "bl_hamgen": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "bl_p2p_job_create": (ctypes.c_int, [ctypes.c_void_p] * 6 + [ctypes.POINTER(ctypes.c_void_p)]),
@@ -568,6 +569,21 @@ class Server:
                       _step_method(step_method), _fave_method(fave_method))
         t = ctypes.c_longlong()
         _check(load().bl_server_submit(self._h, sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(p), ctypes.byref(t)))
+        self._npts[t.value] = int(npts)
+        return t.value
+
+    def submit_p2p(self, sys, pw, ro, det, npts, wr, rotb, base, factor, maxtstep=0.0, sw=0.0, start_t=0.0,
+                   precision=0, step_method=None, rf_chunks=None):
+        """A point-to-point FID request (bl_server_submit_p2p; see oneFID.p2pFID)."""
+        n = sys.dim()
+        ro, det = _cmat(ro, n), _cmat(det, n)
+        rf, nrf = _rf_schedule(rf_chunks)
+        p = P2PParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
+                      _step_method(step_method), int(base), int(factor), float(maxtstep),
+                      ctypes.cast(rf, ctypes.c_void_p), nrf)
+        t = ctypes.c_longlong()
+        _check(load().bl_server_submit_p2p(self._h, sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(p),
+                                           ctypes.byref(t)))
         self._npts[t.value] = int(npts)
         return t.value
 

@@ -442,6 +442,16 @@ bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder
   });
 }
 
+bl_status bl_server_submit_p2p(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
+                               const double *det, const bl_p2p_params *params, long long *ticket) {
+  if (!srv || !sys || !pw || !ro || !det || !params || !ticket) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] {
+    int N = sys->s().dim();
+    if (params->npts <= 0) throw bl::Error(BL_ERR_INVALID, "npts must be positive");
+    *ticket = srv->s->submit(sys->sp, pw->p, load_op(ro, N), load_op(det, N), to_params(params));
+  });
+}
+
 bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *fid_out, double *sw_out,
                          double *latency_ms) {
   if (!srv || !state) return fail(BL_ERR_INVALID, "null argument");

@@ -240,6 +240,9 @@ bl_status bl_server_create(int device, int lanes, size_t pool_bytes, bl_server *
 void bl_server_destroy(bl_server *srv);  /* waits for running jobs */
 bl_status bl_server_submit(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
                            const double *det, const bl_fid_params *params, long long *ticket);
+/* The same for a point-to-point FID (bl_p2p_fid's parameters, rf schedule included). */
+bl_status bl_server_submit_p2p(bl_server *srv, const bl_system *sys, const bl_powder *pw, const double *ro,
+                               const double *det, const bl_p2p_params *params, long long *ticket);
 /* *state as above.  When the job is done (or failed/cancelled) and fid_out is non-NULL, the
  * FID (2*npts doubles) is copied and the ticket is released.  latency_ms: submit to done. */
 bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *fid_out, double *sw_out,

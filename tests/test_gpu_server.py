@@ -87,3 +87,21 @@ def test_admission_waits_for_memory():
     for t in tickets:
         np.testing.assert_array_equal(res[t][1], direct)
     srv.close()
+
+
+def test_point_to_point_requests_are_served():
+    """A point-to-point request (with an rf schedule) through the serving loop, among ordinary
+    ones, gives the direct p2pFID result bit for bit."""
+    srv = bl.Server(0, lanes=4, pool_bytes=8 << 30)
+    j = _job(W.config(1), 192)
+    sched = [(0, "1H", 60000.0, 0.0, 0.0), (2, "1H", 60000.0, 90.0, 500.0)]
+    args = dict(sys=j["sys"], pw=j["pw"], ro=j["ro"], det=j["det"], npts=300, wr=j["wr"], rotb=j["rotb"],
+                base=4, factor=3, maxtstep=3e-6, rf_chunks=sched)
+    others = [srv.submit(**_job(W.config(3, i), 64)) for i in range(6)]
+    t = srv.submit_p2p(**args)
+    res = _wait(srv, others + [t])
+    assert all(r[0] == srv.DONE for r in res.values())
+    direct = bl.oneFID(j["sys"], 300, 0.0, j["wr"], j["rotb"]).p2pFID(j["pw"], j["ro"], j["det"], 4, 3, 3e-6,
+                                                                      rf_chunks=sched)
+    np.testing.assert_array_equal(res[t][1], direct)
+    srv.close()
