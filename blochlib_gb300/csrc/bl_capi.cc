@@ -3,6 +3,7 @@
 
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 
 #include "../../include/blochlib_gb300.h"
@@ -13,6 +14,14 @@
 
 struct bl_ctx {
   bl::Context c;
+  // device memory that bl_powder_fid / bl_p2p_fid carve their work buffers from, kept between
+  // calls (grown when a job needs more): no cudaMalloc / cudaFree per call once it fits
+  std::mutex mu;
+  void *region = nullptr;
+  size_t region_bytes = 0;
+  ~bl_ctx() {
+    if (region) cudaFree(region);
+  }
 };
 struct bl_system {
   // shared, so that a serving request keeps the system alive without copying its operators
@@ -82,6 +91,9 @@ bl::FidParams to_params(const bl_p2p_params *p) {
 }  // namespace
 
 extern "C" {
+
+static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder &pw, const bl::CMatrix &ro,
+                          const bl::CMatrix &det, const bl::FidParams &p, double *fid_out, double *sw_out);
 
 const char *bl_last_error(void) { return g_err.c_str(); }
 const char *bl_version(void) { return "blochlib_gb300 0.1 (sm_103a, FP64 gamma-COMPUTE)"; }
@@ -232,6 +244,13 @@ bl_status bl_p2p_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *
 bl_status bl_p2p_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
                      const bl_p2p_params *params, double *fid_out, double *sw_out) {
   if (!fid_out) return fail(BL_ERR_INVALID, "null output");
+  if (!ctx || !sys || !pw || !ro || !det || !params) return fail(BL_ERR_INVALID, "null argument");
+  bool done = false;
+  const bl_status st0 = guarded([&] {
+    const int N = sys->s().dim();
+    done = fid_in_region(ctx, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out, sw_out);
+  });
+  if (st0 != BL_OK || done) return st0;
   bl_job *job = nullptr;
   bl_status st = bl_p2p_job_create(ctx, sys, pw, ro, det, params, &job);
   if (st != BL_OK) return st;
@@ -320,9 +339,59 @@ bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops) {
   return guarded([&] { *tflops = bl::probe_fp64_tflops(ctx->c); });
 }
 
+// One FID with the job in the context's region when the whole powder fits one batch of the
+// budget (the layout and results of a freshly allocated job; the region is reused by the next
+// call).  Returns false, having done nothing, when it does not fit: the caller then runs a
+// job of its own (batched by the budget).
+static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder &pw, const bl::CMatrix &ro,
+                          const bl::CMatrix &det, const bl::FidParams &p, double *fid_out, double *sw_out) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  size_t lo = 0, full = 0;
+  bl::job_bytes(ctx->c.device, s, pw, ro, det, p, &lo, &full);
+  if (cudaSetDevice(ctx->c.device) != cudaSuccess) return false;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return false;
+  const size_t budget = ctx->c.hbm_budget ? ctx->c.hbm_budget : size_t(0.6 * double(fr + ctx->region_bytes));
+  if (full > budget) return false;
+  if (full > ctx->region_bytes) {
+    if (ctx->region) cudaFree(ctx->region);
+    ctx->region = nullptr, ctx->region_bytes = 0;
+    if (cudaMalloc(&ctx->region, full) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->region = nullptr;
+      return false;
+    }
+    ctx->region_bytes = full;
+  }
+  const size_t saved = ctx->c.hbm_budget;  // job_in_region sets the budget of the region
+  struct Restore {
+    bl::Context &c;
+    size_t v;
+    ~Restore() { c.hbm_budget = v; }
+  } restore{ctx->c, saved};
+  std::unique_ptr<bl::Job> job;
+  try {
+    job = bl::job_in_region(ctx->c, ctx->region, ctx->region_bytes, s, pw, ro, det, p);
+  } catch (const bl::Error &e) {
+    if (e.code == BL_ERR_NOMEM) return false;  // more than the planned bytes: a job of its own
+    throw;
+  }
+  job->run();
+  job->read(fid_out);
+  if (sw_out) *sw_out = job->sw_out();
+  return true;
+}
+
 bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro, const double *det,
                         const bl_fid_params *params, double *fid_out, double *sw_out) {
   if (!fid_out) return fail(BL_ERR_INVALID, "null output");
+  if (!ctx || !sys || !pw || !ro || !det || !params) return fail(BL_ERR_INVALID, "null argument");
+  bool done = false;
+  const bl_status st0 = guarded([&] {
+    const int N = sys->s().dim();
+    done = fid_in_region(ctx, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out, sw_out);
+  });
+  if (st0 != BL_OK || done) return st0;
   bl_job *job = nullptr;
   bl_status st = bl_job_create(ctx, sys, pw, ro, det, params, &job);
   if (st != BL_OK) return st;
