@@ -352,7 +352,11 @@ static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder
   size_t fr = 0, tot = 0;
   if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return false;
   const size_t budget = ctx->c.hbm_budget ? ctx->c.hbm_budget : size_t(0.6 * double(fr + ctx->region_bytes));
-  if (full > budget) return false;
+  if (full > budget) {  // batched job of its own: give it the region's memory back
+    if (ctx->region) cudaFree(ctx->region);
+    ctx->region = nullptr, ctx->region_bytes = 0;
+    return false;
+  }
   if (full > ctx->region_bytes) {
     if (ctx->region) cudaFree(ctx->region);
     ctx->region = nullptr, ctx->region_bytes = 0;
