@@ -109,6 +109,54 @@ __device__ __forceinline__ C cvt(double2 v) { return mkc<C>(v.x, v.y); }
 template <class C>
 __device__ __forceinline__ double2 todbl(C v) { return make_double2(double(v.x), double(v.y)); }
 
+// Double-float values (hi + lo, ~2^-48 relative) for the mixed form's Dyson products, where
+// GB300's FP32 pipe (about 64 times the FP64 rate) does the work.  A complex element is one
+// float4 (re.hi, im.hi, re.lo, im.lo) in the 16-byte slot a double2 would take.  Sums use the
+// compensated dot product of Ogita, Rump and Oishi (2005) with the error-free two-sum of Knuth
+// and the FMA two-product; the _rn intrinsics keep the compiler from contracting them.
+__device__ __forceinline__ float4 df_store(double2 v) {
+  const float rh = __double2float_rn(v.x), ih = __double2float_rn(v.y);
+  return make_float4(rh, ih, __double2float_rn(v.x - double(rh)), __double2float_rn(v.y - double(ih)));
+}
+__device__ __forceinline__ double2 df_load(float4 v) {
+  return make_double2(double(v.x) + double(v.z), double(v.y) + double(v.w));
+}
+// running compensated sum of products: s + c
+struct DfAcc {
+  float s, c;
+};
+__device__ __forceinline__ void df_dot(DfAcc &a, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh), pe = __fmaf_rn(xh, yh, -p);       // two-product
+  const float s = __fadd_rn(a.s, p), bb = __fsub_rn(s, a.s);           // two-sum
+  const float se = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  a.s = s;
+  a.c = __fadd_rn(a.c, __fadd_rn(__fadd_rn(pe, se), __fmaf_rn(xh, yl, __fmul_rn(xl, yh))));
+}
+__device__ __forceinline__ float2 df_fin(const DfAcc &a) {  // (hi, lo) of s + c
+  const float h = __fadd_rn(a.s, a.c);
+  return make_float2(h, __fsub_rn(a.c, __fsub_rn(h, a.s)));
+}
+// double-float scalars (x = hi, y = lo) for the mixed form's step exponential
+__device__ __forceinline__ float2 dfv_of(double d) {
+  const float h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - double(h)));
+}
+__host__ __device__ __forceinline__ constexpr float2 dfv_const(double d) {
+  return float2{float(d), float(d - double(float(d)))};
+}
+__device__ __forceinline__ float2 dfv_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x), bb = __fsub_rn(s, a.x);
+  const float e = __fadd_rn(__fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb)), __fadd_rn(a.y, b.y));
+  const float h = __fadd_rn(s, e);
+  return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ float2 dfv_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  const float e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, __fmaf_rn(a.x, b.x, -p)));
+  const float h = __fadd_rn(p, e);
+  return make_float2(h, __fsub_rn(e, __fsub_rn(h, p)));
+}
+
 // ------------------------------------------------------------------ job description
 struct DevSys {
   int C, Cpad, n, npts, N, nb, S2, nint, nq, nr, ne, J, rosym, step_method;
@@ -475,15 +523,21 @@ __device__ __forceinline__ const double2 *frame_of(const DevSys &s, int i) {
 // Stores u = U'(p,q) = U'(q,p) of a step's real-symmetric-H block; with a frame r the lab-frame
 // U = R U' R^H takes r_p u conj(r_q) at (p,q) and r_q u conj(r_p) at (q,p).
 __device__ __forceinline__ void store_u_pair(double2 *Ub, int c, int Cpad, int bp, int bo, int B, int p, int q,
-                                             double2 u, const double2 *fr) {
-  if (!fr) {
-    Ub[at(bp + p * B + q, c, Cpad)] = u;
-    if (q != p) Ub[at(bp + q * B + p, c, Cpad)] = u;
+                                             double2 u, const double2 *fr, bool dfl) {
+  double2 upq = u, uqp = u;
+  if (fr) {
+    const double2 rp = fr[bo + p], rq = fr[bo + q];
+    upq = cmul(cmul(rp, u), cconj(rq));
+    uqp = cmul(cmul(rq, u), cconj(rp));
+  }
+  if (dfl) {  // mixed form: double-float for k_dyson_df
+    float4 *U4 = reinterpret_cast<float4 *>(Ub);
+    U4[at(bp + p * B + q, c, Cpad)] = df_store(upq);
+    if (q != p) U4[at(bp + q * B + p, c, Cpad)] = df_store(uqp);
     return;
   }
-  const double2 rp = fr[bo + p], rq = fr[bo + q];
-  Ub[at(bp + p * B + q, c, Cpad)] = cmul(cmul(rp, u), cconj(rq));
-  if (q != p) Ub[at(bp + q * B + p, c, Cpad)] = cmul(cmul(rq, u), cconj(rp));
+  Ub[at(bp + p * B + q, c, Cpad)] = upq;
+  if (q != p) Ub[at(bp + q * B + p, c, Cpad)] = uqp;
 }
 
 // H_i block at the midpoint of step i (sys.cc:749-770): rotor phase 2 pi wr t_mid,
@@ -687,7 +741,7 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
         u.x = fma(vv, e[j].x, u.x);
         u.y = fma(vv, e[j].y, u.y);
       }
-      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr);
+      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr, s.mixed != 0);
     }
 }
 
@@ -771,6 +825,123 @@ __device__ __forceinline__ void ps_poly(int d, const double *Y, const double *Y2
   (void)NP;
 }
 
+// The same in double-float (float2 = hi, lo): compensated dot products over l.
+template <int B>
+__device__ __forceinline__ void sym_mul_df(const float2 *X, const float2 *Y, float2 *C, float scale) {
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      DfAcc acc = {0.f, 0.f};
+#pragma unroll
+      for (int l = 0; l < B; ++l) {
+        const float2 x = X[sx<B>(p, l)], y = Y[sx<B>(l, q)];
+        df_dot(acc, x.x, x.y, y.x, y.y);
+      }
+      const float2 v = df_fin(acc);
+      C[sx<B>(p, q)] = make_float2(v.x * scale, v.y * scale);  // scale is +-1 or 2: exact
+    }
+}
+template <int B, bool SIN>
+__device__ __forceinline__ void ps_poly_df(int d, const float2 *Y, const float2 *Y2, float2 *acc, float2 *tmp) {
+  const int top = d / 2;
+#pragma unroll
+  for (int m = 3; m >= 0; --m) {
+    if (m > top) continue;
+    const float2 a0 = dfv_const(SIN ? sin_coef(2 * m) : cos_coef(2 * m));
+    const float2 a1 = (2 * m + 1 <= d) ? dfv_const(SIN ? sin_coef(2 * m + 1) : cos_coef(2 * m + 1)) : float2{0.f, 0.f};
+    if (m < top) sym_mul_df<B>(acc, Y2, tmp, 1.f);
+#pragma unroll
+    for (int p = 0; p < B; ++p)
+#pragma unroll
+      for (int q = p; q < B; ++q) {
+        const int j = sx<B>(p, q);
+        float2 l = dfv_mul(a1, Y[j]);
+        if (p == q) l = dfv_add(l, a0);
+        acc[j] = (m < top) ? dfv_add(tmp[j], l) : l;
+      }
+  }
+}
+
+// The mixed form's step exponential: H, its norm and the scaling in FP64 as in k_step_taylor,
+// the polynomial and the squarings in double-float on the FP32 pipe (~2^-48, against the
+// form's 2^-40 truncation), U stored as double-float for k_dyson_df.
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_step_taylor_df(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * s.n) return;
+  int i = int(rest % s.n);
+  int k = blist[rest / s.n];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  constexpr int NP = B * (B + 1) / 2;
+  double h[B][B];
+  build_h<B>(s, c, i, bp, h);
+  const double tp = s.tau * kPi2;
+  double nrm = 0;
+#pragma unroll
+  for (int p = 0; p < B; ++p) {
+    double rs = 0;
+#pragma unroll
+    for (int q = 0; q < B; ++q) rs += fabs(h[p][q]);
+    nrm = fmax(nrm, rs);
+  }
+  nrm *= tp;
+  int sq = 0;
+  if (nrm > 0.5) {
+    frexp(nrm / 0.5, &sq);
+    sq = min(sq, 60);
+  }
+  const double sc = ldexp(tp, -sq);
+  const int K = taylor_degree(ldexp(nrm, -sq), true);
+  __shared__ float2 Xs[NP * kThreads];
+  float2 Y[NP], Y2[NP], R[NP], S[NP], T[NP];
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) T[sx<B>(p, q)] = dfv_of(sc * h[p][q]);
+#pragma unroll
+  for (int j = 0; j < NP; ++j) Xs[j * blockDim.x + threadIdx.x] = T[j];
+  sym_mul_df<B>(T, T, Y, 1.f);
+  sym_mul_df<B>(Y, Y, Y2, 1.f);
+  ps_poly_df<B, false>(K / 2, Y, Y2, R, T);
+  ps_poly_df<B, true>((K - 1) / 2, Y, Y2, S, T);
+#pragma unroll
+  for (int j = 0; j < NP; ++j) T[j] = Xs[j * blockDim.x + threadIdx.x];
+  float2 *I = Y2;
+  sym_mul_df<B>(T, S, I, -1.f);
+  for (int t = 0; t < sq; ++t) {
+    sym_mul_df<B>(R, R, Y, 1.f);
+    sym_mul_df<B>(I, I, S, 1.f);
+    sym_mul_df<B>(R, I, T, 2.f);
+#pragma unroll
+    for (int j = 0; j < NP; ++j) {
+      R[j] = dfv_add(Y[j], make_float2(-S[j].x, -S[j].y));
+      I[j] = T[j];
+    }
+  }
+  double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+  float4 *U4 = reinterpret_cast<float4 *>(Ub);
+  const double2 *fr = frame_of(s, i);
+  const int bo = s.boff[k];
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = p; q < B; ++q) {
+      const float2 re = R[sx<B>(p, q)], im = I[sx<B>(p, q)];
+      if (fr) {  // rf schedule frames: through FP64
+        const double2 u = cmk(double(re.x) + double(re.y), double(im.x) + double(im.y));
+        store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr, true);
+      } else {
+        const float4 v = make_float4(re.x, im.x, re.y, im.y);
+        U4[at(bp + p * B + q, c, s.Cpad)] = v;
+        if (q != p) U4[at(bp + q * B + p, c, s.Cpad)] = v;
+      }
+    }
+}
+
 // One thread per (crystallite, block k, step i): U_i = exp(-i 2pi tau H_i) by a Taylor
 // series of the scaled real symmetric block plus repeated squaring.  Real and imaginary
 // parts of U are polynomials in H, hence symmetric and commuting, so every product is a
@@ -844,7 +1015,7 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor(DevSys s, const int *_
 #pragma unroll
     for (int q = p; q < B; ++q) {
       double2 u = cmk(R[sx<B>(p, q)], I[sx<B>(p, q)]);
-      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr);
+      store_u_pair(Ub, c, s.Cpad, bp, bo, B, p, q, u, fr, s.mixed != 0);
     }
 }
 
@@ -881,6 +1052,48 @@ __global__ void __launch_bounds__(kThreads) k_dyson(DevSys s, const int *__restr
   }
 }
 
+// The mixed form's Dyson product in double-float: one thread per (crystallite, block, column),
+// U_i and A_{i+1} as float4 double-float elements; each element of U_i x is four compensated
+// dot products (re and im, each of a U-hi/lo x-hi/lo expansion).
+template <int B>
+__global__ void __launch_bounds__(kThreads) k_dyson_df(DevSys s, const int *__restrict__ blist, int nblist) {
+  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = int(tid % s.Cpad);
+  long rest = tid / s.Cpad;
+  if (rest >= long(nblist) * B) return;
+  int j = int(rest % B);
+  int k = blist[rest / B];
+  if (c >= s.C) return;
+  const int bp = s.bpoff[k];
+  float4 x[B];
+#pragma unroll
+  for (int r = 0; r < B; ++r) x[r] = make_float4(r == j ? 1.f : 0.f, 0.f, 0.f, 0.f);
+  for (int i = 0; i < s.n; ++i) {
+    const float4 *Ub = reinterpret_cast<const float4 *>(s.U + size_t(i) * s.S2 * s.Cpad);
+    float4 y[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      DfAcc re = {0.f, 0.f}, im = {0.f, 0.f};
+#pragma unroll
+      for (int l = 0; l < B; ++l) {
+        const float4 u = Ub[at(bp + r * B + l, c, s.Cpad)];
+        df_dot(re, u.x, u.z, x[l].x, x[l].z);    // ur xr
+        df_dot(re, -u.y, -u.w, x[l].y, x[l].w);  // - ui xi
+        df_dot(im, u.x, u.z, x[l].y, x[l].w);    // ur xi
+        df_dot(im, u.y, u.w, x[l].x, x[l].z);    // ui xr
+      }
+      const float2 a = df_fin(re), b = df_fin(im);
+      y[r] = make_float4(a.x, b.x, a.y, b.y);
+    }
+    float4 *Ab = reinterpret_cast<float4 *>(s.A + size_t(i) * s.S2 * s.Cpad);
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+      x[r] = y[r];
+      Ab[at(bp + r * B + j, c, s.Cpad)] = y[r];
+    }
+  }
+}
+
 // One thread per (crystallite, block): Floquet eigen-decomposition of A_n.
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_floquet(DevSys s, const int *__restrict__ blist, int nblist) {
@@ -892,11 +1105,13 @@ __global__ void __launch_bounds__(kThreads) k_floquet(DevSys s, const int *__res
   if (c >= s.C) return;
   const int bp = s.bpoff[k], bo = s.boff[k];
   const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
+  const float4 *An4 = reinterpret_cast<const float4 *>(An);  // mixed form: double-float A
   double2 U[B][B], lam[B], V[B][B];
 #pragma unroll
   for (int r = 0; r < B; ++r)
 #pragma unroll
-    for (int q = 0; q < B; ++q) U[r][q] = An[at(bp + r * B + q, c, s.Cpad)];
+    for (int q = 0; q < B; ++q)
+      U[r][q] = s.mixed ? df_load(An4[at(bp + r * B + q, c, s.Cpad)]) : An[at(bp + r * B + q, c, s.Cpad)];
   int st = unitary_eig<B>(U, lam, V);
   if (st) atomicOr(s.status, st);
 #pragma unroll
@@ -941,9 +1156,11 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
   const LaneGroup<B> g{((1u << B) - 1u) << (gi * B), gi * B};
   const int bp = s.bpoff[k], bo = s.boff[k];
   const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
+  const float4 *An4 = reinterpret_cast<const float4 *>(An);  // mixed form: double-float A
   double2 U[B], V[B], K[B], lam[B];
 #pragma unroll
-  for (int q = 0; q < B; ++q) U[q] = An[at(bp + r * B + q, c, s.Cpad)];
+  for (int q = 0; q < B; ++q)
+    U[q] = s.mixed ? df_load(An4[at(bp + r * B + q, c, s.Cpad)]) : An[at(bp + r * B + q, c, s.Cpad)];
   int st = 0;
   double a = 0.5;
   for (int pass = 0; pass < 2; ++pass) {
@@ -1179,12 +1396,20 @@ __global__ void __launch_bounds__(kThreads) k_eigframe(DevSys s, const int *__re
 #pragma unroll
     for (int q = 0; q < B; ++q) V[r][q] = cvt<C>(s.VF[at(bp + r * B + q, c, s.Cpad)]);
   const double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
+  const float4 *Ab4 = reinterpret_cast<const float4 *>(Ab);  // mixed form: double-float A
   C *Wb = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
 #pragma unroll
   for (int r = 0; r < B; ++r) {
     C a[B];
 #pragma unroll
-    for (int l = 0; l < B; ++l) a[l] = cvt<C>(Ab[at(bp + r * B + l, c, s.Cpad)]);
+    for (int l = 0; l < B; ++l) {
+      if (s.mixed) {  // single precision from here on: the high parts
+        const float4 v = Ab4[at(bp + r * B + l, c, s.Cpad)];
+        a[l] = mkc<C>(v.x, v.y);
+      } else {
+        a[l] = cvt<C>(Ab[at(bp + r * B + l, c, s.Cpad)]);
+      }
+    }
 #pragma unroll
     for (int q = 0; q < B; ++q) {
       C acc = mkc<C>(0, 0);
@@ -2454,10 +2679,14 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
   }
   switch (stage) {
     case 0:
-      if (s.step_method == 1) k_step_taylor<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      if (s.step_method == 1 && s.mixed) k_step_taylor_df<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
+      else if (s.step_method == 1) k_step_taylor<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
       else k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
       break;
-    case 1: k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl); break;
+    case 1:
+      if (s.mixed) k_dyson_df<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl);
+      else k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl);
+      break;
     case 2:
       if (B == 1) {
         k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl);
