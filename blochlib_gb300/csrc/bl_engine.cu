@@ -178,6 +178,11 @@ struct DevSys {
   // chunk i / psub); frames (chunk x N, permuted index) rotate each step's U into the lab frame
   int hc_chunks;
   const double2 *frames;
+  // double-float copies for the mixed form's step (hi, lo): term operators, constant parts,
+  // and fk_df = 1 when k_coef stores the coefficients as float2 in fk's slots
+  const float2 *Tk_df, *Hc_df;
+  int fk_df;
+  float2 tpdf;  // 2 pi tau as double-float
   const int *ikind;  // per term: 0 first order, 1 / 2 second-order quadrupolar (c4 / c2)
   int has2;
   // Q pairs (D blocks) and R pairs (rho blocks)
@@ -576,7 +581,12 @@ __global__ void __launch_bounds__(kThreads) k_coef(DevSys s, double *fk) {
   sincos(tmid * s.wr * kPi2, &sp, &cp);
   double m[3][3];
   orient_rows(s, c, sp, cp, m);
-  for (int kk = 0; kk < s.nint; ++kk) fk[at(i * s.nint + kk, c, s.Cpad)] = term_coef(s, kk, m);
+  float2 *fk2 = reinterpret_cast<float2 *>(fk);
+  for (int kk = 0; kk < s.nint; ++kk) {
+    const double f = term_coef(s, kk, m);
+    if (s.fk_df) fk2[at(i * s.nint + kk, c, s.Cpad)] = dfv_of(f);
+    else fk[at(i * s.nint + kk, c, s.Cpad)] = f;
+  }
 }
 
 template <int B>
@@ -863,9 +873,33 @@ __device__ __forceinline__ void ps_poly_df(int d, const float2 *Y, const float2 
   }
 }
 
-// The mixed form's step exponential: H, its norm and the scaling in FP64 as in k_step_taylor,
-// the polynomial and the squarings in double-float on the FP32 pipe (~2^-48, against the
-// form's 2^-40 truncation), U stored as double-float for k_dyson_df.
+// H of step i in double-float from the double-float copies of Hc, the operators and k_coef's
+// coefficients.
+template <int B>
+__device__ __forceinline__ void build_h_df(const DevSys &s, int c, int i, int bp, float2 (&h)[B][B]) {
+  const float2 *Hcb = s.Hc_df + (s.hc_chunks ? size_t(i / s.psub) * s.S2 : 0) + bp;
+#pragma unroll
+  for (int p = 0; p < B; ++p)
+#pragma unroll
+    for (int q = 0; q < B; ++q) h[p][q] = Hcb[p * B + q];
+  const float2 *fk2 = reinterpret_cast<const float2 *>(s.fk);
+  for (int kk = 0; kk < s.nint; ++kk) {
+    const float2 f = fk2[at(i * s.nint + kk, c, s.Cpad)];
+    const float2 *T = s.Tk_df + size_t(kk) * s.S2 + bp;
+#pragma unroll
+    for (int p = 0; p < B; ++p)
+#pragma unroll
+      for (int q = 0; q < B; ++q) {
+        const float2 t = T[p * B + q];  // same for every lane: the skip is warp-uniform
+        if (t.x != 0.f) h[p][q] = dfv_add(h[p][q], dfv_mul(f, t));
+      }
+  }
+}
+
+// The mixed form's step exponential in double-float on the FP32 pipe (~2^-48, against the
+// form's 2^-40 truncation): H from build_h_df, its norm from the high parts (it only picks the
+// scaling and the degree), the polynomial and the squarings; U stored as double-float for
+// k_dyson_df.
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_step_taylor_df(DevSys s, const int *__restrict__ blist, int nblist) {
   long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -877,31 +911,31 @@ __global__ void __launch_bounds__(kThreads) k_step_taylor_df(DevSys s, const int
   if (c >= s.C) return;
   const int bp = s.bpoff[k];
   constexpr int NP = B * (B + 1) / 2;
-  double h[B][B];
-  build_h<B>(s, c, i, bp, h);
-  const double tp = s.tau * kPi2;
-  double nrm = 0;
+  float2 h[B][B];
+  build_h_df<B>(s, c, i, bp, h);
+  const float tpf = float(s.tau * kPi2);
+  float nrm = 0.f;
 #pragma unroll
   for (int p = 0; p < B; ++p) {
-    double rs = 0;
+    float rs = 0.f;
 #pragma unroll
-    for (int q = 0; q < B; ++q) rs += fabs(h[p][q]);
-    nrm = fmax(nrm, rs);
+    for (int q = 0; q < B; ++q) rs += fabsf(h[p][q].x);
+    nrm = fmaxf(nrm, rs);
   }
-  nrm *= tp;
+  nrm *= tpf * (1.f + 1e-6f);  // margin over the rounding of the high parts
   int sq = 0;
-  if (nrm > 0.5) {
-    frexp(nrm / 0.5, &sq);
+  if (nrm > 0.5f) {
+    frexpf(nrm / 0.5f, &sq);
     sq = min(sq, 60);
   }
-  const double sc = ldexp(tp, -sq);
-  const int K = taylor_degree(ldexp(nrm, -sq), true);
+  float2 sc = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));  // 2 pi tau 2^-sq, exact scaling
+  const int K = taylor_degree(double(ldexpf(nrm, -sq)), true);
   __shared__ float2 Xs[NP * kThreads];
   float2 Y[NP], Y2[NP], R[NP], S[NP], T[NP];
 #pragma unroll
   for (int p = 0; p < B; ++p)
 #pragma unroll
-    for (int q = p; q < B; ++q) T[sx<B>(p, q)] = dfv_of(sc * h[p][q]);
+    for (int q = p; q < B; ++q) T[sx<B>(p, q)] = dfv_mul(sc, h[p][q]);
 #pragma unroll
   for (int j = 0; j < NP; ++j) Xs[j * blockDim.x + threadIdx.x] = T[j];
   sym_mul_df<B>(T, T, Y, 1.f);
@@ -1958,7 +1992,8 @@ static thread_local ScratchArena *g_arena = nullptr;
 struct JobSizing {
   size_t per_c = 0;
   long cpad = 0;
-  size_t extra = 0;  // bytes independent of the batch size (huge-block workspace)
+  size_t extra = 0;   // bytes independent of the batch size (huge-block workspace)
+  size_t tables = 0;  // the system's operator tables on the device (and their double-float copies)
 };
 static thread_local JobSizing *g_sizing = nullptr;
 
@@ -2026,6 +2061,7 @@ struct JobImpl {
   int p2p = 0, pb = 1, pf = 1, psub = 1;  // point-to-point FID: base, factor, steps per chunk
   DevBuf<double> fkc;                      // k_coef's term coefficients (small blocks)
   DevBuf<double2> frames;                  // rf schedule: per chunk frame (permuted index)
+  DevBuf<float2> Tk_df, Hc_df;             // mixed form: double-float operators and constant parts
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
@@ -2342,6 +2378,12 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     g_sizing->per_c = per_c;
     g_sizing->cpad = cpad_all;
     g_sizing->extra = huge_fixed;
+    // Tk and Hc (per chunk), their double-float copies in the mixed form, the D and rho
+    // blocks, the rf frames, and 256-byte alignment per buffer
+    const size_t tk = size_t(J.nint) * L.S2, hc = size_t(L.S2) * (sched ? J.pb : 1);
+    g_sizing->tables = (tk + hc) * sizeof(double) * ((p.precision == 1 && !J.is_static) ? 2 : 1) +
+                       (Dblk.size() + Rhoblk.size()) * sizeof(double2) + size_t(N) * J.pb * sizeof(double2) +
+                       64 * 256;
     return;
   }
   size_t budget = ctx.hbm_budget;
@@ -2496,6 +2538,18 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.huge_pairs[t].rp = J.big_rp.p + J.huge_rp_off[t], J.huge_pairs[t].ci = J.big_ci.p,
     J.huge_pairs[t].cv = J.big_cv.p;
   J.pas.upload(pas, st), J.iscale.upload(isc, st), J.Tk.upload(Tk, st), J.Hc.upload(Hc, st);
+  if (p.precision == 1 && !J.is_static) {  // hi, lo splits for the mixed form's double-float step
+    auto split = [](const std::vector<double> &v) {
+      std::vector<float2> o(v.size());
+      for (size_t x = 0; x < v.size(); ++x) {
+        const float h = float(v[x]);
+        o[x] = make_float2(h, float(v[x] - double(h)));
+      }
+      return o;
+    };
+    J.Tk_df.upload(split(Tk), st);
+    J.Hc_df.upload(split(Hc), st);
+  }
   if (sched) {  // per chunk: the rf frame of each permuted index (1 where a chunk has none)
     bool any = false;
     for (const auto &cs : chunk_sys) any = any || !cs.frame().empty();
@@ -2647,6 +2701,13 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.fk = use_fk ? J.fkc.p : nullptr;
   s.hc_chunks = sched ? J.pb : 0;
   s.frames = J.frames.n ? J.frames.p : nullptr;
+  s.Tk_df = J.Tk_df.p, s.Hc_df = J.Hc_df.p;
+  s.fk_df = (J.mixed && p.step_method == 1 && use_fk) ? 1 : 0;
+  {
+    const double tp = J.tau * kPi2;
+    const float h = float(tp);
+    s.tpdf = make_float2(h, float(tp - double(h)));
+  }
   s.ikind = J.ikind.p, s.has2 = J.has2;
   s.npq = J.npq, s.npr = J.npr;
   s.qa = J.qa.p, s.qb = J.qb.p, s.qoff = J.qoff.p, s.doff = J.doff.p;
@@ -3269,7 +3330,7 @@ void job_bytes(int device, const SpinSystem &sys, const Powder &pw, const CMatri
   } scope(&plan);
   Job job(ctx, sys, pw, ro, det, p);
   // work buffers are carved with 256-byte alignment: allow for it on each of ~40 buffers
-  size_t fixed = fixed_bytes(pw, p) + 40 * 256;
+  size_t fixed = fixed_bytes(pw, p) + 40 * 256 + plan.extra + plan.tables;
   if (min_bytes) *min_bytes = fixed + plan.per_c * 32;
   if (full_bytes) *full_bytes = fixed + plan.per_c * size_t(plan.cpad);
 }
