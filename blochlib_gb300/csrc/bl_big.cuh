@@ -9,6 +9,9 @@
 //   k_big_floquet   (c)         A_n = V diag(lam) V^H: Cayley transform, parallel Jacobi
 //   k_big_eigframe  (c)         W_i = A_{i+1} V_F for i < n
 //   k_big_qr        (c, step) per pair  Q = W_a^H M_ab W_b for block pairs with a big block
+// and, for the mixed form, the same step and Dyson in double-float on the FP32 pipe:
+//   k_big_step_df   (c, step)   U_i in double-float (the Taylor series term by term)
+//   k_big_dyson_df  (c)         A_{i+1} = U_i A_i in double-float
 
 constexpr int kMaxBigBlock = 74;   // 5 real b x b matrices fit 227 KB of shared memory
 constexpr int kBigThreads = 256;   // k_big_floquet
@@ -325,7 +328,15 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_eigframe(DevSys s,
   for (int i = 0; i < s.n; ++i) {
     const double2 *Ab = s.A + size_t(i) * s.S2 * s.Cpad;
     C *Wb = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
-    for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = cvt<C>(Ab[at(bp + e, c, s.Cpad)]);
+    const float4 *Ab4 = reinterpret_cast<const float4 *>(Ab);  // mixed form: double-float A, high parts
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      if (s.mixed) {
+        const float4 v = Ab4[at(bp + e, c, s.Cpad)];
+        As[e] = mkc<C>(v.x, v.y);
+      } else {
+        As[e] = cvt<C>(Ab[at(bp + e, c, s.Cpad)]);
+      }
+    }
     __syncthreads();
     cta_mm_cplx_regs<NT, false, C>(As, b, Vs, b, b, b, b, acc);
     cta_tiles_store<NT>(b, b, acc, [&](int r, int q, C v) { Wb[at(bp + r * b + q, c, s.Cpad)] = v; });
@@ -396,7 +407,7 @@ struct FloqWork {
 
 // sweeps0 < kMaxSweeps: the first pass only locates the spectrum (that many sweeps); the
 // second pass, with -1 in the widest gap of those eigenphases, always follows.
-__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps) {
+__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps, bool dfA = false) {
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
@@ -406,7 +417,10 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
   auto rot = [&](int t, int q) -> double2 & { return wk.rot[2 * t + q]; };
   auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
   const double2 *U = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;  // U(r,q) = U[at(bp + r*b + q, c)]
-  auto Ug = [&](int r, int q) { return U[at(bp + r * b + q, c, s.Cpad)]; };
+  const float4 *U4 = reinterpret_cast<const float4 *>(U);      // dfA: double-float A (mixed form)
+  auto Ug = [&](int r, int q) {
+    return dfA ? df_load(U4[at(bp + r * b + q, c, s.Cpad)]) : U[at(bp + r * b + q, c, s.Cpad)];
+  };
   if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {
@@ -631,5 +645,216 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   __shared__ double2 lam[kMaxBigBlock];
   __shared__ double red[kBigThreads];
   const int b = s.bs[k];
-  floquet_cta(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red});
+  floquet_cta(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red}, kMaxSweeps, s.mixed != 0);
 }
+
+// ------------------------------------------------------------------ mixed form, double-float
+// The large-block step and Dyson of the mixed form in double-float on the FP32 pipe (float2 =
+// hi, lo; complex elements float4 = re.hi, im.hi, re.lo, im.lo), with the same tiling as the
+// FP64 kernels and sums as compensated dot products.
+
+// C = alpha A B for symmetric commuting A, B (upper tiles, mirrored), double-float.
+__device__ void cta_mm_sym_df(const float2 *A, const float2 *B, float2 *C, int m, float2 alpha) {
+  const int tm = (m + 1) / 2;
+  for (int t = threadIdx.x; t < big_sym_tiles(m); t += blockDim.x) {
+    int ti, tj;
+    sym_tile(t, tm, ti, tj);
+    const int i0 = 2 * ti, j0 = 2 * tj;
+    const int i1 = min(i0 + 1, m - 1), j1 = min(j0 + 1, m - 1);
+    DfAcc c00 = {0.f, 0.f}, c01 = c00, c10 = c00, c11 = c00;
+    for (int l = 0; l < m; ++l) {
+      const float2 a0 = A[i0 * m + l], a1 = A[i1 * m + l], b0 = B[l * m + j0], b1 = B[l * m + j1];
+      df_dot(c00, a0.x, a0.y, b0.x, b0.y);
+      df_dot(c01, a0.x, a0.y, b1.x, b1.y);
+      df_dot(c10, a1.x, a1.y, b0.x, b0.y);
+      df_dot(c11, a1.x, a1.y, b1.x, b1.y);
+    }
+    auto put = [&](int i, int j, const DfAcc &v) {
+      const float2 x = dfv_mul(alpha, df_fin(v));
+      C[i * m + j] = x;
+      if (i != j) C[j * m + i] = x;
+    };
+    put(i0, j0, c00);
+    if (j0 + 1 < m) put(i0, j0 + 1, c01);
+    if (i0 + 1 < m) {
+      if (ti != tj) put(i0 + 1, j0, c10);
+      if (j0 + 1 < m) put(i0 + 1, j0 + 1, c11);
+    }
+  }
+}
+
+// 1/k for the Taylor terms, double-float
+__device__ __forceinline__ float2 inv_df(int kt) {
+  switch (kt) {
+    case 2: return dfv_const(1.0 / 2); case 3: return dfv_const(1.0 / 3); case 4: return dfv_const(1.0 / 4);
+    case 5: return dfv_const(1.0 / 5); case 6: return dfv_const(1.0 / 6); case 7: return dfv_const(1.0 / 7);
+    case 8: return dfv_const(1.0 / 8); case 9: return dfv_const(1.0 / 9); case 10: return dfv_const(1.0 / 10);
+    case 11: return dfv_const(1.0 / 11); case 12: return dfv_const(1.0 / 12); case 13: return dfv_const(1.0 / 13);
+    case 14: return dfv_const(1.0 / 14); default: return dfv_const(1.0 / 15);
+  }
+}
+
+__host__ __device__ constexpr size_t big_step_df_smem(int b) { return sizeof(float2) * 5 * size_t(b) * size_t(b); }
+
+// One CTA per (crystallite, step): the large block's U_i in double-float: H from the hi/lo
+// tables, the series term by term to the degree taylor_degree gives at 2^-40, squarings.
+__global__ void __launch_bounds__(1024) k_big_step_df(DevSys s, int k) {
+  extern __shared__ __align__(16) unsigned char bsd[];
+  __shared__ float2 fk[kMaxInt];
+  __shared__ float red[kMaxBigBlock];
+  __shared__ float2 scl;
+  __shared__ int nsq, nterms;
+  const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  if (threadIdx.x == 0) {
+    double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
+    double tmid = (t2 - t1) / 2.0 + t1;
+    double sp, cp;
+    sincos(tmid * s.wr * kPi2, &sp, &cp);
+    double m[3][3];
+    orient_rows(s, c, sp, cp, m);
+    for (int kk = 0; kk < s.nint; ++kk) fk[kk] = dfv_of(term_coef(s, kk, m));
+  }
+  __syncthreads();
+  float2 *X = reinterpret_cast<float2 *>(bsd), *P = X + bb, *Q = P + bb, *R = Q + bb, *I = R + bb;
+  const float2 *Hcb = s.Hc_df + (s.hc_chunks ? size_t(i / s.psub) * s.S2 : 0) + bp;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    float2 h = Hcb[e];
+    for (int kk = 0; kk < s.nint; ++kk) {
+      const float2 t = s.Tk_df[size_t(kk) * s.S2 + bp + e];
+      if (t.x != 0.f) h = dfv_add(h, dfv_mul(fk[kk], t));
+    }
+    X[e] = h;
+  }
+  __syncthreads();
+  for (int p = threadIdx.x; p < b; p += blockDim.x) {
+    float rs = 0.f;
+    for (int q = 0; q < b; ++q) rs += fabsf(X[p * b + q].x);
+    red[p] = rs;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float nrm = 0.f;
+    for (int p = 0; p < b; ++p) nrm = fmaxf(nrm, red[p]);
+    nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
+    int sq = 0;
+    if (nrm > 0.5f) {
+      frexpf(nrm / 0.5f, &sq);
+      sq = min(sq, 60);
+    }
+    scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
+    nsq = sq;
+    nterms = taylor_degree(double(ldexpf(nrm, -sq)), true);
+  }
+  __syncthreads();
+  const float2 sc = scl;
+  const int sq = nsq, K = nterms;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    const float2 x = dfv_mul(sc, X[e]);
+    X[e] = x, P[e] = x;
+    R[e] = make_float2((e / b == e % b) ? 1.f : 0.f, 0.f);
+    I[e] = make_float2(-x.x, -x.y);
+  }
+  __syncthreads();
+  for (int kt = 2; kt <= K; ++kt) {
+    cta_mm_sym_df(P, X, Q, b, inv_df(kt));
+    __syncthreads();
+    const int m4 = kt & 3;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const float2 v = Q[e], nv = make_float2(-v.x, -v.y);
+      if (m4 == 2) R[e] = dfv_add(R[e], nv);
+      else if (m4 == 3) I[e] = dfv_add(I[e], v);
+      else if (m4 == 0) R[e] = dfv_add(R[e], v);
+      else I[e] = dfv_add(I[e], nv);
+    }
+    float2 *t = P;
+    P = Q, Q = t;
+    __syncthreads();
+  }
+  // squarings: (R + iI)^2 = (RR - II) + i 2RI, in P, Q, X
+  for (int t = 0; t < sq; ++t) {
+    cta_mm_sym_df(R, R, P, b, make_float2(1.f, 0.f));
+    cta_mm_sym_df(I, I, Q, b, make_float2(1.f, 0.f));
+    cta_mm_sym_df(R, I, X, b, make_float2(2.f, 0.f));
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const float2 q = Q[e];
+      R[e] = dfv_add(P[e], make_float2(-q.x, -q.y)), I[e] = X[e];
+    }
+    __syncthreads();
+  }
+  double2 *Ub = s.U + size_t(i) * s.S2 * s.Cpad;
+  float4 *U4 = reinterpret_cast<float4 *>(Ub);
+  const double2 *fr = frame_of(s, i);
+  const int bo = s.boff[k];
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+    const float2 re = R[e], im = I[e];
+    if (fr) {  // rf schedule frames: through FP64
+      const double2 u = cmk(double(re.x) + double(re.y), double(im.x) + double(im.y));
+      U4[at(bp + e, c, s.Cpad)] = df_store(cmul(cmul(fr[bo + e / b], u), cconj(fr[bo + e % b])));
+    } else {
+      U4[at(bp + e, c, s.Cpad)] = make_float4(re.x, im.x, re.y, im.y);
+    }
+  }
+}
+
+// Complex double-float 2x2-tiled product into registers (compensated sums per re / im).
+struct CdfAcc {
+  DfAcc re, im;
+};
+__device__ __forceinline__ void cdf_mac(CdfAcc &a, float4 x, float4 y) {  // a += x y
+  df_dot(a.re, x.x, x.z, y.x, y.z);
+  df_dot(a.re, -x.y, -x.w, y.y, y.w);
+  df_dot(a.im, x.x, x.z, y.y, y.w);
+  df_dot(a.im, x.y, x.w, y.x, y.z);
+}
+__device__ __forceinline__ float4 cdf_fin(const CdfAcc &a) {
+  const float2 r = df_fin(a.re), m = df_fin(a.im);
+  return make_float4(r.x, m.x, r.y, m.y);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_dyson_df(DevSys s, int k) {
+  extern __shared__ __align__(16) unsigned char bsy[];
+  const int c = blockIdx.x;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  float4 *Us = reinterpret_cast<float4 *>(bsy), *As = Us + bb;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) As[e] = make_float4(e / b == e % b ? 1.f : 0.f, 0.f, 0.f, 0.f);
+  const int tm = (b + 1) / 2;
+  for (int i = 0; i < s.n; ++i) {
+    const float4 *Ub = reinterpret_cast<const float4 *>(s.U + size_t(i) * s.S2 * s.Cpad);
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) Us[e] = Ub[at(bp + e, c, s.Cpad)];
+    __syncthreads();
+    float4 out[NT][4];
+#pragma unroll
+    for (int q = 0; q < NT; ++q) {
+      const int t = threadIdx.x + q * blockDim.x;
+      if (t >= tm * tm) continue;
+      const int i0 = (t / tm) * 2, j0 = (t % tm) * 2;
+      const int i1 = min(i0 + 1, b - 1), j1 = min(j0 + 1, b - 1);
+      CdfAcc c00 = {{0.f, 0.f}, {0.f, 0.f}}, c01 = c00, c10 = c00, c11 = c00;
+      for (int l = 0; l < b; ++l) {
+        const float4 a0 = Us[i0 * b + l], a1 = Us[i1 * b + l], b0 = As[l * b + j0], b1 = As[l * b + j1];
+        cdf_mac(c00, a0, b0), cdf_mac(c01, a0, b1), cdf_mac(c10, a1, b0), cdf_mac(c11, a1, b1);
+      }
+      out[q][0] = cdf_fin(c00), out[q][1] = cdf_fin(c01), out[q][2] = cdf_fin(c10), out[q][3] = cdf_fin(c11);
+    }
+    __syncthreads();
+    float4 *Ab = reinterpret_cast<float4 *>(s.A + size_t(i) * s.S2 * s.Cpad);
+#pragma unroll
+    for (int q = 0; q < NT; ++q) {
+      const int t = threadIdx.x + q * blockDim.x;
+      if (t >= tm * tm) continue;
+      const int i0 = (t / tm) * 2, j0 = (t % tm) * 2;
+      for (int d = 0; d < 4; ++d) {
+        const int r = i0 + (d >> 1), col = j0 + (d & 1);
+        if (r < b && col < b) {
+          As[r * b + col] = out[q][d];
+          Ab[at(bp + r * b + col, c, s.Cpad)] = out[q][d];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+

@@ -2490,6 +2490,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_step, smem_step);
       attr((const void *)k_big_dyson<1>, smem_mat);
       attr((const void *)k_big_dyson<2>, smem_mat);
+      attr((const void *)k_big_step_df, smem_step);  // 5 b^2 float2 <= the FP64 step's 5 or 7 b^2 doubles
+      attr((const void *)k_big_dyson_df<1>, smem_mat);
+      attr((const void *)k_big_dyson_df<2>, smem_mat);
       attr((const void *)k_big_eigframe<1, double2>, smem_mat);
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
@@ -2962,10 +2965,18 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
     const unsigned th = big_threads(b, b), th_step = unsigned((big_sym_tiles(b) + 31) / 32 * 32);
     const bool nt1 = big_nt(b, b) == 1;
     switch (stage) {
-      case 0: k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k); break;
+      case 0:
+        if (s.mixed) k_big_step_df<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_df_smem(b), st>>>(s, k);
+        else k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k);
+        break;
       case 1:
-        if (nt1) k_big_dyson<1><<<unsigned(s.C), th, smat, st>>>(s, k);
-        else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);
+        if (s.mixed) {
+          if (nt1) k_big_dyson_df<1><<<unsigned(s.C), th, smat, st>>>(s, k);
+          else k_big_dyson_df<2><<<unsigned(s.C), th, smat, st>>>(s, k);
+        } else {
+          if (nt1) k_big_dyson<1><<<unsigned(s.C), th, smat, st>>>(s, k);
+          else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);
+        }
         break;
       case 2: k_big_floquet<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
       case 3:

@@ -1,6 +1,7 @@
-"""The mixed-precision form (precision=1): FP64 step exponential, Dyson product, Floquet
-eigen-decomposition and powder sum; eigenframe, Q/R, Fave and FID reconstruction in single
-precision.  Gate: <= 1e-6 relative L2 FID error against the FP64 path and the reference."""
+"""The mixed-precision form (precision=1): step exponential and Dyson product in double-float
+(hi + lo floats) on the FP32 pipe, Floquet eigen-decomposition and powder sum in FP64;
+eigenframe, Q/R, Fave and FID reconstruction in single precision.  Gate: <= 1e-6 relative L2
+FID error against the FP64 path and the reference."""
 import numpy as np
 import pytest
 

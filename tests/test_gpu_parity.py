@@ -210,6 +210,29 @@ def test_big_blocks_match_oracle(seed, nspin, rho, det):
     assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
+@pytest.mark.parametrize("seed,nspin,rho,det", [(0, 5, "Fx", "Fp"), (3, 6, "Fx", "Fp"), (4, 7, "Fx", "Fp")])
+def test_big_blocks_mixed_within_1e6(seed, nspin, rho, det):
+    """The mixed form on the CTA-per-block kernels: step and Dyson in double-float, Floquet
+    from the double-float A, eigenframe from its high parts; <= 1e-6 against the oracle."""
+    job, rows = big_system(seed, nspin, rho, det)
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method="taylor", precision=1)
+    assert 0 < rel(fid, ref) <= 1e-6, rel(fid, ref)
+
+
+def test_big_blocks_mixed_batch_invariant():
+    """Each crystallite's double-float arithmetic is its own: one crystallite alone gives the
+    bits it gets beside others."""
+    job, rows = big_system(1, 6, "Fx", "Fp")
+    rows = np.concatenate([rows, rows[::-1] * [1.1, 0.9, 1.05, 1.0]])
+    both = gpu_fid(job, rows, step_method="taylor", precision=1)
+    alone = gpu_fid(job, rows[:1], step_method="taylor", precision=1)
+    masked = rows.copy()
+    masked[1:, 3] = 0.0
+    np.testing.assert_array_equal(alone, gpu_fid(job, masked, step_method="taylor", precision=1))
+    assert np.any(both != alone)
+
+
 def test_c2_subset_batches_consistently():
     """c2 (8 x 1H, blocks up to 70): 64 crystallites in one batch and in two."""
     cfg = W.config(2)
