@@ -166,7 +166,9 @@ __global__ void __launch_bounds__(1024) k_big_step(DevSys s, int k) {
   __shared__ double scl[3];
   const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
-  if (threadIdx.x == 0) {
+  if (s.fk && !s.fk_df) {  // k_coef's coefficients (same arithmetic), read in parallel
+    for (int kk = threadIdx.x; kk < s.nint; kk += blockDim.x) fk[kk] = s.fk[at(i * s.nint + kk, c, s.Cpad)];
+  } else if (threadIdx.x == 0) {
     double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
     double tmid = (t2 - t1) / 2.0 + t1;
     double sp, cp;
@@ -706,7 +708,13 @@ __global__ void __launch_bounds__(1024) k_big_step_df(DevSys s, int k) {
   __shared__ int nsq, nterms;
   const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
-  if (threadIdx.x == 0) {
+  if (s.fk) {  // k_coef's coefficients: hi/lo pairs after the Taylor step, doubles after eigh
+    const float2 *fk2 = reinterpret_cast<const float2 *>(s.fk);
+    for (int kk = threadIdx.x; kk < s.nint; kk += blockDim.x) {
+      const size_t a = at(i * s.nint + kk, c, s.Cpad);
+      fk[kk] = s.fk_df ? fk2[a] : dfv_of(s.fk[a]);
+    }
+  } else if (threadIdx.x == 0) {
     double t1 = s.t0[c] + double(i) * s.tau, t2 = t1 + s.tau;
     double tmid = (t2 - t1) / 2.0 + t1;
     double sp, cp;
