@@ -65,10 +65,13 @@ typedef struct {
   double wr;       /* rotor speed, Hz (0 = static powder FID, as is rotor angle 0) */
   double rotb_deg; /* rotor angle, degrees */
   double start_t;  /* start time, s */
-  int precision;   /* 0 = FP64; 1 = mixed (FP64 propagators, single-precision eigenframe, Q/R,
-                      Fave and FID terms; <= 1e-6 relative to FP64) */
+  int precision;   /* 0 = FP64; 1 = mixed (propagators in double-float, hi + lo floats, for
+                      Hamiltonian blocks up to 74; FP64 Floquet step and powder sum;
+                      single-precision eigenframe, Q/R, Fave and FID terms; <= 1e-6 relative
+                      to FP64) */
   int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
-                      1 = Taylor series with scaling and squaring; both FP64 */
+                      1 = Taylor series with scaling and squaring; FP64, or double-float in
+                      the mixed form (blocks up to 8 with step_method 1, blocks 9-74 always) */
   int fave_method; /* correlation over the rotor period: 0 = automatic (FFT for n <= 2048),
                       1 = direct O(n^2) sum, 2 = zero-padded FFT; both FP64 */
 } bl_fid_params;
