@@ -95,6 +95,10 @@ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2
 __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 acc) {
   return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
 }
+__device__ __forceinline__ float2 cdiv(float2 a, float2 b) {
+  float d = b.x * b.x + b.y * b.y;
+  return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
 __device__ __forceinline__ float2 cfmaconj(float2 a, float2 b, float2 acc) {
   return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(-a.y, b.x, acc.y)));
 }
@@ -1173,10 +1177,29 @@ struct LaneGroup {
   __device__ __forceinline__ double shfl(double v, int src) const { return __shfl_sync(mask, v, base + src); }
   __device__ __forceinline__ double2 shfl(double2 v, int src) const { return cmk(shfl(v.x, src), shfl(v.y, src)); }
   __device__ __forceinline__ int shfl(int v, int src) const { return __shfl_sync(mask, v, base + src); }
+  __device__ __forceinline__ float shfl(float v, int src) const { return __shfl_sync(mask, v, base + src); }
+  __device__ __forceinline__ float2 shfl(float2 v, int src) const {
+    return make_float2(shfl(v.x, src), shfl(v.y, src));
+  }
 };
+template <class T> struct LaneCx;
+template <> struct LaneCx<double> { using type = double2; };
+template <> struct LaneCx<float> { using type = float2; };
+__device__ __forceinline__ double2 cxm(double r, double i) { return make_double2(r, i); }
+__device__ __forceinline__ float2 cxm(float r, float i) { return make_float2(r, i); }
 
-template <int B>
+//
+// T = double: the FP64 form.  T = float (mixed form): the Cayley transform and the sweeps
+// over K in single precision; the sweeps stop one sweep after off(K)^2 <= 1e-10 diag(K)^2
+// (quadratic convergence takes that to the float floor).  V accumulates the rotations in FP64,
+// each scaled to exact unitarity first: the FID's reconstruction takes V^-1 = V^H, which a
+// single-precision V (unitary to ~1e-7 per rotation) breaks by more than 1e-6.  The
+// eigenvalues stay FP64 Rayleigh quotients of the double-float A_n: their error is quadratic
+// in V's, so the phases that the FID carries over npts points keep FP64 accuracy.
+template <int B, class T>
 __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int *__restrict__ blist, int nblist) {
+  using CT = typename LaneCx<T>::type;
+  constexpr bool F32 = sizeof(T) == sizeof(float);
   constexpr int GPW = 32 / B;             // matrices per warp
   constexpr int BQ = B + (B & 1), NP = BQ / 2;  // round-robin players (one dummy when B is odd)
   const int lane = threadIdx.x & 31;
@@ -1191,7 +1214,8 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
   const int bp = s.bpoff[k], bo = s.boff[k];
   const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
   const float4 *An4 = reinterpret_cast<const float4 *>(An);  // mixed form: double-float A
-  double2 U[B], V[B], K[B], lam[B];
+  double2 U[B], lam[B], V[B];  // V accumulates in FP64 in both forms
+  CT K[B];
 #pragma unroll
   for (int q = 0; q < B; ++q)
     U[q] = s.mixed ? df_load(An4[at(bp + r * B + q, c, s.Cpad)]) : An[at(bp + r * B + q, c, s.Cpad)];
@@ -1201,34 +1225,34 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
     double sa, ca;
     sincos(a, &sa, &ca);
     const double2 ea = cmk(ca, sa);
-    double2 M[B], X[B];
+    CT M[B], X[B];
 #pragma unroll
     for (int q = 0; q < B; ++q) {
       const double2 w = cmul(ea, U[q]);
       const double id = (q == r) ? 1.0 : 0.0;
-      M[q] = cmk(id + w.x, w.y);
-      X[q] = cmk(id - w.x, -w.y);
+      M[q] = cxm(T(id + w.x), T(w.y));
+      X[q] = cxm(T(id - w.x), T(-w.y));
     }
     // Gaussian elimination with partial pivoting (first largest |M[i][k]|, i >= k): M X' = X
 #pragma unroll
     for (int kc = 0; kc < B; ++kc) {
-      const double m2 = (r >= kc) ? M[kc].x * M[kc].x + M[kc].y * M[kc].y : -1.0;
+      const T m2 = (r >= kc) ? M[kc].x * M[kc].x + M[kc].y * M[kc].y : T(-1);
       int piv = kc;
-      double best = g.shfl(m2, kc);
+      T best = g.shfl(m2, kc);
 #pragma unroll
       for (int i = kc + 1; i < B; ++i) {
-        const double v = g.shfl(m2, i);
+        const T v = g.shfl(m2, i);
         if (v > best) best = v, piv = i;
       }
-      if (best == 0.0) st |= kSingularCayley;
+      if (best == T(0)) st |= kSingularCayley;
       const int src = (r == kc) ? piv : (r == piv ? kc : r);
 #pragma unroll
       for (int q = 0; q < B; ++q) M[q] = g.shfl(M[q], src), X[q] = g.shfl(X[q], src);
-      double2 Mk[B], Xk[B];
+      CT Mk[B], Xk[B];
 #pragma unroll
       for (int q = 0; q < B; ++q) Mk[q] = g.shfl(M[q], kc), Xk[q] = g.shfl(X[q], kc);
       if (r > kc) {
-        const double2 f = cmul(M[kc], cdiv(cmk(1, 0), Mk[kc]));
+        const CT f = cmul(M[kc], cdiv(cxm(T(1), T(0)), Mk[kc]));
 #pragma unroll
         for (int q = kc; q < B; ++q) M[q] = csub(M[q], cmul(f, Mk[q]));
 #pragma unroll
@@ -1238,20 +1262,20 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
     // back substitution, row kc on lane kc from the final rows below it
 #pragma unroll
     for (int kc = B - 1; kc >= 0; --kc) {
-      double2 acc[B];
+      CT acc[B];
 #pragma unroll
       for (int q = 0; q < B; ++q) acc[q] = X[q];
 #pragma unroll
       for (int i = kc + 1; i < B; ++i) {
-        const double2 mki = M[i];  // M[kc][i] on lane kc
+        const CT mki = M[i];  // M[kc][i] on lane kc
 #pragma unroll
         for (int q = 0; q < B; ++q) {
-          const double2 xiq = g.shfl(X[q], i);
+          const CT xiq = g.shfl(X[q], i);
           acc[q] = csub(acc[q], cmul(mki, xiq));
         }
       }
       if (r == kc) {
-        const double2 inv = cdiv(cmk(1, 0), M[kc]);
+        const CT inv = cdiv(cxm(T(1), T(0)), M[kc]);
 #pragma unroll
         for (int q = 0; q < B; ++q) X[q] = cmul(acc[q], inv);
       }
@@ -1259,31 +1283,38 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
     // K = Hermitian part of i X (row r needs column r of X: X[q][r] from lane q), V = I
 #pragma unroll
     for (int q = 0; q < B; ++q) {
-      double2 xqr = cmk(0, 0);
+      CT xqr = cxm(T(0), T(0));
 #pragma unroll
       for (int t = 0; t < B; ++t) {
-        const double2 v = g.shfl(X[t], q);
+        const CT v = g.shfl(X[t], q);
         if (t == r) xqr = v;
       }
-      const double2 krq = cmk(-X[q].y, X[q].x), kqr = cmk(-xqr.y, xqr.x);
-      K[q] = cscale(cadd(krq, cconj(kqr)), 0.5);
+      const CT krq = cxm(-X[q].y, X[q].x), kqr = cxm(-xqr.y, xqr.x);
+      K[q] = cscale(cadd(krq, cconj(kqr)), T(0.5));
       V[q] = cmk(q == r ? 1.0 : 0.0, 0.0);
     }
 #pragma unroll
     for (int q = 0; q < B; ++q)
-      if (q == r) K[q].y = 0.0;
-    bool conv = false;
+      if (q == r) K[q].y = T(0);
+    bool conv = false, polish = false;
     for (int sweep = 0; sweep < kMaxSweeps && !conv; ++sweep) {
-      double off = 0, dg = 0;
+      T off = 0, dg = 0;
 #pragma unroll
       for (int q = 0; q < B; ++q) {
         if (q > r) off += K[q].x * K[q].x + K[q].y * K[q].y;
         if (q == r) dg += K[q].x * K[q].x;
       }
-      double offs = 0, dgs = 0;
+      T offs = 0, dgs = 0;
 #pragma unroll
       for (int t = 0; t < B; ++t) offs += g.shfl(off, t), dgs += g.shfl(dg, t);
-      if (offs <= 1e-34 * dgs || offs == 0.0) {
+      if (F32) {
+        const bool small = offs <= T(1e-10) * dgs || offs == T(0);
+        if (small && (polish || offs == T(0))) {
+          conv = true;
+          break;
+        }
+        polish = polish || small;
+      } else if (offs <= 1e-34 * dgs || offs == 0.0) {
         conv = true;
         break;
       }
@@ -1302,25 +1333,25 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
         }
         // the pair's rotation, computed identically by both of its lanes from K[p][q]
         // (lane p's entry q), K[p][p] and K[q][q]
-        double2 own_q = cmk(0, 0), own_d = cmk(0, 0);
+        CT own_q = cxm(T(0), T(0)), own_d = cxm(T(0), T(0));
 #pragma unroll
         for (int q2 = 0; q2 < B; ++q2) {
           if (q2 == mq) own_q = K[q2];
           if (q2 == r) own_d = K[q2];
         }
-        const double2 hpq = g.shfl(own_q, mp);
-        const double kpp = g.shfl(own_d.x, mp), kqq = g.shfl(own_d.x, mq);
-        double cs = 1.0;
-        double2 sp = cmk(0, 0);
+        const CT hpq = g.shfl(own_q, mp);
+        const T kpp = g.shfl(own_d.x, mp), kqq = g.shfl(own_d.x, mq);
+        T cs = T(1);
+        CT sp = cxm(T(0), T(0));
         if (paired) {
-          const double ab = hypot(hpq.x, hpq.y);
-          if (ab != 0.0) {
-            const double2 ph = cmk(hpq.x / ab, hpq.y / ab);
-            const double theta = 0.5 * (kqq - kpp) / ab;
-            double tt;
-            if (fabs(theta) > 1e100) tt = 0.5 / theta;
-            else tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
-            cs = rsqrt(fma(tt, tt, 1.0));
+          const T ab = hypot(hpq.x, hpq.y);
+          if (ab != T(0)) {
+            const CT ph = cxm(hpq.x / ab, hpq.y / ab);
+            const T theta = T(0.5) * (kqq - kpp) / ab;
+            T tt;
+            if (fabs(theta) > T(F32 ? 1e18 : 1e100)) tt = T(0.5) / theta;  // theta^2 stays finite
+            else tt = copysign(T(1), theta) / (fabs(theta) + sqrt(fma(theta, theta, T(1))));
+            cs = rsqrt(fma(tt, tt, T(1)));
             sp = cscale(ph, tt * cs);
           }
         }
@@ -1332,31 +1363,39 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
           int q = j2 == 0 ? 0 : 1 + (j2 - 1 + round) % (BQ - 1);
           if (p > q) { const int x = p; p = q; q = x; }
           if (q >= B) continue;
-          const double cst = g.shfl(cs, p);
-          const double2 spt = g.shfl(sp, p), spc = cconj(spt);
-          const double2 kp = K[p], kq = K[q];
+          const T cst = g.shfl(cs, p);
+          const CT spt = g.shfl(sp, p), spc = cconj(spt);
+          const CT kp = K[p], kq = K[q];
           K[p] = csub(cscale(kp, cst), cmul(spc, kq));
           K[q] = cadd(cmul(spt, kp), cscale(kq, cst));
+          // V in FP64; a single-precision rotation is first scaled to c^2 + |s|^2 = 1 in FP64,
+          // so that V stays unitary to FP64 rounding
+          double cd = cst;
+          double2 sd = todbl(spt);
+          if (F32) {
+            const double nn = 1.0 / sqrt(fma(cd, cd, fma(sd.x, sd.x, sd.y * sd.y)));
+            cd *= nn, sd = cscale(sd, nn);
+          }
           const double2 vp = V[p], vq = V[q];
-          V[p] = csub(cscale(vp, cst), cmul(spc, vq));
-          V[q] = cadd(cmul(spt, vp), cscale(vq, cst));
+          V[p] = csub(cscale(vp, cd), cmul(cconj(sd), vq));
+          V[q] = cadd(cmul(sd, vp), cscale(vq, cd));
         }
         // rows p, q of K: K <- G^H K, as row = alpha row_p + beta row_q in every lane
         // (lane p: cs, -sp; lane q: conj(sp), cs; a lane without a pair keeps its row)
         const bool isp = paired && r == mp;
-        const double2 al = !paired ? cmk(1, 0) : (isp ? cmk(cs, 0) : cconj(sp));
-        const double2 be = !paired ? cmk(0, 0) : (isp ? cmk(-sp.x, -sp.y) : cmk(cs, 0));
+        const CT al = !paired ? cxm(T(1), T(0)) : (isp ? cxm(cs, T(0)) : cconj(sp));
+        const CT be = !paired ? cxm(T(0), T(0)) : (isp ? cxm(-sp.x, -sp.y) : cxm(cs, T(0)));
 #pragma unroll
         for (int q2 = 0; q2 < B; ++q2) {
-          const double2 kpk = g.shfl(K[q2], mp), kqk = g.shfl(K[q2], mq);
+          const CT kpk = g.shfl(K[q2], mp), kqk = g.shfl(K[q2], mq);
           if (paired) K[q2] = cadd(cmul(al, kpk), cmul(be, kqk));
         }
-        if (paired && !(sp.x == 0.0 && sp.y == 0.0)) {
+        if (paired && !(sp.x == T(0) && sp.y == T(0))) {
           const int other = isp ? mq : mp;
 #pragma unroll
           for (int q2 = 0; q2 < B; ++q2) {
-            if (q2 == other) K[q2] = cmk(0, 0);
-            if (q2 == r) K[q2].y = 0.0;
+            if (q2 == other) K[q2] = cxm(T(0), T(0));
+            if (q2 == r) K[q2].y = T(0);
           }
         }
       }
@@ -1369,13 +1408,13 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
 #pragma unroll
     for (int l = 0; l < B; ++l)
 #pragma unroll
-      for (int q = 0; q < B; ++q) uv[q] = cfma(U[l], g.shfl(V[q], l), uv[q]);  // (U V)[r][q], l ascending
+      for (int q = 0; q < B; ++q) uv[q] = cfma(U[l], todbl(g.shfl(V[q], l)), uv[q]);  // (U V)[r][q], l ascending
 #pragma unroll
     for (int q = 0; q < B; ++q) lam[q] = cmk(0, 0);
 #pragma unroll
     for (int kk = 0; kk < B; ++kk)
 #pragma unroll
-      for (int q = 0; q < B; ++q) lam[q] = cfmaconj(g.shfl(V[q], kk), g.shfl(uv[q], kk), lam[q]);
+      for (int q = 0; q < B; ++q) lam[q] = cfmaconj(todbl(g.shfl(V[q], kk)), g.shfl(uv[q], kk), lam[q]);
     if (pass == 1) break;
     double mind = 4.0;
 #pragma unroll
@@ -1403,7 +1442,7 @@ __global__ void __launch_bounds__(kThreads) k_floquet_lanes(DevSys s, const int 
   }
   if (st && r == 0) atomicOr(s.status, st);
 #pragma unroll
-  for (int q = 0; q < B; ++q) s.VF[at(bp + r * B + q, c, s.Cpad)] = V[q];
+  for (int q = 0; q < B; ++q) s.VF[at(bp + r * B + q, c, s.Cpad)] = todbl(V[q]);
   double2 lr = cmk(0, 0);
 #pragma unroll
   for (int q = 0; q < B; ++q)
@@ -2756,7 +2795,8 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
         k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl);
       } else {  // B lanes per matrix, 32/B matrices per warp
         const long warps = (Cp * nl + (32 / B) - 1) / (32 / B);
-        k_floquet_lanes<B><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
+        if (s.mixed) k_floquet_lanes<B, float><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
+        else k_floquet_lanes<B, double><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
       }
       break;
     case 3:
