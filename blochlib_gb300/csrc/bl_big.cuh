@@ -405,19 +405,153 @@ struct FloqWork {
   double2 *Mm, *Xk, *rot, *fv, *lam;
   int *rpair;
   double *red;
+  float2 *Kf;  // MIX: b x b single-precision K
 };
 
+// The parallel Jacobi sweeps of floquet_cta over K (Xk, element type KC) with V (Mm, FP64)
+// accumulating the rotations; returns convergence.  KC = double2: the FP64 form.  KC =
+// float2 (mixed form): K in single precision, the sweeps stop one sweep after
+// off(K)^2 <= 1e-10 diag(K)^2, and each rotation is scaled to c^2 + |s|^2 = 1 in FP64
+// before V takes it, so that V stays unitary to FP64 rounding.
+template <class KC>
+__device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const FloqWork &wk) {
+  using R = decltype(KC::x);
+  constexpr bool F32 = sizeof(R) == sizeof(float);
+  auto rot = [&](int t, int q) -> double2 & { return wk.rot[2 * t + q]; };
+  auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
+  double *red = wk.red;
+  const int bb = b * b;
+  const int bq = b + (b & 1);  // players in the round-robin (one dummy when b is odd)
+  const int np = bq / 2;
+  bool conv = false, polish = false;
+  for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
+    double off = 0, dg = 0;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const int r = e / b, q = e % b;
+      const double2 v = todbl(Xk[e]);
+      if (r < q) off += v.x * v.x + v.y * v.y;
+      else if (r == q) dg += v.x * v.x;
+    }
+    red[threadIdx.x] = off;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double so = 0;
+      for (int t = 0; t < blockDim.x; ++t) so += red[t];
+      red[0] = so;
+    }
+    __syncthreads();
+    const double offs = red[0];
+    __syncthreads();
+    red[threadIdx.x] = dg;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sd = 0;
+      for (int t = 0; t < blockDim.x; ++t) sd += red[t];
+      red[0] = sd;
+    }
+    __syncthreads();
+    const double dgs = red[0];
+    __syncthreads();
+    if (F32) {  // offs, dgs are the same in every thread: polish too
+      const bool small = offs <= 1e-10 * dgs || offs == 0.0;
+      if (small && (polish || offs == 0.0)) {
+        conv = true;
+        break;
+      }
+      polish = polish || small;
+    } else if (offs <= 1e-34 * dgs || offs == 0.0) {
+      conv = true;
+      break;
+    }
+    for (int round = 0; round < bq - 1; ++round) {
+      for (int t = threadIdx.x; t < np; t += blockDim.x) {
+        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (bq - 1); };
+        int p = player(t), q = player(bq - 1 - t);
+        if (p > q) {
+          int tmp = p;
+          p = q, q = tmp;
+        }
+        rpair(t, 0) = p, rpair(t, 1) = q;
+        rot(t, 0) = cmk(1, 0), rot(t, 1) = cmk(0, 0);
+        if (q < b) {
+          const KC hpq = Xk[p * b + q];
+          const R ab = hypot(hpq.x, hpq.y);
+          if (ab != R(0)) {
+            const R phx = hpq.x / ab, phy = hpq.y / ab;
+            const R theta = R(0.5) * (Xk[q * b + q].x - Xk[p * b + p].x) / ab;
+            R tt;
+            if (fabs(theta) > R(F32 ? 1e18 : 1e100)) tt = R(0.5) / theta;  // theta^2 stays finite
+            else tt = copysign(R(1), theta) / (fabs(theta) + sqrt(fma(theta, theta, R(1))));
+            const R cc = rsqrt(fma(tt, tt, R(1)));
+            double cd = cc;
+            double2 sd = cmk(double(phx * (tt * cc)), double(phy * (tt * cc)));
+            if (F32) {
+              const double nn = 1.0 / sqrt(fma(cd, cd, fma(sd.x, sd.x, sd.y * sd.y)));
+              cd *= nn, sd = cscale(sd, nn);
+            }
+            rot(t, 0) = cmk(cd, 0.0);
+            rot(t, 1) = sd;
+          }
+        }
+      }
+      __syncthreads();
+      // columns p, q of K and V:  K <- K G, V <- V G  with G = [[c, sp], [-conj(sp), c]]
+      for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
+        const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        if (q >= b) continue;
+        const double cc = rot(t, 0).x;
+        const double2 sp = rot(t, 1), spc = cconj(sp);
+        if (rem2 < b) {
+          const R ccr = R(cc);
+          const KC spr = cxm(R(sp.x), R(sp.y)), spcr = cxm(R(spc.x), R(spc.y));
+          const KC xkp = Xk[kk * b + p], xkq = Xk[kk * b + q];
+          Xk[kk * b + p] = csub(cscale(xkp, ccr), cmul(spcr, xkq));
+          Xk[kk * b + q] = cadd(cmul(spr, xkp), cscale(xkq, ccr));
+        } else {
+          const double2 xkp = Mm[kk * b + p], xkq = Mm[kk * b + q];
+          Mm[kk * b + p] = csub(cscale(xkp, cc), cmul(spc, xkq));
+          Mm[kk * b + q] = cadd(cmul(sp, xkp), cscale(xkq, cc));
+        }
+      }
+      __syncthreads();
+      // rows p, q of K:  K <- G^H K
+      for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
+        const int t = e / b, kk = e % b;
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        if (q >= b) continue;
+        const R cc = R(rot(t, 0).x);
+        const KC sp = cxm(R(rot(t, 1).x), R(rot(t, 1).y)), spc = cconj(sp);
+        const KC xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
+        Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
+        Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < np; t += blockDim.x) {
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        if (q >= b || (rot(t, 1).x == 0.0 && rot(t, 1).y == 0.0)) continue;
+        Xk[p * b + q] = cxm(R(0), R(0)), Xk[q * b + p] = cxm(R(0), R(0));
+        Xk[p * b + p].y = R(0), Xk[q * b + q].y = R(0);
+      }
+      __syncthreads();
+    }
+  }
+  return conv;
+}
+
 // sweeps0 < kMaxSweeps: the first pass only locates the spectrum (that many sweeps); the
-// second pass, with -1 in the widest gap of those eigenphases, always follows.
-__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps, bool dfA = false) {
+// second pass, with -1 in the widest gap of those eigenphases, always follows.  MIX (mixed
+// form): A_n is double-float and the sweeps run over a single-precision K (wk.Kf); the
+// eigenvalues stay FP64 Rayleigh quotients, whose error is quadratic in V's.
+template <bool MIX>
+__device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps) {
+  constexpr bool dfA = MIX;
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
   const int b = s.bs[k], bp = s.bpoff[k], bo = s.boff[k], bb = b * b;
   double2 *Mm = wk.Mm, *Xk = wk.Xk, *fv = wk.fv, *lam = wk.lam;
   double *red = wk.red;
-  auto rot = [&](int t, int q) -> double2 & { return wk.rot[2 * t + q]; };
-  auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
   const double2 *U = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;  // U(r,q) = U[at(bp + r*b + q, c)]
   const float4 *U4 = reinterpret_cast<const float4 *>(U);      // dfA: double-float A (mixed form)
   auto Ug = [&](int r, int q) {
@@ -498,101 +632,14 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
     __syncthreads();
     for (int e = threadIdx.x; e < b; e += blockDim.x) Xk[e * b + e].y = 0.0;
     __syncthreads();
-    const int bq = b + (b & 1);  // players in the round-robin (one dummy when b is odd)
-    const int np = bq / 2;
-    bool conv = false;
     const int max_sweeps = pass == 0 ? sweeps0 : kMaxSweeps;
-    for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
-      double off = 0, dg = 0;
-      for (int e = threadIdx.x; e < bb; e += blockDim.x) {
-        const int r = e / b, q = e % b;
-        const double2 v = Xk[e];
-        if (r < q) off += v.x * v.x + v.y * v.y;
-        else if (r == q) dg += v.x * v.x;
-      }
-      red[threadIdx.x] = off;
+    bool conv;
+    if (MIX) {
+      for (int e = threadIdx.x; e < bb; e += blockDim.x) wk.Kf[e] = make_float2(float(Xk[e].x), float(Xk[e].y));
       __syncthreads();
-      if (threadIdx.x == 0) {
-        double so = 0;
-        for (int t = 0; t < blockDim.x; ++t) so += red[t];
-        red[0] = so;
-      }
-      __syncthreads();
-      const double offs = red[0];
-      __syncthreads();
-      red[threadIdx.x] = dg;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double sd = 0;
-        for (int t = 0; t < blockDim.x; ++t) sd += red[t];
-        red[0] = sd;
-      }
-      __syncthreads();
-      const double dgs = red[0];
-      __syncthreads();
-      if (offs <= 1e-34 * dgs || offs == 0.0) {
-        conv = true;
-        break;
-      }
-      for (int round = 0; round < bq - 1; ++round) {
-        for (int t = threadIdx.x; t < np; t += blockDim.x) {
-          auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (bq - 1); };
-          int p = player(t), q = player(bq - 1 - t);
-          if (p > q) {
-            int tmp = p;
-            p = q, q = tmp;
-          }
-          rpair(t, 0) = p, rpair(t, 1) = q;
-          rot(t, 0) = cmk(1, 0), rot(t, 1) = cmk(0, 0);
-          if (q < b) {
-            const double2 hpq = Xk[p * b + q];
-            const double ab = hypot(hpq.x, hpq.y);
-            if (ab != 0.0) {
-              const double2 ph = cmk(hpq.x / ab, hpq.y / ab);
-              const double theta = 0.5 * (Xk[q * b + q].x - Xk[p * b + p].x) / ab;
-              double tt;
-              if (fabs(theta) > 1e100) tt = 0.5 / theta;
-              else tt = copysign(1.0, theta) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
-              const double cc = rsqrt(fma(tt, tt, 1.0));
-              rot(t, 0) = cmk(cc, 0.0);
-              rot(t, 1) = cscale(ph, tt * cc);
-            }
-          }
-        }
-        __syncthreads();
-        // columns p, q of K and V:  K <- K G, V <- V G  with G = [[c, sp], [-conj(sp), c]]
-        for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
-          const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
-          double2 *Mx = rem2 < b ? Xk : Mm;
-          const int p = rpair(t, 0), q = rpair(t, 1);
-          if (q >= b) continue;
-          const double cc = rot(t, 0).x;
-          const double2 sp = rot(t, 1), spc = cconj(sp);
-          const double2 xkp = Mx[kk * b + p], xkq = Mx[kk * b + q];
-          Mx[kk * b + p] = csub(cscale(xkp, cc), cmul(spc, xkq));
-          Mx[kk * b + q] = cadd(cmul(sp, xkp), cscale(xkq, cc));
-        }
-        __syncthreads();
-        // rows p, q of K:  K <- G^H K
-        for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
-          const int t = e / b, kk = e % b;
-          const int p = rpair(t, 0), q = rpair(t, 1);
-          if (q >= b) continue;
-          const double cc = rot(t, 0).x;
-          const double2 sp = rot(t, 1), spc = cconj(sp);
-          const double2 xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
-          Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
-          Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
-        }
-        __syncthreads();
-        for (int t = threadIdx.x; t < np; t += blockDim.x) {
-          const int p = rpair(t, 0), q = rpair(t, 1);
-          if (q >= b || (rot(t, 1).x == 0.0 && rot(t, 1).y == 0.0)) continue;
-          Xk[p * b + q] = cmk(0, 0), Xk[q * b + p] = cmk(0, 0);
-          Xk[p * b + p].y = 0.0, Xk[q * b + q].y = 0.0;
-        }
-        __syncthreads();
-      }
+      conv = floquet_sweeps<float2>(wk.Kf, Mm, b, max_sweeps, wk);
+    } else {
+      conv = floquet_sweeps<double2>(Xk, Mm, b, max_sweeps, wk);
     }
     if (!conv && max_sweeps == kMaxSweeps) atomicOr(s.status, kNoConvergeFloquet);
     // Rayleigh quotients lam_r = v_r^H U v_r
@@ -647,7 +694,12 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   __shared__ double2 lam[kMaxBigBlock];
   __shared__ double red[kBigThreads];
   const int b = s.bs[k];
-  floquet_cta(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red}, kMaxSweeps, s.mixed != 0);
+  if (s.mixed) {  // K in single precision after the two b x b double2 arrays
+    floquet_cta<true>(s, k, blockIdx.x,
+                      FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, reinterpret_cast<float2 *>(bsc + 2 * b * b)});
+  } else {
+    floquet_cta<false>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, nullptr});
+  }
 }
 
 // ------------------------------------------------------------------ mixed form, double-float

@@ -2536,7 +2536,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
       attr((const void *)k_big_eigframe<2, float2>, smem_mat);
-      attr((const void *)k_big_floquet, smem_mat);
+      attr((const void *)k_big_floquet, smem_mat + (J.mixed ? smem_mat / 4 : 0));  // + b^2 float2 (K)
       size_t smem_hf = 0;
       for (int k : J.huge_blocks) smem_hf = std::max(smem_hf, huge_floquet_smem(L.size[k]));
       if (smem_hf > (size_t(48) << 10)) attr((const void *)k_huge_floquet, smem_hf);
@@ -3018,7 +3018,9 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
           else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);
         }
         break;
-      case 2: k_big_floquet<<<unsigned(s.C), kBigThreads, smat, st>>>(s, k); break;
+      case 2:  // the mixed form's single-precision K follows the two b x b double2 arrays
+        k_big_floquet<<<unsigned(s.C), kBigThreads, smat + (s.mixed ? sizeof(float2) * size_t(b) * b : 0), st>>>(s, k);
+        break;
       case 3:
         if (s.mixed) {
           if (nt1) k_big_eigframe<1, float2><<<unsigned(s.C), th, sw, st>>>(s, k);

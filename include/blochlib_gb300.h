@@ -67,7 +67,7 @@ typedef struct {
   double start_t;  /* start time, s */
   int precision;   /* 0 = FP64; 1 = mixed (propagators in double-float, hi + lo floats, for
                       Hamiltonian blocks up to 74; Floquet eigenvalues and vectors and the
-                      powder sum in FP64 (blocks up to 8 sweep in FP32);
+                      powder sum in FP64, the Jacobi sweeps over the Cayley K in FP32;
                       single-precision eigenframe, Q/R, Fave and FID terms; <= 1e-6 relative
                       to FP64) */
   int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
