@@ -540,12 +540,12 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
 }
 
 // sweeps0 < kMaxSweeps: the first pass only locates the spectrum (that many sweeps); the
-// second pass, with -1 in the widest gap of those eigenphases, always follows.  MIX (mixed
-// form): A_n is double-float and the sweeps run over a single-precision K (wk.Kf); the
+// second pass, with -1 in the widest gap of those eigenphases, always follows.  DFA: A_n is
+// double-float (mixed form).  K32: the sweeps run over a single-precision K (wk.Kf); the
 // eigenvalues stay FP64 Rayleigh quotients, whose error is quadratic in V's.
-template <bool MIX>
+template <bool DFA, bool K32>
 __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int sweeps0 = kMaxSweeps) {
-  constexpr bool dfA = MIX;
+  constexpr bool dfA = DFA;
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
@@ -634,7 +634,7 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
     __syncthreads();
     const int max_sweeps = pass == 0 ? sweeps0 : kMaxSweeps;
     bool conv;
-    if (MIX) {
+    if (K32) {
       for (int e = threadIdx.x; e < bb; e += blockDim.x) wk.Kf[e] = make_float2(float(Xk[e].x), float(Xk[e].y));
       __syncthreads();
       conv = floquet_sweeps<float2>(wk.Kf, Mm, b, max_sweeps, wk);
@@ -694,11 +694,13 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   __shared__ double2 lam[kMaxBigBlock];
   __shared__ double red[kBigThreads];
   const int b = s.bs[k];
-  if (s.mixed) {  // K in single precision after the two b x b double2 arrays
-    floquet_cta<true>(s, k, blockIdx.x,
-                      FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, reinterpret_cast<float2 *>(bsc + 2 * b * b)});
+  if (s.floq32) {  // K in single precision after the two b x b double2 arrays
+    floquet_cta<true, true>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red,
+                                                       reinterpret_cast<float2 *>(bsc + 2 * b * b)});
+  } else if (s.mixed) {
+    floquet_cta<true, false>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, nullptr});
   } else {
-    floquet_cta<false>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, nullptr});
+    floquet_cta<false, false>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, nullptr});
   }
 }
 
@@ -738,6 +740,7 @@ __device__ void cta_mm_sym_df(const float2 *A, const float2 *B, float2 *C, int m
 }
 
 // 1/k for the Taylor terms, double-float
+static_assert(kTaylorTerms == 15, "inv_df covers the terms 2..15");
 __device__ __forceinline__ float2 inv_df(int kt) {
   switch (kt) {
     case 2: return dfv_const(1.0 / 2); case 3: return dfv_const(1.0 / 3); case 4: return dfv_const(1.0 / 4);

@@ -169,6 +169,9 @@ struct DevSys {
   int is_static;             // static powder FID (oneFID.h:292-336): dt = 1/sw, n = p-period
   int gper;                  // period of the FID split fid[j*gper + p] (n, or the p2p base)
   int p2p, pb, pf, psub;     // point-to-point FID: base, factor, steps per chunk
+  // mixed form: 1 when the Floquet sweeps over K may run in FP32, i.e. the FID raises the
+  // Floquet eigenvalues to at most kFloq32MaxPeriods periods (phase errors grow with the power)
+  int floq32;
   double dt;
   const int *srp, *seo;      // per D pair (a,b): the rho pair (b,a) and first element, or -1
   const double2 *tw;         // exp(-2 pi i k / M), k < M/2
@@ -759,6 +762,11 @@ __global__ void __launch_bounds__(kThreads) k_step_prop(DevSys s, const int *__r
     }
 }
 
+// Largest power of the period propagator (periods the FID spans: npts/n for the gamma-COMPUTE
+// FID, npts*factor/base for the point-to-point one) for which the mixed form sweeps over the
+// Floquet K in FP32: the residual ~1e-7 off-diagonal of V's basis grows into the eigenphases
+// with the power, and the c-workloads' FIDs span at most 21 periods.
+constexpr long kFloq32MaxPeriods = 64;
 constexpr int kTaylorTerms = 15;  // ||x|| <= 1/2: remainder 0.5^16/16! < 1e-18
 
 // Taylor degree for exp(-iX) with ||X||_inf = x <= 1/2: the smallest K whose first omitted
@@ -2756,6 +2764,11 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.ra = J.ra.p, s.rb = J.rb.p, s.roff = J.roff.p, s.rhooff = J.rhooff.p;
   s.Dblk = J.Dblk.p, s.Rhoblk = J.Rhoblk.p;
   s.mixed = J.mixed;
+  s.floq32 = 0;
+  if (J.mixed && J.n > 0 && J.pb > 0) {  // the mixed form spins (never static)
+    const long periods = J.p2p ? (long(p.npts) - 1) * J.pf / J.pb + 1 : (long(p.npts) - 1) / J.n + 1;
+    s.floq32 = periods <= kFloq32MaxPeriods ? 1 : 0;
+  }
   s.Wf = J.Wf.p, s.Qf = J.Qf.p, s.Rf = J.Rf.p, s.Gf = J.Gf.p, s.Zf = J.Zf.p;
   s.eq = J.eq.p, s.erev = J.erev.p, s.er = J.er.p, s.erg = J.erg.p, s.esg = J.esg.p;
   s.U = J.U.p, s.A = J.A.p, s.VF = J.VF.p, s.L = J.Lb.p, s.Q = J.Q.p, s.R = J.R.p, s.G = J.G.p, s.Z = J.Z.p;
@@ -2795,7 +2808,7 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
         k_floquet<B><<<grid_for(Cp * nl), kThreads, 0, st>>>(s, bl, nl);
       } else {  // B lanes per matrix, 32/B matrices per warp
         const long warps = (Cp * nl + (32 / B) - 1) / (32 / B);
-        if (s.mixed) k_floquet_lanes<B, float><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
+        if (s.floq32) k_floquet_lanes<B, float><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
         else k_floquet_lanes<B, double><<<grid_for(warps * 32), kThreads, 0, st>>>(s, bl, nl);
       }
       break;
@@ -3019,7 +3032,7 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         }
         break;
       case 2:  // the mixed form's single-precision K follows the two b x b double2 arrays
-        k_big_floquet<<<unsigned(s.C), kBigThreads, smat + (s.mixed ? sizeof(float2) * size_t(b) * b : 0), st>>>(s, k);
+        k_big_floquet<<<unsigned(s.C), kBigThreads, smat + (s.floq32 ? sizeof(float2) * size_t(b) * b : 0), st>>>(s, k);
         break;
       case 3:
         if (s.mixed) {

@@ -321,5 +321,5 @@ __global__ void __launch_bounds__(kHugeFloqThreads) k_huge_floquet(DevSys s, Hug
   double *red = reinterpret_cast<double *>(lam + b);
   int *rpair = reinterpret_cast<int *>(red + (b > kHugeFloqThreads ? b : kHugeFloqThreads));
   double2 *Mm = ws + hf.ws[blockIdx.y] + size_t(blockIdx.x) * 2 * b * b;
-  floquet_cta<false>(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red, nullptr}, kHugeFloqSweeps0);
+  floquet_cta<false, false>(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red, nullptr}, kHugeFloqSweeps0);
 }

@@ -63,6 +63,20 @@ def test_p2p_big_blocks_match_oracle(seed, nspin, rho, det):
     assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
+@pytest.mark.parametrize("seed,nspin", [(0, 5), (2, 6)])
+def test_p2p_big_blocks_mixed_within_1e6(seed, nspin):
+    """The mixed form's large-block kernels (double-float step and Dyson, FP32 sweeps over K)
+    on the point-to-point path, with a chunk rf schedule on top: <= 1e-6 against the oracle."""
+    rng = np.random.default_rng(950 + seed)
+    job, rows = big_system(seed, nspin, "Fx", "Fp")
+    b = int(rng.integers(2, 6))
+    job = as_p2p(job, rng, base=b, factor=int(rng.integers(1, 8)))
+    job += f"rfc: {int(rng.integers(0, b))} 1H {rng.uniform(1e4, 5e4):.9g} 0 0\n"
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method="taylor", precision=1)
+    assert 0 < rel(fid, ref) <= 1e-6, rel(fid, ref)
+
+
 def test_p2p_gcd_reduction():
     """PropReduce divides base and factor by their gcd: (12, 8) is (3, 2)."""
     rng = np.random.default_rng(3)
