@@ -38,6 +38,9 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "powder FIDs/s & p50/p99 latency, mixed vs FP64 GPU path at ≤1e-6 rel err"
 UNIT = "powder FIDs/s"
+# the mixed form's arithmetic: step and Dyson in double-float (hi + lo floats) on the FP32 pipe,
+# Floquet eigenvalues/vectors and the powder sum in FP64, eigenframe, Q/R, Fave and FID terms in FP32
+MIXED_DTYPE = "f64+df32+f32 (double-float: step, Dyson; f64: Floquet, powder sum; f32: eigenframe, Q/R, Fave, FID)"
 
 
 def dist_env():
@@ -329,7 +332,7 @@ def run_batch(args):
     print(json.dumps({
         "metric": METRIC, "value": forms["mixed"]["fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
         "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["seconds"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded, workloads.py config 3)",
+        "vs_baseline": None, "dtype": MIXED_DTYPE, "data": "synthetic (seeded, workloads.py config 3)",
         "config": {"workload": f"c3 batching form: {len(cfgs)} seeded systems, dims {dims}, n 64-256, 1024 points, "
                                "powders 144/320/678/1154, all submitted at once", "lanes": args.lanes,
                    "pool_gib": args.pool_gib, "precision": "mixed (FP64 row for comparison)"},
@@ -397,7 +400,7 @@ def run_serving(args):
     print(json.dumps({
         "metric": METRIC, "value": forms["mixed"]["achieved_fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
         "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["total_s"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic seeded Poisson stream (workloads.py)",
+        "vs_baseline": None, "dtype": MIXED_DTYPE, "data": "synthetic seeded Poisson stream (workloads.py)",
         "config": {"workload": f"c4 serving form: Poisson {args.rate}/s for {args.duration} s, 90% c3-like, 10% "
                                "9-10 x 1H (dims 512-1024) on rep100", "lanes": args.lanes, "pool_gib": args.pool_gib,
                    "drain_s": args.drain},
@@ -513,7 +516,7 @@ def main():
     h2d += 8 * 4 * len(cfg["powder"][0]) + 2 * ro.nbytes  # the caller's powder arrays and rho/det
     if d.rank != 0:
         return 0
-    dtype = "f64" if prec == "fp64" else "f64+df32+f32 (double-float: step, Dyson; f64: Floquet, powder sum)"
+    dtype = "f64" if prec == "fp64" else MIXED_DTYPE
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
