@@ -1,20 +1,27 @@
 #!/usr/bin/env python3
-"""Benchmark: powder FIDs/s of the spinning powder-FID path on one GB300.
+"""Benchmark: powder FIDs/s of the spinning powder-FID path on one GB300, mixed precision
+against plain FP64.
 
-A step is one powder-averaged FID of the workload (default c1: 4 x 1H, dim 16, 3722 ZCW
-crystallites, 128 steps per rotor period, 2048 points; blochlib_gb300/workloads.py).
+A step is one powder-averaged FID of the workload.  Default: c2 (8 x 1H, dim 256, 1154 ZCW
+crystallites, 200 steps per rotor period, 4096 points; blochlib_gb300/workloads.py) in the
+mixed form, with the FP64 form of the same job beside it, and the other configurations as
+extra keys of the same line: c1 (both forms), c3 (the batching form: 512 seeded systems
+through the serving loop, both forms) and c4 (the serving form: a 60 s Poisson stream, both
+forms, p50/p99).
 
-  value     FIDs/s with every input resident in HBM (bl_job_run), CUDA events on the
-            engine's stream around exactly K steps, max over ranks.
-  e2e       FIDs/s through the reference-facing call (bl_powder_fid: host buffers in,
-            upload, compute, FID read back), wall clock around K calls.
-  roofline  the stage with the largest share of the timed region: its algorithmic FP64
-            flop per run / its CUDA-event time per run, against the DFMA peak measured
-            live by the engine's probe kernel.
-  cpu_baseline  the reference's own CPU path (oracle/_ref/ref_fid, as shipped), one
-            process per host core over contiguous crystallite ranges, on a bounded sample,
-            scaled to FIDs/s; the CPU restatement (oracle) where the reference binary is
-            absent.
+  value     FIDs/s of the mixed form with every input resident in HBM (bl_job_run), CUDA
+            events on the engine's stream around exactly K steps, max over ranks.
+  precision_forms  the FP64 form of the same job, the mixed form's relative L2 error against
+            it and the speed-up.
+  e2e       FIDs/s through the reference-facing call (oneFID.FID -> bl_powder_fid: host buffers
+            in, upload, compute, FID read back), wall clock around the calls.
+  roofline  per stage: algorithmic flop per run / CUDA-event time per run against the unit
+            that bounds the stage (FP64 pipe: live DFMA probe; FP32 pipe: live FFMA probe;
+            tensor pipe: MEASURED_PEAKS.json bf16); the headline is the stage with the largest
+            share of the timed region.
+  cpu_baseline  the reference's own CPU path (oracle/_ref/ref_fid, as shipped), one process
+            per host core on a bounded crystallite sample, scaled to FIDs/s; the CPU
+            restatement (oracle) where the reference binary is absent.
 
 --impl reference times only that CPU path (rank 0), on the same workload and metric.
 Multi-GPU: crystallites are independent, so N ranks run N replicas (weak scaling) with no
@@ -189,7 +196,6 @@ def _ref_binary():
 
 def _cpu_run(binary, cfg, ranges, tmp):
     """Runs one process per (start, count) range concurrently; returns wall seconds."""
-    from blochlib_gb300 import workloads as W
     phi, theta, gamma, w = cfg["powder"]
     procs = []
     t0 = time.perf_counter()
@@ -210,20 +216,36 @@ def _cpu_run(binary, cfg, ranges, tmp):
 
 
 def cpu_baseline(cfg, target_s=15.0, cores=None):
+    """One process per core, each on its own contiguous crystallite range of k crystallites:
+    first k = 1 (one crystallite per core already exceeds target_s for c2), then, if that
+    took well under target_s, k scaled up to fill it.  Returns FIDs/s scaled from the sample."""
     binary, kind = _ref_binary()
     cores = cores or os.cpu_count() or 1
     C = len(cfg["powder"][0])
     with tempfile.TemporaryDirectory() as tmp:
-        t2 = _cpu_run(binary, cfg, [(0, 2)], tmp)
-        per = max(t2 / 2, 1e-4)
-        k = int(max(1, min(C // cores, round(target_s / per))))
-        ranges = [(i * k % max(C - k, 1), k) for i in range(cores)]
+        k = 1
+        ranges = [(i * max(1, C // cores) % max(C - k + 1, 1), k) for i in range(cores)]
         wall = _cpu_run(binary, cfg, ranges, tmp)
+        if wall < 0.4 * target_s:
+            k = int(max(1, min(max(1, C // cores), round(target_s / max(wall, 1e-4)))))
+            if k > 1:
+                ranges = [(i * k % max(C - k + 1, 1), k) for i in range(cores)]
+                wall = _cpu_run(binary, cfg, ranges, tmp)
     fids = cores * k / C
-    return {"value": fids / wall, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"{cores} processes x {k} crystallites ({cores * k} of {C}) of the full workload, "
-                      f"{wall:.1f} s wall, scaled to powder FIDs/s",
+    return {"value": fids / wall, "unit": UNIT, "cores": cores, "kind": kind, "wall_s": wall,
+            "sample": f"{cores} processes x {k} crystallite(s) ({cores * k} of {C}) of the full workload, "
+                      f"{wall:.1f} s wall, extrapolated linearly to the whole powder (FIDs/s)",
             "binary": str(binary.relative_to(ROOT))}
+
+
+def workload_name(cfg):
+    """The workload string both arms print (the precision form goes in its own config key)."""
+    dim = 2 ** int(cfg["lines"][0].split()[1]) if cfg["lines"][0].startswith("numspin") else 0
+    spins = [l.split()[1] for l in cfg["lines"] if l.startswith("T ")]
+    kinds = sorted(set(spins))
+    desc = " + ".join(f"{spins.count(x)} x {x}" for x in kinds)
+    return (f"{cfg['name']}: {desc} (dim {dim}), {len(cfg['powder'][0])} crystallites, "
+            f"{describe(cfg, dim)}, npts={cfg['npts']}")
 
 
 # ------------------------------------------------------------------ main
@@ -232,25 +254,27 @@ def run_reference(args):
     if rank != 0:
         return 0
     cfg = workload(args)
+    if args.crystallites:
+        cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
     binary, kind = _ref_binary()
-    vals = []
-    # each step is a bounded sample; the whole run stays within about two minutes
-    step_s = max(1.0, min(args.cpu_seconds, 120.0 / max(args.steps, 1)))
-    for i in range(args.warmup):
-        cpu_baseline(cfg, target_s=1.0)
-    for i in range(args.steps):
-        vals.append(cpu_baseline(cfg, target_s=step_s)["value"])
+    from blochlib_gb300 import workloads as W
+    small = W.config(0)
+    small = dict(small, powder=tuple(np.asarray(x)[:1] for x in small["powder"]))
+    for _ in range(args.warmup):  # pages the binary in; the CPU path has no device to warm
+        cpu_baseline(small, target_s=0.0, cores=1)
+    vals, walls = [], []
+    for _ in range(args.steps):
+        r = cpu_baseline(cfg, target_s=args.cpu_seconds)
+        vals.append(r["value"])
+        walls.append(r["wall_s"])
     v = statistics.median(vals)
-    last = cpu_baseline(cfg, target_s=1.0)
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls),
+           "ms_per_fid_extrapolated": 1e3 / v, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, workloads.py)",
-           "config": {"workload": f"{cfg['name']}: {cfg['lines'][0]}, dim {2 ** int(cfg['lines'][0].split()[1])}, "
-                                  f"{len(cfg['powder'][0])} crystallites, {describe(cfg, 0)}, "
-                                  f"npts={cfg['npts']}"},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": kind,
-                            "sample": f"per step: {last['cores']} processes, contiguous crystallite ranges, "
-                                      f"~{args.cpu_seconds:.0f} s of CPU work, scaled to powder FIDs/s"},
+           "config": {"workload": workload_name(cfg), "precision": "fp64 (the reference's CPU path)"},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": kind,
+                            "sample": "per step: " + r["sample"]},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
     return 0
@@ -293,17 +317,13 @@ def _collect(srv, t, out):
     return True
 
 
-def run_batch(args):
-    """c3: a set of seeded spin systems (2..7 1H, n 64..256, 1024 points, powders of 144..1154)
+def batch_form(args, local, systems):
+    """c3: seeded spin systems (2..7 1H, n 64..256, 1024 points, powders of 144..1154)
     submitted at once to the serving loop; FIDs/s of the whole batch, mixed and FP64."""
     import blochlib_gb300 as bl
     from blochlib_gb300 import workloads as W
-    rank, world, local = dist_env()
-    cfgs = [W.config(3, i) for i in range(args.systems)]
+    cfgs = [W.config(3, i) for i in range(systems)]
     jobs = [_job_inputs(bl, c) for c in cfgs]
-    peak = bl.probe_fp64_tflops(bl.Context(local))
-    clocks = Clocks(local)
-    clocks.start()
     forms, fids = {}, {}
     for prec in ("mixed", "fp64"):
         srv = bl.Server(local, lanes=args.lanes, pool_bytes=args.pool_gib << 30)
@@ -322,20 +342,32 @@ def run_batch(args):
                        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))}}
         fids[prec] = [res[t][1] for t in tickets]
         srv.close()
-    clk = clocks.stop()
     errs = [_rel(a, b) for a, b in zip(fids["mixed"], fids["fp64"]) if a is not None and b is not None]
     forms["mixed"]["rel_err_vs_fp64_max"] = max(errs) if errs else None
     forms["mixed_speedup_vs_fp64"] = forms["mixed"]["fids_per_s"] / forms["fp64"]["fids_per_s"]
+    dims = sorted({2 ** int(c["lines"][0].split()[1]) for c in cfgs})
+    forms["workload"] = (f"c3 batching form: {len(cfgs)} seeded systems, dims {dims}, n 64-256, 1024 points, "
+                         "powders 144/320/678/1154, all submitted at once")
+    forms["lanes"] = args.lanes
+    return forms
+
+
+def run_batch(args):
+    rank, world, local = dist_env()
+    import blochlib_gb300 as bl
+    peak = bl.probe_fp64_tflops(bl.Context(local))
+    clocks = Clocks(local)
+    clocks.start()
+    forms = batch_form(args, local, args.systems)
+    clk = clocks.stop()
     if rank != 0:
         return 0
-    dims = sorted({2 ** int(c["lines"][0].split()[1]) for c in cfgs})
     print(json.dumps({
         "metric": METRIC, "value": forms["mixed"]["fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
         "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["seconds"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": MIXED_DTYPE, "data": "synthetic (seeded, workloads.py config 3)",
-        "config": {"workload": f"c3 batching form: {len(cfgs)} seeded systems, dims {dims}, n 64-256, 1024 points, "
-                               "powders 144/320/678/1154, all submitted at once", "lanes": args.lanes,
-                   "pool_gib": args.pool_gib, "precision": "mixed (FP64 row for comparison)"},
+        "config": {"workload": forms["workload"], "lanes": args.lanes, "pool_gib": args.pool_gib,
+                   "precision": "mixed (FP64 row for comparison)"},
         "latency_ms": forms["mixed"]["latency_ms"], "precision_forms": forms,
         "roofline": {"bound": "fp64", "kernel": "whole batch (all stages)", "form": "fp64",
                      "achieved": forms["fp64"]["tflops_algorithmic"], "peak": peak, "unit": "TFLOP/s",
@@ -345,17 +377,16 @@ def run_batch(args):
     return 0
 
 
-def run_serving(args):
+def serving_form(args, local, duration):
     """c4: Poisson request stream (seeded) of c3-like jobs plus 10% large jobs (9-10 x 1H,
     dims 512-1024, on the 100-point repulsion set), for a fixed window; the backlog left at
     the end is cancelled and reported.  Mixed and FP64 on the same stream."""
     import blochlib_gb300 as bl
     from blochlib_gb300 import workloads as W
-    rank, world, local = dist_env()
     rng = np.random.default_rng(W.SEED0 + 4)
     small = [_job_inputs(bl, W.config(3, 1000 + i)) for i in range(48)]
     large = [_job_inputs(bl, W.config(4, i)) for i in range(4)]
-    n_req = int(args.rate * args.duration)
+    n_req = int(args.rate * duration)
     arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n_req))
     picks = [(large[rng.integers(len(large))] if rng.uniform() < 0.1 else small[rng.integers(len(small))])
              for _ in range(n_req)]
@@ -389,51 +420,189 @@ def run_serving(args):
         ok = [v[2] for v in done.values() if v[0] == srv.DONE]
         forms[prec] = {"offered_per_s": args.rate, "submitted": n_req, "completed": len(ok),
                        "cancelled_backlog": cancelled,
-                       "finished_after_drain": sum(v[0] == srv.DONE for v in late.values()), "achieved_fids_per_s": len(ok) / total,
-                       "window_s": window, "total_s": total,
+                       "finished_after_drain": sum(v[0] == srv.DONE for v in late.values()),
+                       "achieved_fids_per_s": len(ok) / total, "window_s": window, "total_s": total,
                        "latency_ms": {"p50": float(np.percentile(ok, 50)) if ok else None,
                                       "p99": float(np.percentile(ok, 99)) if ok else None}}
         srv.close()
     forms["mixed_speedup_vs_fp64"] = forms["mixed"]["achieved_fids_per_s"] / forms["fp64"]["achieved_fids_per_s"]
+    forms["workload"] = (f"c4 serving form: Poisson {args.rate:g}/s for {duration:g} s, 90% c3-like, 10% 9-10 x 1H "
+                         "(dims 512-1024) on rep100")
+    forms["lanes"] = args.lanes
+    forms["drain_s"] = args.drain
+    return forms
+
+
+def run_serving(args):
+    rank, world, local = dist_env()
+    forms = serving_form(args, local, args.duration)
     if rank != 0:
         return 0
     print(json.dumps({
         "metric": METRIC, "value": forms["mixed"]["achieved_fids_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
         "warmup": 1, "ms_per_step": 1e3 * forms["mixed"]["total_s"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": MIXED_DTYPE, "data": "synthetic seeded Poisson stream (workloads.py)",
-        "config": {"workload": f"c4 serving form: Poisson {args.rate}/s for {args.duration} s, 90% c3-like, 10% "
-                               "9-10 x 1H (dims 512-1024) on rep100", "lanes": args.lanes, "pool_gib": args.pool_gib,
+        "config": {"workload": forms["workload"], "lanes": args.lanes, "pool_gib": args.pool_gib,
                    "drain_s": args.drain},
         "latency_ms": forms["mixed"]["latency_ms"], "precision_forms": forms}))
     return 0
 
 
+# stage -> (pipe of the FP64 form, pipe of the mixed form); the mixed form's Dyson runs its
+# large blocks on the tensor cores (exact BF16 slices), its step in double-float (FP32 pipe)
+STAGE_PIPE = {"k_step_prop": ("fp64", "fp32"), "k_dyson": ("fp64", "tensor"), "k_floquet": ("fp64", "fp64"),
+              "k_eigframe": ("fp64", "fp32"), "k_qr": ("fp64", "fp32"), "k_fave": ("fp64", "fp32"),
+              "k_fid": ("fp64", "fp32"), "k_reduce": ("fp64", "fp64")}
+
+
+def measured_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return json.loads(f.read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def tensor_flops(layout, n, C):
+    """BF16 flops the tensor-core Dyson issues per run (unpadded): 10 slice pairs x 4 real
+    b x b x b products x 2 flop, per large block, step and crystallite."""
+    return sum(80.0 * b ** 3 for b in layout["blocks"] if 8 < b <= 74) * n * C
+
+
+def measure_job(args, d, ctx, cfg, prec, steps, warmup, compare, e2e_steps, peaks):
+    """One workload as a single resident job: the timed form `prec`, the other form for the
+    error and the speed-up, and the e2e call.  Returns the fields of the JSON line."""
+    import blochlib_gb300 as bl
+    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if prec == "mixed" else 0)
+    for _ in range(warmup):
+        job.run()
+    job.sync()
+    clocks = Clocks(d.local)
+    clocks.start()
+    time.sleep(0.5)
+    job.set_profiling(True)
+    job.reset_stage_times()
+    d.barrier()
+    job.sync()
+    per_step = [job.run_timed(1) for _ in range(steps)]
+    job.sync()
+    d.barrier()
+    ms_total = sum(per_step)
+    clk = clocks.stop()
+    ms_max = d.max(ms_total)
+    value = d.world * steps / (ms_max / 1e3)
+    fid_main = job.read()
+    stages = job.stage_times()
+    sflops = job.stage_flops()
+    if "p2p" in cfg:  # stage 5 runs the point-to-point terms instead of the Fave correlation
+        stages = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in stages.items()}
+        sflops = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in sflops.items()}
+    layout = json.loads(job.describe())
+    launches_per_run = job.launches
+    job.set_profiling(False)
+    # per-stage roofline against the unit that bounds the stage
+    col = 1 if prec == "mixed" else 0
+    per_stage = {}
+    for k, (ms, nl) in stages.items():
+        if ms <= 0:
+            continue
+        t = ms / steps / 1e3
+        pipe = STAGE_PIPE.get(k, ("fp64", "fp32"))[col]
+        e = {"share": ms / ms_total, "ms_per_run": ms / steps, "launches_per_run": nl / steps, "pipe": pipe,
+             "algorithmic_tflops_fp64_equiv": sflops.get(k, 0.0) / t / 1e12}
+        if pipe == "fp64":
+            e.update(peak=peaks["fp64"], frac=e["algorithmic_tflops_fp64_equiv"] / peaks["fp64"])
+        elif pipe == "tensor":
+            tf = tensor_flops(layout, layout["n"], layout["crystallites"]) / t / 1e12
+            e.update(bf16_tflops_issued=tf, peak=peaks["bf16"], frac=tf / peaks["bf16"])
+        else:
+            e.update(peak=peaks["fp32"])
+        per_stage[k] = e
+    dom = max(per_stage, key=lambda k: per_stage[k]["share"])
+    D = per_stage[dom]
+    if D["pipe"] == "tensor":
+        roof = {"bound": "tensor", "achieved": D["bf16_tflops_issued"], "peak": peaks["bf16"], "unit": "TFLOP/s",
+                "frac": D["frac"], "peak_source": peaks["bf16_source"],
+                "algorithmic_unit": "BF16 slice products issued (unpadded): 80 b^3 per large block, step, crystallite"}
+    elif D["pipe"] == "fp32":
+        ach = D["algorithmic_tflops_fp64_equiv"]
+        roof = {"bound": "fp32", "achieved": ach, "peak": peaks["fp64"], "unit": "TFLOP/s (FP64-equivalent)",
+                "frac": ach / peaks["fp64"], "fp32_pipe_peak": peaks["fp32"],
+                "peak_source": "measured live: DFMA probe kernel (frac = FP64-equivalent work over the FP64 "
+                               "pipe's peak; the stage runs it as double-float on the FP32 pipe, FFMA probe "
+                               "peak beside it)"}
+    else:
+        ach = D["algorithmic_tflops_fp64_equiv"]
+        roof = {"bound": "fp64", "achieved": ach, "peak": peaks["fp64"], "unit": "TFLOP/s", "frac": ach / peaks["fp64"],
+                "peak_source": "measured live: DFMA probe kernel (MEASURED_PEAKS.json has no FP64 figure)"}
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(cfg["name"], {}).get(prec, {}).get(dom)
+        except (ValueError, AttributeError):
+            traffic = None
+    roof.update(kernel=dom, form=prec, traffic=traffic, stages=per_stage)
+    forms = {prec: {"fids_per_s": value, "ms_per_fid": ms_max / steps}}
+    if compare:
+        other = "fp64" if prec == "mixed" else "mixed"
+        _, _, _, _, job2 = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if other == "mixed" else 0)
+        job2.run()
+        job2.sync()
+        k2 = max(1, min(steps, args.compare_steps))
+        ms2 = job2.run_timed(k2) / k2
+        fid_other = job2.read()
+        forms[other] = {"fids_per_s": 1e3 / ms2, "ms_per_fid": ms2, "timed_steps": k2, "warmup": 1}
+        f64, fmx = (fid_main, fid_other) if prec == "fp64" else (fid_other, fid_main)
+        forms["mixed"]["rel_err_vs_fp64"] = _rel(fmx, f64)
+        forms["mixed_speedup_vs_fp64"] = forms["mixed"]["fids_per_s"] / forms["fp64"]["fids_per_s"]
+        job2.close()
+    # e2e through the reference-facing call with host buffers
+    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method,
+                    fave_method=args.fave_method, precision=1 if prec == "mixed" else 0)
+    drive_fid(bl, cfg, drv, pw, ro, det)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        drive_fid(bl, cfg, drv, pw, ro, det)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d, d2h = job.io_bytes()
+    h2d += 8 * 4 * len(cfg["powder"][0]) + 2 * ro.nbytes  # the caller's powder arrays and rho/det
+    job.close()
+    return {"value": value, "ms_per_step": ms_max / steps, "per_step": per_step, "forms": forms, "roofline": roof,
+            "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "steps": e2e_steps, "call": "oneFID.FID -> bl_powder_fid"},
+            "gpu_launches": launches_per_run * steps, "clocks": clk, "layout": layout, "dim": s.dim()}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c1", choices=["c0", "c1", "c2", "c3", "c4"])
-    ap.add_argument("--systems", type=int, default=128, help="c3: number of seeded systems in the batch")
+    ap.add_argument("--config", default="c2", choices=["c0", "c1", "c2", "c3", "c4"])
+    ap.add_argument("--systems", type=int, default=512, help="c3: number of seeded systems in the batch")
     ap.add_argument("--system", type=int, default=None,
                     help="c3/c4: time this one seeded system as a single job instead of the batching/serving form")
     ap.add_argument("--period-steps", type=int, default=0, help="override the steps per rotor period (sw = n wr)")
     ap.add_argument("--lanes", type=int, default=16, help="c3/c4: serving lanes (CUDA streams)")
     ap.add_argument("--pool-gib", type=int, default=128, help="c3/c4: serving memory pool (GiB)")
     ap.add_argument("--rate", type=float, default=200.0, help="c4: offered requests per second")
-    ap.add_argument("--duration", type=float, default=10.0, help="c4: arrival window (s)")
+    ap.add_argument("--duration", type=float, default=60.0, help="c4: arrival window (s)")
     ap.add_argument("--drain", type=float, default=20.0, help="c4: wait after the window (s)")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--compare-steps", type=int, default=2, help="timed runs of the other precision form")
     ap.add_argument("--p2p", type=int, nargs=2, default=None, metavar=("BASE", "FACTOR"),
                     help="point-to-point FID every FACTOR/BASE rotor periods instead of gamma-COMPUTE")
     ap.add_argument("--maxtstep", type=float, default=0.0, help="--p2p: longest step inside a chunk (s)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default c2 run: skip the c1, c3 (batching) and c4 (serving) keys")
     ap.add_argument("--crystallites", type=int, default=0,
                     help="use only the first N crystallites (smaller case for profiler captures)")
     ap.add_argument("--precision", default=None, choices=["fp64", "mixed"],
-                    help="path timed for 'value' (default: fp64 for c0/c1, mixed for c2)")
+                    help="path timed for 'value' (default: mixed for c2, fp64 for c0/c1)")
     ap.add_argument("--no-compare", action="store_true", help="skip the other precision form")
     ap.add_argument("--fave-method", default=None, choices=["auto", "direct", "fft"])
     ap.add_argument("--step-method", default="taylor", choices=["eigh", "taylor"],
@@ -453,97 +622,42 @@ def main():
     cfg = workload(args)
     if args.crystallites:
         cfg = dict(cfg, powder=tuple(np.asarray(x)[:args.crystallites] for x in cfg["powder"]))
-    s, pw, ro, det, job = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if prec == "mixed" else 0)
-    for _ in range(args.warmup):
-        job.run()
-    job.sync()
-    peak = bl.probe_fp64_tflops(ctx)
-    clocks = Clocks(d.local)
-    clocks.start()
-    time.sleep(0.5)
-    job.set_profiling(True)
-    job.reset_stage_times()
-    d.barrier()
-    job.sync()
-    per_step = [job.run_timed(1) for _ in range(args.steps)]
-    job.sync()
-    d.barrier()
-    ms_total = sum(per_step)
-    clk = clocks.stop()
-    ms_max = d.max(ms_total)
-    value = d.world * args.steps / (ms_max / 1e3)
-    fid_main = job.read()
-    stages = job.stage_times()
-    sflops = job.stage_flops()
-    if "p2p" in cfg:  # stage 5 runs the point-to-point terms instead of the Fave correlation
-        stages = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in stages.items()}
-        sflops = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in sflops.items()}
-    dom = max(stages, key=lambda k: stages[k][0])
-    dom_ms_per_run = stages[dom][0] / args.steps
-    achieved = sflops[dom] / (dom_ms_per_run / 1e3) / 1e12
-    traffic = None
-    tf = ROOT / "profiles" / "traffic.json"
-    if tf.exists():
-        try:
-            traffic = json.loads(tf.read_text()).get(args.config, {}).get(dom)
-        except (ValueError, AttributeError):
-            traffic = None
-    launches_per_run = job.launches
-    job.set_profiling(False)
-    forms = {prec: {"fids_per_s": value, "ms_per_fid": ms_max / args.steps}}
-    if not args.no_compare:
-        other = "fp64" if prec == "mixed" else "mixed"
-        _, _, _, _, job2 = make_job(bl, cfg, ctx, args.step_method, args.fave_method, 1 if other == "mixed" else 0)
-        job2.run()
-        job2.sync()
-        k2 = max(1, min(args.steps, 10))
-        ms2 = job2.run_timed(k2) / k2
-        fid_other = job2.read()
-        forms[other] = {"fids_per_s": 1e3 / ms2, "ms_per_fid": ms2}
-        f64, fmx = (fid_main, fid_other) if prec == "fp64" else (fid_other, fid_main)
-        forms["mixed"]["rel_err_vs_fp64"] = _rel(fmx, f64)
-        forms["mixed_speedup_vs_fp64"] = forms["mixed"]["fids_per_s"] / forms["fp64"]["fids_per_s"]
-        job2.close()
-    # e2e through the reference-facing call with host buffers
-    drv = bl.oneFID(s, cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], ctx=ctx, step_method=args.step_method,
-                    fave_method=args.fave_method, precision=1 if prec == "mixed" else 0)
-    drive_fid(bl, cfg, drv, pw, ro, det)
-    t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        drive_fid(bl, cfg, drv, pw, ro, det)
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    h2d, d2h = job.io_bytes()
-    h2d += 8 * 4 * len(cfg["powder"][0]) + 2 * ro.nbytes  # the caller's powder arrays and rho/det
+    mp = measured_peaks()
+    peaks = {"fp64": bl.probe_fp64_tflops(ctx), "fp32": bl.probe_fp32_tflops(ctx),
+             "bf16": mp.get("bf16_tflops_sustained") or 1700.0,
+             "bf16_source": ("MEASURED_PEAKS.json bf16_tflops_sustained (kernel inside a long step)"
+                             if mp.get("bf16_tflops_sustained") else "fallback 1.7 PFLOP/s sustained")}
+    r = measure_job(args, d, ctx, cfg, prec, args.steps, args.warmup, not args.no_compare, args.e2e_steps, peaks)
+    extras = {}
+    if (args.config == "c2" and not args.no_extras and not args.crystallites and not args.period_steps
+            and not args.p2p):
+        c1 = workload(argparse.Namespace(config="c1", system=None, period_steps=0, p2p=None, maxtstep=0.0))
+        r1 = measure_job(args, d, ctx, c1, "mixed", 5, 3, True, 2, peaks)
+        extras["c1"] = {"workload": workload_name(c1), "precision_forms": r1["forms"],
+                        "e2e_mixed": r1["e2e"]["value"],
+                        "roofline_dominant": {k: r1["roofline"][k] for k in ("kernel", "bound", "frac")}}
+        extras["c3_batching"] = batch_form(args, d.local, args.systems)
+        extras["c4_serving"] = serving_form(args, d.local, args.duration)
     if d.rank != 0:
         return 0
     dtype = "f64" if prec == "fp64" else MIXED_DTYPE
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": d.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded spin systems and ZCW powder, workloads.py)",
-        "config": {"workload": f"{cfg['name']}: {cfg['lines'][0]} ({' '.join(cfg['lines'][1:2])}...), "
-                               f"dim {s.dim()}, {len(cfg['powder'][0])} crystallites, "
-                               f"{describe(cfg, s.dim())}, npts={cfg['npts']}, "
-                               f"{'plain FP64' if prec == 'fp64' else 'mixed precision'}",
-                   "precision": prec, "step_method": args.step_method,
+        "config": {"workload": workload_name(cfg), "precision": prec, "step_method": args.step_method,
                    "parallelism": f"replicas x{d.world}",
                    "l2": "inputs larger than L2: each step streams the per-crystallite work buffers (GBs)",
-                   "layout": job.describe()},
-        "latency_ms": {"p50": float(np.percentile(per_step, 50)), "p99": float(np.percentile(per_step, 99))},
-        "precision_forms": forms,
-        "roofline": {"bound": "fp64", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": traffic,
-                     "peak_source": "measured live: DFMA probe kernel (MEASURED_PEAKS.json has no FP64 figure)",
-                     "stage_share": {k: v[0] / ms_total for k, v in stages.items()}},
-        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "gpu_launches": launches_per_run * args.steps,
-        "clocks": clk,
+                   "layout": r["layout"]},
+        "latency_ms": {"p50": float(np.percentile(r["per_step"], 50)), "p99": float(np.percentile(r["per_step"], 99))},
+        "precision_forms": r["forms"],
+        "roofline": r["roofline"],
+        "e2e": r["e2e"],
+        "gpu_launches": r["gpu_launches"],
+        "clocks": r["clocks"],
+        "peaks": {k: v for k, v in peaks.items()},
     }
-    if prec == "mixed":  # the step and Dyson run double-float on the FP32 pipe, Floquet on the FP64 pipe
-        out["roofline"]["form"] = "mixed"
-        out["roofline"]["note"] = ("achieved counts the FP64-equivalent algorithmic flops; in the mixed form the "
-                                   "step and Dyson run them as double-float on the FP32 pipe, so frac (of the "
-                                   "FP64 pipe's measured peak) can exceed 1")
+    out.update(extras)
     if not args.no_cpu:
         try:
             out["cpu_baseline"] = cpu_baseline(cfg, target_s=args.cpu_seconds)

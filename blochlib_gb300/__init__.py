@@ -87,6 +87,7 @@ _SIGS = {
     "bl_job_run_timed": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "bl_job_io_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     "bl_probe_fp64": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "bl_probe_fp32": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
     "bl_powder_fid_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 8),
     "bl_rotation3": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
     "bl_rotation2": (ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_void_p]),
@@ -264,6 +265,14 @@ def probe_fp64_tflops(ctx=None):
     """Measured DFMA throughput of the device (TFLOP/s)."""
     t = ctypes.c_double()
     _check(load().bl_probe_fp64((ctx or default_context())._h, ctypes.byref(t)))
+    return t.value
+
+
+def probe_fp32_tflops(ctx=None):
+    """Measured FFMA throughput of the device (TFLOP/s): the FP32 pipe of the mixed form's
+    double-float stages."""
+    t = ctypes.c_double()
+    _check(load().bl_probe_fp32((ctx or default_context())._h, ctypes.byref(t)))
     return t.value
 
 

@@ -106,11 +106,18 @@ def build_oracle(force=False):
     return ORACLE_LIB
 
 
+def reference_tree():
+    """The reference tree's path as oracle/build_ref.sh resolves it (BLOCHLIB_REF or the
+    recipe's default), or None where it is absent."""
+    r = subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh"), "where"], stdout=subprocess.PIPE,
+                       stderr=subprocess.DEVNULL, text=True)
+    return Path(r.stdout.strip()) if r.returncode == 0 and r.stdout.strip() else None
+
+
 def build_reference():
     """The reference's own path (oracle/_ref), when its sources are present."""
     script = ROOT / "oracle" / "build_ref.sh"
-    ref = Path(os.environ.get("BLOCHLIB_REF", "/root/reference"))
-    have_src = (ref / "src").is_dir() or (ROOT / "oracle" / "_ref" / "src" / ".patched").exists()
+    have_src = (reference_tree() is not None) or (ROOT / "oracle" / "_ref" / "src" / ".patched").exists()
     if not have_src:
         return None
     r = subprocess.run(["bash", str(script), "all"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)

@@ -339,6 +339,11 @@ bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops) {
   return guarded([&] { *tflops = bl::probe_fp64_tflops(ctx->c); });
 }
 
+bl_status bl_probe_fp32(bl_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return fail(BL_ERR_INVALID, "null argument");
+  return guarded([&] { *tflops = bl::probe_fp32_tflops(ctx->c); });
+}
+
 // One FID with the job in the context's region when the whole powder fits one batch of the
 // budget (the layout and results of a freshly allocated job; the region is reused by the next
 // call).  Returns false, having done nothing, when it does not fit: the caller then runs a

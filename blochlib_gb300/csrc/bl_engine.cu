@@ -25,13 +25,14 @@
 //   k_p2p_elems  (c, element)       point-to-point FID terms from Q/R and the Floquet phases
 //   k_fid        (c, j, p)          fid[jn+p] = sum_e z_e^j G_p(e); weighted warp sum
 //   k_reduce     (k)                compensated sum of warp partials (fixed order)
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <sstream>
 #include <stdexcept>
 
@@ -1871,6 +1872,7 @@ static size_t fave_twist_bytes(const DevSys &s, int cg) {
 
 #include "bl_big.cuh"
 #include "bl_huge.cuh"
+#include "bl_tc.cuh"
 
 constexpr int kFidJT = 4, kFidPT = 4;
 
@@ -2538,8 +2540,9 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_dyson<1>, smem_mat);
       attr((const void *)k_big_dyson<2>, smem_mat);
       attr((const void *)k_big_step_df, smem_step);  // 5 b^2 float2 <= the FP64 step's 5 or 7 b^2 doubles
-      attr((const void *)k_big_dyson_df<1>, smem_mat);
-      attr((const void *)k_big_dyson_df<2>, smem_mat);
+      size_t smem_tc = 0;
+      for (int k : J.big_blocks) smem_tc = std::max(smem_tc, tc::dyson_smem(L.size[k]));
+      if (J.mixed) attr((const void *)k_tc_dyson, smem_tc);
       attr((const void *)k_big_eigframe<1, double2>, smem_mat);
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
@@ -3023,9 +3026,8 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         else k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k);
         break;
       case 1:
-        if (s.mixed) {
-          if (nt1) k_big_dyson_df<1><<<unsigned(s.C), th, smat, st>>>(s, k);
-          else k_big_dyson_df<2><<<unsigned(s.C), th, smat, st>>>(s, k);
+        if (s.mixed) {  // exact-slice BF16 products on the tensor cores
+          k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc::dyson_smem(b), st>>>(s, k);
         } else {
           if (nt1) k_big_dyson<1><<<unsigned(s.C), th, smat, st>>>(s, k);
           else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);
@@ -3240,6 +3242,7 @@ void Job::read(double *fid_out) {
   if (status & (kNoConvergeStep | kNoConvergeFloquet))
     throw Error(7, "an eigen-decomposition did not converge within its sweep limit");
   if (status & kSingularCayley) throw Error(7, "singular Cayley transform in the Floquet eigen-decomposition");
+  if (status & kTcTimeout) throw Error(7, "a tensor-core product did not complete within its wait limit");
 }
 
 const char *Job::stage_name(int s) {
@@ -3292,7 +3295,46 @@ __global__ void k_dfma_probe(double *out, int iters, double a, double b) {
   for (int c = 0; c < 8; ++c) s += x[c];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
+// The same with FP32 FMA chains: the FP32 pipe that the mixed form's double-float stages use.
+__global__ void k_ffma_probe(float *out, int iters, float a, float b) {
+  float x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = threadIdx.x + c;
+  for (int it = 0; it < iters; ++it)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = fmaf(x[c], a, b);
+  float s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 }  // namespace
+
+double probe_fp32_tflops(Context &ctx) {
+  CUDA_OK(cudaSetDevice(ctx.device));
+  int sms = 0;
+  CUDA_OK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx.device));
+  int blocks = sms * 8, threads = 256, iters = 40000;
+  DevBuf<float> out;
+  out.alloc(size_t(blocks) * threads);
+  cudaEvent_t a, b;
+  CUDA_OK(cudaEventCreate(&a));
+  CUDA_OK(cudaEventCreate(&b));
+  k_ffma_probe<<<blocks, threads, 0, ctx.stream>>>(out.p, 10, 0.999f, 0.001f);
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    CUDA_OK(cudaEventRecord(a, ctx.stream));
+    k_ffma_probe<<<blocks, threads, 0, ctx.stream>>>(out.p, iters, 0.999f, 0.001f);
+    CUDA_OK(cudaEventRecord(b, ctx.stream));
+    CUDA_OK(cudaEventSynchronize(b));
+    float ms = 0;
+    CUDA_OK(cudaEventElapsedTime(&ms, a, b));
+    best = std::max(best, 2.0 * 8 * double(iters) * blocks * threads / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return best;
+}
 
 double probe_fp64_tflops(Context &ctx) {
   CUDA_OK(cudaSetDevice(ctx.device));
@@ -3352,26 +3394,21 @@ std::string Job::describe() const {
 namespace {
 constexpr size_t kNoAllocScratch = size_t(64) << 20;
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch];
-std::mutex g_noalloc_mu;
-constexpr int kNoAllocMaxDevices = 64;
-void *g_noalloc_addr[kNoAllocMaxDevices] = {};
 }  // namespace
 
 size_t noalloc_scratch_bytes() { return kNoAllocScratch; }
 
-// Device address of the static array on the current device, looked up once per device
-// (host code may not use the symbol itself as a device pointer).  The first call on a
-// device performs this lookup, so it should come before any stream capture.
-static char *noalloc_base(int device) {
-  if (device < 0 || device >= kNoAllocMaxDevices) throw Error(1, "device index out of range");
-  std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_addr[device]) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess || !ptr) throw Error(3, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-    g_noalloc_addr[device] = ptr;
-  }
-  return static_cast<char *>(g_noalloc_addr[device]);
+// Device address of the static array in the current device's context.  Host code may not
+// use the symbol itself as a device pointer, so every call asks the runtime (a host-side
+// lookup that allocates nothing); an address kept from an earlier call would dangle once the
+// host program resets the device or its primary context is rebuilt.  The first lookup on a
+// device loads this library's device code, and with it the array, so the first call should
+// come before any stream capture and before the host program claims the device's memory.
+static char *noalloc_base() {
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess || !ptr) throw Error(3, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  return static_cast<char *>(ptr);
 }
 
 // Device bytes outside the batch-sized work buffers: tables, per-crystallite inputs (11
@@ -3404,17 +3441,33 @@ void job_bytes(int device, const SpinSystem &sys, const Powder &pw, const CMatri
 void powder_fid_noalloc(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
                         const FidParams &p, double *fid_out, double *sw_out) {
   CUDA_OK(cudaSetDevice(ctx.device));
-  ScratchArena arena;
-  arena.base = noalloc_base(ctx.device);
-  arena.cap = kNoAllocScratch;
-  size_t fixed = fixed_bytes(pw, p);
-  if (fixed >= kNoAllocScratch)
-    throw Error(4, "job needs more than the " + std::to_string(kNoAllocScratch >> 20) +
+  // the host-side plan (no device memory is touched): the batch-independent bytes as the
+  // arena will carve them, and the bytes each crystallite of a batch adds
+  JobSizing plan;
+  {
+    struct Scope {
+      JobSizing *prev;
+      explicit Scope(JobSizing *z) : prev(g_sizing) { g_sizing = z; }
+      ~Scope() { g_sizing = prev; }
+    } scope(&plan);
+    Context probe;
+    probe.device = ctx.device;
+    Job sizing(probe, sys, pw, ro, det, p);
+  }
+  // work buffers are carved with 256-byte alignment: allow for it on each of ~40 buffers
+  const size_t fixed = fixed_bytes(pw, p) + 40 * 256 + plan.extra + plan.tables;
+  const size_t smallest = fixed + plan.per_c * 32;  // with one 32-crystallite batch
+  if (smallest > kNoAllocScratch)
+    throw Error(4, "job needs " + std::to_string((smallest + (size_t(1) << 20) - 1) >> 20) +
+                       " MiB for its smallest batch, more than the " + std::to_string(kNoAllocScratch >> 20) +
                        " MiB static device scratch of the allocation-free entry point");
+  ScratchArena arena;
+  arena.base = noalloc_base();
+  arena.cap = kNoAllocScratch;
   Context view;  // same device and stream; budget = what the scratch leaves for work buffers
   view.device = ctx.device;
   view.stream = ctx.stream;
-  view.hbm_budget = kNoAllocScratch - fixed;
+  view.hbm_budget = kNoAllocScratch - (fixed - plan.extra);  // the Job sets the workspace (extra) aside itself
   struct Release {
     Context &c;
     ~Release() { c.stream = nullptr; }  // the stream belongs to the caller's context

@@ -79,6 +79,8 @@ class Job {
 
 // Measured FP64 FMA throughput of the device (TFLOP/s), from a short DFMA probe kernel.
 double probe_fp64_tflops(Context &ctx);
+// Measured FP32 FMA throughput (TFLOP/s): the pipe of the mixed form's double-float stages.
+double probe_fp32_tflops(Context &ctx);
 
 // The powder FID with every device buffer taken from one static device array (no device
 // allocation or free during the call); see bl_powder_fid_noalloc.

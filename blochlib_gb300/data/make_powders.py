@@ -4,9 +4,9 @@
 144/320/678-crystallite powders (rep678 holds 677 points) and the 100-crystallite powder of
 the large serving jobs from this file.
 
-    BLOCHLIB_REF=<reference checkout> python blochlib_gb300/data/make_powders.py
+    python blochlib_gb300/data/make_powders.py   (reference tree: BLOCHLIB_REF, resolved
+                                                  by oracle/build_ref.sh)
 """
-import os
 import sys
 from pathlib import Path
 
@@ -18,7 +18,10 @@ import blochlib_gb300 as bl  # noqa: E402
 
 
 def main():
-    ref = Path(os.environ.get("BLOCHLIB_REF", "/root/reference"))
+    from blochlib_gb300.build import reference_tree
+    ref = reference_tree()
+    if ref is None:
+        sys.exit("reference tree not found (set BLOCHLIB_REF)")
     out = {}
     for n in (100, 144, 320, 678):
         pw = bl.powder.read(ref / "crystals" / f"rep{n}")

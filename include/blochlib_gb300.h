@@ -201,6 +201,9 @@ bl_status bl_job_run_timed(bl_job *job, int iters, double *ms_total);
 bl_status bl_job_io_bytes(const bl_job *job, size_t *h2d, size_t *d2h);
 /* Measured FP64 FMA throughput of the context's device (TFLOP/s), DFMA probe kernel. */
 bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops);
+/* Measured FP32 FMA throughput (TFLOP/s), FFMA probe kernel: the pipe of the mixed form's
+ * double-float stages.  Measurement only; no counterpart in the reference. */
+bl_status bl_probe_fp32(bl_ctx *ctx, double *tflops);
 
 /* Allocation-free powder FID.  No counterpart in the reference: BlochLib has no GPU and
  * no device memory.  Same inputs, outputs and results as bl_powder_fid, for callers that
@@ -211,8 +214,11 @@ bl_status bl_probe_fp64(bl_ctx *ctx, double *tflops);
  * BL_NOALLOC_SCRATCH_BYTES that each GPU loading this library keeps until the process
  * exits; nothing is allocated or freed.  Larger powders are processed in crystallite
  * batches that fit it; a job whose smallest batch (32 crystallites plus tables) does not
- * fit returns BL_ERR_NOMEM.  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress), so make it before any stream capture.  All calls share
+ * fit returns BL_ERR_NOMEM.  Each call looks up the array's device address
+ * (cudaGetSymbolAddress, which allocates nothing).  The first such lookup on a device
+ * loads this library's device code and with it the array, so make the first call (or any
+ * earlier compute call of this library on that device) before any stream capture and
+ * before the host program claims the device's memory.  All calls share
  * the array and it keeps the previous call's contents (each call clears what must start
  * at zero); calls that overlap on the GPU, from any thread or context, race on it. */
 #define BL_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)

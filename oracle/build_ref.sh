@@ -7,17 +7,22 @@
 #   ref_fid    the reference as shipped (its QL eigen-iteration runs in float)
 #   ref_fid64  the same sources with that iteration in double (the FP64 oracle)
 #
-# Source: $BLOCHLIB_REF/src (default /root/reference/src) is copied to oracle/_ref/src
+# Source: $BLOCHLIB_REF/src (default: the reference tree's mount point below) is copied to oracle/_ref/src
 # and build-fixed by patch_ref.py; the propagator-reduction class of the MMMQMAS example
 # (examples/qmsims/MMMQMAS/propreduce.{h,cc}) is copied unchanged to oracle/_ref/mmmqmas,
 # beside a one-line blochlib.h that includes only QMspins/sys.h (the umbrella header pulls
 # in unrelated, unpatched parts of the tree).  Where the reference tree is absent but a
 # scratch copy already sits in oracle/_ref, that copy is built as is.
 #   usage: build_ref.sh [f32|f64|all]   (default all)
+#          build_ref.sh where             prints the reference tree's path (exit 3 if absent)
 set -euo pipefail
 here="$(cd "$(dirname "$0")" && pwd)"
 ref="${BLOCHLIB_REF:-/root/reference}"
 which="${1:-all}"
+if [ "$which" = where ]; then
+  if [ -d "$ref/src" ]; then echo "$ref"; exit 0; fi
+  exit 3
+fi
 mkdir -p "$here/_ref"
 if [ -d "$ref/src" ]; then
   if [ ! -f "$here/_ref/src/.patched" ] || [ "$here/patch_ref.py" -nt "$here/_ref/src/.patched" ]; then

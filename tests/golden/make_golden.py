@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Generates the golden FID fixtures by running the BlochLib reference itself.
 
-Run here, where the reference tree is mounted (BLOCHLIB_REF, default /root/reference):
+Run where the reference tree is present (BLOCHLIB_REF, resolved by oracle/build_ref.sh):
     oracle/build_ref.sh all && python3 tests/golden/make_golden.py
 
 Each case is a seeded job in the text format of oracle/ref_harness.cc.  For every case
@@ -25,7 +25,9 @@ sys.path.insert(0, str(ROOT))
 from blochlib_gb300 import workloads as W  # noqa: E402
 
 OUT = Path(__file__).resolve().parent
-REF = Path(os.environ.get("BLOCHLIB_REF", "/root/reference"))
+from blochlib_gb300.build import reference_tree  # noqa: E402
+
+REF = reference_tree() or Path(os.environ.get("BLOCHLIB_REF", "reference-not-found"))
 BIN64 = ROOT / "oracle" / "_ref" / "ref_fid64"
 BIN32 = ROOT / "oracle" / "_ref" / "ref_fid"
 

@@ -53,7 +53,7 @@ def test_reference_arm_two_ranks_prints_one_line():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(_port()), str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2",
-           "--steps", "1", "--warmup", "0", "--cpu-seconds", "1"]
+           "--steps", "1", "--warmup", "0", "--cpu-seconds", "1", "--config", "c0"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
