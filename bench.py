@@ -497,7 +497,7 @@ def measure_job(args, d, ctx, cfg, prec, steps, warmup, compare, e2e_steps, peak
     if "p2p" in cfg:  # stage 5 runs the point-to-point terms instead of the Fave correlation
         stages = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in stages.items()}
         sflops = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in sflops.items()}
-    layout = json.loads(job.describe())
+    layout = job.describe()
     launches_per_run = job.launches
     job.set_profiling(False)
     # per-stage roofline against the unit that bounds the stage

@@ -189,6 +189,10 @@ struct DevSys {
   // double-float copies for the mixed form's step (hi, lo): term operators, constant parts,
   // and fk_df = 1 when k_coef stores the coefficients as float2 in fk's slots
   const float2 *Tk_df, *Hc_df;
+  // the same operators by element for the tensor-core step: element e (packed block index)
+  // holds entries [tk_ptr[e], tk_ptr[e+1]) of (term, double-float value), terms ascending
+  const int *tk_ptr, *tk_term;
+  const float2 *tk_val;
   int fk_df;
   float2 tpdf;  // 2 pi tau as double-float
   const int *ikind;  // per term: 0 first order, 1 / 2 second-order quadrupolar (c4 / c2)
@@ -2111,9 +2115,16 @@ struct JobImpl {
   DevBuf<double> fkc;                      // k_coef's term coefficients (small blocks)
   DevBuf<double2> frames;                  // rf schedule: per chunk frame (permuted index)
   DevBuf<float2> Tk_df, Hc_df;             // mixed form: double-float operators and constant parts
+  DevBuf<int> tk_ptr, tk_term;             // tensor-core step: the operators' non-zeros by element
+  DevBuf<float2> tk_val;
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
   DevBuf<float2> Wf, Qf, Rf, Gf, Zf, twf;  // mixed-precision form
+  // mixed form on the tensor cores (large blocks): the step writes each (crystallite, step)'s
+  // U slices to a slab the Dyson product reads; one region per large block
+  bool tc = false;
+  DevBuf<unsigned char> usl;
+  std::vector<size_t> usl_off;  // per block index: byte offset of its region (large blocks)
   int mixed = 0;
   DevBuf<double> Rp_b, t0_b, w_b;
   std::vector<double> h_Rp, h_t0, h_w;  // all virtual crystallites (C * gammaloop)
@@ -2397,6 +2408,16 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   // term coefficients per (step, term), computed once for all small blocks (k_coef)
   const bool use_fk = !J.is_static && J.nint > 0;
   if (use_fk) per_c += sizeof(double) * size_t(J.n) * size_t(J.nint);
+  // tensor-core step and Dyson of the mixed form's large blocks (double-float coefficients
+  // from k_coef, no rf schedule): the U slab of every (step, large block)
+  J.tc = J.mixed && use_fk && p.step_method == 1 && !sched;
+  size_t usl_per_c = 0;
+  if (J.tc) {
+    J.usl_off.assign(nb, 0);
+    for (int k = 0; k < nb; ++k)
+      if (L.size[k] > kMaxBlock && L.size[k] <= kMaxBigBlock) usl_per_c += nsteps * tc::slab_bytes(L.size[k]);
+    per_c += usl_per_c;
+  }
   long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
   // huge blocks: one workspace for their batched products, at least one item of each use
   // (exponential: 7 real b x b; Floquet: 2 complex b x b; eigenframe, Q/R: one complex
@@ -2540,9 +2561,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_dyson<1>, smem_mat);
       attr((const void *)k_big_dyson<2>, smem_mat);
       attr((const void *)k_big_step_df, smem_step);  // 5 b^2 float2 <= the FP64 step's 5 or 7 b^2 doubles
-      size_t smem_tc = 0;
-      for (int k : J.big_blocks) smem_tc = std::max(smem_tc, tc::dyson_smem(L.size[k]));
-      if (J.mixed) attr((const void *)k_tc_dyson, smem_tc);
+      attr((const void *)k_big_dyson_df<1>, smem_mat);
+      attr((const void *)k_big_dyson_df<2>, smem_mat);
+      if (J.tc) {
+        size_t sm_step = 0, sm_dy = 0;
+        for (int k : J.big_blocks)
+          sm_step = std::max(sm_step, tc_step_smem(L.size[k])), sm_dy = std::max(sm_dy, tc_dyson_smem(L.size[k]));
+        attr((const void *)k_tc_step, sm_step);
+        attr((const void *)k_tc_dyson, sm_dy);
+      }
       attr((const void *)k_big_eigframe<1, double2>, smem_mat);
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
@@ -2602,6 +2629,22 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     };
     J.Tk_df.upload(split(Tk), st);
     J.Hc_df.upload(split(Hc), st);
+    if (J.tc) {
+      std::vector<int> ptr(size_t(L.S2) + 1, 0), term;
+      std::vector<float2> val;
+      for (size_t e = 0; e < size_t(L.S2); ++e) {
+        ptr[e] = int(term.size());
+        for (int kk = 0; kk < J.nint; ++kk) {
+          const double v = Tk[size_t(kk) * L.S2 + e];
+          if (v != 0.0) {
+            const float h = float(v);
+            term.push_back(kk), val.push_back(make_float2(h, float(v - double(h))));
+          }
+        }
+      }
+      ptr[L.S2] = int(term.size());
+      J.tk_ptr.upload(ptr, st), J.tk_term.upload(term, st), J.tk_val.upload(val, st);
+    }
   }
   if (sched) {  // per chunk: the rf frame of each permuted index (1 where a chunk has none)
     bool any = false;
@@ -2656,6 +2699,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   J.fid.alloc(p.npts);
   if (use_fk) J.fkc.alloc(size_t(J.n) * J.nint * Cb);
+  if (J.tc && usl_per_c) {
+    J.usl.alloc(usl_per_c * Cb);
+    size_t off = 0;
+    for (int k = 0; k < nb; ++k)
+      if (L.size[k] > kMaxBlock && L.size[k] <= kMaxBigBlock) {
+        J.usl_off[k] = off;
+        off += nsteps * tc::slab_bytes(L.size[k]) * Cb;
+      }
+  }
   CUDA_OK(cudaMemsetAsync(J.partial.p, 0, J.partial.n * sizeof(double2), st));
   CUDA_OK(cudaStreamSynchronize(st));
   // algorithmic flop count (one complex MAC = 8 flop; eigh counted as 32 b^3, the
@@ -2755,6 +2807,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.hc_chunks = sched ? J.pb : 0;
   s.frames = J.frames.n ? J.frames.p : nullptr;
   s.Tk_df = J.Tk_df.p, s.Hc_df = J.Hc_df.p;
+  s.tk_ptr = J.tk_ptr.p, s.tk_term = J.tk_term.p, s.tk_val = J.tk_val.p;
   s.fk_df = (J.mixed && p.step_method == 1 && use_fk) ? 1 : 0;
   {
     const double tp = J.tau * kPi2;
@@ -3022,12 +3075,17 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
     const bool nt1 = big_nt(b, b) == 1;
     switch (stage) {
       case 0:
-        if (s.mixed) k_big_step_df<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_df_smem(b), st>>>(s, k);
+        if (J.tc)
+          k_tc_step<<<unsigned(s.C) * unsigned(s.n), tc::kTcThreads, tc_step_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
+        else if (s.mixed) k_big_step_df<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_df_smem(b), st>>>(s, k);
         else k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k);
         break;
       case 1:
-        if (s.mixed) {  // exact-slice BF16 products on the tensor cores
-          k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc::dyson_smem(b), st>>>(s, k);
+        if (J.tc) {  // exact-slice BF16 products on the tensor cores
+          k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc_dyson_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
+        } else if (s.mixed) {
+          if (nt1) k_big_dyson_df<1><<<unsigned(s.C), th, smat, st>>>(s, k);
+          else k_big_dyson_df<2><<<unsigned(s.C), th, smat, st>>>(s, k);
         } else {
           if (nt1) k_big_dyson<1><<<unsigned(s.C), th, smat, st>>>(s, k);
           else k_big_dyson<2><<<unsigned(s.C), th, smat, st>>>(s, k);

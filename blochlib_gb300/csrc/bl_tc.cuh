@@ -14,36 +14,54 @@
 // and a chain of n ~ 200 of them stays far inside the mixed form's 1e-6 FID bar (a numpy
 // emulation of this exact scheme on 5- and 7-spin systems: 2.6e-9 and 2.7e-9 against FP64).
 // The products run on the BF16 tensor pipe (about 2.25 PFLOP/s dense) instead of the FP32
-// pipe, 10 slice pairs x 4 real products per complex product.
+// pipe, 10 slice pairs per real product.
+//
+// Slice tiles.  A b x b matrix (b <= kMaxB) is held as 4 planes (levels) of R x R BF16,
+// R = up16(b), zero outside b x b, in the K-major canonical layout without swizzle: core
+// matrices of 8 rows x 16 bytes; the K-adjacent core matrix 128 bytes on (leading byte
+// offset), the next 8-row group R * 16 + 16 bytes on (stride byte offset; the 16 bytes of
+// padding put the 8-row groups on different shared-memory banks, so that an epilogue lane
+// per row stores whole 16-byte core-matrix rows without bank conflicts).  The matrices of
+// the step exponential are symmetric, so one tile serves as either MMA operand.
 //
 // tcgen05 usage (PTX ISA, sm_100a family): one elected thread issues tcgen05.mma with
-// 128-row tiles (cta_group::1, kind::f16, BF16 x BF16 -> FP32) whose operands sit in shared
-// memory in the K-major canonical layout without swizzle; tcgen05.commit arrives on an
-// mbarrier; every warp then reads its 32-lane quarter of the accumulators with tcgen05.ld.
-// Every wait is bounded: on a time-out the kernel sets kTcTimeout in the status word,
-// waits (bounded) once more for its own MMAs, frees its TMEM and returns.
+// 128-row tiles (cta_group::1, kind::f16, BF16 x BF16 -> FP32); an M = 128 MMA reads 128
+// rows of its A tile, and rows past R fall into whatever follows (their products land in
+// accumulator rows that are never read; the kernels keep memory after every tile).
+// tcgen05.commit arrives on an mbarrier; every warp reads its 32-lane quarter of the
+// accumulators with tcgen05.ld (four warps per quarter, on alternate 8-column chunks).
+// Every wait is bounded (1 s): on a time-out the kernel sets kTcTimeout in the status word,
+// waits (bounded) once more, frees its TMEM and returns.
 // (bl_engine.cu includes <cuda_bf16.h> and <cstdint> at file scope.)
 
 namespace tc {
 
-constexpr int kTcThreads = 256;                // 8 warps: two per TMEM lane quarter
-constexpr int kMaxB = kMaxBigBlock;            // largest block: 6 accumulators of up16(74) = 80 columns
-constexpr int kEPT = (kMaxB * kMaxB + kTcThreads - 1) / kTcThreads;  // U elements per thread
-constexpr long kWaitLimit = 1L << 26;          // mbarrier polls before a time-out
+constexpr int kTcThreads = 512;          // 16 warps: four per TMEM lane quarter
+constexpr int kMaxB = kMaxBigBlock;      // largest block on these kernels (up16 = 80)
+constexpr unsigned long long kWaitNs = 1000000000ull;  // an mbarrier wait gives up after 1 s
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
 
-// Element (r, k) of a rows x K BF16 operand tile, K-major without swizzle: core matrices of
-// 8 rows x 16 bytes, the K-adjacent core matrix 128 bytes on (leading byte offset), the next
-// 8-row group K * 16 bytes on (stride byte offset).
-__host__ __device__ __forceinline__ int kmaj(int r, int k, int K) {
-  return (r >> 3) * (K * 8) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+__host__ __device__ constexpr int up16(int x) { return (x + 15) / 16 * 16; }
+// bytes of one plane (R x R BF16 with padded 8-row groups) and of one 4-level tile
+__host__ __device__ constexpr int sbo_bytes(int R) { return R * 16 + 16; }
+__host__ __device__ constexpr size_t plane_bytes(int b) { return size_t(up16(b) / 8) * sbo_bytes(up16(b)); }
+__host__ __device__ constexpr size_t tile_bytes(int b) { return 4 * plane_bytes(b); }
+// bytes an M = 128 MMA may read past the end of an A tile
+__host__ __device__ constexpr size_t overread_bytes(int b) {
+  return size_t((128 - up16(b)) / 8) * sbo_bytes(up16(b));
 }
-// Shared-memory matrix descriptor of such a tile (tcgen05 layout: start >> 4 in bits 0-13,
-// leading byte offset >> 4 in 16-29, stride byte offset >> 4 in 32-45, version 1 at bit 46,
-// swizzle mode 0 in bits 61-63).
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr, int K) {
-  return uint64_t((addr & 0x3FFFF) >> 4) | (uint64_t(128 >> 4) << 16) | (uint64_t((K * 16) >> 4) << 32) |
+// the step's output per (crystallite, step): 4 planes of C = cos X, then 4 planes of S = sin X
+__host__ __device__ constexpr size_t slab_bytes(int b) { return 2 * tile_bytes(b); }
+// element offset (BF16 units) of (r, k) in a plane of row length R
+__device__ __forceinline__ int tix(int r, int k, int R) {
+  return (r >> 3) * (R * 8 + 8) + (k >> 3) * 64 + (r & 7) * 8 + (k & 7);
+}
+
+// Shared-memory matrix descriptor of a plane (start >> 4 in bits 0-13, leading byte offset
+// >> 4 in 16-29, stride byte offset >> 4 in 32-45, version 1 at bit 46, no swizzle).
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, int R) {
+  return uint64_t((addr & 0x3FFFF) >> 4) | (uint64_t(128 >> 4) << 16) | (uint64_t(sbo_bytes(R) >> 4) << 32) |
          (1ull << 46);
 }
 // Instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), A and B BF16 (bits
@@ -68,17 +86,34 @@ __device__ __forceinline__ void mbar_init(uint64_t *mbar) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(saddr(mbar)));
   asm volatile("fence.mbarrier_init.release.cluster;");
 }
-// Polls the mbarrier's phase `parity` at most kWaitLimit times; true once it completed.
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits for the mbarrier's phase `parity`: each try_wait suspends the warp in hardware for up
+// to 20 us (no issue slots spent polling); gives up after kWaitNs.  True once it completed.
 __device__ __forceinline__ bool wait_parity(uint64_t *mbar, uint32_t parity) {
-  uint32_t done = 0;
-  for (long it = 0; it < kWaitLimit && !done; ++it) {
+  const unsigned long long t0 = gtimer();
+  for (;;) {
+    uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
-        : "r"(saddr(mbar)), "r"(parity)
+        : "r"(saddr(mbar)), "r"(parity), "r"(20000u)
         : "memory");
+    if (done) return true;
+    if (gtimer() - t0 > kWaitNs) return false;
   }
-  return done != 0;
+}
+// One thread: expect `bytes` on the mbarrier and start a bulk copy global -> shared of
+// `bytes` (16-byte aligned addresses, a multiple of 16 bytes) that completes on it.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(mbar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(saddr(dst)),
+      "l"(src), "r"(bytes), "r"(saddr(mbar))
+      : "memory");
 }
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -103,27 +138,14 @@ __device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
 }
 __device__ __forceinline__ void wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__host__ __device__ constexpr int up16(int x) { return (x + 15) / 16 * 16; }
-__host__ __device__ constexpr int up8(int x) { return (x + 7) / 8 * 8; }
-// TMEM columns for the six accumulators (level 0, 1, 2+3; real and imaginary), rounded up
-// to the power of two tcgen05.alloc takes
-__host__ __device__ constexpr int tmem_cols(int b) {
-  return 6 * up16(b) <= 32 ? 32 : 6 * up16(b) <= 64 ? 64 : 6 * up16(b) <= 128 ? 128 : 6 * up16(b) <= 256 ? 256 : 512;
-}
-// Shared memory of k_tc_dyson: 8 U slices (4 levels x re/im, up8(b) rows) and 8 A slices
-// (up16(b) rows), both up16(b) wide in K, plus 1 KB for alignment.  An M = 128 MMA reads
-// 128 rows of a U slice; rows past up8(b) fall into the following slices (their products
-// land in accumulator rows >= b, which are never read), and the 8 A slices behind the last
-// U slice always cover that reach (8 up16(b) >= 128 - up8(b)).
-__host__ __device__ constexpr size_t dyson_smem(int b) {
-  return size_t(2) * 8 * (size_t(up8(b)) + size_t(up16(b))) * size_t(up16(b)) + 1024;
+__host__ __device__ constexpr int pow2_cols(int c) {
+  return c <= 32 ? 32 : c <= 64 ? 64 : c <= 128 ? 128 : c <= 256 ? 256 : 512;
 }
 
-// Four natural-scale BF16 slices of the double-float x = hi + lo (|x| <= ~1).  Each residual
-// d_j is exact (a rounded multiple of the previous one's ulp, below 1/2 in size); lo enters
-// every stage through one FMA.
-__device__ __forceinline__ void slice4(float hi, float lo, __nv_bfloat16 &s0, __nv_bfloat16 &s1,
-                                       __nv_bfloat16 &s2, __nv_bfloat16 &s3) {
+// Four natural-scale slices of the double-float x = hi + lo (|x| <= ~1), as floats (each an
+// integer times 2^-8j, exact in BF16).  Each residual d_j is exact (a rounded multiple of the
+// previous one's ulp, below 1/2 in size); lo enters every stage through one FMA.
+__device__ __forceinline__ void slice4f(float hi, float lo, float (&q)[4]) {
   const float q0 = rintf(hi * 256.f);
   const float d0 = __fmaf_rn(hi, 256.f, -q0);
   const float q1 = rintf(__fmaf_rn(lo, 65536.f, d0 * 256.f));
@@ -131,10 +153,28 @@ __device__ __forceinline__ void slice4(float hi, float lo, __nv_bfloat16 &s0, __
   const float q2 = rintf(__fmaf_rn(lo, 16777216.f, d1 * 256.f));
   const float d2 = __fmaf_rn(d1, 256.f, -q2);
   const float q3 = rintf(__fmaf_rn(lo, 4294967296.f, d2 * 256.f));
-  s0 = __float2bfloat16_rn(q0);
-  s1 = __float2bfloat16_rn(q1 * 0x1p-8f);
-  s2 = __float2bfloat16_rn(q2 * 0x1p-16f);
-  s3 = __float2bfloat16_rn(q3 * 0x1p-24f);
+  q[0] = q0, q[1] = q1 * 0x1p-8f, q[2] = q2 * 0x1p-16f, q[3] = q3 * 0x1p-24f;
+}
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {  // a in the low half (lower address)
+  const __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+// Slices of 8 consecutive elements (one core-matrix row) stored as one 16-byte vector per
+// plane: planes at base + l * plane_elems (BF16 units), row offset o (a multiple of 8).
+__device__ __forceinline__ void store_row8(__nv_bfloat16 *base, int plane_elems, int o, const float (&hi)[8],
+                                           const float (&lo)[8]) {
+  float q[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) slice4f(hi[j], lo[j], q[j]);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) {
+    uint4 v;
+    v.x = pack_bf16(q[0][l], q[1][l]);
+    v.y = pack_bf16(q[2][l], q[3][l]);
+    v.z = pack_bf16(q[4][l], q[5][l]);
+    v.w = pack_bf16(q[6][l], q[7][l]);
+    *reinterpret_cast<uint4 *>(base + size_t(l) * plane_elems + o) = v;
+  }
 }
 // (hi, lo) of a + b + c for FP32 a, b (exact sums) and c: Knuth's two-sum twice
 __device__ __forceinline__ float2 sum3(float a, float b, float c) {
@@ -147,154 +187,422 @@ __device__ __forceinline__ float2 sum3(float a, float b, float c) {
   return make_float2(h, __fsub_rn(e, __fsub_rn(h, s2)));
 }
 
+// Issues the 10 slice pairs of one real product into the three accumulators at TMEM column
+// `col` (level 0, 1, 2+3 at col, col + R, col + 2R): A tile planes at a (plane stride pl
+// bytes), B tile planes at b, R = up16(b) output columns, R / 16 K steps.  `accumulate`
+// adds to what the accumulators hold instead of starting them.
+__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint32_t a, uint32_t b, uint32_t pl,
+                                              int R, bool negA, bool accumulate) {
+  const uint32_t id = idesc_bf16(R, negA);
+  const int sp[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3}, tp[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+  const int lev[10] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2};
+#pragma unroll
+  for (int q = 0; q < 10; ++q) {
+    const uint32_t d = tmem + col + uint32_t(lev[q] * R);
+    const bool first = !accumulate && (q == 0 || q == 1 || q == 3);
+    const uint32_t a0 = a + uint32_t(sp[q]) * pl, b0 = b + uint32_t(tp[q]) * pl;
+    for (int kk = 0; kk < R / 16; ++kk)
+      mma(d, sdesc(a0 + kk * 256, R), sdesc(b0 + kk * 256, R), id, (first && kk == 0) ? 0u : 1u);
+  }
+}
+
 }  // namespace tc
 
 enum { kTcTimeout = 64 };  // status bit: a tensor-core wait ran out
 
-// One CTA per crystallite: A_{i+1} = U_i A_i for i < n on the tensor cores, the large block k
-// (b <= tc::kMaxB) of the mixed form, U and A as double-float (float4 re.hi, im.hi, re.lo,
-// im.lo in the [item][c] layout).  Per step: the elected thread issues the 10 slice pairs x 4
-// real products (Cr = Ur Ar - Ui Ai, Ci = Ur Ai + Ui Ar; the minus by the descriptor's
-// negate-A bit) into the six accumulators and commits; meanwhile every thread loads its part
-// of U_{i+1} into registers; after the commit's barrier, the epilogue forms A_{i+1} =
-// 2^-16 (acc0 + acc1 + acc23) in double-float, stores it and writes its slices (the next
-// step's B operand, transposed: row = column of A) into shared memory, and the prefetched
-// U_{i+1} is sliced into the A operand.
-__global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k) {
-  using namespace tc;
+// ------------------------------------------------------------------ step exponential
+// One CTA per (crystallite, step) of a large block b <= tc::kMaxB of the mixed form (no rf
+// schedule): H_i in double-float from k_coef's coefficients (as k_big_step_df),
+// X = 2 pi tau H / 2^sq with ||X||_inf <= 1, and
+//     C = cos X = sum_j (-1)^j Y^j / (2j)!,  S = sin X = X sum_j (-1)^j Y^j / (2j+1)!,  Y = X^2,
+// to the degree K that taylor_degree gives at 2^-40, each by Horner's rule
+//     T <- I - Y T / (k (k + 1))
+// on the tensor cores; the C and S chains alternate between two accumulator sets so that
+// one chain's epilogue runs while the other's products run.  Then sq squarings
+// (C, S) <- (C^2 - S^2, 2 C S) and the slices of U = C - i S go to the step's slab.
+// Shared memory: four tiles (X, Y, T_C, T_S), then the over-read margin.
+__host__ __device__ constexpr size_t tc_step_smem(int b) {
+  return 4 * tc::tile_bytes(b) + tc::overread_bytes(b) + 1024;
+}
+
+__global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, unsigned char *slab0) {
+  using tc::kTcThreads;
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ uint32_t tbase;
-  __shared__ __align__(8) uint64_t mbar;
-  const int c = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ float2 fk[kMaxInt];
+  __shared__ float red[tc::kMaxB];
+  __shared__ float2 scl;
+  __shared__ int nsq, nterms;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
-  const int Kp = up16(b), Np = Kp, Mr = up8(b), ncols = tmem_cols(b);
-  unsigned char *base = tsm + ((1024 - (saddr(tsm) & 1023)) & 1023);
-  __nv_bfloat16 *Us = reinterpret_cast<__nv_bfloat16 *>(base);  // [level][re, im] Mr x Kp
-  __nv_bfloat16 *As = Us + 8 * Mr * Kp;                            // [level][re, im] Np x Kp
-  const int us_sz = Mr * Kp, as_sz = Np * Kp;
-  // zero both operand sets (K and N padding stays zero), A_0 = I
-  {
-    uint4 *z = reinterpret_cast<uint4 *>(base);
-    const int n16 = (8 * (us_sz + as_sz) * 2) / 16;
-    for (int e = tid; e < n16; e += kTcThreads) z[e] = make_uint4(0, 0, 0, 0);
+  const int R = tc::up16(b), pe = int(tc::plane_bytes(b) / 2);  // plane stride in BF16 units
+  const int ncols = tc::pow2_cols(6 * R);
+  unsigned char *base = tsm + ((1024 - (tc::saddr(tsm) & 1023)) & 1023);
+  __nv_bfloat16 *Bf[4];
+  uint32_t ba[4];
+  for (int t = 0; t < 4; ++t) {
+    Bf[t] = reinterpret_cast<__nv_bfloat16 *>(base + t * tc::tile_bytes(b));
+    ba[t] = tc::saddr(Bf[t]);
+  }
+  if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+  if (tid == 0) tc::mbar_init(&mbar[0]), tc::mbar_init(&mbar[1]);
+  {  // term coefficients (double-float pairs from k_coef)
+    const float2 *fk2 = reinterpret_cast<const float2 *>(s.fk);
+    for (int kk = tid; kk < s.nint; kk += kTcThreads) fk[kk] = fk2[at(i * s.nint + kk, c, s.Cpad)];
   }
   __syncthreads();
-  for (int r = tid; r < b; r += kTcThreads) As[kmaj(r, r, Kp)] = __float2bfloat16_rn(256.f);
-  if (warp == 0) tmem_alloc(&tbase, ncols);
-  if (tid == 0) mbar_init(&mbar);
-  // U_0 slices
-  const float4 *U4 = reinterpret_cast<const float4 *>(s.U);
-  float4 ureg[kEPT];
-  auto load_u = [&](int i) {
-    const float4 *Ub = U4 + size_t(i) * s.S2 * s.Cpad;
-#pragma unroll
-    for (int j = 0; j < kEPT; ++j) {
-      const int e = tid + j * kTcThreads;
-      if (e < bb) ureg[j] = Ub[at(bp + e, c, s.Cpad)];
+  // H (double-float) into the fourth tile as scratch; row sums of |H| for the norm
+  float2 *H = reinterpret_cast<float2 *>(Bf[3]);
+  const float2 *Hcb = s.Hc_df + bp;
+  for (int e = tid; e < bb; e += kTcThreads) {
+    float2 h = Hcb[e];
+    for (int j = s.tk_ptr[bp + e]; j < s.tk_ptr[bp + e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[s.tk_term[j]], s.tk_val[j]));
+    H[e] = h;
+  }
+  __syncthreads();
+  for (int p = tid; p < b; p += kTcThreads) {
+    float rs = 0.f;
+    for (int q = 0; q < b; ++q) rs += fabsf(H[p * b + q].x);
+    red[p] = rs;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    float nrm = 0.f;
+    for (int p = 0; p < b; ++p) nrm = fmaxf(nrm, red[p]);
+    nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
+    int sq = 0;
+    if (nrm > 1.f) {
+      frexpf(nrm, &sq);  // nrm < 2^sq
+      sq = min(sq, 60);
     }
-  };
-  auto store_u = [&]() {
+    scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
+    nsq = sq;
+    nterms = taylor_degree(double(ldexpf(nrm, -sq)), true);
+  }
+  __syncthreads();
+  const int sq = nsq, K = nterms;
+  const int mC = K / 2, mS = (K - 1) / 2;  // C to X^(2 mC), S to X^(2 mS + 1)
+  {  // X slices into the first tile: one 8-column row chunk per thread and iteration
+    const float2 sc = scl;
+    const int nch = R * (R / 8);
+    for (int t = tid; t < nch; t += kTcThreads) {
+      const int r = t / (R / 8), c0 = (t % (R / 8)) * 8;
+      float hi[8], lo[8];
 #pragma unroll
-    for (int j = 0; j < kEPT; ++j) {
-      const int e = tid + j * kTcThreads;
-      if (e < bb) {
-        const int r = e / b, q = e - r * b, o = kmaj(r, q, Kp);
-        const float4 u = ureg[j];
-        slice4(u.x, u.z, Us[o], Us[2 * us_sz + o], Us[4 * us_sz + o], Us[6 * us_sz + o]);
-        slice4(u.y, u.w, Us[us_sz + o], Us[3 * us_sz + o], Us[5 * us_sz + o], Us[7 * us_sz + o]);
+      for (int j = 0; j < 8; ++j) {
+        const int q = c0 + j;
+        float2 x = make_float2(0.f, 0.f);
+        if (r < b && q < b) x = dfv_mul(sc, H[r * b + q]);
+        hi[j] = x.x, lo[j] = x.y;
+      }
+      tc::store_row8(Bf[0], pe, tc::tix(r, c0, R), hi, lo);
+    }
+  }
+  tc::fence_smem_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tbase;
+  const uint32_t pl = uint32_t(tc::plane_bytes(b));
+  const uint32_t set_col[2] = {0u, uint32_t(3 * R)};
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  const int q4 = warp & 3, part = warp >> 2;  // lane quarter; 8-column chunks part, part+4, ...
+  // Epilogue of accumulator set `set` for this thread's row and 8-column chunks:
+  // out = diag I + coef P with P = 2^-16 (acc0 + acc1 + acc23), or with `second`
+  // P = P_set0 - P_set1 (the squaring's C^2 - S^2); slices into tile dst, zero padding.
+  auto epilogue = [&](int set, float2 coef, float diag, bool second, __nv_bfloat16 *dst) {
+    const int r = 32 * q4 + lane;
+    if (32 * q4 >= R) return;  // warp-uniform: no stored row in this lane quarter
+    for (int c0 = 8 * part; c0 < R; c0 += 32) {
+      float a0[8], a1[8], a2[8], b0[8], b1[8], b2[8];
+      const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + set_col[set] + uint32_t(c0);
+      tc::ld8(ta, a0);
+      tc::ld8(ta + uint32_t(R), a1);
+      tc::ld8(ta + uint32_t(2 * R), a2);
+      if (second) {
+        const uint32_t tb = tmem + (uint32_t(32 * q4) << 16) + set_col[1] + uint32_t(c0);
+        tc::ld8(tb, b0);
+        tc::ld8(tb + uint32_t(R), b1);
+        tc::ld8(tb + uint32_t(2 * R), b2);
+      }
+      tc::wait_ld();
+      if (r < R) {
+        float hi[8], lo[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int q = c0 + j;
+          float2 v = make_float2(0.f, 0.f);
+          if (r < b && q < b) {
+            const float2 p = tc::sum3(a0[j], a1[j], a2[j]);
+            v = make_float2(p.x * 0x1p-16f, p.y * 0x1p-16f);
+            if (second) {
+              const float2 p2 = tc::sum3(b0[j], b1[j], b2[j]);
+              v = dfv_add(v, make_float2(-p2.x * 0x1p-16f, -p2.y * 0x1p-16f));
+            }
+            v = dfv_mul(coef, v);
+            if (r == q) v = dfv_add(v, make_float2(diag, 0.f));
+          }
+          hi[j] = v.x, lo[j] = v.y;
+        }
+        tc::store_row8(dst, pe, tc::tix(r, c0, R), hi, lo);
       }
     }
   };
-  load_u(0);
-  store_u();
-  fence_smem_async();
-  fence_before();
-  __syncthreads();
-  fence_after();
-  const uint32_t tmem = tbase;
-  const uint32_t ua = saddr(Us), aa = saddr(As);
-  const uint32_t idp = idesc_bf16(Np, false), idn = idesc_bf16(Np, true);
-  const int q4 = warp & 3, half = warp >> 2, hcols = Np / 2;
-  float4 *A4 = reinterpret_cast<float4 *>(s.A);
-  bool ok = true;
-  for (int i = 0; i < s.n; ++i) {
-    if (tid == 0) {
-      // U slice (level l, part p) at ua + (2l + p) us_sz * 2 bytes; A slice likewise
-      auto gemm = [&](uint32_t col, int ul, int up, int al, int ap, bool neg, bool first) {
-        const uint32_t u0 = ua + uint32_t((2 * ul + up) * us_sz * 2), a0 = aa + uint32_t((2 * al + ap) * as_sz * 2);
-        for (int kk = 0; kk < Kp / 16; ++kk)
-          mma(tmem + col, sdesc(u0 + kk * 256, Kp), sdesc(a0 + kk * 256, Kp), neg ? idn : idp,
-              (first && kk == 0) ? 0u : 1u);
-      };
-      auto pair = [&](int lev, int us_, int at_, bool first) {
-        const uint32_t cre = uint32_t(2 * lev * Np), cim = uint32_t((2 * lev + 1) * Np);
-        gemm(cre, us_, 0, at_, 0, false, first);
-        gemm(cre, us_, 1, at_, 1, true, false);
-        gemm(cim, us_, 0, at_, 1, false, first);
-        gemm(cim, us_, 1, at_, 0, false, false);
-      };
-      pair(0, 0, 0, true);
-      pair(1, 0, 1, true);
-      pair(1, 1, 0, false);
-      pair(2, 0, 2, true);
-      pair(2, 1, 1, false);
-      pair(2, 2, 0, false);
-      pair(2, 0, 3, false);
-      pair(2, 1, 2, false);
-      pair(2, 2, 1, false);
-      pair(2, 3, 0, false);
-      commit(&mbar);
+  auto identity = [&](__nv_bfloat16 *dst) {  // the identity tile (C = I when mC == 0)
+    const int nch = R * (R / 8);
+    for (int t = tid; t < nch; t += kTcThreads) {
+      const int r = t / (R / 8), c0 = (t % (R / 8)) * 8;
+      float hi[8], lo[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) hi[j] = (r < b && r == c0 + j) ? 1.f : 0.f, lo[j] = 0.f;
+      tc::store_row8(dst, pe, tc::tix(r, c0, R), hi, lo);
     }
-    if (i + 1 < s.n) load_u(i + 1);  // overlaps the MMAs
-    const bool done = wait_parity(&mbar, uint32_t(i & 1));
-    if (!__syncthreads_and(done)) {
+  };
+  auto sync_async = [&]() {  // epilogue writes -> the next MMAs
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  };
+  auto wait_set = [&](int set) -> bool {
+    const bool done = tc::wait_parity(&mbar[set], phase[set]);
+    phase[set] ^= 1u;
+    const bool all = __syncthreads_and(done);
+    tc::fence_after();
+    return all;
+  };
+  auto hcoef = [](int kk) { return dfv_of(-1.0 / (double(kk) * double(kk + 1))); };  // -1/(k(k+1))
+  __nv_bfloat16 *Y = Bf[1], *TC = Bf[2], *TS = Bf[3];
+  const uint32_t aX = ba[0], aY = ba[1], aTC = ba[2], aTS = ba[3];
+  // Y = X X, then the innermost Horner terms straight from Y
+  if (tid == 0) {
+    tc::issue_product(tmem, set_col[0], aX, aX, pl, R, false, false);
+    tc::commit(&mbar[0]);
+  }
+  if (!wait_set(0)) ok = false;
+  if (ok) {
+    epilogue(0, make_float2(1.f, 0.f), 0.f, false, Y);
+    if (mC >= 1) epilogue(0, hcoef(2 * mC - 1), 1.f, false, TC);
+    else identity(TC);
+    if (mS >= 1) epilogue(0, hcoef(2 * mS), 1.f, false, TS);
+    sync_async();
+  }
+  // the two Horner chains: T_C <- I - Y T_C / ((2j-1) 2j) for j = mC-1..1 (set 0),
+  // T_S <- I - Y T_S / (2j (2j+1)) for j = mS-1..1 (set 1)
+  int jc = mC - 1, js = mS - 1;
+  bool busyC = ok && jc >= 1, busyS = ok && js >= 1;
+  if (tid == 0) {
+    if (busyC) tc::issue_product(tmem, set_col[0], aY, aTC, pl, R, false, false), tc::commit(&mbar[0]);
+    if (busyS) tc::issue_product(tmem, set_col[1], aY, aTS, pl, R, false, false), tc::commit(&mbar[1]);
+  }
+  while (ok && (busyC || busyS)) {
+    if (busyC) {
+      if (!wait_set(0)) {
+        ok = false;
+        break;
+      }
+      epilogue(0, hcoef(2 * jc - 1), 1.f, false, TC);
+      --jc;
+      sync_async();
+      busyC = jc >= 1;
+      if (busyC && tid == 0) tc::issue_product(tmem, set_col[0], aY, aTC, pl, R, false, false), tc::commit(&mbar[0]);
+    }
+    if (busyS) {
+      if (!wait_set(1)) {
+        ok = false;
+        break;
+      }
+      epilogue(1, hcoef(2 * js), 1.f, false, TS);
+      --js;
+      sync_async();
+      busyS = js >= 1;
+      if (busyS && tid == 0) tc::issue_product(tmem, set_col[1], aY, aTS, pl, R, false, false), tc::commit(&mbar[1]);
+    }
+  }
+  // S = X S' into Y's tile (S = X when mS == 0)
+  __nv_bfloat16 *Ct = TC, *St = Bf[0];
+  uint32_t aC = aTC, aS = aX;
+  if (ok && mS >= 1) {
+    if (tid == 0) tc::issue_product(tmem, set_col[1], aX, aTS, pl, R, false, false), tc::commit(&mbar[1]);
+    if (!wait_set(1)) ok = false;
+    if (ok) {
+      epilogue(1, make_float2(1.f, 0.f), 0.f, false, Y);
+      sync_async();
+      St = Y, aS = aY;
+    }
+  }
+  // squarings: C' = C^2 - S^2 (sets 0 and 1), S' = 2 C S (set 0), into the two free tiles
+  for (int t = 0; ok && t < sq; ++t) {
+    __nv_bfloat16 *fr[2] = {nullptr, nullptr};
+    uint32_t fa[2] = {0u, 0u};
+    int nf = 0;
+    for (int u = 0; u < 4; ++u)
+      if (Bf[u] != Ct && Bf[u] != St && nf < 2) fr[nf] = Bf[u], fa[nf] = ba[u], ++nf;
+    if (tid == 0) {
+      tc::issue_product(tmem, set_col[0], aC, aC, pl, R, false, false);
+      tc::commit(&mbar[0]);
+      tc::issue_product(tmem, set_col[1], aS, aS, pl, R, false, false);
+      tc::commit(&mbar[1]);
+    }
+    const bool w0 = wait_set(0), w1 = wait_set(1);
+    if (!w0 || !w1) {
       ok = false;
       break;
     }
-    fence_after();
-    // epilogue: this thread's row r of A_{i+1}, columns of its half
-    const int r = 32 * q4 + lane;
+    epilogue(0, make_float2(1.f, 0.f), 0.f, true, fr[0]);
+    sync_async();
+    if (tid == 0) tc::issue_product(tmem, set_col[0], aC, aS, pl, R, false, false), tc::commit(&mbar[0]);
+    if (!wait_set(0)) {
+      ok = false;
+      break;
+    }
+    epilogue(0, make_float2(2.f, 0.f), 0.f, false, fr[1]);
+    sync_async();
+    Ct = fr[0], aC = fa[0], St = fr[1], aS = fa[1];
+  }
+  if (ok) {  // the slab: C tile, then S tile (U = C - i S), 16-byte coalesced copies
+    uint4 *dst = reinterpret_cast<uint4 *>(slab0 + (size_t(c) * s.n + i) * tc::slab_bytes(b));
+    const int nv = int(tc::tile_bytes(b) / 16);
+    const uint4 *cs = reinterpret_cast<const uint4 *>(Ct), *ss = reinterpret_cast<const uint4 *>(St);
+    for (int v = tid; v < nv; v += kTcThreads) dst[v] = cs[v], dst[nv + v] = ss[v];
+  } else {
+    if (tid == 0) atomicOr(s.status, kTcTimeout);
+    tc::wait_parity(&mbar[0], phase[0]);  // bounded: let MMAs in flight drain before TMEM is freed
+    tc::wait_parity(&mbar[1], phase[1]);
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
+// ------------------------------------------------------------------ Dyson product
+// One CTA per crystallite: A_{i+1} = U_i A_i for i < n, large block k of the mixed form.
+// The product is formed transposed, A_{i+1}^T = A_i^T U_i (U_i = C - i S is symmetric):
+//   re = Ar^T C + Ai^T S,   im = Ai^T C - Ar^T S   (the minus by the negate-A bit),
+// so that the epilogue lane of column m of A_{i+1} stores row m of the next A_i^T tile as
+// whole 16-byte core-matrix rows.  U_i's slab (written by k_tc_step) arrives by a bulk copy
+// that overlaps the previous step's epilogue.  A_{i+1} also goes to s.A as double-float
+// (float4 re.hi, im.hi, re.lo, im.lo in the [item][c] layout) for the eigenframe and the
+// Floquet step.  Shared memory: the A^T tiles (re, im), the U slab (C, S), the margin.
+__host__ __device__ constexpr size_t tc_dyson_smem(int b) {
+  return 4 * tc::tile_bytes(b) + tc::overread_bytes(b) + 1024;
+}
+
+__global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k, const unsigned char *slab0) {
+  using tc::kTcThreads;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ uint32_t tbase;
+  __shared__ __align__(8) uint64_t mbar[2];  // 0: MMAs done, 1: U slab arrived
+  const int c = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int b = s.bs[k], bp = s.bpoff[k];
+  const int R = tc::up16(b), pe = int(tc::plane_bytes(b) / 2);
+  const int ncols = tc::pow2_cols(6 * R);
+  unsigned char *base = tsm + ((1024 - (tc::saddr(tsm) & 1023)) & 1023);
+  __nv_bfloat16 *Ar = reinterpret_cast<__nv_bfloat16 *>(base);
+  __nv_bfloat16 *Ai = reinterpret_cast<__nv_bfloat16 *>(base + tc::tile_bytes(b));
+  unsigned char *Us = base + 2 * tc::tile_bytes(b);  // C tile, then S tile
+  const uint32_t slab = uint32_t(tc::slab_bytes(b));
+  const unsigned char *src = slab0 + size_t(c) * s.n * tc::slab_bytes(b);
+  {  // A_0^T = I: zero both A tiles, 256 (= 1 at natural scale) on the level-0 real diagonal
+    uint4 *z = reinterpret_cast<uint4 *>(base);
+    const int n16 = int(2 * tc::tile_bytes(b) / 16);
+    for (int e = tid; e < n16; e += kTcThreads) z[e] = make_uint4(0, 0, 0, 0);
+  }
+  __syncthreads();
+  for (int r = tid; r < b; r += kTcThreads) Ar[tc::tix(r, r, R)] = __float2bfloat16_rn(256.f);
+  if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0]), tc::mbar_init(&mbar[1]);
+    tc::bulk_load(Us, src, slab, &mbar[1]);
+  }
+  tc::fence_smem_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tbase;
+  const uint32_t aAr = tc::saddr(Ar), aAi = tc::saddr(Ai), aC = tc::saddr(Us);
+  const uint32_t aS = aC + uint32_t(tc::tile_bytes(b)), pl = uint32_t(tc::plane_bytes(b));
+  const int q4 = warp & 3, part = warp >> 2;  // lane quarter; 8-column chunks part, part+4, ...
+  float4 *A4 = reinterpret_cast<float4 *>(s.A);
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  for (int i = 0; i < s.n; ++i) {
+    {  // U_i's slab must have landed
+      const bool got = tc::wait_parity(&mbar[1], ph[1]);
+      ph[1] ^= 1u;
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
+    }
+    if (tid == 0) {
+      tc::fence_after();
+      tc::issue_product(tmem, 0, aAr, aC, pl, R, false, false);                // re  = Ar^T C
+      tc::issue_product(tmem, 0, aAi, aS, pl, R, false, true);                 // re += Ai^T S
+      tc::issue_product(tmem, uint32_t(3 * R), aAi, aC, pl, R, false, false);  // im  = Ai^T C
+      tc::issue_product(tmem, uint32_t(3 * R), aAr, aS, pl, R, true, true);    // im -= Ar^T S
+      tc::commit(&mbar[0]);
+    }
+    {
+      const bool done = tc::wait_parity(&mbar[0], ph[0]);
+      ph[0] ^= 1u;
+      if (!__syncthreads_and(done)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+    }
+    // U_{i+1} streams in while the epilogue runs (the products no longer read the slab)
+    if (tid == 0 && i + 1 < s.n) tc::bulk_load(Us, src + size_t(i + 1) * slab, slab, &mbar[1]);
+    // epilogue: lane m = column m of A_{i+1}, 8 rows n at a time
     float4 *Ab = A4 + size_t(i) * s.S2 * s.Cpad;
-    if (32 * q4 < b) {
-      for (int c0 = half * hcols; c0 < (half + 1) * hcols; c0 += 8) {
-        float a0r[8], a0i[8], a1r[8], a1i[8], a2r[8], a2i[8];
+    const int m = 32 * q4 + lane;
+    if (32 * q4 < R) {
+      for (int c0 = 8 * part; c0 < R; c0 += 32) {
+        float r0[8], r1[8], r2[8], i0[8], i1[8], i2[8];
         const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + uint32_t(c0);
-        ld8(ta, a0r);
-        ld8(ta + uint32_t(Np), a0i);
-        ld8(ta + uint32_t(2 * Np), a1r);
-        ld8(ta + uint32_t(3 * Np), a1i);
-        ld8(ta + uint32_t(4 * Np), a2r);
-        ld8(ta + uint32_t(5 * Np), a2i);
-        wait_ld();
-        if (r < b) {
+        tc::ld8(ta, r0);
+        tc::ld8(ta + uint32_t(R), r1);
+        tc::ld8(ta + uint32_t(2 * R), r2);
+        tc::ld8(ta + uint32_t(3 * R), i0);
+        tc::ld8(ta + uint32_t(4 * R), i1);
+        tc::ld8(ta + uint32_t(5 * R), i2);
+        tc::wait_ld();
+        if (m < R) {
+          float rh[8], rl[8], ih[8], il[8];
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const int col = c0 + j;
-            if (col < b) {
-              const float2 re = sum3(a0r[j], a1r[j], a2r[j]), im = sum3(a0i[j], a1i[j], a2i[j]);
-              const float rh = re.x * 0x1p-16f, rl = re.y * 0x1p-16f, ih = im.x * 0x1p-16f, il = im.y * 0x1p-16f;
-              Ab[at(bp + r * b + col, c, s.Cpad)] = make_float4(rh, ih, rl, il);
-              const int o = kmaj(col, r, Kp);  // B operand: row = column of A, K = row of A
-              slice4(rh, rl, As[o], As[2 * as_sz + o], As[4 * as_sz + o], As[6 * as_sz + o]);
-              slice4(ih, il, As[as_sz + o], As[3 * as_sz + o], As[5 * as_sz + o], As[7 * as_sz + o]);
+            const int n = c0 + j;
+            float2 re = make_float2(0.f, 0.f), im = re;
+            if (m < b && n < b) {
+              const float2 pr = tc::sum3(r0[j], r1[j], r2[j]), pi = tc::sum3(i0[j], i1[j], i2[j]);
+              re = make_float2(pr.x * 0x1p-16f, pr.y * 0x1p-16f);
+              im = make_float2(pi.x * 0x1p-16f, pi.y * 0x1p-16f);
+              Ab[at(bp + n * b + m, c, s.Cpad)] = make_float4(re.x, im.x, re.y, im.y);
             }
+            rh[j] = re.x, rl[j] = re.y, ih[j] = im.x, il[j] = im.y;
           }
+          const int o = tc::tix(m, c0, R);
+          tc::store_row8(Ar, pe, o, rh, rl);
+          tc::store_row8(Ai, pe, o, ih, il);
         }
       }
     }
-    if (i + 1 < s.n) store_u();
-    fence_smem_async();
-    fence_before();
+    tc::fence_smem_async();
+    tc::fence_before();
     __syncthreads();
-    fence_after();
   }
   if (!ok) {
     if (tid == 0) atomicOr(s.status, kTcTimeout);
-    wait_parity(&mbar, 0);  // bounded: let any MMA still in flight drain before TMEM is freed
-    wait_parity(&mbar, 1);
-    fence_before();
-    __syncthreads();
-    fence_after();
+    tc::wait_parity(&mbar[0], ph[0]);  // bounded: let MMAs and the copy in flight drain
+    tc::wait_parity(&mbar[1], ph[1]);
   }
-  if (warp == 0) tmem_free(tmem, ncols);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
 }
