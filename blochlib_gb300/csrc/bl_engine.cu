@@ -2415,7 +2415,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   if (J.tc) {
     J.usl_off.assign(nb, 0);
     for (int k = 0; k < nb; ++k)
-      if (L.size[k] > kMaxBlock && L.size[k] <= kMaxBigBlock) usl_per_c += nsteps * tc::slab_bytes(L.size[k]);
+      if (L.size[k] >= tc::kMinB && L.size[k] <= tc::kMaxB) usl_per_c += nsteps * tc::slab_bytes(L.size[k]);
     per_c += usl_per_c;
   }
   long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
@@ -2566,7 +2566,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       if (J.tc) {
         size_t sm_step = 0, sm_dy = 0;
         for (int k : J.big_blocks)
-          sm_step = std::max(sm_step, tc_step_smem(L.size[k])), sm_dy = std::max(sm_dy, tc_dyson_smem(L.size[k]));
+          if (L.size[k] >= tc::kMinB)
+            sm_step = std::max(sm_step, tc_step_smem(L.size[k])), sm_dy = std::max(sm_dy, tc_dyson_smem(L.size[k]));
         attr((const void *)k_tc_step, sm_step);
         attr((const void *)k_tc_dyson, sm_dy);
       }
@@ -2703,7 +2704,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     J.usl.alloc(usl_per_c * Cb);
     size_t off = 0;
     for (int k = 0; k < nb; ++k)
-      if (L.size[k] > kMaxBlock && L.size[k] <= kMaxBigBlock) {
+      if (L.size[k] >= tc::kMinB && L.size[k] <= tc::kMaxB) {
         J.usl_off[k] = off;
         off += nsteps * tc::slab_bytes(L.size[k]) * Cb;
       }
@@ -3075,13 +3076,13 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
     const bool nt1 = big_nt(b, b) == 1;
     switch (stage) {
       case 0:
-        if (J.tc)
+        if (J.tc && b >= tc::kMinB)
           k_tc_step<<<unsigned(s.C) * unsigned(s.n), tc::kTcThreads, tc_step_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
         else if (s.mixed) k_big_step_df<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_df_smem(b), st>>>(s, k);
         else k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k);
         break;
       case 1:
-        if (J.tc) {  // exact-slice BF16 products on the tensor cores
+        if (J.tc && b >= tc::kMinB) {  // exact-slice BF16 products on the tensor cores
           k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc_dyson_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
         } else if (s.mixed) {
           if (nt1) k_big_dyson_df<1><<<unsigned(s.C), th, smat, st>>>(s, k);

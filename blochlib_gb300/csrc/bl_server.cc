@@ -226,7 +226,9 @@ void Server::loop() {
       std::lock_guard<std::mutex> lk(mu_);
       stopping = stop_;
     }
-    // admissions, first come first served, while a lane is idle and the head's grant fits
+    // admissions while a lane is idle: the head of the queue when its grant fits; otherwise
+    // the first of the next kSkipWindow requests whose grant fits, as long as the head has
+    // been passed over fewer than kMaxSkips times (then only the head, so it cannot starve)
     for (auto &sp : lanes_) {
       if (stopping) break;
       Lane &s = *sp;
@@ -237,10 +239,25 @@ void Server::loop() {
         std::lock_guard<std::mutex> lk(mu_);
         while (!queue_.empty() && queue_.front()->state != 0) queue_.pop_front();  // cancelled
         if (queue_.empty()) break;
+        size_t pick = queue_.size();
         bytes = grant(*queue_.front());
-        if (!ranges_.take(bytes, &off)) break;  // wait for a completion to free memory
-        r = queue_.front();
-        queue_.pop_front();
+        if (ranges_.take(bytes, &off)) {
+          pick = 0;
+        } else if (queue_.front()->skipped < kMaxSkips) {
+          const size_t end = std::min(queue_.size(), size_t(1) + kSkipWindow);
+          for (size_t q = 1; q < end; ++q) {
+            if (queue_[q]->state != 0) continue;
+            bytes = grant(*queue_[q]);
+            if (ranges_.take(bytes, &off)) {
+              pick = q;
+              ++queue_.front()->skipped;
+              break;
+            }
+          }
+        }
+        if (pick == queue_.size()) break;  // wait for a completion to free memory
+        r = queue_[pick];
+        queue_.erase(queue_.begin() + std::ptrdiff_t(pick));
         r->state = 1;
         r->t_start = std::chrono::steady_clock::now();
       }

@@ -11,11 +11,13 @@
 //     (job_bytes: the bytes for one warp of crystallites per batch and for all crystallites
 //     at once) and fails those whose one-warp size exceeds the pool, so that submitting
 //     never waits on host-side planning;
-//   * admission is first come first served: the head of the queue is admitted when a lane
-//     is idle and the pool holds a free range of its grant, grant = its full size capped at
-//     pool/lanes but never below its one-warp size.  The job is built inside that range (no
-//     further allocation), batching its crystallites to fit, enqueued on the lane's stream,
-//     and its completion recorded with an event;
+//   * admission: when a lane is idle, the head of the queue is admitted if the pool holds a
+//     free range of its grant, grant = its full size capped at pool/lanes but never below
+//     its one-warp size; if it does not, the first of the next kSkipWindow requests whose
+//     grant fits is admitted instead (a small job does not wait behind a large one), but the
+//     head is passed over at most kMaxSkips times, after which admission waits for it.  The
+//     job is built inside that range (no further allocation), batching its crystallites to
+//     fit, enqueued on the lane's stream, and its completion recorded with an event;
 //   * a worker thread polls completions, copies the FID back and returns the range;
 //   * latency = completion - submission, measured on the host steady clock.
 // Jobs never share arithmetic and the crystallite batching does not change the powder sum
@@ -48,6 +50,7 @@ struct ServeRequest {
   size_t min_bytes = 0, full_bytes = 0;
   std::chrono::steady_clock::time_point t_submit, t_start, t_done;
   int state = 0;  // 0 queued, 1 running, 2 done, 3 failed, 4 cancelled
+  int skipped = 0;  // times a later request was admitted ahead of this one at the queue's head
   std::vector<double> fid;
   double sw = 0;
   std::string err;
@@ -69,6 +72,8 @@ class RangePool {
 
 class Server {
  public:
+  static constexpr size_t kSkipWindow = 16;  // requests behind a blocked head that may go first
+  static constexpr int kMaxSkips = 32;       // times the head may be passed over
   Server(int device, int lanes, size_t pool_bytes);
   ~Server();
   // queues the job (the planner fails it later if one warp of it exceeds the pool)

@@ -38,6 +38,10 @@ namespace tc {
 
 constexpr int kTcThreads = 512;          // 16 warps: four per TMEM lane quarter
 constexpr int kMaxB = kMaxBigBlock;      // largest block on these kernels (up16 = 80)
+// smallest block on these kernels: below it the per-item costs (TMEM allocation, H assembly,
+// one synchronised epilogue per product) outweigh the products, and the double-float kernels
+// are faster (b = 28: the tensor-core step takes 3x the double-float step's time per item)
+constexpr int kMinB = 40;
 constexpr unsigned long long kWaitNs = 1000000000ull;  // an mbarrier wait gives up after 1 s
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return uint32_t(__cvta_generic_to_shared(p)); }
@@ -217,8 +221,9 @@ enum { kTcTimeout = 64 };  // status bit: a tensor-core wait ran out
 //     C = cos X = sum_j (-1)^j Y^j / (2j)!,  S = sin X = X sum_j (-1)^j Y^j / (2j+1)!,  Y = X^2,
 // to the degree K that taylor_degree gives at 2^-40, each by Horner's rule
 //     T <- I - Y T / (k (k + 1))
-// on the tensor cores; the C and S chains alternate between two accumulator sets so that
-// one chain's epilogue runs while the other's products run.  Then sq squarings
+// on the tensor cores; the C and S chains run in two groups of 8 warps with their own
+// accumulator sets, named barriers and MMA-issuing threads, so that one chain's epilogue
+// runs while the other's products (and epilogue) run.  Then sq squarings
 // (C, S) <- (C^2 - S^2, 2 C S) and the slices of U = C - i S go to the step's slab.
 // Shared memory: four tiles (X, Y, T_C, T_S), then the over-read margin.
 __host__ __device__ constexpr size_t tc_step_smem(int b) {
@@ -233,9 +238,10 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
   __shared__ float2 fk[kMaxInt];
   __shared__ float red[tc::kMaxB];
   __shared__ float2 scl;
-  __shared__ int nsq, nterms;
+  __shared__ int nsq, nterms, gfail[2];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
+  if (tid < 2) gfail[tid] = 0;
   const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
   const int R = tc::up16(b), pe = int(tc::plane_bytes(b) / 2);  // plane stride in BF16 units
   const int ncols = tc::pow2_cols(6 * R);
@@ -309,14 +315,15 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
   const uint32_t set_col[2] = {0u, uint32_t(3 * R)};
   uint32_t phase[2] = {0u, 0u};
   bool ok = true;
-  const int q4 = warp & 3, part = warp >> 2;  // lane quarter; 8-column chunks part, part+4, ...
-  // Epilogue of accumulator set `set` for this thread's row and 8-column chunks:
-  // out = diag I + coef P with P = 2^-16 (acc0 + acc1 + acc23), or with `second`
-  // P = P_set0 - P_set1 (the squaring's C^2 - S^2); slices into tile dst, zero padding.
-  auto epilogue = [&](int set, float2 coef, float diag, bool second, __nv_bfloat16 *dst) {
+  const int q4 = warp & 3;  // this warp's TMEM lane quarter
+  // Epilogue of accumulator set `set` over this thread's row and its 8-column chunks
+  // (chunk index part, part + nparts, ...): out = diag I + coef P with
+  // P = 2^-16 (acc0 + acc1 + acc23), or with `second` P = P_set0 - P_set1 (the squaring's
+  // C^2 - S^2); slices into tile dst, zero padding.
+  auto epilogue = [&](int set, float2 coef, float diag, bool second, __nv_bfloat16 *dst, int part, int nparts) {
     const int r = 32 * q4 + lane;
     if (32 * q4 >= R) return;  // warp-uniform: no stored row in this lane quarter
-    for (int c0 = 8 * part; c0 < R; c0 += 32) {
+    for (int c0 = 8 * part; c0 < R; c0 += 8 * nparts) {
       float a0[8], a1[8], a2[8], b0[8], b1[8], b2[8];
       const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + set_col[set] + uint32_t(c0);
       tc::ld8(ta, a0);
@@ -361,13 +368,13 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
       tc::store_row8(dst, pe, tc::tix(r, c0, R), hi, lo);
     }
   };
-  auto sync_async = [&]() {  // epilogue writes -> the next MMAs
+  auto sync_all = [&]() {  // epilogue writes -> the next MMAs, whole CTA
     tc::fence_smem_async();
     tc::fence_before();
     __syncthreads();
     tc::fence_after();
   };
-  auto wait_set = [&](int set) -> bool {
+  auto wait_all = [&](int set) -> bool {
     const bool done = tc::wait_parity(&mbar[set], phase[set]);
     phase[set] ^= 1u;
     const bool all = __syncthreads_and(done);
@@ -375,65 +382,69 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
     return all;
   };
   auto hcoef = [](int kk) { return dfv_of(-1.0 / (double(kk) * double(kk + 1))); };  // -1/(k(k+1))
-  __nv_bfloat16 *Y = Bf[1], *TC = Bf[2], *TS = Bf[3];
+  __nv_bfloat16 *X = Bf[0], *Y = Bf[1], *TC = Bf[2], *TS = Bf[3];
   const uint32_t aX = ba[0], aY = ba[1], aTC = ba[2], aTS = ba[3];
-  // Y = X X, then the innermost Horner terms straight from Y
+  // Y = X X, then the innermost Horner terms straight from Y (all 16 warps)
   if (tid == 0) {
     tc::issue_product(tmem, set_col[0], aX, aX, pl, R, false, false);
     tc::commit(&mbar[0]);
   }
-  if (!wait_set(0)) ok = false;
+  if (!wait_all(0)) ok = false;
   if (ok) {
-    epilogue(0, make_float2(1.f, 0.f), 0.f, false, Y);
-    if (mC >= 1) epilogue(0, hcoef(2 * mC - 1), 1.f, false, TC);
+    epilogue(0, make_float2(1.f, 0.f), 0.f, false, Y, warp >> 2, 4);
+    if (mC >= 1) epilogue(0, hcoef(2 * mC - 1), 1.f, false, TC, warp >> 2, 4);
     else identity(TC);
-    if (mS >= 1) epilogue(0, hcoef(2 * mS), 1.f, false, TS);
-    sync_async();
+    if (mS >= 1) epilogue(0, hcoef(2 * mS), 1.f, false, TS, warp >> 2, 4);
+    sync_all();
   }
-  // the two Horner chains: T_C <- I - Y T_C / ((2j-1) 2j) for j = mC-1..1 (set 0),
-  // T_S <- I - Y T_S / (2j (2j+1)) for j = mS-1..1 (set 1)
-  int jc = mC - 1, js = mS - 1;
-  bool busyC = ok && jc >= 1, busyS = ok && js >= 1;
-  if (tid == 0) {
-    if (busyC) tc::issue_product(tmem, set_col[0], aY, aTC, pl, R, false, false), tc::commit(&mbar[0]);
-    if (busyS) tc::issue_product(tmem, set_col[1], aY, aTS, pl, R, false, false), tc::commit(&mbar[1]);
-  }
-  while (ok && (busyC || busyS)) {
-    if (busyC) {
-      if (!wait_set(0)) {
-        ok = false;
-        break;
-      }
-      epilogue(0, hcoef(2 * jc - 1), 1.f, false, TC);
-      --jc;
-      sync_async();
-      busyC = jc >= 1;
-      if (busyC && tid == 0) tc::issue_product(tmem, set_col[0], aY, aTC, pl, R, false, false), tc::commit(&mbar[0]);
+  // The two Horner chains, each in its own group of 8 warps (two per lane quarter) with its
+  // own named barrier and MMA-issuing thread, so that their epilogues and products overlap:
+  //   group 0: T_C <- I - Y T_C / ((2j-1) 2j) for j = mC-1..1 (set 0), C = T_C;
+  //   group 1: T_S <- I - Y T_S / (2j (2j+1)) for j = mS-1..1 (set 1), then S = X T_S into
+  //            X's tile (S = X when mS == 0).
+  const int grp = warp >> 3, gpart = (warp >> 2) & 1, gbar = 1 + grp;
+  const int leader = grp * (kTcThreads / 2);
+  auto sync_grp = [&]() {
+    tc::fence_smem_async();
+    tc::fence_before();
+    asm volatile("bar.sync %0, %1;" ::"r"(gbar), "r"(kTcThreads / 2) : "memory");
+    tc::fence_after();
+  };
+  auto wait_grp = [&](int set) -> bool {
+    const bool done = tc::wait_parity(&mbar[set], phase[set]);
+    phase[set] ^= 1u;
+    if (!done) gfail[grp] = 1;
+    asm volatile("bar.sync %0, %1;" ::"r"(gbar), "r"(kTcThreads / 2) : "memory");
+    tc::fence_after();
+    return gfail[grp] == 0;
+  };
+  if (ok) {
+    const int set = grp;
+    __nv_bfloat16 *T = grp == 0 ? TC : TS;
+    const uint32_t aT = grp == 0 ? aTC : aTS;
+    int j = grp == 0 ? mC - 1 : mS - 1;
+    while (j >= 1) {
+      if (tid == leader) tc::issue_product(tmem, set_col[set], aY, aT, pl, R, false, false), tc::commit(&mbar[set]);
+      if (!wait_grp(set)) break;
+      epilogue(set, hcoef(grp == 0 ? 2 * j - 1 : 2 * j), 1.f, false, T, gpart, 2);
+      --j;
+      sync_grp();
     }
-    if (busyS) {
-      if (!wait_set(1)) {
-        ok = false;
-        break;
+    if (grp == 1 && mS >= 1 && gfail[1] == 0) {
+      if (tid == leader) tc::issue_product(tmem, set_col[1], aX, aTS, pl, R, false, false), tc::commit(&mbar[1]);
+      if (wait_grp(1)) {
+        epilogue(1, make_float2(1.f, 0.f), 0.f, false, X, gpart, 2);
+        sync_grp();
       }
-      epilogue(1, hcoef(2 * js), 1.f, false, TS);
-      --js;
-      sync_async();
-      busyS = js >= 1;
-      if (busyS && tid == 0) tc::issue_product(tmem, set_col[1], aY, aTS, pl, R, false, false), tc::commit(&mbar[1]);
     }
   }
-  // S = X S' into Y's tile (S = X when mS == 0)
-  __nv_bfloat16 *Ct = TC, *St = Bf[0];
+  sync_all();
+  if (gfail[0] || gfail[1]) ok = false;
+  // each group advanced only its own barrier's phase: both from the products committed
+  phase[0] = uint32_t(1 + max(mC - 1, 0)) & 1u;
+  phase[1] = uint32_t(max(mS - 1, 0) + (mS >= 1 ? 1 : 0)) & 1u;
+  __nv_bfloat16 *Ct = TC, *St = X;
   uint32_t aC = aTC, aS = aX;
-  if (ok && mS >= 1) {
-    if (tid == 0) tc::issue_product(tmem, set_col[1], aX, aTS, pl, R, false, false), tc::commit(&mbar[1]);
-    if (!wait_set(1)) ok = false;
-    if (ok) {
-      epilogue(1, make_float2(1.f, 0.f), 0.f, false, Y);
-      sync_async();
-      St = Y, aS = aY;
-    }
-  }
   // squarings: C' = C^2 - S^2 (sets 0 and 1), S' = 2 C S (set 0), into the two free tiles
   for (int t = 0; ok && t < sq; ++t) {
     __nv_bfloat16 *fr[2] = {nullptr, nullptr};
@@ -447,20 +458,20 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
       tc::issue_product(tmem, set_col[1], aS, aS, pl, R, false, false);
       tc::commit(&mbar[1]);
     }
-    const bool w0 = wait_set(0), w1 = wait_set(1);
+    const bool w0 = wait_all(0), w1 = wait_all(1);
     if (!w0 || !w1) {
       ok = false;
       break;
     }
-    epilogue(0, make_float2(1.f, 0.f), 0.f, true, fr[0]);
-    sync_async();
+    epilogue(0, make_float2(1.f, 0.f), 0.f, true, fr[0], warp >> 2, 4);
+    sync_all();
     if (tid == 0) tc::issue_product(tmem, set_col[0], aC, aS, pl, R, false, false), tc::commit(&mbar[0]);
-    if (!wait_set(0)) {
+    if (!wait_all(0)) {
       ok = false;
       break;
     }
-    epilogue(0, make_float2(2.f, 0.f), 0.f, false, fr[1]);
-    sync_async();
+    epilogue(0, make_float2(2.f, 0.f), 0.f, false, fr[1], warp >> 2, 4);
+    sync_all();
     Ct = fr[0], aC = fa[0], St = fr[1], aS = fa[1];
   }
   if (ok) {  // the slab: C tile, then S tile (U = C - i S), 16-byte coalesced copies

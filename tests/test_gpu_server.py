@@ -105,3 +105,52 @@ def test_point_to_point_requests_are_served():
                                                                       rf_chunks=sched)
     np.testing.assert_array_equal(res[t][1], direct)
     srv.close()
+
+
+def test_mixed_result_is_the_same_alone_and_in_the_mix():
+    """The form the target measures: a mixed-precision request (6 x 1H: its blocks of 15 and
+    20 run on the tensor-core step and Dyson kernels) gives the same FID bit for bit alone and
+    among mixed and FP64 requests of other systems, within 1e-6 of its FP64 result."""
+    srv = bl.Server(0, lanes=6, pool_bytes=12 << 30)
+    probe = _job(W.config(3, 2), 64)
+    t = srv.submit(**probe, precision=1, step_method="taylor")
+    alone = _wait(srv, [t])[t][1]
+    tickets = []
+    for i in range(16):
+        tickets.append(srv.submit(**_job(W.config(3, 100 + i), 64), precision=i % 2, step_method="taylor"))
+        if i == 7:
+            tp = srv.submit(**probe, precision=1, step_method="taylor")
+    tf = srv.submit(**probe, precision=0, step_method="taylor")
+    res = _wait(srv, tickets + [tp, tf], timeout=300)
+    assert all(r[0] == srv.DONE for r in res.values())
+    np.testing.assert_array_equal(res[tp][1], alone)
+    err = np.linalg.norm(alone - res[tf][1]) / np.linalg.norm(res[tf][1])
+    assert 0 < err <= 1e-6, err
+    srv.close()
+
+
+def test_small_requests_pass_a_blocked_large_head():
+    """Bounded skip-ahead: a pool that holds one large job's grant (its one-warp size, so it
+    runs in many batches) plus one small job.  With the first large job running, the second
+    waits at the head of the queue; the small jobs behind it are admitted on the other lane
+    and finish long before the first large job does.  Results equal the direct call."""
+    big = _job(W.config(1), 3722)
+    lo, hi = bl.job_bytes(**big)
+    small = _job(W.config(0), 64)
+    slo, shi = bl.job_bytes(**small)
+    pool = lo + shi + (1 << 20)  # < 2 lo: one large grant at a time; share = pool / 2 < lo
+    assert pool < 2 * lo
+    srv = bl.Server(0, lanes=2, pool_bytes=int(pool))
+    ta = srv.submit(**big)
+    tb = srv.submit(**big)
+    ts = [srv.submit(**small) for _ in range(4)]
+    res = _wait(srv, [ta, tb] + ts, timeout=600)
+    assert all(r[0] == srv.DONE for r in res.values())
+    lat_a = res[ta][2]
+    assert max(res[t][2] for t in ts) < lat_a, (lat_a, [res[t][2] for t in ts])
+    np.testing.assert_array_equal(res[ta][1], res[tb][1])
+    direct = bl.oneFID(small["sys"], small["npts"], small["sw"], small["wr"], small["rotb"]).FID(
+        small["pw"], small["ro"], small["det"])
+    for t in ts:
+        np.testing.assert_array_equal(res[t][1], direct)
+    srv.close()
