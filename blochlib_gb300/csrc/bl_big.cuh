@@ -685,6 +685,8 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
     s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
 }
 
+__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk);
+
 // One CTA per crystallite: unitary eigen-decomposition of a large block of A_n.
 __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   extern __shared__ double2 bsc[];
@@ -694,9 +696,9 @@ __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
   __shared__ double2 lam[kMaxBigBlock];
   __shared__ double red[kBigThreads];
   const int b = s.bs[k];
-  if (s.floq32) {  // K in single precision after the two b x b double2 arrays
-    floquet_cta<true, true>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red,
-                                                       reinterpret_cast<float2 *>(bsc + 2 * b * b)});
+  if (s.floq32) {  // K in single precision after the two b x b arrays; the rest double-float
+    floquet_cta_df(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red,
+                                              reinterpret_cast<float2 *>(bsc + 2 * b * b)});
   } else if (s.mixed) {
     floquet_cta<true, false>(s, k, blockIdx.x, FloqWork{bsc, bsc + b * b, rot, fv, lam, rpair, red, nullptr});
   } else {
@@ -921,3 +923,309 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_dyson_df(DevSys s,
   }
 }
 
+
+// ------------------------------------------------------------------ mixed form, Floquet step
+// floquet_cta's algorithm for the mixed form's large blocks when the FID spans at most
+// kFloq32MaxPeriods periods, with every FP64 part moved to double-float on the FP32 pipe
+// (GB300 issues about 2 FP64 FMAs per clock per SM against 128 FP32 FMAs): the Cayley
+// transform, by Gauss-Jordan elimination with partial pivoting (the pivot search is a warp
+// reduction; every update is parallel, no serial back substitution); V's accumulation of the
+// Jacobi rotations, each rotation renormalised in double-float to c^2 + |s|^2 = 1; and the
+// Rayleigh quotients lam_r = v_r^H A_n v_r through the CTA-wide product A_n V.  The sweeps over
+// K run in FP32 with floquet_sweeps' rules.  Complex double-float elements are float4
+// (re.hi, im.hi, re.lo, im.lo) in the 16-byte slots of the FP64 work arrays; the results
+// (V, ln lambda) are stored in FP64 as by floquet_cta.
+
+// x - f y, complex double-float
+__device__ __forceinline__ float4 cdf_fms(float4 x, float4 f, float4 y) {
+  CdfAcc a = {{x.x, x.z}, {x.y, x.w}};
+  cdf_mac(a, make_float4(-f.x, -f.y, -f.z, -f.w), y);
+  return cdf_fin(a);
+}
+__device__ __forceinline__ float4 cdf_mul(float4 x, float4 y) {
+  CdfAcc a = {{0.f, 0.f}, {0.f, 0.f}};
+  cdf_mac(a, x, y);
+  return cdf_fin(a);
+}
+
+// The sweeps over the FP32 K (Kf) with V (double-float, Vd) accumulating the rotations.
+__device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps, const FloqWork &wk) {
+  float4 *rot = reinterpret_cast<float4 *>(wk.rot);  // per pair: (c.hi, 0, c.lo, 0), (s as complex df)
+  auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
+  double *red = wk.red;
+  const int bb = b * b;
+  const int bq = b + (b & 1);
+  const int np = bq / 2;
+  bool conv = false, polish = false;
+  for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
+    double off = 0, dg = 0;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const int r = e / b, q = e % b;
+      const float2 v = Xk[e];
+      if (r < q) off += double(v.x) * v.x + double(v.y) * v.y;
+      else if (r == q) dg += double(v.x) * v.x;
+    }
+    red[threadIdx.x] = off;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double so = 0;
+      for (int t = 0; t < blockDim.x; ++t) so += red[t];
+      red[0] = so;
+    }
+    __syncthreads();
+    const double offs = red[0];
+    __syncthreads();
+    red[threadIdx.x] = dg;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sd = 0;
+      for (int t = 0; t < blockDim.x; ++t) sd += red[t];
+      red[0] = sd;
+    }
+    __syncthreads();
+    const double dgs = red[0];
+    __syncthreads();
+    const bool small = offs <= 1e-10 * dgs || offs == 0.0;
+    if (small && (polish || offs == 0.0)) {
+      conv = true;
+      break;
+    }
+    polish = polish || small;
+    for (int round = 0; round < bq - 1; ++round) {
+      for (int t = threadIdx.x; t < np; t += blockDim.x) {
+        auto player = [&](int j) { return j == 0 ? 0 : 1 + (j - 1 + round) % (bq - 1); };
+        int p = player(t), q = player(bq - 1 - t);
+        if (p > q) {
+          const int tmp = p;
+          p = q, q = tmp;
+        }
+        rpair(t, 0) = p, rpair(t, 1) = q;
+        float4 cr = make_float4(1.f, 0.f, 0.f, 0.f), sr = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (q < b) {
+          const float2 hpq = Xk[p * b + q];
+          const float ab = hypotf(hpq.x, hpq.y);
+          if (ab != 0.f) {
+            const float phx = hpq.x / ab, phy = hpq.y / ab;
+            const float theta = 0.5f * (Xk[q * b + q].x - Xk[p * b + p].x) / ab;
+            float tt;
+            if (fabsf(theta) > 1e18f) tt = 0.5f / theta;
+            else tt = copysignf(1.f, theta) / (fabsf(theta) + sqrtf(fmaf(theta, theta, 1.f)));
+            const float cc = rsqrtf(fmaf(tt, tt, 1.f));
+            const float sx = phx * (tt * cc), sy = phy * (tt * cc);
+            // renormalise: n2 = c^2 + |s|^2 in double-float (exact products), nn = n2^-1/2
+            // = 1 - d/2 + 3d^2/8 with d = n2 - 1 (|d| ~ 1e-7)
+            DfAcc n2 = {0.f, 0.f};
+            df_dot(n2, cc, 0.f, cc, 0.f);
+            df_dot(n2, sx, 0.f, sx, 0.f);
+            df_dot(n2, sy, 0.f, sy, 0.f);
+            const float2 nv = df_fin(n2);
+            const float d = __fadd_rn(__fsub_rn(nv.x, 1.f), nv.y);
+            const float2 nn = dfv_add(make_float2(1.f, 0.f), make_float2(fmaf(0.375f * d, d, -0.5f * d), 0.f));
+            const float2 c2 = dfv_mul(nn, make_float2(cc, 0.f)), s2x = dfv_mul(nn, make_float2(sx, 0.f)),
+                         s2y = dfv_mul(nn, make_float2(sy, 0.f));
+            cr = make_float4(c2.x, 0.f, c2.y, 0.f);
+            sr = make_float4(s2x.x, s2y.x, s2x.y, s2y.y);
+          }
+        }
+        rot[2 * t] = cr, rot[2 * t + 1] = sr;
+      }
+      __syncthreads();
+      // columns p, q of K (FP32) and of V (double-float): X <- X G, G = [[c, sp], [-conj(sp), c]]
+      for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
+        const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        if (q >= b) continue;
+        const float4 cr = rot[2 * t], sp = rot[2 * t + 1];
+        if (rem2 < b) {
+          const float ccr = cr.x + cr.z;
+          const float2 spr = make_float2(sp.x + sp.z, sp.y + sp.w), spcr = cconj(spr);
+          const float2 xkp = Xk[kk * b + p], xkq = Xk[kk * b + q];
+          Xk[kk * b + p] = csub(cscale(xkp, ccr), cmul(spcr, xkq));
+          Xk[kk * b + q] = cadd(cmul(spr, xkp), cscale(xkq, ccr));
+        } else {
+          const float4 vp = Vd[kk * b + p], vq = Vd[kk * b + q];
+          // vp' = c vp - conj(sp) vq,  vq' = sp vp + c vq
+          CdfAcc ap = {{0.f, 0.f}, {0.f, 0.f}}, aq = ap;
+          cdf_mac(ap, cr, vp);
+          cdf_mac(ap, make_float4(-sp.x, sp.y, -sp.z, sp.w), vq);
+          cdf_mac(aq, sp, vp);
+          cdf_mac(aq, cr, vq);
+          Vd[kk * b + p] = cdf_fin(ap);
+          Vd[kk * b + q] = cdf_fin(aq);
+        }
+      }
+      __syncthreads();
+      // rows p, q of K:  K <- G^H K
+      for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
+        const int t = e / b, kk = e % b;
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        if (q >= b) continue;
+        const float4 cr = rot[2 * t], s4 = rot[2 * t + 1];
+        const float cc = cr.x + cr.z;
+        const float2 sp = make_float2(s4.x + s4.z, s4.y + s4.w), spc = cconj(sp);
+        const float2 xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
+        Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
+        Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < np; t += blockDim.x) {
+        const int p = rpair(t, 0), q = rpair(t, 1);
+        const float4 s4 = rot[2 * t + 1];
+        if (q >= b || (s4.x == 0.f && s4.y == 0.f)) continue;
+        Xk[p * b + q] = make_float2(0.f, 0.f), Xk[q * b + p] = make_float2(0.f, 0.f);
+        Xk[p * b + p].y = 0.f, Xk[q * b + q].y = 0.f;
+      }
+      __syncthreads();
+    }
+  }
+  return conv;
+}
+
+__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
+  __shared__ int piv_s;
+  __shared__ double a_s;
+  __shared__ int done_s;
+  __shared__ float4 inv_s;
+  const int b = s.bs[k], bp = s.bpoff[k], bo = s.boff[k], bb = b * b;
+  float4 *M4 = reinterpret_cast<float4 *>(wk.Mm), *X4 = reinterpret_cast<float4 *>(wk.Xk);
+  float4 *fv = reinterpret_cast<float4 *>(wk.fv);
+  double2 *lam = wk.lam;
+  double *red = wk.red;
+  float2 *Kf = wk.Kf;
+  const float4 *U4 = reinterpret_cast<const float4 *>(s.A + size_t(s.n - 1) * s.S2 * s.Cpad);
+  auto Ug = [&](int r, int q) { return U4[at(bp + r * b + q, c, s.Cpad)]; };
+  if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
+  __syncthreads();
+  for (int pass = 0; pass < 2; ++pass) {
+    double sa, ca;
+    sincos(a_s, &sa, &ca);
+    const float4 ea = df_store(cmk(ca, sa));
+    // M = I + e^{ia} A_n, X = I - e^{ia} A_n
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const float4 w = cdf_mul(ea, Ug(e / b, e % b));
+      const float id = (e / b == e % b) ? 1.f : 0.f;
+      const float2 re = dfv_add(make_float2(id, 0.f), make_float2(w.x, w.z));
+      const float2 mre = dfv_add(make_float2(id, 0.f), make_float2(-w.x, -w.z));
+      M4[e] = make_float4(re.x, w.y, re.y, w.w);
+      X4[e] = make_float4(mre.x, -w.y, mre.y, -w.w);
+    }
+    __syncthreads();
+    // Gauss-Jordan with partial pivoting: M X' = X, then X' = diag(M)^-1 X
+    for (int kc = 0; kc < b; ++kc) {
+      if (threadIdx.x < 32) {
+        float best = -1.f;
+        int pv = kc;
+        for (int r = kc + threadIdx.x; r < b; r += 32) {
+          const float4 v = M4[r * b + kc];
+          const float m2 = v.x * v.x + v.y * v.y;
+          if (m2 > best) best = m2, pv = r;
+        }
+        for (int o = 16; o; o >>= 1) {
+          const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+          const int op = __shfl_xor_sync(0xffffffffu, pv, o);
+          if (ob > best || (ob == best && op < pv)) best = ob, pv = op;
+        }
+        if (threadIdx.x == 0) {
+          piv_s = pv;
+          if (!(best > 0.f)) atomicOr(s.status, kSingularCayley);
+        }
+      }
+      __syncthreads();
+      const int pv = piv_s;
+      if (pv != kc)
+        for (int j = threadIdx.x; j < 2 * b; j += blockDim.x) {
+          float4 *Mx = j < b ? M4 : X4;
+          const int jj = j < b ? j : j - b;
+          const float4 t = Mx[kc * b + jj];
+          Mx[kc * b + jj] = Mx[pv * b + jj];
+          Mx[pv * b + jj] = t;
+        }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        const double2 piv = df_load(M4[kc * b + kc]);
+        inv_s = (piv.x != 0.0 || piv.y != 0.0) ? df_store(cdiv(cmk(1, 0), piv)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      __syncthreads();
+      const float4 inv = inv_s;
+      for (int r = threadIdx.x; r < b; r += blockDim.x) fv[r] = r == kc ? make_float4(0.f, 0.f, 0.f, 0.f) : cdf_mul(M4[r * b + kc], inv);
+      __syncthreads();
+      const int wM = b - kc - 1, w = wM + b;  // columns kc+1..b-1 of M, all of X
+      for (int e = threadIdx.x; e < (b - 1) * w; e += blockDim.x) {
+        int r = e / w;
+        r += (r >= kc);
+        const int j = e % w;
+        if (j < wM) M4[r * b + kc + 1 + j] = cdf_fms(M4[r * b + kc + 1 + j], fv[r], M4[kc * b + kc + 1 + j]);
+        else X4[r * b + (j - wM)] = cdf_fms(X4[r * b + (j - wM)], fv[r], X4[kc * b + (j - wM)]);
+      }
+      __syncthreads();
+    }
+    // X' = diag(M)^-1 X, then K = Hermitian part of i X' in FP32, V = I (double-float)
+    for (int r = threadIdx.x; r < b; r += blockDim.x) {
+      const double2 d = df_load(M4[r * b + r]);
+      fv[r] = df_store(cdiv(cmk(1, 0), d));
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) X4[e] = cdf_mul(fv[e / b], X4[e]);
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const int r = e / b, q = e % b;
+      const float4 xrq = X4[r * b + q], xqr = X4[q * b + r];
+      // i X_rq = (-Im, Re); conj(i X_qr) = (-Im X_qr, -Re X_qr)
+      const float re = 0.5f * (-(xrq.y + xrq.w) - (xqr.y + xqr.w));
+      const float im = r == q ? 0.f : 0.5f * ((xrq.x + xrq.z) - (xqr.x + xqr.z));
+      Kf[e] = make_float2(re, im);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) M4[e] = make_float4(e / b == e % b ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    const int max_sweeps = kMaxSweeps;
+    const bool conv = floquet_sweeps_df(Kf, M4, b, max_sweeps, wk);
+    if (!conv) atomicOr(s.status, kNoConvergeFloquet);
+    // Rayleigh quotients: Y = A_n V (into X's array), lam_r = sum_k conj(V_kr) Y_kr
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const int kr = e / b, r = e % b;
+      CdfAcc a = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int l = 0; l < b; ++l) cdf_mac(a, Ug(kr, l), M4[l * b + r]);
+      X4[e] = cdf_fin(a);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < b; r += blockDim.x) {
+      CdfAcc a = {{0.f, 0.f}, {0.f, 0.f}};
+      for (int kk = 0; kk < b; ++kk) {
+        const float4 v = M4[kk * b + r];
+        cdf_mac(a, make_float4(v.x, -v.y, v.z, -v.w), X4[kk * b + r]);
+      }
+      lam[r] = df_load(cdf_fin(a));
+    }
+    __syncthreads();
+    if (pass == 1) break;
+    if (threadIdx.x == 0) {
+      double mind = 4.0;
+      const double2 e2 = cmk(ca, sa);
+      for (int r = 0; r < b; ++r) {
+        const double2 w = cmul(e2, lam[r]);
+        mind = fmin(mind, (1.0 + w.x) * (1.0 + w.x) + w.y * w.y);
+      }
+      done_s = conv && mind >= 0.0625;
+      if (!done_s) {
+        for (int r = 0; r < b; ++r) {
+          const double th = atan2(lam[r].y, lam[r].x);
+          int j = r;
+          while (j > 0 && red[j - 1] > th) red[j] = red[j - 1], --j;
+          red[j] = th;
+        }
+        double best = -1, mid = 0;
+        for (int r = 0; r < b; ++r) {
+          const double lo = red[r], hi = (r + 1 < b) ? red[r + 1] : red[0] + kPi2;
+          if (hi - lo > best) best = hi - lo, mid = 0.5 * (lo + hi);
+        }
+        a_s = kPi - mid;
+      }
+    }
+    __syncthreads();
+    if (done_s) break;
+  }
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) s.VF[at(bp + e, c, s.Cpad)] = df_load(M4[e]);
+  for (int r = threadIdx.x; r < b; r += blockDim.x)
+    s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
+}
