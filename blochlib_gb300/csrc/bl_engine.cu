@@ -2006,6 +2006,114 @@ __global__ void __launch_bounds__(kThreads) k_p2p_elems(DevSys s) {
 }
 
 // Compensated (Kahan) sum of the warp partials in fixed order: deterministic.
+// Mixed form: the FID terms as a tiled product.  fid[j gper + p] = sum_c w_c sum_e
+// z_e^j(c) G_p(e, c) is a product with K = (crystallite, element); one CTA takes a group of
+// 32 crystallites (one warp of the batch layout), a range of the elements (kFtR ranges), 16
+// j's and 64 p's.  Per element it stages z_e^j and G_p(e) of its 32 crystallites in shared
+// memory by asynchronous copies (coalesced: crystallites are fastest in HBM; double-buffered,
+// so the next element's copies are in flight while this one is summed), and each thread
+// updates a 4 x 4 (j, p) register tile with w_c scale z, accumulating one element in FP32
+// and folding it into double-float (hi + lo) sums.  Every element of G is read once per j range and every z once
+// per p range, against once per 4-wide tile of the other index in k_fid.  The CTA writes its
+// tile to partial row (warp * kFtR + range); k_reduce sums the rows of the populated warps in
+// a fixed order, so a crystallite's contribution does not depend on its neighbours.
+constexpr int kFtThreads = 64, kFtJ = 16, kFtP = 64, kFtR = 4;
+// 8-byte asynchronous copy global -> shared (cp.async); src_bytes 0 writes zeros
+__device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(uint32_t(__cvta_generic_to_shared(dst))), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__global__ void __launch_bounds__(kFtThreads) k_fid_tiled(DevSys s) {
+  __shared__ __align__(16) float2 zs[2][32][kFtJ];  // [buffer][c][j]
+  __shared__ __align__(16) float2 gs[2][32][kFtP];  // [buffer][c][p]
+  __shared__ float ws[32];
+  const int tid = threadIdx.x;
+  const int g = blockIdx.x;  // group of 32 crystallites in this batch
+  const int npr = (s.gper + kFtP - 1) / kFtP;
+  const int pr = blockIdx.y % npr, jr = blockIdx.y / npr, er = blockIdx.z;
+  const int p0 = pr * kFtP, j0 = jr * kFtJ;
+  const int e_lo = int((long(s.ne) * er) / kFtR), e_hi = int((long(s.ne) * (er + 1)) / kFtR);
+  const int c0 = g * 32;
+  if (tid < 32) {
+    const int c = c0 + tid;
+    ws[tid] = c < s.C ? float(s.w[c] * s.scale) : 0.f;
+  }
+  const int jt = tid / 16, pt = tid % 16;  // this thread's j's: j0 + 4 jt + a; p's: p0 + 4 pt + b
+  float2 acc[4][4];
+  float2 hi[4][4], lo[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) hi[a][b] = lo[a][b] = make_float2(0.f, 0.f);
+  const float2 *Zb = s.Zf, *Gb = s.Gf;
+  // z (16 x 32) and G (64 x 32) of element e into buffer buf, zeros outside J, gper and C
+  auto stage = [&](int e, int buf) {
+    for (int t = tid; t < kFtJ * 32; t += kFtThreads) {
+      const int jj = t / 32, c = t % 32, j = j0 + jj;
+      const bool ok = j < s.J && c0 + c < s.C;
+      cp_async8(&zs[buf][c][jj], ok ? &Zb[at(j * s.ne + e, c0 + c, s.Cpad)] : Zb, ok ? 8 : 0);
+    }
+    for (int t = tid; t < kFtP * 32; t += kFtThreads) {
+      const int pp = t / 32, c = t % 32, p = p0 + pp;
+      const bool ok = p < s.gper && c0 + c < s.C;
+      cp_async8(&gs[buf][c][pp], ok ? &Gb[at(p * s.ne + e, c0 + c, s.Cpad)] : Gb, ok ? 8 : 0);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  if (e_lo < e_hi) stage(e_lo, 0);
+  int buf = 0;
+  for (int e = e_lo; e < e_hi; ++e) {
+    if (e + 1 < e_hi) {
+      stage(e + 1, buf ^ 1);  // in flight while this element is summed
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
+    for (int c = 0; c < 32; ++c) {
+      const float w = ws[c];
+      const float4 z01 = *reinterpret_cast<const float4 *>(&zs[buf][c][4 * jt]);
+      const float4 z23 = *reinterpret_cast<const float4 *>(&zs[buf][c][4 * jt + 2]);
+      const float4 g01 = *reinterpret_cast<const float4 *>(&gs[buf][c][4 * pt]);
+      const float4 g23 = *reinterpret_cast<const float4 *>(&gs[buf][c][4 * pt + 2]);
+      const float2 zz[4] = {make_float2(w * z01.x, w * z01.y), make_float2(w * z01.z, w * z01.w),
+                            make_float2(w * z23.x, w * z23.y), make_float2(w * z23.z, w * z23.w)};
+      const float2 gg[4] = {make_float2(g01.x, g01.y), make_float2(g01.z, g01.w), make_float2(g23.x, g23.y),
+                            make_float2(g23.z, g23.w)};
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = cfma(zz[a], gg[b], acc[a][b]);
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        const float2 x = dfv_add(make_float2(hi[a][b].x, lo[a][b].x), make_float2(acc[a][b].x, 0.f));
+        const float2 y = dfv_add(make_float2(hi[a][b].y, lo[a][b].y), make_float2(acc[a][b].y, 0.f));
+        hi[a][b] = make_float2(x.x, y.x), lo[a][b] = make_float2(x.y, y.y);
+      }
+    __syncthreads();  // the next stage() overwrites this buffer
+    buf ^= 1;
+  }
+  const long row = long(s.warp_base + g) * kFtR + er;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const int j = j0 + 4 * jt + a, p = p0 + 4 * pt + b;
+      const long k = long(j) * s.gper + p;
+      if (j < s.J && p < s.gper && k < s.npts)
+        s.partial[row * s.npts + k] = make_double2(double(hi[a][b].x) + double(lo[a][b].x),
+                                                   double(hi[a][b].y) + double(lo[a][b].y));
+    }
+}
+
 __global__ void k_reduce(const double2 *__restrict__ partial, int nw, int npts, double2 *__restrict__ fid) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= npts) return;
@@ -2690,7 +2798,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   } else {
     J.Q.alloc(nQ), J.R.alloc(nR), J.G.alloc(nG), J.Z.alloc(nZ);
   }
-  J.partial.alloc(size_t(J.nwarps_total) * p.npts);
+  J.partial.alloc(size_t(J.nwarps_total) * (J.mixed ? kFtR : 1) * p.npts);
   if (J.huge_ws_bytes) {
     J.huge_ws.alloc(J.huge_ws_bytes / sizeof(double2));
     J.hfk.alloc(size_t(J.huge_items) * std::max(J.nint, 1));
@@ -2748,7 +2856,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     if (J.p2p) J.stage_fl[5] = Ce * 16.0 * J.pb * J.ne;  // two complex products per (k, element)
   }
   J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
-  J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total;                // compensated powder sum
+  J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total * (J.mixed ? kFtR : 1);  // compensated powder sum
   J.flops = 0;
   for (double f : J.stage_fl) J.flops += f;
   // static part of the device description
@@ -3251,14 +3359,19 @@ void Job::run() {
     // k_fid writes every (warp, k) of this batch, so partials need no clearing; it exits
     // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
     mark_begin(J, 6);
-    if (s.mixed) launch_fid<float2>(s, Cp, J.J, st);
-    else launch_fid<double2>(s, Cp, J.J, st);
+    if (s.mixed) {
+      const unsigned npr = unsigned((s.gper + kFtP - 1) / kFtP), njr = unsigned((J.J + kFtJ - 1) / kFtJ);
+      k_fid_tiled<<<dim3(unsigned(Cp / 32), npr * njr, kFtR), kFtThreads, 0, st>>>(s);
+    } else {
+      launch_fid<double2>(s, Cp, J.J, st);
+    }
     ++J.launches;
     mark_end(J, 6, 1);
   }
   mark_begin(J, 7);
   // only warps that hold crystallites: the sum is then independent of the batch size
-  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, (J.Ceff + 31) / 32, J.P.npts, J.fid.p);
+  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, (J.Ceff + 31) / 32 * (J.mixed ? kFtR : 1),
+                                                    J.P.npts, J.fid.p);
   ++J.launches;
   mark_end(J, 7, 1);
   CUDA_OK(cudaGetLastError());
@@ -3476,8 +3589,9 @@ static size_t fixed_bytes(const Powder &pw, const FidParams &p) {
   long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
   long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
   size_t ceff = size_t(pw.size()) * size_t(g) + 32;
+  // warp partials: kFtR rows per warp in the mixed form (k_fid_tiled's element ranges)
   return (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
-         (ceff / 32 + 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
+         (ceff / 32 + 1) * size_t(p.precision == 1 ? kFtR : 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
 }
 
 void job_bytes(int device, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
