@@ -45,9 +45,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "powder FIDs/s & p50/p99 latency, mixed vs FP64 GPU path at ≤1e-6 rel err"
 UNIT = "powder FIDs/s"
-# the mixed form's arithmetic: step and Dyson in double-float (hi + lo floats) on the FP32 pipe,
-# Floquet eigenvalues/vectors and the powder sum in FP64, eigenframe, Q/R, Fave and FID terms in FP32
-MIXED_DTYPE = "f64+df32+f32 (double-float: step, Dyson; f64: Floquet, powder sum; f32: eigenframe, Q/R, Fave, FID)"
+# the mixed form's arithmetic (blocks up to 8: double-float step and Dyson; 9-39: the same on CTA-wide kernels;
+# 40-74: exact-slice BF16 products on the tensor cores)
+MIXED_DTYPE = ("bf16 tensor-core exact slices (step, Dyson, blocks 40-74) + df32 double-float (smaller blocks' step "
+               "and Dyson; Floquet Cayley, V, eigenvalues) + f32 (Floquet sweeps, eigenframe, Q/R, Fave, FID) + "
+               "f64 (powder sum)")
 
 
 def dist_env():
@@ -448,9 +450,10 @@ def run_serving(args):
     return 0
 
 
-# stage -> (pipe of the FP64 form, pipe of the mixed form); the mixed form's Dyson runs its
-# large blocks on the tensor cores (exact BF16 slices), its step in double-float (FP32 pipe)
-STAGE_PIPE = {"k_step_prop": ("fp64", "fp32"), "k_dyson": ("fp64", "tensor"), "k_floquet": ("fp64", "fp64"),
+# stage -> (pipe of the FP64 form, pipe of the mixed form); in the mixed form the step and Dyson of
+# blocks of 40-74 run on the tensor cores (their stages are reported as "tensor" when the kernels
+# counted tensor flops), smaller blocks and the Floquet step in double-float on the FP32 pipe
+STAGE_PIPE = {"k_step_prop": ("fp64", "fp32"), "k_dyson": ("fp64", "fp32"), "k_floquet": ("fp64", "fp32"),
               "k_eigframe": ("fp64", "fp32"), "k_qr": ("fp64", "fp32"), "k_fave": ("fp64", "fp32"),
               "k_fid": ("fp64", "fp32"), "k_reduce": ("fp64", "fp64")}
 
@@ -461,12 +464,6 @@ def measured_peaks():
         return json.loads(f.read_text())
     except (OSError, ValueError):
         return {}
-
-
-def tensor_flops(layout, n, C):
-    """BF16 flops the tensor-core Dyson issues per run (unpadded): 10 slice pairs x 4 real
-    b x b x b products x 2 flop, per large block, step and crystallite."""
-    return sum(80.0 * b ** 3 for b in layout["blocks"] if 8 < b <= 74) * n * C
 
 
 def measure_job(args, d, ctx, cfg, prec, steps, warmup, compare, e2e_steps, peaks):
@@ -498,6 +495,7 @@ def measure_job(args, d, ctx, cfg, prec, steps, warmup, compare, e2e_steps, peak
         stages = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in stages.items()}
         sflops = {("k_p2p_elems" if k == "k_fave" else k): v for k, v in sflops.items()}
     layout = job.describe()
+    tf_step, tf_dyson = job.tensor_flops() if prec == "mixed" else (0.0, 0.0)
     launches_per_run = job.launches
     job.set_profiling(False)
     # per-stage roofline against the unit that bounds the stage
@@ -508,22 +506,30 @@ def measure_job(args, d, ctx, cfg, prec, steps, warmup, compare, e2e_steps, peak
             continue
         t = ms / steps / 1e3
         pipe = STAGE_PIPE.get(k, ("fp64", "fp32"))[col]
+        tfl = {"k_step_prop": tf_step, "k_dyson": tf_dyson}.get(k, 0.0)
+        if tfl > 0:
+            pipe = "tensor"
+        elif pipe == "tensor":
+            pipe = "fp32"  # no tensor-core block in this job: double-float on the FP32 pipe
         e = {"share": ms / ms_total, "ms_per_run": ms / steps, "launches_per_run": nl / steps, "pipe": pipe,
              "algorithmic_tflops_fp64_equiv": sflops.get(k, 0.0) / t / 1e12}
         if pipe == "fp64":
             e.update(peak=peaks["fp64"], frac=e["algorithmic_tflops_fp64_equiv"] / peaks["fp64"])
         elif pipe == "tensor":
-            tf = tensor_flops(layout, layout["n"], layout["crystallites"]) / t / 1e12
-            e.update(bf16_tflops_issued=tf, peak=peaks["bf16"], frac=tf / peaks["bf16"])
-        else:
-            e.update(peak=peaks["fp32"])
+            tf = tfl / t / 1e12
+            e.update(bf16_tflops_issued=tf, peak=peaks["bf16"], frac=tf / peaks["bf16"],
+                     note="BF16 flops of the exact-slice products (counted by the kernels) over the stage's "
+                          "CUDA-event time, which also covers the stage's double-float small-block kernels")
+        else:  # single precision: the algorithmic count is the FP32 count (double-float stages issue ~12x more)
+            e.update(peak=peaks["fp32"], frac=e["algorithmic_tflops_fp64_equiv"] / peaks["fp32"])
         per_stage[k] = e
     dom = max(per_stage, key=lambda k: per_stage[k]["share"])
     D = per_stage[dom]
     if D["pipe"] == "tensor":
         roof = {"bound": "tensor", "achieved": D["bf16_tflops_issued"], "peak": peaks["bf16"], "unit": "TFLOP/s",
                 "frac": D["frac"], "peak_source": peaks["bf16_source"],
-                "algorithmic_unit": "BF16 slice products issued (unpadded): 80 b^3 per large block, step, crystallite"}
+                "algorithmic_unit": "BF16 flops of the exact-slice products: 10 slice pairs x 2 b^3 per real "
+                                    "b x b product (unpadded), counted by the tensor-core kernels"}
     elif D["pipe"] == "fp32":
         ach = D["algorithmic_tflops_fp64_equiv"]
         roof = {"bound": "fp32", "achieved": ach, "peak": peaks["fp64"], "unit": "TFLOP/s (FP64-equivalent)",

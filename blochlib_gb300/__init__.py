@@ -67,6 +67,8 @@ _SIGS = {
     "bl_job_sync": (ctypes.c_int, [ctypes.c_void_p]),
     "bl_job_launches": (ctypes.c_int, [ctypes.c_void_p]),
     "bl_job_flops": (ctypes.c_double, [ctypes.c_void_p]),
+    "bl_job_tensor_flops": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double)]),
     "bl_job_sw": (ctypes.c_double, [ctypes.c_void_p]),
     "bl_job_describe": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]),
     "bl_job_destroy": (None, [ctypes.c_void_p]),
@@ -440,6 +442,12 @@ class Job:
     @property
     def flops(self):
         return load().bl_job_flops(self._h)
+
+    def tensor_flops(self):
+        """(step, Dyson): BF16 tensor-core flops of the last run's exact-slice products."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        _check(load().bl_job_tensor_flops(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     @property
     def sw(self):

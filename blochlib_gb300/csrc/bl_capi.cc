@@ -283,6 +283,10 @@ bl_status bl_job_sync(bl_job *job) {
 
 int bl_job_launches(const bl_job *job) { return job ? job->j->kernels_per_run() : 0; }
 double bl_job_flops(const bl_job *job) { return job ? job->j->flops() : 0.0; }
+bl_status bl_job_tensor_flops(const bl_job *job, double *step, double *dyson) {
+  if (!job) return fail(BL_ERR_INVALID, "null job");
+  return guarded([&] { job->j->tensor_flops(step, dyson); });
+}
 double bl_job_sw(const bl_job *job) { return job ? job->j->sw_out() : 0.0; }
 
 int bl_job_describe(const bl_job *job, char *buf, int cap) {

@@ -214,6 +214,7 @@ struct DevSys {
   const float2 *twf;
   int warp_base;  // global warp index of this batch's first crystallite
   int *status;
+  unsigned long long *tc_flops;  // [2]: BF16 tensor flops issued by the step and Dyson kernels
 };
 
 // Precision-dependent arrays: W (eigenframe; in place over A in FP64), Q, R, G, Z, twiddles.
@@ -2232,6 +2233,7 @@ struct JobImpl {
   // U slices to a slab the Dyson product reads; one region per large block
   bool tc = false;
   DevBuf<unsigned char> usl;
+  DevBuf<unsigned long long> tcf;  // the two tensor-flop counters
   std::vector<size_t> usl_off;  // per block index: byte offset of its region (large blocks)
   int mixed = 0;
   DevBuf<double> Rp_b, t0_b, w_b;
@@ -2808,6 +2810,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   J.fid.alloc(p.npts);
   if (use_fk) J.fkc.alloc(size_t(J.n) * J.nint * Cb);
+  J.tcf.alloc(2);
   if (J.tc && usl_per_c) {
     J.usl.alloc(usl_per_c * Cb);
     size_t off = 0;
@@ -2939,6 +2942,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.U = J.U.p, s.A = J.A.p, s.VF = J.VF.p, s.L = J.Lb.p, s.Q = J.Q.p, s.R = J.R.p, s.G = J.G.p, s.Z = J.Z.p;
   s.partial = J.partial.p;
   s.status = J.status.p;
+  s.tc_flops = J.tcf.p;
   s.Cpad = J.Cb;
 }
 
@@ -3270,6 +3274,7 @@ void Job::run() {
     for (auto &e : J.evpool) CUDA_OK(cudaEventCreate(&e));
   }
   CUDA_OK(cudaMemsetAsync(J.status.p, 0, sizeof(int), st));
+  CUDA_OK(cudaMemsetAsync(J.tcf.p, 0, 2 * sizeof(unsigned long long), st));
   for (int bi = 0; bi < J.nbatch; ++bi) {
     DevSys s = J.base;
     int c0 = bi * J.Cb;
@@ -3539,6 +3544,13 @@ int Job::npts() const { return d_->P.npts; }
 int Job::kernels_per_run() const { return d_->launches; }
 const double *Job::device_fid() const { return reinterpret_cast<const double *>(d_->fid.p); }
 double Job::flops() const { return d_->flops; }
+void Job::tensor_flops(double *step, double *dyson) const {
+  unsigned long long v[2] = {0, 0};
+  CUDA_OK(cudaMemcpyAsync(v, d_->tcf.p, sizeof(v), cudaMemcpyDeviceToHost, d_->ctx->stream));
+  CUDA_OK(cudaStreamSynchronize(d_->ctx->stream));
+  if (step) *step = double(v[0]);
+  if (dyson) *dyson = double(v[1]);
+}
 
 std::string Job::describe() const {
   const JobImpl &J = *d_;

@@ -59,6 +59,9 @@ class Job {
   std::string describe() const;     // layout summary (JSON)
   // algorithmic FP64 flop count of one run() (one complex MAC = 8 flop)
   double flops() const;
+  // BF16 tensor-core flops the last run() issued in its exact-slice products (step, Dyson;
+  // 10 slice pairs x 2 b^3 per real b x b product, unpadded); synchronises the stream
+  void tensor_flops(double *step, double *dyson) const;
 
   // Per-stage CUDA-event timing of run() (stages: see stage_name), accumulated while on.
   static constexpr int kStages = 8;

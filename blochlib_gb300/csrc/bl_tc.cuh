@@ -474,6 +474,10 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
     sync_all();
     Ct = fr[0], aC = fa[0], St = fr[1], aS = fa[1];
   }
+  if (ok && tid == 0) {  // real products issued: Y, the two chains, X S', 3 per squaring
+    const int nprod = 1 + max(mC - 1, 0) + max(mS - 1, 0) + (mS >= 1 ? 1 : 0) + 3 * sq;
+    atomicAdd(s.tc_flops, 20ull * (unsigned long long)nprod * (unsigned long long)(b * b * b));
+  }
   if (ok) {  // the slab: C tile, then S tile (U = C - i S), 16-byte coalesced copies
     uint4 *dst = reinterpret_cast<uint4 *>(slab0 + (size_t(c) * s.n + i) * tc::slab_bytes(b));
     const int nv = int(tc::tile_bytes(b) / 16);
@@ -607,6 +611,8 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k,
     tc::fence_before();
     __syncthreads();
   }
+  if (ok && tid == 0)  // 4 real products per step
+    atomicAdd(s.tc_flops + 1, 80ull * (unsigned long long)s.n * (unsigned long long)(b * b * b));
   if (!ok) {
     if (tid == 0) atomicOr(s.status, kTcTimeout);
     tc::wait_parity(&mbar[0], ph[0]);  // bounded: let MMAs and the copy in flight drain

@@ -180,6 +180,10 @@ bl_status bl_job_read(bl_job *job, double *fid_out);  /* synchronises; 2*npts do
 bl_status bl_job_sync(bl_job *job);
 int bl_job_launches(const bl_job *job);               /* kernel launches per run */
 double bl_job_flops(const bl_job *job);               /* algorithmic FP64 flop per run */
+/* BF16 tensor-core flops the job's last run issued in the mixed form's exact-slice products
+ * (step exponential, Dyson product; 10 slice pairs x 2 b^3 per real b x b product).  Either
+ * output may be NULL.  Measurement only; no counterpart in the reference. */
+bl_status bl_job_tensor_flops(const bl_job *job, double *step, double *dyson);
 double bl_job_sw(const bl_job *job);
 /* JSON description of the job's layout; returns the length written (truncated to cap). */
 int bl_job_describe(const bl_job *job, char *buf, int cap);
