@@ -39,6 +39,7 @@ class BlochError(RuntimeError):
 
 _SIGS = {
     "bl_last_error": (ctypes.c_char_p, []),
+    "bl_last_error_statement": (ctypes.c_double, []),
     "bl_version": (ctypes.c_char_p, []),
     "bl_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
     "bl_ctx_destroy": (None, [ctypes.c_void_p]),
@@ -135,7 +136,7 @@ def _fave_method(m):
 class FidParams(ctypes.Structure):
     _fields_ = [("npts", ctypes.c_int), ("sw", ctypes.c_double), ("wr", ctypes.c_double),
                 ("rotb_deg", ctypes.c_double), ("start_t", ctypes.c_double), ("precision", ctypes.c_int),
-                ("step_method", ctypes.c_int), ("fave_method", ctypes.c_int)]
+                ("step_method", ctypes.c_int), ("fave_method", ctypes.c_int), ("error_sample", ctypes.c_int)]
 
 
 class RfChunk(ctypes.Structure):
@@ -505,9 +506,12 @@ class oneFID:
     """oneFID<SolidSys>(sys, npts, sw, wr, rotb_deg, startT)  (oneFID.h:103-108)."""
 
     def __init__(self, sys, npts, sw=20000.0, wr=0.0, rotb=0.0, startT=0.0, precision=0, ctx=None, step_method=None,
-                 fave_method=None):
+                 fave_method=None, error_sample=0):
         self.sys, self.npts, self.sw, self.wr, self.rotb, self.startT = sys, int(npts), float(sw), float(wr), float(rotb), float(startT)
         self.precision = precision
+        # mixed form: crystallites on which FID() restates the result against FP64 (error_statement)
+        self.error_sample = int(error_sample)
+        self.error_statement = None
         self.step_method = step_method
         self.fave_method = fave_method
         self.ctx = ctx
@@ -521,9 +525,11 @@ class oneFID:
         out = np.zeros(self.npts, dtype=np.complex128)
         sw_out = np.zeros(1)
         params = FidParams(self.npts, self.sw, self.wr, self.rotb, self.startT, int(self.precision),
-                           _step_method(self.step_method), _fave_method(self.fave_method))
+                           _step_method(self.step_method), _fave_method(self.fave_method), self.error_sample)
         _check(load().bl_powder_fid(ctx._h, self.sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(params),
                                     _ptr(out), _ptr(sw_out)))
+        stmt = load().bl_last_error_statement()
+        self.error_statement = stmt if stmt >= 0 else None
         self.sw = float(sw_out[0])
         self.fid_ = out
         return out
@@ -577,13 +583,16 @@ class Server:
         _check(load().bl_server_create(int(device), int(lanes), int(pool_bytes), ctypes.byref(h)))
         self._h = h
         self._npts = {}
+        # stated error of the last finished request result() returned (mixed form with
+        # error_sample > 0), else None
+        self.last_error_statement = None
 
     def submit(self, sys, pw, ro, det, npts, sw, wr, rotb, start_t=0.0, precision=0, step_method=None,
-               fave_method=None):
+               fave_method=None, error_sample=0):
         n = sys.dim()
         ro, det = _cmat(ro, n), _cmat(det, n)
         p = FidParams(int(npts), float(sw), float(wr), float(rotb), float(start_t), int(precision),
-                      _step_method(step_method), _fave_method(fave_method))
+                      _step_method(step_method), _fave_method(fave_method), int(error_sample))
         t = ctypes.c_longlong()
         _check(load().bl_server_submit(self._h, sys._h, pw._h, _ptr(ro), _ptr(det), ctypes.byref(p), ctypes.byref(t)))
         self._npts[t.value] = int(npts)
@@ -620,6 +629,9 @@ class Server:
             self._npts.pop(ticket, None)
             if st.value == self.FAILED:
                 raise BlochError(5, load().bl_last_error().decode())
+            if st.value == self.DONE:
+                stmt = load().bl_last_error_statement()
+                self.last_error_statement = stmt if stmt >= 0 else None
             return st.value, (fid if st.value == self.DONE else None), sw.value, lat.value
         return st.value, None, None, None
 

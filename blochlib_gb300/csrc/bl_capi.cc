@@ -37,6 +37,7 @@ struct bl_job {
 
 namespace {
 thread_local std::string g_err;
+thread_local double g_stmt = -1.0;  // stated error of this thread's last FID (-1: none)
 
 bl_status fail(int code, const std::string &msg) {
   g_err = msg;
@@ -70,6 +71,7 @@ bl::FidParams to_params(const bl_fid_params *p) {
   f.precision = p->precision;
   f.step_method = p->step_method;
   f.fave_method = p->fave_method;
+  f.error_sample = p->error_sample;
   return f;
 }
 
@@ -96,6 +98,7 @@ static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder
                           const bl::CMatrix &det, const bl::FidParams &p, double *fid_out, double *sw_out);
 
 const char *bl_last_error(void) { return g_err.c_str(); }
+double bl_last_error_statement(void) { return g_stmt; }
 const char *bl_version(void) { return "blochlib_gb300 0.1 (sm_103a, FP64 gamma-COMPUTE)"; }
 
 bl_status bl_ctx_create(int device, size_t hbm_budget, bl_ctx **out) {
@@ -399,21 +402,34 @@ bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
                         const bl_fid_params *params, double *fid_out, double *sw_out) {
   if (!fid_out) return fail(BL_ERR_INVALID, "null output");
   if (!ctx || !sys || !pw || !ro || !det || !params) return fail(BL_ERR_INVALID, "null argument");
+  g_stmt = -1.0;
   bool done = false;
   const bl_status st0 = guarded([&] {
     const int N = sys->s().dim();
     done = fid_in_region(ctx, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params), fid_out, sw_out);
   });
-  if (st0 != BL_OK || done) return st0;
-  bl_job *job = nullptr;
-  bl_status st = bl_job_create(ctx, sys, pw, ro, det, params, &job);
-  if (st != BL_OK) return st;
-  st = bl_job_run(job);
-  if (st == BL_OK) st = bl_job_read(job, fid_out);
-  if (st == BL_OK && sw_out) *sw_out = job->j->sw_out();
-  std::string keep = g_err;
-  bl_job_destroy(job);
-  g_err = keep;
+  if (st0 != BL_OK) return st0;
+  bl_status st = BL_OK;
+  if (!done) {
+    bl_job *job = nullptr;
+    st = bl_job_create(ctx, sys, pw, ro, det, params, &job);
+    if (st != BL_OK) return st;
+    st = bl_job_run(job);
+    if (st == BL_OK) st = bl_job_read(job, fid_out);
+    if (st == BL_OK && sw_out) *sw_out = job->j->sw_out();
+    std::string keep = g_err;
+    bl_job_destroy(job);
+    g_err = keep;
+  }
+  if (st == BL_OK && params->precision == 1 && params->error_sample > 0) {
+    double stmt = -1.0;
+    st = guarded([&] {
+      const int N = sys->s().dim();
+      stmt = bl::error_statement(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params),
+                                 params->error_sample);
+    });
+    g_stmt = stmt;
+  }
   return st;
 }
 
@@ -539,8 +555,10 @@ bl_status bl_server_poll(bl_server *srv, long long ticket, int *state, double *f
   if (!srv || !state) return fail(BL_ERR_INVALID, "null argument");
   return guarded([&] {
     std::string err;
-    *state = srv->s->poll(ticket, fid_out, sw_out, latency_ms, &err);
+    double stmt = -1.0;
+    *state = srv->s->poll(ticket, fid_out, sw_out, latency_ms, &err, &stmt);
     if (*state == 3) g_err = err;
+    if (*state == 2 && fid_out) g_stmt = stmt;
   });
 }
 

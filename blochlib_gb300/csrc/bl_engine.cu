@@ -3487,6 +3487,35 @@ __global__ void k_ffma_probe(float *out, int iters, float a, float b) {
 }
 }  // namespace
 
+double error_statement(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+                       const FidParams &p, int sample) {
+  const int C = pw.size();
+  const int m = std::min(std::max(sample, 1), C);
+  Powder sub;
+  for (int k = 0; k < m; ++k) {
+    const int c = int((2L * k + 1) * C / (2L * m));
+    sub.theta.push_back(pw.theta[c]), sub.phi.push_back(pw.phi[c]), sub.gamma.push_back(pw.gamma[c]);
+    sub.weight.push_back(pw.weight[c]);
+  }
+  FidParams p1 = p, p0 = p;
+  p1.precision = 1, p0.precision = 0;
+  p1.error_sample = p0.error_sample = 0;
+  std::vector<double> f1(2 * size_t(p.npts)), f0(2 * size_t(p.npts));
+  {
+    Job j(ctx, sys, sub, ro, det, p1);
+    j.run();
+    j.read(f1.data());
+  }
+  {
+    Job j(ctx, sys, sub, ro, det, p0);
+    j.run();
+    j.read(f0.data());
+  }
+  double num = 0, den = 0;
+  for (size_t x = 0; x < f0.size(); ++x) num += (f1[x] - f0[x]) * (f1[x] - f0[x]), den += f0[x] * f0[x];
+  return den > 0 ? std::sqrt(num / den) : 0.0;
+}
+
 double probe_fp32_tflops(Context &ctx) {
   CUDA_OK(cudaSetDevice(ctx.device));
   int sms = 0;

@@ -18,6 +18,9 @@ struct FidParams {
                       // single-precision eigenframe, Q/R, Fave and FID terms)
   int step_method = 0;  // step exponential: 0 Jacobi eigen-decomposition, 1 Taylor + squaring
   int fave_method = 0;  // Fave correlation: 0 auto (FFT when n <= 2048), 1 direct, 2 FFT
+  // mixed form: crystallites (spread evenly over the powder) on which error_statement()
+  // recomputes the FID in FP64 and in the mixed form; 0 = no statement
+  int error_sample = 0;
   // Point-to-point FID (p2p_base > 0): points every p2p_factor/p2p_base rotor periods,
   // fid[p] = sum_c w_c Tr(rho_c(t_p) det) / Tr(det det^H); each rotor period is cut into
   // p2p_base chunks of ceil(chunk / maxtstep) steps (one step when maxtstep <= 0).  Static
@@ -81,6 +84,11 @@ class Job {
 };
 
 // Measured FP64 FMA throughput of the device (TFLOP/s), from a short DFMA probe kernel.
+// The mixed form's stated error: the relative L2 difference between the mixed-form and the
+// FP64 FID of `sample` crystallites of the powder (indices (2k+1) C / (2 sample)), run as two
+// jobs on the context's stream (device memory of their own).
+double error_statement(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &ro, const CMatrix &det,
+                       const FidParams &p, int sample);
 double probe_fp64_tflops(Context &ctx);
 // Measured FP32 FMA throughput (TFLOP/s): the pipe of the mixed form's double-float stages.
 double probe_fp32_tflops(Context &ctx);

@@ -144,7 +144,8 @@ void Server::plan() {
   }
 }
 
-int Server::poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err) {
+int Server::poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err,
+                 double *stmt_out) {
   std::lock_guard<std::mutex> lk(mu_);
   auto it = all_.find(id);
   if (it == all_.end()) return -1;
@@ -154,6 +155,7 @@ int Server::poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms
       *latency_ms = std::chrono::duration<double, std::milli>(r.t_done - r.t_submit).count();
     if (err) *err = r.err;
     if (r.state == 2 && sw_out) *sw_out = r.sw;
+    if (r.state == 2 && stmt_out) *stmt_out = r.stmt;
     if (fid_out) {
       if (r.state == 2) std::copy(r.fid.begin(), r.fid.end(), fid_out);
       int st = r.state;
@@ -208,11 +210,21 @@ void Server::loop() {
       double fl = s.job ? s.job->flops() : 0;
       s.job.reset();
       ranges_.give(s.off, s.bytes);
+      double stmt = -1;
+      if (err.empty() && s.req->p.precision == 1 && s.req->p.error_sample > 0) {
+        try {
+          stmt = error_statement(s.ctx, *s.req->sys, s.req->pw, s.req->ro, s.req->det, s.req->p,
+                                 s.req->p.error_sample);
+        } catch (const std::exception &e) {
+          err = std::string("error statement: ") + e.what();
+        }
+      }
       {
         std::lock_guard<std::mutex> lk(mu_);
         s.req->t_done = std::chrono::steady_clock::now();
         s.req->fid.swap(fid);
         s.req->sw = sw;
+        s.req->stmt = stmt;
         s.req->err = err;
         s.req->state = err.empty() ? 2 : 3;
         if (err.empty()) flops_done_ += fl;

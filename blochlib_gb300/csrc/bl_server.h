@@ -18,7 +18,9 @@
 //     head is passed over at most kMaxSkips times, after which admission waits for it.  The
 //     job is built inside that range (no further allocation), batching its crystallites to
 //     fit, enqueued on the lane's stream, and its completion recorded with an event;
-//   * a worker thread polls completions, copies the FID back and returns the range;
+//   * a worker thread polls completions, copies the FID back and returns the range; a
+//     mixed-form request with error_sample > 0 then gets its error statement (two small jobs
+//     on the lane's stream, run by the worker before it admits more work);
 //   * latency = completion - submission, measured on the host steady clock.
 // Jobs never share arithmetic and the crystallite batching does not change the powder sum
 // (warp partials are reduced in a fixed order), so a result is bitwise the same alone, in
@@ -53,6 +55,7 @@ struct ServeRequest {
   int skipped = 0;  // times a later request was admitted ahead of this one at the queue's head
   std::vector<double> fid;
   double sw = 0;
+  double stmt = -1;  // stated error (mixed form with error_sample > 0), else -1
   std::string err;
   ServeRequest(std::shared_ptr<const SpinSystem> s, const Powder &w, CMatrix r, CMatrix d, const FidParams &q)
       : sys(std::move(s)), pw(w), ro(std::move(r)), det(std::move(d)), p(q) {}
@@ -79,7 +82,9 @@ class Server {
   // queues the job (the planner fails it later if one warp of it exceeds the pool)
   int64_t submit(std::shared_ptr<const SpinSystem> sys, const Powder &pw, CMatrix ro, CMatrix det, const FidParams &p);
   // state of a ticket; when done and fid_out is given, copies the FID and forgets the ticket
-  int poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err);
+  // (stmt_out: the mixed form's stated error when the request asked for one, else -1)
+  int poll(int64_t id, double *fid_out, double *sw_out, double *latency_ms, std::string *err,
+           double *stmt_out = nullptr);
   bool cancel(int64_t id);
   // requests queued/running, finished (any outcome), and the algorithmic flop of the
   // completed ones (one complex multiply-add = 8 flop)

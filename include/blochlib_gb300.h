@@ -75,6 +75,11 @@ typedef struct {
                       the mixed form (blocks up to 8 with step_method 1, blocks 9-74 always) */
   int fave_method; /* correlation over the rotor period: 0 = automatic (FFT for n <= 2048),
                       1 = direct O(n^2) sum, 2 = zero-padded FFT; both FP64 */
+  int error_sample; /* mixed form: state the result's error.  The FID of this many crystallites
+                      (spread evenly over the powder) is computed again in FP64 and in the mixed
+                      form; their relative L2 difference is read with bl_last_error_statement.
+                      0 = no statement (no extra work).  Honoured by bl_powder_fid and the
+                      serving loop; ignored by the job and allocation-free entry points. */
 } bl_fid_params;
 
 /* Message of the calling thread's last failed call ("" if none). */
@@ -134,6 +139,12 @@ void bl_powder_destroy(bl_powder *pw);
 /* Powder FID: fid_out = 2*npts doubles; *sw_out = the sweep width actually used. */
 bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
                         const double *det, const bl_fid_params *params, double *fid_out, double *sw_out);
+/* The stated error of the last FID this thread received (bl_powder_fid, or bl_server_poll
+ * copying out a finished request) when it was computed in the mixed form with
+ * error_sample > 0: the relative L2 difference between the mixed-form and the FP64 FID of the
+ * sampled crystallites; -1 when that FID carried no statement.  No counterpart in the
+ * reference (its results are FP64 only). */
+double bl_last_error_statement(void);
 
 /* Point-to-point powder FID.  A rotor period is cut into 'base' chunks (each of
  * ceil(chunk/maxtstep) steps exp(-i 2pi tau H(t)), one when maxtstep <= 0); point p sits at
