@@ -635,6 +635,11 @@ void write_fid_text(const std::string &path, const cplx *fid, int npts, double d
   while (n < npts) n *= 2;
   std::vector<cplx> tf(fid, fid + npts);
   tf.resize(n, cplx(0, 0));
+  // The reference zero-fills a length that is not a power of two with
+  // Vector::resizeAndPreserve(n, 0) (src/container/Vector/Vector.h:505-513), whose fill loop
+  // starts at the old length minus one: the last FID point becomes zero in both the time
+  // columns and the spectrum.  Kept, so that the files are the same.
+  if (n != npts && npts > 0) tf[size_t(npts) - 1] = cplx(0, 0);
   std::vector<cplx> sp = fft_pos(tf);
   int sh = int(std::ceil(double(n) / 2.0));
   std::vector<cplx> sh_sp(n);

@@ -27,6 +27,11 @@
 //           added to SolidSys::Hamiltonian by RfSys below, as solid-2.0's PulseData::Pulse)
 //   rfc: <chunk> <iso> <amp Hz> [phase deg] [offset Hz]   (p2p only, repeatable: rf on during
 //           one chunk of every rotor period; base and factor are then used as given)
+//   writers: <fid binary> <npts> <dt> <text out> <mat out>   (instead of a FID: reads npts
+//           (re, im) doubles and writes them with the reference's own writers, plotterFID
+//           (utils/plotter.cc:49-135) to <text out> and Matlab5/matstream
+//           (utils/matlab5.h:700-721, matlab5.cc) to <mat out> as the complex column vector
+//           'vdat' and the real scalar 'dt'; the output file argument is then unused)
 //   p2p: <base> <factor>   maxtstep: <s>   (point-to-point FID instead of oneFID::FID: see
 //           p2p_fid below; a rotor period in 'base' chunks of ceil(chunk/maxtstep) steps,
 //           a point every 'factor' chunks)
@@ -39,6 +44,8 @@
 #include "QMspins/driver/oneFID.h"
 #include "propreduce.h"  // examples/qmsims/MMMQMAS (scratch copy, built by oracle/ref.mk)
 #include "QMspins/driver/ham_gen.h"
+#include "utils/plotter.h"
+#include "utils/matlab5.h"
 
 #include <cstdio>
 #include <fstream>
@@ -281,6 +288,30 @@ int main(int argc, char **argv) {
       rf.push_back(r);
     }
     else if (key == "hamgen_angles") std::sscanf(val.c_str(), "%lf %lf %lf", &hg_theta, &hg_phi, &hg_gamma);
+    else if (key == "writers") {
+      char fin[512] = {0}, ftxt[512] = {0}, fmat[512] = {0};
+      int n = 0;
+      double dt = 1;
+      std::sscanf(val.c_str(), "%511s %d %lf %511s %511s", fin, &n, &dt, ftxt, fmat);
+      FILE *fi = std::fopen(fin, "rb");
+      if (!fi || n <= 0) { std::cerr << "ref_harness: bad writers line\n"; return 2; }
+      Vector<complex> v(n, complex(0, 0));
+      for (int k = 0; k < n; ++k) {
+        double re = 0, im = 0;
+        if (std::fread(&re, sizeof(double), 1, fi) != 1 || std::fread(&im, sizeof(double), 1, fi) != 1) {
+          std::cerr << "ref_harness: short FID file\n";
+          return 2;
+        }
+        v(k) = complex(re, im);
+      }
+      std::fclose(fi);
+      plotterFID(v, std::string(ftxt), dt);
+      matstream ms(fmat, std::ios::binary | std::ios::out);
+      ms.put("vdat", v);
+      ms.put("dt", dt);
+      ms.close();
+      return 0;
+    }
   }
   SolidSys sys(spin_lines);
   sys.setBfield(bfield);

@@ -3,6 +3,7 @@
 
 Run where the reference tree is present (BLOCHLIB_REF, resolved by oracle/build_ref.sh):
     oracle/build_ref.sh all && python3 tests/golden/make_golden.py
+    (--hamgen, --writers, --p2p, ...: the other fixture sets, see main())
 
 Each case is a seeded job in the text format of oracle/ref_harness.cc.  For every case
 the fixture holds the job text, the crystallites (phi, theta, gamma, weight rows), the
@@ -322,9 +323,39 @@ def rfc_cases():
            powder_rows(c0["powder"], spread(1154, 2)))
 
 
+# FIDs written by the reference's own plotterFID (ref_harness 'writers:'): lengths that are
+# and are not powers of two, sweep widths with long decimal expansions, values over 6 decades
+WRITER_CASES = ((100, 1e-5, 1), (128, 2.5e-6, 2), (1000, 3.3e-5, 3), (4096, 1.6666666666666667e-07, 4),
+                (7, 0.001, 5))
+
+
+def writer_fixtures():
+    """plotter_ref.npz: per case the FID, dt and the reference's plotterFID text, byte for byte."""
+    out = {}
+    for n, dt, seed in WRITER_CASES:
+        rng = np.random.default_rng(seed)
+        fid = rng.normal(size=n) * 10 ** rng.uniform(-3, 3) + 1j * rng.normal(size=n)
+        with tempfile.TemporaryDirectory() as td:
+            t = Path(td)
+            np.ascontiguousarray(np.stack([fid.real, fid.imag], 1)).tofile(t / "fid.bin")
+            (t / "j.txt").write_text(f"writers: {t / 'fid.bin'} {n} {dt!r} {t / 'fid.txt'} {t / 'fid.mat'}\n")
+            r = subprocess.run([str(BIN64), str(t / "j.txt"), str(t / "unused.bin")], capture_output=True, timeout=60)
+            if r.returncode != 0:
+                sys.exit("reference writers failed: " + r.stderr.decode()[-300:])
+            text = (t / "fid.txt").read_bytes()
+        out[f"fid_{n}"] = fid
+        out[f"dt_{n}"] = np.array(dt)
+        out[f"text_{n}"] = np.frombuffer(text, dtype=np.uint8)
+    np.savez_compressed(OUT / "plotter_ref.npz", **out)
+    print("plotter fixtures:", len(WRITER_CASES))
+
+
 def main():
     if "--hamgen" in sys.argv:
         hamgen_fixtures()
+        return
+    if "--writers" in sys.argv:
+        writer_fixtures()
         return
     if not BIN64.exists():
         sys.exit("oracle/_ref/ref_fid64 missing: run oracle/build_ref.sh first")

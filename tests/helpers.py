@@ -85,7 +85,7 @@ def rel(a, b):
 
 
 def golden_cases():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem not in ("zcw_builtin", "hamgen"))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if p.stem not in ("zcw_builtin", "hamgen", "plotter_ref"))
 
 
 def load_golden(name):

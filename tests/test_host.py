@@ -80,6 +80,20 @@ def test_powder_file_reader_column_rules(tmp_path):
     np.testing.assert_array_equal(w, [0.4, 0.7, 1.0, 1.0])    # 3 columns: weight; fewer: 1
 
 
+def test_plotter_fid_text_matches_the_reference_byte_for_byte(tmp_path):
+    """plotterFID's 7-column text equals, byte for byte, what the reference's own plotterFID
+    (utils/plotter.cc:49-135, run by tests/golden/make_golden.py --writers) wrote for the same
+    FID and dt: lengths that are and are not powers of two (the reference's zero-fill drops the
+    last point), values over six decades."""
+    g = np.load(GOLDEN / "plotter_ref.npz")
+    ns = sorted(int(k[4:]) for k in g.files if k.startswith("fid_"))
+    assert len(ns) >= 5
+    for n in ns:
+        path = tmp_path / f"fid{n}.txt"
+        bl.plotterFID(g[f"fid_{n}"], path, float(g[f"dt_{n}"]))
+        assert path.read_bytes() == g[f"text_{n}"].tobytes(), n
+
+
 def test_plotter_fid_text(tmp_path):
     rng = np.random.default_rng(1)
     fid = rng.normal(size=100) + 1j * rng.normal(size=100)
@@ -89,6 +103,7 @@ def test_plotter_fid_text(tmp_path):
     n = 128  # zero-filled to the next power of two
     assert d.shape == (n, 7)
     x = np.concatenate([fid, np.zeros(n - 100)])
+    x[99] = 0  # the reference's zero-fill (resizeAndPreserve) overwrites the last point
     S = np.fft.ifft(x) * n  # the reference's FFT has the +i sign and no scaling
     S = np.roll(S, -(n // 2))
     np.testing.assert_allclose(d[:, 0], np.arange(n) * 1e-5, rtol=1e-5, atol=1e-12)
