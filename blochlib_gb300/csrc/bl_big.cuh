@@ -18,6 +18,14 @@ constexpr int kBigThreads = 256;   // k_big_floquet
 constexpr int kBigPSMax = 63;      // 7 real b x b matrices (Paterson-Stockmeyer step) fit
 constexpr int kMaxInt = 128;       // interactions per system on the large-block path
 
+// Element e of block (size b, packed offset bp) of crystallite c inside one step's A or W
+// array: [item][c] as at(), or, for the large blocks of a crystallite-major job (s.clay), the
+// block's region [bp Cpad, (bp + b^2) Cpad) taken as [c][e].
+__device__ __forceinline__ size_t big_at(const DevSys &s, int b, int bp, int e, int c) {
+  return (s.clay && b > kMaxBlock && b <= kMaxBigBlock) ? size_t(bp) * s.Cpad + size_t(c) * b * b + e
+                                                        : size_t(bp + e) * s.Cpad + c;
+}
+
 __host__ __device__ constexpr int big_tiles(int m, int n) { return ((m + 1) / 2) * ((n + 1) / 2); }
 // tiles per thread of an m x n product, and the CTA size that gives each thread NT tiles
 __host__ __device__ constexpr int big_nt(int m, int n) { return big_tiles(m, n) <= 1024 ? 1 : 2; }
@@ -333,7 +341,7 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_eigframe(DevSys s,
     const float4 *Ab4 = reinterpret_cast<const float4 *>(Ab);  // mixed form: double-float A, high parts
     for (int e = threadIdx.x; e < bb; e += blockDim.x) {
       if (s.mixed) {
-        const float4 v = Ab4[at(bp + e, c, s.Cpad)];
+        const float4 v = Ab4[big_at(s, b, bp, e, c)];
         As[e] = mkc<C>(v.x, v.y);
       } else {
         As[e] = cvt<C>(Ab[at(bp + e, c, s.Cpad)]);
@@ -341,7 +349,7 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_eigframe(DevSys s,
     }
     __syncthreads();
     cta_mm_cplx_regs<NT, false, C>(As, b, Vs, b, b, b, b, acc);
-    cta_tiles_store<NT>(b, b, acc, [&](int r, int q, C v) { Wb[at(bp + r * b + q, c, s.Cpad)] = v; });
+    cta_tiles_store<NT>(b, b, acc, [&](int r, int q, C v) { Wb[big_at(s, b, bp, r * b + q, c)] = v; });
     __syncthreads();
   }
 }
@@ -371,14 +379,14 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_qr(DevSys s, BigPa
   C *out = bp2.isq ? Bufs<C>::Q(s) : Bufs<C>::R(s);
   const C *W = Bufs<C>::W(s) + size_t(i) * s.S2 * s.Cpad;
   C *Wa = reinterpret_cast<C *>(bsr), *Wb = Wa + ba * ba, *X = Wb + bb * w;
-  for (int e = threadIdx.x; e < ba * ba; e += blockDim.x) Wa[e] = W[at(pa + e, c, s.Cpad)];
+  for (int e = threadIdx.x; e < ba * ba; e += blockDim.x) Wa[e] = W[big_at(s, ba, pa, e, c)];
   C *ob = out + size_t(i) * bp2.nitems * s.Cpad;
   C acc[NT][4];
   for (int q0 = 0; q0 < bb; q0 += w) {
     const int wc = min(w, bb - q0);
     for (int e = threadIdx.x; e < bb * wc; e += blockDim.x) {
       const int m = e / wc, q = e % wc;
-      Wb[e] = W[at(pb + m * bb + q0 + q, c, s.Cpad)];
+      Wb[e] = W[big_at(s, bb, pb, m * bb + q0 + q, c)];
     }
     __syncthreads();
     for (int e = threadIdx.x; e < ba * wc; e += blockDim.x) {
@@ -555,7 +563,7 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
   const double2 *U = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;  // U(r,q) = U[at(bp + r*b + q, c)]
   const float4 *U4 = reinterpret_cast<const float4 *>(U);      // dfA: double-float A (mixed form)
   auto Ug = [&](int r, int q) {
-    return dfA ? df_load(U4[at(bp + r * b + q, c, s.Cpad)]) : U[at(bp + r * b + q, c, s.Cpad)];
+    return dfA ? df_load(U4[big_at(s, b, bp, r * b + q, c)]) : U[big_at(s, b, bp, r * b + q, c)];
   };
   if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
   __syncthreads();
@@ -915,7 +923,7 @@ __global__ void __launch_bounds__(NT == 1 ? 1024 : 768) k_big_dyson_df(DevSys s,
         const int r = i0 + (d >> 1), col = j0 + (d & 1);
         if (r < b && col < b) {
           As[r * b + col] = out[q][d];
-          Ab[at(bp + r * b + col, c, s.Cpad)] = out[q][d];
+          Ab[big_at(s, b, bp, r * b + col, c)] = out[q][d];
         }
       }
     }
@@ -1093,7 +1101,7 @@ __device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
   double *red = wk.red;
   float2 *Kf = wk.Kf;
   const float4 *U4 = reinterpret_cast<const float4 *>(s.A + size_t(s.n - 1) * s.S2 * s.Cpad);
-  auto Ug = [&](int r, int q) { return U4[at(bp + r * b + q, c, s.Cpad)]; };
+  auto Ug = [&](int r, int q) { return U4[big_at(s, b, bp, r * b + q, c)]; };
   if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {

@@ -215,6 +215,10 @@ struct DevSys {
   int warp_base;  // global warp index of this batch's first crystallite
   int *status;
   unsigned long long *tc_flops;  // [2]: BF16 tensor flops issued by the step and Dyson kernels
+  // 1: in the mixed form, A and W of the large blocks (kMaxBlock < b <= kMaxBigBlock) are
+  // stored crystallite-major inside each (step, block) region (big_at), so that the
+  // one-CTA-per-crystallite kernels move contiguous rows; the other blocks keep [item][c]
+  int clay;
 };
 
 // Precision-dependent arrays: W (eigenframe; in place over A in FP64), Q, R, G, Z, twiddles.
@@ -2943,6 +2947,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.partial = J.partial.p;
   s.status = J.status.p;
   s.tc_flops = J.tcf.p;
+  s.clay = (J.mixed && J.huge_blocks.empty()) ? 1 : 0;
   s.Cpad = J.Cb;
 }
 

@@ -501,8 +501,8 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
 // so that the epilogue lane of column m of A_{i+1} stores row m of the next A_i^T tile as
 // whole 16-byte core-matrix rows.  U_i's slab (written by k_tc_step) arrives by a bulk copy
 // that overlaps the previous step's epilogue.  A_{i+1} also goes to s.A as double-float
-// (float4 re.hi, im.hi, re.lo, im.lo in the [item][c] layout) for the eigenframe and the
-// Floquet step.  Shared memory: the A^T tiles (re, im), the U slab (C, S), the margin.
+// (float4 re.hi, im.hi, re.lo, im.lo; crystallite-major per block, big_at, so that the lanes'
+// stores are contiguous) for the eigenframe and the Floquet step.  Shared memory: the A^T tiles (re, im), the U slab (C, S), the margin.
 __host__ __device__ constexpr size_t tc_dyson_smem(int b) {
   return 4 * tc::tile_bytes(b) + tc::overread_bytes(b) + 1024;
 }
@@ -597,7 +597,7 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k,
               const float2 pr = tc::sum3(r0[j], r1[j], r2[j]), pi = tc::sum3(i0[j], i1[j], i2[j]);
               re = make_float2(pr.x * 0x1p-16f, pr.y * 0x1p-16f);
               im = make_float2(pi.x * 0x1p-16f, pi.y * 0x1p-16f);
-              Ab[at(bp + n * b + m, c, s.Cpad)] = make_float4(re.x, im.x, re.y, im.y);
+              Ab[big_at(s, b, bp, n * b + m, c)] = make_float4(re.x, im.x, re.y, im.y);
             }
             rh[j] = re.x, rl[j] = re.y, ih[j] = im.x, il[j] = im.y;
           }
