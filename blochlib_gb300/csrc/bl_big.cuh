@@ -956,19 +956,29 @@ __device__ __forceinline__ float4 cdf_mul(float4 x, float4 y) {
   return cdf_fin(a);
 }
 
+// q = e / d and r = e - q d without an integer division: (e + 1/2) / d in FP32 is at least
+// 1/(2 d) away from an integer and its rounding error is far smaller (e < 2^20, d <= 2^8)
+__device__ __forceinline__ int fdiv(int e, float invd, int d, int &r) {
+  const int q = __float2int_rz((float(e) + 0.5f) * invd);
+  r = e - q * d;
+  return q;
+}
+
 // The sweeps over the FP32 K (Kf) with V (double-float, Vd) accumulating the rotations.
 __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps, const FloqWork &wk) {
   float4 *rot = reinterpret_cast<float4 *>(wk.rot);  // per pair: (c.hi, 0, c.lo, 0), (s as complex df)
   auto rpair = [&](int t, int q) -> int & { return wk.rpair[2 * t + q]; };
   double *red = wk.red;
   const int bb = b * b;
+  const float invb = 1.f / float(b);
   const int bq = b + (b & 1);
   const int np = bq / 2;
   bool conv = false, polish = false;
   for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
     double off = 0, dg = 0;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) {
-      const int r = e / b, q = e % b;
+      int q;
+      const int r = fdiv(e, invb, b, q);
       const float2 v = Xk[e];
       if (r < q) off += double(v.x) * v.x + double(v.y) * v.y;
       else if (r == q) dg += double(v.x) * v.x;
@@ -1038,19 +1048,22 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
         rot[2 * t] = cr, rot[2 * t + 1] = sr;
       }
       __syncthreads();
-      // columns p, q of K (FP32) and of V (double-float): X <- X G, G = [[c, sp], [-conj(sp), c]]
-      for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
-        const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
+      // columns p, q of K (FP32) and of V (double-float): X <- X G, G = [[c, sp], [-conj(sp), c]];
+      // one (pair, row) per iteration updates both
+      for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
+        int kk;
+        const int t = fdiv(e, invb, b, kk);
         const int p = rpair(t, 0), q = rpair(t, 1);
         if (q >= b) continue;
         const float4 cr = rot[2 * t], sp = rot[2 * t + 1];
-        if (rem2 < b) {
+        {
           const float ccr = cr.x + cr.z;
           const float2 spr = make_float2(sp.x + sp.z, sp.y + sp.w), spcr = cconj(spr);
           const float2 xkp = Xk[kk * b + p], xkq = Xk[kk * b + q];
           Xk[kk * b + p] = csub(cscale(xkp, ccr), cmul(spcr, xkq));
           Xk[kk * b + q] = cadd(cmul(spr, xkp), cscale(xkq, ccr));
-        } else {
+        }
+        {
           const float4 vp = Vd[kk * b + p], vq = Vd[kk * b + q];
           // vp' = c vp - conj(sp) vq,  vq' = sp vp + c vq
           CdfAcc ap = {{0.f, 0.f}, {0.f, 0.f}}, aq = ap;
@@ -1065,7 +1078,8 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
       __syncthreads();
       // rows p, q of K:  K <- G^H K
       for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
-        const int t = e / b, kk = e % b;
+        int kk;
+        const int t = fdiv(e, invb, b, kk);
         const int p = rpair(t, 0), q = rpair(t, 1);
         if (q >= b) continue;
         const float4 cr = rot[2 * t], s4 = rot[2 * t + 1];
@@ -1158,10 +1172,11 @@ __device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
       for (int r = threadIdx.x; r < b; r += blockDim.x) fv[r] = r == kc ? make_float4(0.f, 0.f, 0.f, 0.f) : cdf_mul(M4[r * b + kc], inv);
       __syncthreads();
       const int wM = b - kc - 1, w = wM + b;  // columns kc+1..b-1 of M, all of X
+      const float invw = 1.f / float(w);
       for (int e = threadIdx.x; e < (b - 1) * w; e += blockDim.x) {
-        int r = e / w;
+        int j;
+        int r = fdiv(e, invw, w, j);
         r += (r >= kc);
-        const int j = e % w;
         if (j < wM) M4[r * b + kc + 1 + j] = cdf_fms(M4[r * b + kc + 1 + j], fv[r], M4[kc * b + kc + 1 + j]);
         else X4[r * b + (j - wM)] = cdf_fms(X4[r * b + (j - wM)], fv[r], X4[kc * b + (j - wM)]);
       }
@@ -1236,4 +1251,72 @@ __device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
   for (int e = threadIdx.x; e < bb; e += blockDim.x) s.VF[at(bp + e, c, s.Cpad)] = df_load(M4[e]);
   for (int r = threadIdx.x; r < b; r += blockDim.x)
     s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
+}
+
+// ------------------------------------------------------------------ mixed form, 4 x 4 tiles
+// The mixed form's single-precision eigenframe with 4 x 4 output tiles per thread: 8 shared-memory loads per 16 complex multiply-adds (the 2 x 2 tiles of
+// cta_mm_cplx_regs take 4 per 4), one tile per thread (blocks up to 74: at most 19 x 19
+// tiles).  Same operands and the same sum per output element, in the same order.
+__host__ __device__ constexpr int big4_tiles(int m, int n) { return ((m + 3) / 4) * ((n + 3) / 4); }
+__host__ __device__ constexpr int big4_threads(int m, int n) { return (big4_tiles(m, n) + 31) / 32 * 32; }
+
+// acc (this thread's tile; zero when it has none) = op(A) B, op = ^H if CONJ_A
+template <bool CONJ_A>
+__device__ __forceinline__ void cta_mm_cplx4(const float2 *A, int lda, const float2 *B, int ldb, int m, int n, int k,
+                                             float2 (&acc)[4][4]) {
+  const int tm = (m + 3) / 4, tn = (n + 3) / 4, t = threadIdx.x;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
+  if (t >= tm * tn) return;
+  const int i0 = (t / tn) * 4, j0 = (t % tn) * 4;
+  int ii[4], jj[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) ii[a] = min(i0 + a, m - 1), jj[a] = min(j0 + a, n - 1);
+  for (int l = 0; l < k; ++l) {
+    float2 av[4], bv[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) av[a] = CONJ_A ? cconj(A[l * lda + ii[a]]) : A[ii[a] * lda + l];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) bv[b] = B[l * ldb + jj[b]];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] = cfma(av[a], bv[b], acc[a][b]);
+  }
+}
+template <class F>
+__device__ __forceinline__ void cta_tiles4_store(int m, int n, const float2 (&acc)[4][4], F f) {
+  const int tm = (m + 3) / 4, tn = (n + 3) / 4, t = threadIdx.x;
+  if (t >= tm * tn) return;
+  const int i0 = (t / tn) * 4, j0 = (t % tn) * 4;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      if (i0 + a < m && j0 + b < n) f(i0 + a, j0 + b, acc[a][b]);
+}
+
+// One CTA per crystallite: W_i = A_{i+1} V_F for i < n (mixed form: high parts of the
+// double-float A, single-precision V and W), 4 x 4 tiles.
+__global__ void __launch_bounds__(384) k_big_eigframe4(DevSys s, int k) {
+  extern __shared__ __align__(16) unsigned char bsr4[];
+  const int c = blockIdx.x;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  float2 *Vs = reinterpret_cast<float2 *>(bsr4), *As = Vs + bb;
+  for (int e = threadIdx.x; e < bb; e += blockDim.x) Vs[e] = cvt<float2>(s.VF[at(bp + e, c, s.Cpad)]);
+  float2 acc[4][4];
+  for (int i = 0; i < s.n; ++i) {
+    const float4 *Ab4 = reinterpret_cast<const float4 *>(s.A + size_t(i) * s.S2 * s.Cpad);
+    float2 *Wb = s.Wf + size_t(i) * s.S2 * s.Cpad;
+    for (int e = threadIdx.x; e < bb; e += blockDim.x) {
+      const float4 v = Ab4[big_at(s, b, bp, e, c)];
+      As[e] = make_float2(v.x, v.y);
+    }
+    __syncthreads();
+    cta_mm_cplx4<false>(As, b, Vs, b, b, b, b, acc);
+    cta_tiles4_store(b, b, acc, [&](int r, int q, float2 v) { Wb[big_at(s, b, bp, r * b + q, c)] = v; });
+    __syncthreads();
+  }
 }

@@ -2689,6 +2689,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
       attr((const void *)k_big_eigframe<1, float2>, smem_mat);
       attr((const void *)k_big_eigframe<2, float2>, smem_mat);
+      attr((const void *)k_big_eigframe4, smem_mat);
       attr((const void *)k_big_floquet, smem_mat + (J.mixed ? smem_mat / 4 : 0));  // + b^2 float2 (K)
       size_t smem_hf = 0;
       for (int k : J.huge_blocks) smem_hf = std::max(smem_hf, huge_floquet_smem(L.size[k]));
@@ -3214,8 +3215,7 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         break;
       case 3:
         if (s.mixed) {
-          if (nt1) k_big_eigframe<1, float2><<<unsigned(s.C), th, sw, st>>>(s, k);
-          else k_big_eigframe<2, float2><<<unsigned(s.C), th, sw, st>>>(s, k);
+          k_big_eigframe4<<<unsigned(s.C), unsigned(big4_threads(b, b)), sw, st>>>(s, k);
         } else {
           if (nt1) k_big_eigframe<1, double2><<<unsigned(s.C), th, sw, st>>>(s, k);
           else k_big_eigframe<2, double2><<<unsigned(s.C), th, sw, st>>>(s, k);

@@ -210,6 +210,30 @@ __device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint3
   }
 }
 
+// -1 / (k (k + 1)) as double-float for the Horner steps (k = 1 .. 31), folded at compile time
+// into constant memory (k is the same in every thread), so that no epilogue divides in FP64
+#define BL_HC(k) dfv_const(-1.0 / (double(k) * double((k) + 1)))
+__constant__ float2 kHornerCoef[32] = {BL_HC(1),  BL_HC(1),  BL_HC(2),  BL_HC(3),  BL_HC(4),  BL_HC(5),  BL_HC(6),
+                                       BL_HC(7),  BL_HC(8),  BL_HC(9),  BL_HC(10), BL_HC(11), BL_HC(12), BL_HC(13),
+                                       BL_HC(14), BL_HC(15), BL_HC(16), BL_HC(17), BL_HC(18), BL_HC(19), BL_HC(20),
+                                       BL_HC(21), BL_HC(22), BL_HC(23), BL_HC(24), BL_HC(25), BL_HC(26), BL_HC(27),
+                                       BL_HC(28), BL_HC(29), BL_HC(30), BL_HC(31)};
+#undef BL_HC
+__device__ __forceinline__ float2 horner_coef(int k) { return kHornerCoef[k < 1 ? 1 : (k > 31 ? 31 : k)]; }
+
+// Taylor degree of the tensor-core step: the smallest K with x^(K+1)/(K+1)! <= 2^-35 (x <= 1):
+// the exact-slice products carry ~2^-32 each, so a tighter series buys nothing
+__device__ __forceinline__ int taylor_degree_tc(float x) {
+  constexpr float thr[14] = {7.62939453125e-06f, 0.00055894250f, 0.0051409141f, 0.020352899f, 0.052506585f,
+                             0.10562547f,        0.18141945f,    0.27994921f,   0.40028685f,  0.54099275f,
+                             0.70041794f,        0.87688129f,    1.0687663f,    1.2745689f};
+  int K = 15;
+#pragma unroll
+  for (int j = 13; j >= 0; --j)
+    if (x <= thr[j]) K = j + 1;
+  return K;
+}
+
 }  // namespace tc
 
 enum { kTcTimeout = 64 };  // status bit: a tensor-core wait ran out
@@ -219,7 +243,7 @@ enum { kTcTimeout = 64 };  // status bit: a tensor-core wait ran out
 // schedule): H_i in double-float from k_coef's coefficients (as k_big_step_df),
 // X = 2 pi tau H / 2^sq with ||X||_inf <= 1, and
 //     C = cos X = sum_j (-1)^j Y^j / (2j)!,  S = sin X = X sum_j (-1)^j Y^j / (2j+1)!,  Y = X^2,
-// to the degree K that taylor_degree gives at 2^-40, each by Horner's rule
+// to the degree K that taylor_degree_tc gives at 2^-35, each by Horner's rule
 //     T <- I - Y T / (k (k + 1))
 // on the tensor cores; the C and S chains run in two groups of 8 warps with their own
 // accumulator sets, named barriers and MMA-issuing threads, so that one chain's epilogue
@@ -285,7 +309,7 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
     }
     scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
     nsq = sq;
-    nterms = taylor_degree(double(ldexpf(nrm, -sq)), true);
+    nterms = tc::taylor_degree_tc(ldexpf(nrm, -sq));
   }
   __syncthreads();
   const int sq = nsq, K = nterms;
@@ -381,7 +405,7 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
     tc::fence_after();
     return all;
   };
-  auto hcoef = [](int kk) { return dfv_of(-1.0 / (double(kk) * double(kk + 1))); };  // -1/(k(k+1))
+  auto hcoef = [](int kk) { return tc::horner_coef(kk); };  // -1/(k(k+1)), double-float
   __nv_bfloat16 *X = Bf[0], *Y = Bf[1], *TC = Bf[2], *TS = Bf[3];
   const uint32_t aX = ba[0], aY = ba[1], aTC = ba[2], aTS = ba[3];
   // Y = X X, then the innermost Horner terms straight from Y (all 16 warps)
