@@ -35,6 +35,7 @@
 #include <cstring>
 #include <sstream>
 #include <stdexcept>
+#include <type_traits>
 
 #include "bl_engine.h"
 
@@ -213,6 +214,7 @@ struct DevSys {
   float2 *Wf, *Qf, *Rf, *Gf, *Zf;
   const float2 *twf;
   int warp_base;  // global warp index of this batch's first crystallite
+  int ft_jt, ft_pt, ft_r;  // k_fid_tiled: thread rows (4 j each), columns (4 p each), element ranges
   int *status;
   unsigned long long *tc_flops;  // [2]: BF16 tensor flops issued by the step and Dyson kernels
   // 1: in the mixed form, A and W of the large blocks (kMaxBlock < b <= kMaxBigBlock) are
@@ -1650,48 +1652,111 @@ __global__ void __launch_bounds__(kThreads) k_fave(DevSys s) {
   }
 }
 
-// In-place radix-2 decimation-in-time FFT (negative exponent) of CG interleaved sequences
-// of length M = 2^logM held in shared memory as X[i * CG + cc], input in bit-reversed
-// order, output in natural order.  tw[k] = exp(-2 pi i k / (M twm)), k < M twm / 2 (twm = 2:
-// a half-length transform on the table of the full length).  Y (optional) is transformed
-// alongside X.  Ends with a barrier.
-template <int CG, class C>
-__device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw, int twm = 1) {
-  const int nb = (M / 2) * CG;
-  for (int st = 0; st < logM; ++st) {
-    const int h = 1 << st, tstride = M >> (st + 1);
-    for (int idx = threadIdx.x; idx < nb; idx += blockDim.x) {
-      const int cc = idx % CG, b = idx / CG;
-      const int pos = b & (h - 1), grp = b >> st;
-      const int i0 = ((grp << (st + 1)) + pos) * CG + cc, i1 = i0 + h * CG;
-      if (st == 0) {
-        C a = X[i0], d = X[i1];
-        X[i0] = cadd(a, d), X[i1] = csub(a, d);
-        if (Y) {
-          a = Y[i0], d = Y[i1];
-          Y[i0] = cadd(a, d), Y[i1] = csub(a, d);
-        }
-      } else if (st == 1) {  // twiddles 1 and -i: no multiplication
-        C a = X[i0], d = X[i1];
-        C t = pos ? mkc<C>(d.y, -d.x) : d;
-        X[i0] = cadd(a, t), X[i1] = csub(a, t);
-        if (Y) {
-          a = Y[i0], d = Y[i1];
-          t = pos ? mkc<C>(d.y, -d.x) : d;
-          Y[i0] = cadd(a, t), Y[i1] = csub(a, t);
-        }
-      } else {
-        const C w = tw[pos * tstride * twm];
-        C a = X[i0], t = cmul(w, X[i1]);
-        X[i0] = cadd(a, t), X[i1] = csub(a, t);
-        if (Y) {
-          a = Y[i0], t = cmul(w, Y[i1]);
-          Y[i0] = cadd(a, t), Y[i1] = csub(a, t);
-        }
+// Radix-2 decimation-in-time FFT (negative exponent) of CG interleaved sequences of length
+// M = 2^logM held in shared memory as X[i * CG + cc], input in bit-reversed order, output in
+// natural order.  tw[k] = exp(-2 pi i k / (M twm)), k < M twm / 2 (twm = 2: a half-length
+// transform on the table of the full length).  Stage st pairs the points i and i + 2^st of
+// each block of 2^(st+1) with twiddle tw[(i mod 2^st) (M >> (st+1)) twm]; stages 0 and 1
+// multiply by 1 and -i only.  The stages run in passes of up to three: a thread holds the
+// 2^LR points of one group in registers and applies LR stages to them, so a pass costs one
+// shared-memory round trip and one barrier, and every point sees the same butterflies in
+// the same order as stage by stage (the result does not depend on the grouping).
+
+// Stages st .. st+LR-1 on x[k] = point (group base) + pos + k 2^st, pos < 2^st.
+template <class C, int LR>
+__device__ __forceinline__ void fft_regs(C (&x)[1 << LR], int st, int pos, int M, const C *__restrict__ tw,
+                                         int twm) {
+#pragma unroll
+  for (int l = 0; l < LR; ++l) {
+    const int sl = st + l, tstride = M >> (sl + 1);
+#pragma unroll
+    for (int k = 0; k < (1 << LR); ++k) {
+      if ((k >> l) & 1) continue;
+      const int k1 = k + (1 << l);
+      const int p = pos + ((k & ((1 << l) - 1)) << st);  // position within the half block
+      const C a = x[k], d = x[k1];
+      C t = d;
+      if (sl == 1) {
+        if (p) t.x = d.y, t.y = -d.x;
+      } else if (sl > 1) {
+        t = cmul(tw[p * tstride * twm], d);
       }
+      x[k] = cadd(a, t), x[k1] = csub(a, t);
     }
-    __syncthreads();
   }
+}
+
+// One pass of LR stages from st over X (and Y), in place; ends with a barrier.
+template <int CG, class C, int LR>
+__device__ void fft_pass(C *X, C *Y, int M, int st, const C *__restrict__ tw, int twm) {
+  constexpr int R = 1 << LR;
+  const int h = 1 << st, items = (M >> LR) * CG;
+  for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
+    const int cc = idx % CG, b = idx / CG;
+    const int pos = b & (h - 1), grp = b >> st;
+    const int base = ((grp << (st + LR)) + pos) * CG + cc;
+    for (int w = 0; w < (Y ? 2 : 1); ++w) {
+      C *V = w ? Y : X;
+      C x[R];
+#pragma unroll
+      for (int k = 0; k < R; ++k) x[k] = V[base + k * h * CG];
+      fft_regs<C, LR>(x, st, pos, M, tw, twm);
+#pragma unroll
+      for (int k = 0; k < R; ++k) V[base + k * h * CG] = x[k];
+    }
+  }
+  __syncthreads();
+}
+
+// Stages st0 .. logM-1 in passes of three (the last pass two or one).
+template <int CG, class C>
+__device__ void fft_dit(C *X, C *Y, int M, int logM, const C *__restrict__ tw, int twm = 1, int st0 = 0) {
+  int st = st0;
+  for (; st + 3 <= logM; st += 3) fft_pass<CG, C, 3>(X, Y, M, st, tw, twm);
+  if (logM - st == 2) fft_pass<CG, C, 2>(X, Y, M, st, tw, twm);
+  else if (logM - st == 1) fft_pass<CG, C, 1>(X, Y, M, st, tw, twm);
+}
+
+// The first pass (stages 0..2, logM >= 3) fused with the load: point (bit-reversed position)
+// j of column cc is load(natural index brev(j), cc, x, y); the transformed groups go to X
+// (and Y when it is given).  Ends with a barrier; fft_dit(..., st0 = 3) continues.
+template <int CG, class C, class F>
+__device__ void fft_first_pass(C *X, C *Y, int M, int logM, const C *__restrict__ tw, int twm, F &&load) {
+  const int items = (M >> 3) * CG;
+  for (int idx = threadIdx.x; idx < items; idx += blockDim.x) {
+    const int cc = idx % CG, grp = idx / CG;
+    C x[8], y[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int i = int(__brev(unsigned(grp * 8 + k)) >> (32 - logM));
+      load(i, cc, x[k], y[k]);
+    }
+    fft_regs<C, 3>(x, 0, 0, M, tw, twm);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) X[(grp * 8 + k) * CG + cc] = x[k];
+    if (Y) {
+      fft_regs<C, 3>(y, 0, 0, M, tw, twm);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) Y[(grp * 8 + k) * CG + cc] = y[k];
+    }
+  }
+  __syncthreads();
+}
+
+// z^j rounded to float for z = e^{a + i b} (l = (a, b) in FP64): the phase j b reduced
+// modulo 2 pi in FP64 against a two-term 2 pi (Cody-Waite), the reduced phase split into a
+// float and its float remainder, then float sincos with a first-order correction for the
+// remainder and a float exp of j a.  Error a few float ulp (the result is stored as float).
+__device__ __forceinline__ float2 z_pow_f(double2 l, int j) {
+  constexpr double kInv2Pi = 0.15915494309189535, k2PiHi = 6.283185307179586, k2PiLo = 2.4492935982947064e-16;
+  const double ph = double(j) * l.y;
+  const double k = rint(ph * kInv2Pi);
+  const double r = fma(-k, k2PiLo, fma(-k, k2PiHi, ph));
+  const float rf = float(r), rl = float(r - double(rf));
+  float sn, cs;
+  sincosf(rf, &sn, &cs);
+  const float m = expf(float(double(j) * l.x));
+  return make_float2(m * fmaf(-rl, sn, cs), m * fmaf(rl, cs, sn));
 }
 
 // Fave by FFT.  One CTA per (element e, group of CG crystallites).  With q zero outside
@@ -1725,21 +1790,36 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   const C *Qb = Bufs<C>::Q(s), *Rb = Bufs<C>::R(s);
   const double nt = double(n) * s.tau;
   // per crystallite of the group: w_rs = chop((l_r - l_s)/(i n tau), 1e-10), z = e^{i n tau w},
-  // and the powers z^j of the FID reconstruction (always computed in FP64)
-  // (four powers per thread: one cexp and three products, error a few ulp)
-  constexpr int kZrun = 4;
-  const int nzr = (s.J + 1 + kZrun - 1) / kZrun;
-  for (int idx = threadIdx.x; idx < CG * nzr; idx += blockDim.x) {
-    const int cc = idx % CG, j0 = (idx / CG) * kZrun, c = c0 + cc;
-    if (c >= s.C) continue;
-    double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
-    double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
-    const double2 z1 = cexp(cmk(-nt * w.y, nt * w.x));
-    double2 zj = cexp(cmk(-double(j0) * nt * w.y, double(j0) * nt * w.x));
-    for (int j = j0; j < min(j0 + kZrun, s.J + 1); ++j) {
-      if (j == s.J) zc[cc] = cvt<C>(z1);
-      else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(zj);
-      zj = cmul(zj, z1);
+  // and the powers z^j of the FID reconstruction.  FP64 form: four powers per thread, one
+  // cexp and three products (error a few ulp).  Single-precision form (the powers are stored
+  // as float): the exponent of z^j in FP64, then z_pow_f per power (after the first pass).
+  constexpr bool kF = std::is_same<C, float2>::value;
+  __shared__ double2 zexp[CG];
+  if constexpr (kF) {
+    for (int cc = threadIdx.x; cc < CG; cc += blockDim.x) {
+      const int c = c0 + cc;
+      double2 w = cmk(0, 0);
+      if (c < s.C) {
+        double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
+        w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+      }
+      zexp[cc] = cmk(-nt * w.y, nt * w.x);
+    }
+  } else {
+    constexpr int kZrun = 4;
+    const int nzr = (s.J + 1 + kZrun - 1) / kZrun;
+    for (int idx = threadIdx.x; idx < CG * nzr; idx += blockDim.x) {
+      const int cc = idx % CG, j0 = (idx / CG) * kZrun, c = c0 + cc;
+      if (c >= s.C) continue;
+      double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
+      double2 w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+      const double2 z1 = cexp(cmk(-nt * w.y, nt * w.x));
+      double2 zj = cexp(cmk(-double(j0) * nt * w.y, double(j0) * nt * w.x));
+      for (int j = j0; j < min(j0 + kZrun, s.J + 1); ++j) {
+        if (j == s.J) zc[cc] = cvt<C>(z1);
+        else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = cvt<C>(zj);
+        zj = cmul(zj, z1);
+      }
     }
   }
   const bool twist = s.fave_twist;
@@ -1775,10 +1855,9 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
     }
     __syncthreads();
   }
-  // load q (and conj r) zero-padded, bit-reversed
-  for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
-    const int cc = idx % CG, i = idx / CG, c = c0 + cc;
-    const int ri = int(__brev(unsigned(i)) >> (32 - logM));
+  // q (and conj r) at natural index i, zero-padded
+  auto load = [&](int i, int cc, C &qo, C &yo) {
+    const int c = c0 + cc;
     C q = mkc<C>(0, 0), y = mkc<C>(0, 0);
     if (i < n && c < s.C) {
       q = Qb[i * qstride + at(eq, c, s.Cpad)];
@@ -1794,11 +1873,32 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
         if (!autoc) y = cconj(cvt<C>(cmul(cmul(tp8[a * CG + cc], tp1[b * CG + cc]), todbl(r))));
       }
     }
-    X[ri * CG + cc] = q;
-    if (!autoc) Y[ri * CG + cc] = y;
+    qo = q, yo = y;
+  };
+  const C *tw = Bufs<C>::tw(s);
+  C *Yf = autoc ? nullptr : Y;
+  if (logM >= 3) {
+    fft_first_pass<CG, C>(X, Yf, M, logM, tw, 1, load);
+  } else {
+    for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+      const int cc = idx % CG, i = idx / CG;
+      const int ri = int(__brev(unsigned(i)) >> (32 - logM));
+      C q, y;
+      load(i, cc, q, y);
+      X[ri * CG + cc] = q;
+      if (!autoc) Y[ri * CG + cc] = y;
+    }
+    __syncthreads();
   }
-  __syncthreads();
-  fft_dit<CG, C>(X, autoc ? nullptr : Y, M, logM, Bufs<C>::tw(s));
+  if constexpr (kF) {  // z^j, j < J, and z itself (the exponents were written before the first pass's barrier)
+    for (int idx = threadIdx.x; idx < CG * (s.J + 1); idx += blockDim.x) {
+      const int cc = idx % CG, j = idx / CG, c = c0 + cc;
+      if (c >= s.C) continue;
+      if (j == s.J) zc[cc] = z_pow_f(zexp[cc], 1);
+      else Bufs<C>::Z(s)[at(j * s.ne + e, c, s.Cpad)] = z_pow_f(zexp[cc], j);
+    }
+  }
+  fft_dit<CG, C>(X, Yf, M, logM, tw, 1, logM >= 3 ? 3 : 0);
   // Inverse transform by a forward one: conj(FFT(x))/M.  Autocorrelation: the spectrum
   // S = |FFT q|^2 is real, so its transform takes one of half length on z_k = S_2k + i S_2k+1
   // (each column on its own, so a crystallite's result does not depend on its neighbours):
@@ -1806,16 +1906,24 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   // FFT(S)_p = E_p + w^p O_p and FFT(S)_{p+M/2} = E_p - w^p O_p, w = exp(-2 pi i / M).
   const int Mh = M / 2;
   const bool half = autoc && M >= 4;
-  const C *twb = Bufs<C>::tw(s);
+  const C *twb = tw;
   if (half) {
-    for (int idx = threadIdx.x; idx < Mh * CG; idx += blockDim.x) {
-      const int cc = idx % CG, k = idx / CG;
+    auto spow = [&](int k, int cc, C &zo, C &) {
       const C xe = X[(2 * k) * CG + cc], xo = X[(2 * k + 1) * CG + cc];
-      Y[int(__brev(unsigned(k)) >> (33 - logM)) * CG + cc] =
-          mkc<C>(xe.x * xe.x + xe.y * xe.y, xo.x * xo.x + xo.y * xo.y);
+      zo = mkc<C>(xe.x * xe.x + xe.y * xe.y, xo.x * xo.x + xo.y * xo.y);
+    };
+    if (logM - 1 >= 3) {
+      fft_first_pass<CG, C>(Y, nullptr, Mh, logM - 1, twb, 2, spow);
+    } else {
+      for (int idx = threadIdx.x; idx < Mh * CG; idx += blockDim.x) {
+        const int cc = idx % CG, k = idx / CG;
+        C z, u;
+        spow(k, cc, z, u);
+        Y[int(__brev(unsigned(k)) >> (33 - logM)) * CG + cc] = z;
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    fft_dit<CG, C>(Y, nullptr, Mh, logM - 1, twb, 2);
+    fft_dit<CG, C>(Y, nullptr, Mh, logM - 1, twb, 2, logM - 1 >= 3 ? 3 : 0);
   } else {
     // conj of the cross spectrum, in place in X (same index read and written)
     for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
@@ -1824,12 +1932,17 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
       else X[idx] = cconj(cmul(x, cconj(Y[idx])));
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
-      const int cc = idx % CG, f = idx / CG;
-      Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
+    auto fromX = [&](int f, int cc, C &xo, C &) { xo = X[f * CG + cc]; };
+    if (logM >= 3) {
+      fft_first_pass<CG, C>(Y, nullptr, M, logM, tw, 1, fromX);
+    } else {
+      for (int idx = threadIdx.x; idx < M * CG; idx += blockDim.x) {
+        const int cc = idx % CG, f = idx / CG;
+        Y[int(__brev(unsigned(f)) >> (32 - logM)) * CG + cc] = X[idx];
+      }
+      __syncthreads();
     }
-    __syncthreads();
-    fft_dit<CG, C>(Y, nullptr, M, logM, Bufs<C>::tw(s));
+    fft_dit<CG, C>(Y, nullptr, M, logM, tw, 1, logM >= 3 ? 3 : 0);
   }
   // transform of column cc at frequency p
   auto spec = [&](int p, int cc) -> C {
@@ -2013,38 +2126,45 @@ __global__ void __launch_bounds__(kThreads) k_p2p_elems(DevSys s) {
 // Compensated (Kahan) sum of the warp partials in fixed order: deterministic.
 // Mixed form: the FID terms as a tiled product.  fid[j gper + p] = sum_c w_c sum_e
 // z_e^j(c) G_p(e, c) is a product with K = (crystallite, element); one CTA takes a group of
-// 32 crystallites (one warp of the batch layout), a range of the elements (kFtR ranges), 16
-// j's and 64 p's.  Per element it stages z_e^j and G_p(e) of its 32 crystallites in shared
-// memory by asynchronous copies (coalesced: crystallites are fastest in HBM; double-buffered,
-// so the next element's copies are in flight while this one is summed), and each thread
-// updates a 4 x 4 (j, p) register tile with w_c scale z, accumulating one element in FP32
-// and folding it into double-float (hi + lo) sums.  Every element of G is read once per j range and every z once
-// per p range, against once per 4-wide tile of the other index in k_fid.  The CTA writes its
-// tile to partial row (warp * kFtR + range); k_reduce sums the rows of the populated warps in
-// a fixed order, so a crystallite's contribution does not depend on its neighbours.
-constexpr int kFtThreads = 64, kFtJ = 16, kFtP = 64, kFtR = 4;
+// 32 crystallites (one warp of the batch layout), a range of the elements (ft_r ranges, a
+// function of the element count only) and a (j, p) tile of ft_jt x ft_pt threads, each
+// thread a 4 x 4 register tile (the tile shape follows J and gper, so little is padded).
+// Per element it stages z_e^j and G_p(e) of its 32 crystallites in shared memory by
+// asynchronous copies (coalesced: crystallites are fastest in HBM; double-buffered, so the
+// next element's copies are in flight while this one is summed), and each thread updates its
+// tile with w_c scale z, accumulating one element in FP32 and folding it into double-float
+// (hi + lo) sums.  The CTA writes its tile to partial row (warp * ft_r + range); k_reduce
+// sums the rows of the populated warps in a fixed order.  Each output's summation order
+// (crystallites 0..31 per element, elements in order within a range) depends on neither
+// the tile shape nor the batch, so a crystallite's contribution does not depend on its
+// neighbours.
+constexpr int kFtThreads = 64, kFtR = 16, kFtJmax = 32;
 // 8-byte asynchronous copy global -> shared (cp.async); src_bytes 0 writes zeros
 __device__ __forceinline__ void cp_async8(void *dst, const void *src, int src_bytes) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(uint32_t(__cvta_generic_to_shared(dst))), "l"(src),
                "r"(src_bytes)
                : "memory");
 }
+// Dynamic shared memory of k_fid_tiled: two buffers of 32 crystallites x (4 jt + 4 pt).
+static size_t fid_tiled_smem(int jt, int pt) { return sizeof(float2) * 2 * 32 * 4 * size_t(jt + pt); }
 __global__ void __launch_bounds__(kFtThreads) k_fid_tiled(DevSys s) {
-  __shared__ __align__(16) float2 zs[2][32][kFtJ];  // [buffer][c][j]
-  __shared__ __align__(16) float2 gs[2][32][kFtP];  // [buffer][c][p]
+  extern __shared__ __align__(16) float2 ftsm[];
+  const int JT = 4 * s.ft_jt, PT = 4 * s.ft_pt;
+  float2 *zs = ftsm, *gs = ftsm + 2 * 32 * JT;  // [buffer][c][j], [buffer][c][p]
   __shared__ float ws[32];
   const int tid = threadIdx.x;
   const int g = blockIdx.x;  // group of 32 crystallites in this batch
-  const int npr = (s.gper + kFtP - 1) / kFtP;
+  const int npr = (s.gper + PT - 1) / PT;
   const int pr = blockIdx.y % npr, jr = blockIdx.y / npr, er = blockIdx.z;
-  const int p0 = pr * kFtP, j0 = jr * kFtJ;
-  const int e_lo = int((long(s.ne) * er) / kFtR), e_hi = int((long(s.ne) * (er + 1)) / kFtR);
+  const int p0 = pr * PT, j0 = jr * JT;
+  const int e_lo = int((long(s.ne) * er) / s.ft_r), e_hi = int((long(s.ne) * (er + 1)) / s.ft_r);
   const int c0 = g * 32;
   if (tid < 32) {
     const int c = c0 + tid;
     ws[tid] = c < s.C ? float(s.w[c] * s.scale) : 0.f;
   }
-  const int jt = tid / 16, pt = tid % 16;  // this thread's j's: j0 + 4 jt + a; p's: p0 + 4 pt + b
+  const bool active = tid < s.ft_jt * s.ft_pt;
+  const int jt = active ? tid / s.ft_pt : 0, pt = active ? tid % s.ft_pt : 0;  // j0 + 4 jt + a, p0 + 4 pt + b
   float2 acc[4][4];
   float2 hi[4][4], lo[4][4];
 #pragma unroll
@@ -2052,17 +2172,17 @@ __global__ void __launch_bounds__(kFtThreads) k_fid_tiled(DevSys s) {
 #pragma unroll
     for (int b = 0; b < 4; ++b) hi[a][b] = lo[a][b] = make_float2(0.f, 0.f);
   const float2 *Zb = s.Zf, *Gb = s.Gf;
-  // z (16 x 32) and G (64 x 32) of element e into buffer buf, zeros outside J, gper and C
+  // z (JT x 32) and G (PT x 32) of element e into buffer buf, zeros outside J, gper and C
   auto stage = [&](int e, int buf) {
-    for (int t = tid; t < kFtJ * 32; t += kFtThreads) {
+    for (int t = tid; t < JT * 32; t += kFtThreads) {
       const int jj = t / 32, c = t % 32, j = j0 + jj;
       const bool ok = j < s.J && c0 + c < s.C;
-      cp_async8(&zs[buf][c][jj], ok ? &Zb[at(j * s.ne + e, c0 + c, s.Cpad)] : Zb, ok ? 8 : 0);
+      cp_async8(&zs[(buf * 32 + c) * JT + jj], ok ? &Zb[at(j * s.ne + e, c0 + c, s.Cpad)] : Zb, ok ? 8 : 0);
     }
-    for (int t = tid; t < kFtP * 32; t += kFtThreads) {
+    for (int t = tid; t < PT * 32; t += kFtThreads) {
       const int pp = t / 32, c = t % 32, p = p0 + pp;
       const bool ok = p < s.gper && c0 + c < s.C;
-      cp_async8(&gs[buf][c][pp], ok ? &Gb[at(p * s.ne + e, c0 + c, s.Cpad)] : Gb, ok ? 8 : 0);
+      cp_async8(&gs[(buf * 32 + c) * PT + pp], ok ? &Gb[at(p * s.ne + e, c0 + c, s.Cpad)] : Gb, ok ? 8 : 0);
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
@@ -2076,37 +2196,42 @@ __global__ void __launch_bounds__(kFtThreads) k_fid_tiled(DevSys s) {
       asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     __syncthreads();
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
-    for (int c = 0; c < 32; ++c) {
-      const float w = ws[c];
-      const float4 z01 = *reinterpret_cast<const float4 *>(&zs[buf][c][4 * jt]);
-      const float4 z23 = *reinterpret_cast<const float4 *>(&zs[buf][c][4 * jt + 2]);
-      const float4 g01 = *reinterpret_cast<const float4 *>(&gs[buf][c][4 * pt]);
-      const float4 g23 = *reinterpret_cast<const float4 *>(&gs[buf][c][4 * pt + 2]);
-      const float2 zz[4] = {make_float2(w * z01.x, w * z01.y), make_float2(w * z01.z, w * z01.w),
-                            make_float2(w * z23.x, w * z23.y), make_float2(w * z23.z, w * z23.w)};
-      const float2 gg[4] = {make_float2(g01.x, g01.y), make_float2(g01.z, g01.w), make_float2(g23.x, g23.y),
-                            make_float2(g23.z, g23.w)};
+    if (active) {
 #pragma unroll
       for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = cfma(zz[a], gg[b], acc[a][b]);
-    }
+        for (int b = 0; b < 4; ++b) acc[a][b] = make_float2(0.f, 0.f);
+      const float2 *zrow = zs + buf * 32 * JT + 4 * jt, *grow = gs + buf * 32 * PT + 4 * pt;
+#pragma unroll 2
+      for (int c = 0; c < 32; ++c) {
+        const float w = ws[c];
+        const float4 z01 = *reinterpret_cast<const float4 *>(zrow + c * JT);
+        const float4 z23 = *reinterpret_cast<const float4 *>(zrow + c * JT + 2);
+        const float4 g01 = *reinterpret_cast<const float4 *>(grow + c * PT);
+        const float4 g23 = *reinterpret_cast<const float4 *>(grow + c * PT + 2);
+        const float2 zz[4] = {make_float2(w * z01.x, w * z01.y), make_float2(w * z01.z, w * z01.w),
+                              make_float2(w * z23.x, w * z23.y), make_float2(w * z23.z, w * z23.w)};
+        const float2 gg[4] = {make_float2(g01.x, g01.y), make_float2(g01.z, g01.w), make_float2(g23.x, g23.y),
+                              make_float2(g23.z, g23.w)};
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const float2 x = dfv_add(make_float2(hi[a][b].x, lo[a][b].x), make_float2(acc[a][b].x, 0.f));
-        const float2 y = dfv_add(make_float2(hi[a][b].y, lo[a][b].y), make_float2(acc[a][b].y, 0.f));
-        hi[a][b] = make_float2(x.x, y.x), lo[a][b] = make_float2(x.y, y.y);
+          for (int b = 0; b < 4; ++b) acc[a][b] = cfma(zz[a], gg[b], acc[a][b]);
       }
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          const float2 x = dfv_add(make_float2(hi[a][b].x, lo[a][b].x), make_float2(acc[a][b].x, 0.f));
+          const float2 y = dfv_add(make_float2(hi[a][b].y, lo[a][b].y), make_float2(acc[a][b].y, 0.f));
+          hi[a][b] = make_float2(x.x, y.x), lo[a][b] = make_float2(x.y, y.y);
+        }
+    }
     __syncthreads();  // the next stage() overwrites this buffer
     buf ^= 1;
   }
-  const long row = long(s.warp_base + g) * kFtR + er;
+  if (!active) return;
+  const long row = long(s.warp_base + g) * s.ft_r + er;
 #pragma unroll
   for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -2205,6 +2330,7 @@ struct JobImpl {
   BlockLayout L;
   int nint = 0, nq = 0, nr = 0, ne = 0, npq = 0, npr = 0;
   int Cb = 0, nbatch = 0, nwarps_total = 0;
+  int ft_jt = 1, ft_pt = 1, ft_r = 1;  // k_fid_tiled tile shape and element ranges
   std::vector<std::vector<int>> blocks_by_size;  // size -> list of block indices (size <= kMaxBlock)
   std::vector<int> big_blocks;                   // blocks kMaxBlock < b <= kMaxBigBlock
   std::vector<BigPair> big_pairs;                // Q/R pairs whose largest block is one of those
@@ -2495,6 +2621,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   J.ne = int(eq.size());
   J.J = (p.npts + (J.p2p ? J.pb : J.n) - 1) / (J.p2p ? J.pb : J.n);
+  {  // k_fid_tiled: up to kFtJmax j's per tile, then as few p tiles as fit 64 threads, each
+     // as narrow as it can be; element ranges of at least 64 elements (a function of ne only)
+    const int gp = J.p2p ? J.pb : J.n;
+    J.ft_jt = std::max(1, std::min(kFtJmax / 4, (J.J + 3) / 4));
+    const int pt_max = std::max(1, kFtThreads / J.ft_jt);
+    const int ntile = (gp + 4 * pt_max - 1) / (4 * pt_max);
+    J.ft_pt = std::max(1, (gp + 4 * ntile - 1) / (4 * ntile));
+    J.ft_r = std::max(1, std::min(kFtR, J.ne / 64));
+  }
   // crystallites, expanded by the gamma loop (compute.h:294-306: fid summed over q)
   J.C = pw.size();
   J.Ceff = J.C * J.gammaloop;
@@ -2805,7 +2940,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   } else {
     J.Q.alloc(nQ), J.R.alloc(nR), J.G.alloc(nG), J.Z.alloc(nZ);
   }
-  J.partial.alloc(size_t(J.nwarps_total) * (J.mixed ? kFtR : 1) * p.npts);
+  J.partial.alloc(size_t(J.nwarps_total) * (J.mixed ? J.ft_r : 1) * p.npts);
   if (J.huge_ws_bytes) {
     J.huge_ws.alloc(J.huge_ws_bytes / sizeof(double2));
     J.hfk.alloc(size_t(J.huge_items) * std::max(J.nint, 1));
@@ -2864,7 +2999,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     if (J.p2p) J.stage_fl[5] = Ce * 16.0 * J.pb * J.ne;  // two complex products per (k, element)
   }
   J.stage_fl[6] = Ce * 8.0 * p.npts * J.ne;                     // FID reconstruction
-  J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total * (J.mixed ? kFtR : 1);  // compensated powder sum
+  J.stage_fl[7] = 4.0 * p.npts * J.nwarps_total * (J.mixed ? J.ft_r : 1);  // compensated powder sum
   J.flops = 0;
   for (double f : J.stage_fl) J.flops += f;
   // static part of the device description
@@ -2897,12 +3032,15 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
       g_upload_counter = nullptr;
       s.tw = J.tw.p;
       s.twf = J.twf.p;
-      const int cgm = std::max(1, std::min(8, 2048 / s.M));
-      size_t shm_max = sizeof(double2) * size_t(s.M) * 2 * cgm + fave_twist_bytes(s, cgm);
+      // one cap for every job (jobs on other threads launch these kernels concurrently): the
+      // largest M (4096, for 2048 steps) with its twist tables
+      const size_t shm_max = sizeof(double2) * 4096 * 2 + sizeof(double2) * 2 * (8 + 4096 / 8);
       for (auto f : {k_fave_fft<8, double2>, k_fave_fft<4, double2>, k_fave_fft<2, double2>, k_fave_fft<1, double2>,
                      k_fave_fft<8, float2>, k_fave_fft<4, float2>, k_fave_fft<2, float2>, k_fave_fft<1, float2>})
         CUDA_OK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm_max)));
     }
+    CUDA_OK(cudaFuncSetAttribute(k_fid_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 int(fid_tiled_smem(kFtJmax / 4, kFtThreads))));
   } else {  // no Fave: the point-to-point terms come from Q/R and the Floquet phases
     s.fave_twist = 0, s.logM = 0, s.M = 0, s.fave_method = 0;
     s.tw = nullptr, s.twf = nullptr;
@@ -2911,6 +3049,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.is_static = J.is_static, s.dt = J.dt, s.srp = J.srp.p, s.seo = J.seo.p;
   s.scale = J.is_static ? 1.0 : double(1. / double(J.n / (J.rosym ? 2 : 1)));
   s.gper = J.n, s.p2p = J.p2p, s.pb = J.pb, s.pf = J.pf, s.psub = J.psub;
+  s.ft_jt = J.ft_jt, s.ft_pt = J.ft_pt, s.ft_r = J.ft_r;
   if (J.p2p) {  // fid = sum_c w_c Tr(rho_c det) / Tr(det det^H)  (sequencerun_funcs.cc:624-645)
     double dd = 0;
     for (const auto &v : det.a) dd += std::norm(v);
@@ -3370,8 +3509,10 @@ void Job::run() {
     // per warp, and rows it does not cover (p >= n or k >= npts) do not exist
     mark_begin(J, 6);
     if (s.mixed) {
-      const unsigned npr = unsigned((s.gper + kFtP - 1) / kFtP), njr = unsigned((J.J + kFtJ - 1) / kFtJ);
-      k_fid_tiled<<<dim3(unsigned(Cp / 32), npr * njr, kFtR), kFtThreads, 0, st>>>(s);
+      const unsigned npr = unsigned((s.gper + 4 * s.ft_pt - 1) / (4 * s.ft_pt));
+      const unsigned njr = unsigned((J.J + 4 * s.ft_jt - 1) / (4 * s.ft_jt));
+      k_fid_tiled<<<dim3(unsigned(Cp / 32), npr * njr, unsigned(s.ft_r)), kFtThreads,
+                    fid_tiled_smem(s.ft_jt, s.ft_pt), st>>>(s);
     } else {
       launch_fid<double2>(s, Cp, J.J, st);
     }
@@ -3380,7 +3521,7 @@ void Job::run() {
   }
   mark_begin(J, 7);
   // only warps that hold crystallites: the sum is then independent of the batch size
-  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, (J.Ceff + 31) / 32 * (J.mixed ? kFtR : 1),
+  k_reduce<<<(J.P.npts + 255) / 256, 256, 0, st>>>(J.partial.p, (J.Ceff + 31) / 32 * (J.mixed ? J.ft_r : 1),
                                                     J.P.npts, J.fid.p);
   ++J.launches;
   mark_end(J, 7, 1);
@@ -3635,7 +3776,7 @@ static size_t fixed_bytes(const Powder &pw, const FidParams &p) {
   long n = p.wr != 0.0 ? long(std::floor(p.sw / p.wr + 0.5)) : 1;
   long g = (n >= 1 && n <= 10) ? std::max(1L, 10 / n) : 1;
   size_t ceff = size_t(pw.size()) * size_t(g) + 32;
-  // warp partials: kFtR rows per warp in the mixed form (k_fid_tiled's element ranges)
+  // warp partials: up to kFtR rows per warp in the mixed form (k_fid_tiled's element ranges)
   return (size_t(8) << 20) + 2 * ceff * 11 * sizeof(double) +
          (ceff / 32 + 1) * size_t(p.precision == 1 ? kFtR : 1) * size_t(std::max(p.npts, 0)) * sizeof(double2);
 }
