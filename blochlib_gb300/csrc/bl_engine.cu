@@ -1110,45 +1110,61 @@ __global__ void __launch_bounds__(kThreads) k_dyson(DevSys s, const int *__restr
   }
 }
 
-// The mixed form's Dyson product in double-float: one thread per (crystallite, block, column),
-// U_i and A_{i+1} as float4 double-float elements; each element of U_i x is four compensated
-// dot products (re and im, each of a U-hi/lo x-hi/lo expansion).
+// The mixed form's Dyson product in double-float: one lane per (crystallite, block, column,
+// row), U_i and A_{i+1} as float4 double-float elements; each element of U_i x is four
+// compensated dot products (re and im, each of a U-hi/lo x-hi/lo expansion).
 template <int B>
 __global__ void __launch_bounds__(kThreads) k_dyson_df(DevSys s, const int *__restrict__ blist, int nblist) {
-  long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  int c = int(tid % s.Cpad);
-  long rest = tid / s.Cpad;
-  if (rest >= long(nblist) * B) return;
-  int j = int(rest % B);
-  int k = blist[rest / B];
-  if (c >= s.C) return;
+  // G lanes per (crystallite, column j): lane r < B owns row r of the column; a warp holds
+  // 32/G consecutive crystallites of one (block, column), so the U rows it loads are whole
+  // 16-byte runs of consecutive crystallites.  y_r = sum_l U_rl x_l, l ascending, each x_l
+  // broadcast from lane l of the group: the same sums in the same order as one thread per
+  // column, with B times the threads on the chain of n dependent steps.  The next step's U
+  // row is loaded while this step is summed.
+  constexpr int G = B <= 1 ? 1 : B <= 2 ? 2 : B <= 4 ? 4 : 8;
+  static_assert(B <= 8, "k_dyson_df takes blocks of at most 8");
+  const long tid = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int r = int(tid % G);
+  const long rest = tid / G;
+  const int c = int(rest % s.Cpad);
+  const long rest2 = rest / s.Cpad;
+  if (rest2 >= long(nblist) * B) return;  // warp-uniform (G Cpad is a multiple of 32)
+  const int j = int(rest2 % B), k = blist[rest2 / B];
   const int bp = s.bpoff[k];
-  float4 x[B];
-#pragma unroll
-  for (int r = 0; r < B; ++r) x[r] = make_float4(r == j ? 1.f : 0.f, 0.f, 0.f, 0.f);
-  for (int i = 0; i < s.n; ++i) {
+  const bool own = r < B;
+  const int lane0 = int(threadIdx.x & 31) & ~(G - 1);
+  float4 u[B], un[B];
+  auto load_row = [&](int i, float4(&d)[B]) {
     const float4 *Ub = reinterpret_cast<const float4 *>(s.U + size_t(i) * s.S2 * s.Cpad);
-    float4 y[B];
 #pragma unroll
-    for (int r = 0; r < B; ++r) {
-      DfAcc re = {0.f, 0.f}, im = {0.f, 0.f};
+    for (int l = 0; l < B; ++l) d[l] = own ? Ub[at(bp + r * B + l, c, s.Cpad)] : make_float4(0.f, 0.f, 0.f, 0.f);
+  };
+  load_row(0, u);
+  float4 x = make_float4(r == j ? 1.f : 0.f, 0.f, 0.f, 0.f);
+  for (int i = 0; i < s.n; ++i) {
+    if (i + 1 < s.n) load_row(i + 1, un);
+    DfAcc re = {0.f, 0.f}, im = {0.f, 0.f};
 #pragma unroll
-      for (int l = 0; l < B; ++l) {
-        const float4 u = Ub[at(bp + r * B + l, c, s.Cpad)];
-        df_dot(re, u.x, u.z, x[l].x, x[l].z);    // ur xr
-        df_dot(re, -u.y, -u.w, x[l].y, x[l].w);  // - ui xi
-        df_dot(im, u.x, u.z, x[l].y, x[l].w);    // ur xi
-        df_dot(im, u.y, u.w, x[l].x, x[l].z);    // ui xr
-      }
-      const float2 a = df_fin(re), b = df_fin(im);
-      y[r] = make_float4(a.x, b.x, a.y, b.y);
+    for (int l = 0; l < B; ++l) {
+      float4 xl;
+      xl.x = __shfl_sync(0xffffffffu, x.x, lane0 + l);
+      xl.y = __shfl_sync(0xffffffffu, x.y, lane0 + l);
+      xl.z = __shfl_sync(0xffffffffu, x.z, lane0 + l);
+      xl.w = __shfl_sync(0xffffffffu, x.w, lane0 + l);
+      const float4 uu = u[l];
+      df_dot(re, uu.x, uu.z, xl.x, xl.z);    // ur xr
+      df_dot(re, -uu.y, -uu.w, xl.y, xl.w);  // - ui xi
+      df_dot(im, uu.x, uu.z, xl.y, xl.w);    // ur xi
+      df_dot(im, uu.y, uu.w, xl.x, xl.z);    // ui xr
     }
-    float4 *Ab = reinterpret_cast<float4 *>(s.A + size_t(i) * s.S2 * s.Cpad);
-#pragma unroll
-    for (int r = 0; r < B; ++r) {
-      x[r] = y[r];
-      Ab[at(bp + r * B + j, c, s.Cpad)] = y[r];
+    const float2 a = df_fin(re), b = df_fin(im);
+    x = make_float4(a.x, b.x, a.y, b.y);
+    if (own && c < s.C) {
+      float4 *Ab = reinterpret_cast<float4 *>(s.A + size_t(i) * s.S2 * s.Cpad);
+      Ab[at(bp + r * B + j, c, s.Cpad)] = x;
     }
+#pragma unroll
+    for (int l = 0; l < B; ++l) u[l] = un[l];
   }
 }
 
@@ -1743,20 +1759,24 @@ __device__ void fft_first_pass(C *X, C *Y, int M, int logM, const C *__restrict_
   __syncthreads();
 }
 
-// z^j rounded to float for z = e^{a + i b} (l = (a, b) in FP64): the phase j b reduced
-// modulo 2 pi in FP64 against a two-term 2 pi (Cody-Waite), the reduced phase split into a
-// float and its float remainder, then float sincos with a first-order correction for the
-// remainder and a float exp of j a.  Error a few float ulp (the result is stored as float).
-__device__ __forceinline__ float2 z_pow_f(double2 l, int j) {
-  constexpr double kInv2Pi = 0.15915494309189535, k2PiHi = 6.283185307179586, k2PiLo = 2.4492935982947064e-16;
-  const double ph = double(j) * l.y;
-  const double k = rint(ph * kInv2Pi);
-  const double r = fma(-k, k2PiLo, fma(-k, k2PiHi, ph));
-  const float rf = float(r), rl = float(r - double(rf));
+// z^j in float for z = e^{a + i b}, from e = (a, b_hi, b_lo): b = b_hi + b_lo with |b| < 2 pi
+// (a difference of two principal-branch arguments).  The phase j b is j b_hi (with its exact
+// rounding error, by fma) plus j b_lo, reduced modulo 2 pi against a three-term float 2 pi
+// (Cody-Waite: 6.28125 has 8 significant bits, so k 6.28125 is exact); then float sincos
+// with the small remainder added to the argument and a float exp of j a.  All float
+// arithmetic; error a few float ulp.
+__device__ __forceinline__ float2 z_pow_f(float4 e, int j) {
+  constexpr float kInv2Pi = 0.15915494f, kP1 = 6.28125f, kP2 = 0.0019353071693331003f, kP3 = 1.0253131677018246e-11f;
+  const float jf = float(j);
+  const float p = jf * e.y, pe = __fmaf_rn(jf, e.y, -p), corr = __fmaf_rn(jf, e.z, pe);
+  const float k = rintf(p * kInv2Pi);
+  float r = __fmaf_rn(-k, kP1, p);
+  r = __fmaf_rn(-k, kP2, r);
+  r = __fmaf_rn(-k, kP3, r) + corr;
   float sn, cs;
-  sincosf(rf, &sn, &cs);
-  const float m = expf(float(double(j) * l.x));
-  return make_float2(m * fmaf(-rl, sn, cs), m * fmaf(rl, cs, sn));
+  sincosf(r, &sn, &cs);
+  const float m = expf(jf * e.x);
+  return make_float2(m * cs, m * sn);
 }
 
 // Fave by FFT.  One CTA per (element e, group of CG crystallites).  With q zero outside
@@ -1794,16 +1814,19 @@ __global__ void __launch_bounds__(128) k_fave_fft(DevSys s) {
   // cexp and three products (error a few ulp).  Single-precision form (the powers are stored
   // as float): the exponent of z^j in FP64, then z_pow_f per power (after the first pass).
   constexpr bool kF = std::is_same<C, float2>::value;
-  __shared__ double2 zexp[CG];
-  if constexpr (kF) {
+  __shared__ float4 zexp[CG];
+  if constexpr (kF) {  // z = e^{n tau (i w)} = e^{d} with d = l_r - l_s, chopped as w is
     for (int cc = threadIdx.x; cc < CG; cc += blockDim.x) {
       const int c = c0 + cc;
-      double2 w = cmk(0, 0);
+      float4 ze = make_float4(0.f, 0.f, 0.f, 0.f);
       if (c < s.C) {
-        double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
-        w = cmk(chop1(d.y / nt, 1e-10), chop1(-d.x / nt, 1e-10));
+        const double2 d = csub(s.L[at(s.erg[e], c, s.Cpad)], s.L[at(s.esg[e], c, s.Cpad)]);
+        const double thr = 1e-10 * nt;
+        const double dx = fabs(d.x) < thr ? 0.0 : d.x, dy = fabs(d.y) < thr ? 0.0 : d.y;
+        const float yh = float(dy);
+        ze = make_float4(float(dx), yh, float(dy - double(yh)), 0.f);
       }
-      zexp[cc] = cmk(-nt * w.y, nt * w.x);
+      zexp[cc] = ze;
     }
   } else {
     constexpr int kZrun = 4;
@@ -3114,7 +3137,10 @@ static void launch_block_kernels(JobImpl &J, DevSys &s, int stage) {
       else k_step_prop<B><<<grid_for(Cp * nl * s.n), kThreads, 0, st>>>(s, bl, nl);
       break;
     case 1:
-      if (s.mixed) k_dyson_df<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl);
+      if (s.mixed) {
+        constexpr int G = B <= 1 ? 1 : B <= 2 ? 2 : B <= 4 ? 4 : 8;
+        k_dyson_df<B><<<grid_for(Cp * nl * B * G), kThreads, 0, st>>>(s, bl, nl);
+      }
       else k_dyson<B><<<grid_for(Cp * nl * B), kThreads, 0, st>>>(s, bl, nl);
       break;
     case 2:
