@@ -2842,6 +2842,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
             sm_step = std::max(sm_step, tc_step_smem(L.size[k])), sm_dy = std::max(sm_dy, tc_dyson_smem(L.size[k]));
         attr((const void *)k_tc_step, sm_step);
         attr((const void *)k_tc_dyson, sm_dy);
+        attr((const void *)k_tc_dyson_stk, tc_dyson_stk_smem(64));
       }
       attr((const void *)k_big_eigframe<1, double2>, smem_mat);
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
@@ -3366,7 +3367,10 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
         break;
       case 1:
         if (J.tc && b >= tc::kMinB) {  // exact-slice BF16 products on the tensor cores
-          k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc_dyson_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
+          if (tc::up16(b) <= 64)  // re and im stacked in one M = 128 tile
+            k_tc_dyson_stk<<<unsigned(s.C), tc::kTcThreads, tc_dyson_stk_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
+          else
+            k_tc_dyson<<<unsigned(s.C), tc::kTcThreads, tc_dyson_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
         } else if (s.mixed) {
           if (nt1) k_big_dyson_df<1><<<unsigned(s.C), th, smat, st>>>(s, k);
           else k_big_dyson_df<2><<<unsigned(s.C), th, smat, st>>>(s, k);

@@ -195,8 +195,8 @@ __device__ __forceinline__ float2 sum3(float a, float b, float c) {
 // `col` (level 0, 1, 2+3 at col, col + R, col + 2R): A tile planes at a (plane stride pl
 // bytes), B tile planes at b, R = up16(b) output columns, R / 16 K steps.  `accumulate`
 // adds to what the accumulators hold instead of starting them.
-__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint32_t a, uint32_t b, uint32_t pl,
-                                              int R, bool negA, bool accumulate) {
+__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint32_t a, uint32_t plA, uint32_t b,
+                                              uint32_t plB, int R, bool negA, bool accumulate) {
   const uint32_t id = idesc_bf16(R, negA);
   const int sp[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3}, tp[10] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
   const int lev[10] = {0, 1, 1, 2, 2, 2, 2, 2, 2, 2};
@@ -204,10 +204,14 @@ __device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint3
   for (int q = 0; q < 10; ++q) {
     const uint32_t d = tmem + col + uint32_t(lev[q] * R);
     const bool first = !accumulate && (q == 0 || q == 1 || q == 3);
-    const uint32_t a0 = a + uint32_t(sp[q]) * pl, b0 = b + uint32_t(tp[q]) * pl;
+    const uint32_t a0 = a + uint32_t(sp[q]) * plA, b0 = b + uint32_t(tp[q]) * plB;
     for (int kk = 0; kk < R / 16; ++kk)
       mma(d, sdesc(a0 + kk * 256, R), sdesc(b0 + kk * 256, R), id, (first && kk == 0) ? 0u : 1u);
   }
+}
+__device__ __forceinline__ void issue_product(uint32_t tmem, uint32_t col, uint32_t a, uint32_t b, uint32_t pl,
+                                              int R, bool negA, bool accumulate) {
+  issue_product(tmem, col, a, pl, b, pl, R, negA, accumulate);
 }
 
 // -1 / (k (k + 1)) as double-float for the Horner steps (k = 1 .. 31), folded at compile time
@@ -628,6 +632,139 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k,
           const int o = tc::tix(m, c0, R);
           tc::store_row8(Ar, pe, o, rh, rl);
           tc::store_row8(Ai, pe, o, ih, il);
+        }
+      }
+    }
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+  }
+  if (ok && tid == 0)  // 4 real products per step
+    atomicAdd(s.tc_flops + 1, 80ull * (unsigned long long)s.n * (unsigned long long)(b * b * b));
+  if (!ok) {
+    if (tid == 0) atomicOr(s.status, kTcTimeout);
+    tc::wait_parity(&mbar[0], ph[0]);  // bounded: let MMAs and the copy in flight drain
+    tc::wait_parity(&mbar[1], ph[1]);
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
+// ------------------------------------------------------------------ Dyson product, stacked
+// The same product for blocks with up16(b) = R <= 64, with both halves of the M = 128 tile
+// holding rows: A1 = [Ar^T; Ai^T] and A2 = [Ai^T; -Ar^T] (R rows each, rows 2R.. zero), so
+//   D = A1 C + A2 S = [Ar^T C + Ai^T S; Ai^T C - Ar^T S] = [re; im]
+// in two stacked real products (20 slice pairs) instead of four, and every TMEM lane
+// quarter holds rows for the epilogue: lane m < R is row m of re, lane R + m row m of im.
+// Each epilogue lane writes its row's slices into both stacked tiles (negated in A2's lower
+// half) and its half of the double-float A_{i+1} element (re: .x and .z, im: .y and .w of the
+// float4 re.hi, im.hi, re.lo, im.lo).  Shared memory: A1, A2 (128 rows each), the U slab.
+__host__ __device__ constexpr size_t tc_stk_plane_bytes(int b) { return size_t(16) * tc::sbo_bytes(tc::up16(b)); }
+__host__ __device__ constexpr size_t tc_dyson_stk_smem(int b) {
+  return 2 * 4 * tc_stk_plane_bytes(b) + tc::slab_bytes(b) + 1024;
+}
+
+__global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson_stk(DevSys s, int k, const unsigned char *slab0) {
+  using tc::kTcThreads;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ uint32_t tbase;
+  __shared__ __align__(8) uint64_t mbar[2];  // 0: MMAs done, 1: U slab arrived
+  const int c = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int b = s.bs[k], bp = s.bpoff[k];
+  const int R = tc::up16(b);
+  const int peA = int(tc_stk_plane_bytes(b) / 2);  // stacked plane stride, BF16 units
+  const int ncols = tc::pow2_cols(3 * R);
+  unsigned char *base = tsm + ((1024 - (tc::saddr(tsm) & 1023)) & 1023);
+  __nv_bfloat16 *A1 = reinterpret_cast<__nv_bfloat16 *>(base);
+  __nv_bfloat16 *A2 = reinterpret_cast<__nv_bfloat16 *>(base + 4 * tc_stk_plane_bytes(b));
+  unsigned char *Us = base + 8 * tc_stk_plane_bytes(b);  // C tile, then S tile
+  const uint32_t slab = uint32_t(tc::slab_bytes(b));
+  const unsigned char *src = slab0 + size_t(c) * s.n * tc::slab_bytes(b);
+  {  // A_0^T = I: A1 = [I; 0], A2 = [0; -I] (256 = 1 at natural scale, level-0 plane)
+    uint4 *z = reinterpret_cast<uint4 *>(base);
+    const int n16 = int(8 * tc_stk_plane_bytes(b) / 16);
+    for (int e = tid; e < n16; e += kTcThreads) z[e] = make_uint4(0, 0, 0, 0);
+  }
+  __syncthreads();
+  for (int r = tid; r < b; r += kTcThreads) {
+    A1[tc::tix(r, r, R)] = __float2bfloat16_rn(256.f);
+    A2[tc::tix(R + r, r, R)] = __float2bfloat16_rn(-256.f);
+  }
+  if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+  if (tid == 0) {
+    tc::mbar_init(&mbar[0]), tc::mbar_init(&mbar[1]);
+    tc::bulk_load(Us, src, slab, &mbar[1]);
+  }
+  tc::fence_smem_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tbase;
+  const uint32_t aA1 = tc::saddr(A1), aA2 = tc::saddr(A2), aC = tc::saddr(Us);
+  const uint32_t aS = aC + uint32_t(tc::tile_bytes(b)), plB = uint32_t(tc::plane_bytes(b));
+  const uint32_t plA = uint32_t(tc_stk_plane_bytes(b));
+  const int q4 = warp & 3, part = warp >> 2;  // lane quarter; 8-column chunks part, part+4, ...
+  const int L = 32 * q4 + lane;               // TMEM lane: re row L (L < R) or im row L - R
+  const bool is_im = L >= R, live = L < 2 * R;
+  const int m = is_im ? L - R : L;
+  float *Af = reinterpret_cast<float *>(s.A);
+  uint32_t ph[2] = {0u, 0u};
+  bool ok = true;
+  for (int i = 0; i < s.n; ++i) {
+    {  // U_i's slab must have landed
+      const bool got = tc::wait_parity(&mbar[1], ph[1]);
+      ph[1] ^= 1u;
+      if (!__syncthreads_and(got)) {
+        ok = false;
+        break;
+      }
+    }
+    if (tid == 0) {
+      tc::fence_after();
+      tc::issue_product(tmem, 0, aA1, plA, aC, plB, R, false, false);  // [Ar^T C; Ai^T C]
+      tc::issue_product(tmem, 0, aA2, plA, aS, plB, R, false, true);   // + [Ai^T S; -Ar^T S]
+      tc::commit(&mbar[0]);
+    }
+    {
+      const bool done = tc::wait_parity(&mbar[0], ph[0]);
+      ph[0] ^= 1u;
+      if (!__syncthreads_and(done)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+    }
+    // U_{i+1} streams in while the epilogue runs (the products no longer read the slab)
+    if (tid == 0 && i + 1 < s.n) tc::bulk_load(Us, src + size_t(i + 1) * slab, slab, &mbar[1]);
+    float *Ab = Af + size_t(i) * s.S2 * s.Cpad * 4;
+    if (32 * q4 < 2 * R) {
+      for (int c0 = 8 * part; c0 < R; c0 += 32) {
+        float v0[8], v1[8], v2[8];
+        const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + uint32_t(c0);
+        tc::ld8(ta, v0);
+        tc::ld8(ta + uint32_t(R), v1);
+        tc::ld8(ta + uint32_t(2 * R), v2);
+        tc::wait_ld();
+        if (live) {
+          float h[8], l[8], nh[8], nl[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int n = c0 + j;
+            float2 v = make_float2(0.f, 0.f);
+            if (m < b && n < b) {
+              const float2 p = tc::sum3(v0[j], v1[j], v2[j]);
+              v = make_float2(p.x * 0x1p-16f, p.y * 0x1p-16f);
+              float *e = Ab + 4 * big_at(s, b, bp, n * b + m, c) + (is_im ? 1 : 0);
+              e[0] = v.x, e[2] = v.y;
+            }
+            h[j] = v.x, l[j] = v.y, nh[j] = -v.x, nl[j] = -v.y;
+          }
+          // re row m: A1 row m, A2 row R + m negated; im row m: A1 row R + m, A2 row m
+          tc::store_row8(A1, peA, tc::tix(is_im ? R + m : m, c0, R), h, l);
+          if (is_im) tc::store_row8(A2, peA, tc::tix(m, c0, R), h, l);
+          else tc::store_row8(A2, peA, tc::tix(R + m, c0, R), nh, nl);
         }
       }
     }
