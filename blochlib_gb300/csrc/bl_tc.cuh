@@ -287,33 +287,62 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
     for (int kk = tid; kk < s.nint; kk += kTcThreads) fk[kk] = fk2[at(i * s.nint + kk, c, s.Cpad)];
   }
   __syncthreads();
-  // H (double-float) into the fourth tile as scratch; row sums of |H| for the norm
+  // H (double-float) into the fourth tile as scratch.  The block's operator non-zeros (CSR
+  // rows bp .. bp + bb) are first copied into the three other tiles, which are free until X
+  // is sliced: coalesced, independent loads, after which each entry's walk over its terms
+  // (36 on a diagonal of eight coupled spins) reads shared memory instead of waiting on L2.
   float2 *H = reinterpret_cast<float2 *>(Bf[3]);
   const float2 *Hcb = s.Hc_df + bp;
-  for (int e = tid; e < bb; e += kTcThreads) {
-    float2 h = Hcb[e];
-    for (int j = s.tk_ptr[bp + e]; j < s.tk_ptr[bp + e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[s.tk_term[j]], s.tk_val[j]));
-    H[e] = h;
-  }
-  __syncthreads();
-  for (int p = tid; p < b; p += kTcThreads) {
-    float rs = 0.f;
-    for (int q = 0; q < b; ++q) rs += fabsf(H[p * b + q].x);
-    red[p] = rs;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    float nrm = 0.f;
-    for (int p = 0; p < b; ++p) nrm = fmaxf(nrm, red[p]);
-    nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
-    int sq = 0;
-    if (nrm > 1.f) {
-      frexpf(nrm, &sq);  // nrm < 2^sq
-      sq = min(sq, 60);
+  {
+    const int j0 = s.tk_ptr[bp], nz = s.tk_ptr[bp + bb] - j0;
+    const size_t need = size_t(bb + 1 + nz) * sizeof(int) + size_t(nz) * sizeof(float2) + 16;
+    if (need <= 3 * tc::tile_bytes(b)) {
+      int *sp = reinterpret_cast<int *>(Bf[0]);
+      float2 *sv = reinterpret_cast<float2 *>(sp + ((bb + 1 + nz + 3) & ~3));
+      int *st = sp + bb + 1;
+      for (int x = tid; x <= bb; x += kTcThreads) sp[x] = s.tk_ptr[bp + x] - j0;
+      for (int x = tid; x < nz; x += kTcThreads) st[x] = s.tk_term[j0 + x], sv[x] = s.tk_val[j0 + x];
+      __syncthreads();
+      for (int e = tid; e < bb; e += kTcThreads) {
+        float2 h = Hcb[e];
+        for (int j = sp[e]; j < sp[e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[st[j]], sv[j]));
+        H[e] = h;
+      }
+    } else {
+      for (int e = tid; e < bb; e += kTcThreads) {
+        float2 h = Hcb[e];
+        for (int j = s.tk_ptr[bp + e]; j < s.tk_ptr[bp + e + 1]; ++j)
+          h = dfv_add(h, dfv_mul(fk[s.tk_term[j]], s.tk_val[j]));
+        H[e] = h;
+      }
     }
-    scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
-    nsq = sq;
-    nterms = tc::taylor_degree_tc(ldexpf(nrm, -sq));
+  }
+  __syncthreads();
+  // row sums of |H| (a warp per row, lanes over the columns), then their maximum: the norm
+  for (int p = warp; p < b; p += kTcThreads / 32) {
+    float rs = 0.f;
+    for (int q = lane; q < b; q += 32) rs += fabsf(H[p * b + q].x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+    if (lane == 0) red[p] = rs;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    float nrm = 0.f;
+    for (int p = lane; p < b; p += 32) nrm = fmaxf(nrm, red[p]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+    if (lane == 0) {
+      nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
+      int sq = 0;
+      if (nrm > 1.f) {
+        frexpf(nrm, &sq);  // nrm < 2^sq
+        sq = min(sq, 60);
+      }
+      scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
+      nsq = sq;
+      nterms = tc::taylor_degree_tc(ldexpf(nrm, -sq));
+    }
   }
   __syncthreads();
   const int sq = nsq, K = nterms;
