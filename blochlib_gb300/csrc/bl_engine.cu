@@ -192,7 +192,7 @@ struct DevSys {
   const float2 *Tk_df, *Hc_df;
   // the same operators by element for the tensor-core step: element e (packed block index)
   // holds entries [tk_ptr[e], tk_ptr[e+1]) of (term, double-float value), terms ascending
-  const int *tk_ptr, *tk_term;
+  const int *tk_ptr, *tk_term, *tk_order;
   const float2 *tk_val;
   int fk_df;
   float2 tpdf;  // 2 pi tau as double-float
@@ -2377,7 +2377,7 @@ struct JobImpl {
   DevBuf<double> fkc;                      // k_coef's term coefficients (small blocks)
   DevBuf<double2> frames;                  // rf schedule: per chunk frame (permuted index)
   DevBuf<float2> Tk_df, Hc_df;             // mixed form: double-float operators and constant parts
-  DevBuf<int> tk_ptr, tk_term;             // tensor-core step: the operators' non-zeros by element
+  DevBuf<int> tk_ptr, tk_term, tk_order;  // tensor-core step: the operators' non-zeros by element
   DevBuf<float2> tk_val;
   DevBuf<double2> Dblk, Rhoblk;
   DevBuf<double2> U, A, VF, Lb, Q, R, G, Z, partial, fid, tw;
@@ -2918,7 +2918,19 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         }
       }
       ptr[L.S2] = int(term.size());
+      // per block, its elements by descending term count (ties in element order): the
+      // step's H build visits them in this order, so a warp's lanes walk similar lengths
+      std::vector<int> order(size_t(L.S2), 0);
+      for (size_t kb = 0; kb < L.size.size(); ++kb) {
+        const int b = L.size[kb], bp = L.poff[kb];
+        int *o = order.data() + bp;
+        for (int e = 0; e < b * b; ++e) o[e] = e;
+        std::stable_sort(o, o + b * b, [&](int x, int y) {
+          return ptr[bp + x + 1] - ptr[bp + x] > ptr[bp + y + 1] - ptr[bp + y];
+        });
+      }
       J.tk_ptr.upload(ptr, st), J.tk_term.upload(term, st), J.tk_val.upload(val, st);
+      J.tk_order.upload(order, st);
     }
   }
   if (sched) {  // per chunk: the rf frame of each permuted index (1 where a chunk has none)
@@ -3087,7 +3099,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   s.hc_chunks = sched ? J.pb : 0;
   s.frames = J.frames.n ? J.frames.p : nullptr;
   s.Tk_df = J.Tk_df.p, s.Hc_df = J.Hc_df.p;
-  s.tk_ptr = J.tk_ptr.p, s.tk_term = J.tk_term.p, s.tk_val = J.tk_val.p;
+  s.tk_ptr = J.tk_ptr.p, s.tk_term = J.tk_term.p, s.tk_val = J.tk_val.p, s.tk_order = J.tk_order.p;
   s.fk_df = (J.mixed && p.step_method == 1 && use_fk) ? 1 : 0;
   {
     const double tp = J.tau * kPi2;

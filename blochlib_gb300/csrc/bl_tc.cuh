@@ -295,16 +295,27 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
   const float2 *Hcb = s.Hc_df + bp;
   {
     const int j0 = s.tk_ptr[bp], nz = s.tk_ptr[bp + bb] - j0;
-    const size_t need = size_t(bb + 1 + nz) * sizeof(int) + size_t(nz) * sizeof(float2) + 16;
+    const size_t need = size_t(2 * bb + 1 + nz) * sizeof(int) + size_t(nz) * sizeof(float2) + 16;
     if (need <= 3 * tc::tile_bytes(b)) {
       int *sp = reinterpret_cast<int *>(Bf[0]);
-      float2 *sv = reinterpret_cast<float2 *>(sp + ((bb + 1 + nz + 3) & ~3));
-      int *st = sp + bb + 1;
+      float2 *sv = reinterpret_cast<float2 *>(sp + ((2 * bb + 1 + nz + 3) & ~3));
+      int *so = sp + bb + 1, *st = so + bb;
+      // unrolled so that each thread's loads are in flight together (they do not depend on
+      // one another); Hc goes straight into H, so the walk below touches no global memory
+#pragma unroll 8
       for (int x = tid; x <= bb; x += kTcThreads) sp[x] = s.tk_ptr[bp + x] - j0;
+#pragma unroll 8
+      for (int x = tid; x < bb; x += kTcThreads) so[x] = s.tk_order[bp + x];
+#pragma unroll 8
       for (int x = tid; x < nz; x += kTcThreads) st[x] = s.tk_term[j0 + x], sv[x] = s.tk_val[j0 + x];
+#pragma unroll 8
+      for (int e = tid; e < bb; e += kTcThreads) H[e] = Hcb[e];
       __syncthreads();
-      for (int e = tid; e < bb; e += kTcThreads) {
-        float2 h = Hcb[e];
+      // elements by descending term count: the 32 lanes of a warp walk similar lengths (the
+      // diagonal, with a term for every interaction, together)
+      for (int x = tid; x < bb; x += kTcThreads) {
+        const int e = so[x];
+        float2 h = H[e];
         for (int j = sp[e]; j < sp[e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[st[j]], sv[j]));
         H[e] = h;
       }
