@@ -2843,6 +2843,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
         attr((const void *)k_tc_step, sm_step);
         attr((const void *)k_tc_dyson, sm_dy);
         attr((const void *)k_tc_dyson_stk, tc_dyson_stk_smem(64));
+        attr((const void *)k_tc_step_stk, tc_step_stk_smem(64));
       }
       attr((const void *)k_big_eigframe<1, double2>, smem_mat);
       attr((const void *)k_big_eigframe<2, double2>, smem_mat);
@@ -3372,7 +3373,10 @@ static void launch_stage(JobImpl &J, DevSys &s, int stage) {
     const bool nt1 = big_nt(b, b) == 1;
     switch (stage) {
       case 0:
-        if (J.tc && b >= tc::kMinB)
+        if (J.tc && b >= tc::kMinB && tc::up16(b) <= 64)  // the two Horner chains stacked in one M = 128 tile
+          k_tc_step_stk<<<unsigned(s.C) * unsigned(s.n), tc::kTcThreads, tc_step_stk_smem(b), st>>>(
+              s, k, J.usl.p + J.usl_off[k]);
+        else if (J.tc && b >= tc::kMinB)
           k_tc_step<<<unsigned(s.C) * unsigned(s.n), tc::kTcThreads, tc_step_smem(b), st>>>(s, k, J.usl.p + J.usl_off[k]);
         else if (s.mixed) k_big_step_df<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_df_smem(b), st>>>(s, k);
         else k_big_step<<<unsigned(s.C) * unsigned(s.n), th_step, big_step_smem(b), st>>>(s, k);

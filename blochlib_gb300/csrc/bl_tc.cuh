@@ -242,6 +242,92 @@ __device__ __forceinline__ int taylor_degree_tc(float x) {
 
 enum { kTcTimeout = 64 };  // status bit: a tensor-core wait ran out
 
+// A stacked tile: 128 rows (two R-row halves, the rest zero or unused) of the no-swizzle
+// K-major slice layout, four planes of 16 row groups each.
+__host__ __device__ constexpr size_t tc_stk_plane_bytes(int b) { return size_t(16) * tc::sbo_bytes(tc::up16(b)); }
+
+// The step's prologue (every thread): the term coefficients into fk, H_i (double-float) into
+// H, row sums of |H| into red, then the scale, squarings and Taylor degree into scl, nsq and
+// nterms.  The block's operator non-zeros (CSR rows bp .. bp + bb) are first copied into
+// `stage` (tiles that are free until X is sliced): coalesced, independent loads, after which
+// each entry's walk over its terms (36 on a diagonal of eight coupled spins) reads shared
+// memory instead of waiting on L2.
+__device__ __forceinline__ void tc_step_prologue(const DevSys &s, int k, int c, int i, float2 *fk, float *red,
+                                                 float2 *H, unsigned char *stage, size_t stage_bytes, float2 &scl,
+                                                 int &nsq, int &nterms) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int b = s.bs[k], bp = s.bpoff[k], bb = b * b;
+  {  // term coefficients (double-float pairs from k_coef)
+    const float2 *fk2 = reinterpret_cast<const float2 *>(s.fk);
+    for (int kk = tid; kk < s.nint; kk += tc::kTcThreads) fk[kk] = fk2[at(i * s.nint + kk, c, s.Cpad)];
+  }
+  __syncthreads();
+  const float2 *Hcb = s.Hc_df + bp;
+  {
+    const int j0 = s.tk_ptr[bp], nz = s.tk_ptr[bp + bb] - j0;
+    const size_t need = size_t(2 * bb + 1 + nz) * sizeof(int) + size_t(nz) * sizeof(float2) + 16;
+    if (need <= stage_bytes) {
+      int *sp = reinterpret_cast<int *>(stage);
+      float2 *sv = reinterpret_cast<float2 *>(sp + ((2 * bb + 1 + nz + 3) & ~3));
+      int *so = sp + bb + 1, *st = so + bb;
+      // unrolled so that each thread's loads are in flight together (they do not depend on
+      // one another); Hc goes straight into H, so the walk below touches no global memory
+#pragma unroll 8
+      for (int x = tid; x <= bb; x += tc::kTcThreads) sp[x] = s.tk_ptr[bp + x] - j0;
+#pragma unroll 8
+      for (int x = tid; x < bb; x += tc::kTcThreads) so[x] = s.tk_order[bp + x];
+#pragma unroll 8
+      for (int x = tid; x < nz; x += tc::kTcThreads) st[x] = s.tk_term[j0 + x], sv[x] = s.tk_val[j0 + x];
+#pragma unroll 8
+      for (int e = tid; e < bb; e += tc::kTcThreads) H[e] = Hcb[e];
+      __syncthreads();
+      // elements by descending term count: the 32 lanes of a warp walk similar lengths (the
+      // diagonal, with a term for every interaction, together)
+      for (int x = tid; x < bb; x += tc::kTcThreads) {
+        const int e = so[x];
+        float2 h = H[e];
+        for (int j = sp[e]; j < sp[e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[st[j]], sv[j]));
+        H[e] = h;
+      }
+    } else {
+      for (int e = tid; e < bb; e += tc::kTcThreads) {
+        float2 h = Hcb[e];
+        for (int j = s.tk_ptr[bp + e]; j < s.tk_ptr[bp + e + 1]; ++j)
+          h = dfv_add(h, dfv_mul(fk[s.tk_term[j]], s.tk_val[j]));
+        H[e] = h;
+      }
+    }
+  }
+  __syncthreads();
+  // row sums of |H| (a warp per row, lanes over the columns), then their maximum: the norm
+  for (int p = warp; p < b; p += tc::kTcThreads / 32) {
+    float rs = 0.f;
+    for (int q = lane; q < b; q += 32) rs += fabsf(H[p * b + q].x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+    if (lane == 0) red[p] = rs;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    float nrm = 0.f;
+    for (int p = lane; p < b; p += 32) nrm = fmaxf(nrm, red[p]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
+    if (lane == 0) {
+      nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
+      int sq = 0;
+      if (nrm > 1.f) {
+        frexpf(nrm, &sq);  // nrm < 2^sq
+        sq = min(sq, 60);
+      }
+      scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
+      nsq = sq;
+      nterms = tc::taylor_degree_tc(ldexpf(nrm, -sq));
+    }
+  }
+  __syncthreads();
+}
+
 // ------------------------------------------------------------------ step exponential
 // One CTA per (crystallite, step) of a large block b <= tc::kMaxB of the mixed form (no rf
 // schedule): H_i in double-float from k_coef's coefficients (as k_big_step_df),
@@ -282,80 +368,10 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
   }
   if (warp == 0) tc::tmem_alloc(&tbase, ncols);
   if (tid == 0) tc::mbar_init(&mbar[0]), tc::mbar_init(&mbar[1]);
-  {  // term coefficients (double-float pairs from k_coef)
-    const float2 *fk2 = reinterpret_cast<const float2 *>(s.fk);
-    for (int kk = tid; kk < s.nint; kk += kTcThreads) fk[kk] = fk2[at(i * s.nint + kk, c, s.Cpad)];
-  }
-  __syncthreads();
-  // H (double-float) into the fourth tile as scratch.  The block's operator non-zeros (CSR
-  // rows bp .. bp + bb) are first copied into the three other tiles, which are free until X
-  // is sliced: coalesced, independent loads, after which each entry's walk over its terms
-  // (36 on a diagonal of eight coupled spins) reads shared memory instead of waiting on L2.
+  // H (double-float) into the fourth tile as scratch, the other three as the staging area
   float2 *H = reinterpret_cast<float2 *>(Bf[3]);
-  const float2 *Hcb = s.Hc_df + bp;
-  {
-    const int j0 = s.tk_ptr[bp], nz = s.tk_ptr[bp + bb] - j0;
-    const size_t need = size_t(2 * bb + 1 + nz) * sizeof(int) + size_t(nz) * sizeof(float2) + 16;
-    if (need <= 3 * tc::tile_bytes(b)) {
-      int *sp = reinterpret_cast<int *>(Bf[0]);
-      float2 *sv = reinterpret_cast<float2 *>(sp + ((2 * bb + 1 + nz + 3) & ~3));
-      int *so = sp + bb + 1, *st = so + bb;
-      // unrolled so that each thread's loads are in flight together (they do not depend on
-      // one another); Hc goes straight into H, so the walk below touches no global memory
-#pragma unroll 8
-      for (int x = tid; x <= bb; x += kTcThreads) sp[x] = s.tk_ptr[bp + x] - j0;
-#pragma unroll 8
-      for (int x = tid; x < bb; x += kTcThreads) so[x] = s.tk_order[bp + x];
-#pragma unroll 8
-      for (int x = tid; x < nz; x += kTcThreads) st[x] = s.tk_term[j0 + x], sv[x] = s.tk_val[j0 + x];
-#pragma unroll 8
-      for (int e = tid; e < bb; e += kTcThreads) H[e] = Hcb[e];
-      __syncthreads();
-      // elements by descending term count: the 32 lanes of a warp walk similar lengths (the
-      // diagonal, with a term for every interaction, together)
-      for (int x = tid; x < bb; x += kTcThreads) {
-        const int e = so[x];
-        float2 h = H[e];
-        for (int j = sp[e]; j < sp[e + 1]; ++j) h = dfv_add(h, dfv_mul(fk[st[j]], sv[j]));
-        H[e] = h;
-      }
-    } else {
-      for (int e = tid; e < bb; e += kTcThreads) {
-        float2 h = Hcb[e];
-        for (int j = s.tk_ptr[bp + e]; j < s.tk_ptr[bp + e + 1]; ++j)
-          h = dfv_add(h, dfv_mul(fk[s.tk_term[j]], s.tk_val[j]));
-        H[e] = h;
-      }
-    }
-  }
-  __syncthreads();
-  // row sums of |H| (a warp per row, lanes over the columns), then their maximum: the norm
-  for (int p = warp; p < b; p += kTcThreads / 32) {
-    float rs = 0.f;
-    for (int q = lane; q < b; q += 32) rs += fabsf(H[p * b + q].x);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) rs += __shfl_xor_sync(0xffffffffu, rs, o);
-    if (lane == 0) red[p] = rs;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    float nrm = 0.f;
-    for (int p = lane; p < b; p += 32) nrm = fmaxf(nrm, red[p]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) nrm = fmaxf(nrm, __shfl_xor_sync(0xffffffffu, nrm, o));
-    if (lane == 0) {
-      nrm *= float(s.tau * kPi2) * (1.f + 1e-6f);
-      int sq = 0;
-      if (nrm > 1.f) {
-        frexpf(nrm, &sq);  // nrm < 2^sq
-        sq = min(sq, 60);
-      }
-      scl = make_float2(ldexpf(s.tpdf.x, -sq), ldexpf(s.tpdf.y, -sq));
-      nsq = sq;
-      nterms = tc::taylor_degree_tc(ldexpf(nrm, -sq));
-    }
-  }
-  __syncthreads();
+  tc_step_prologue(s, k, c, i, fk, red, H, reinterpret_cast<unsigned char *>(Bf[0]), 3 * tc::tile_bytes(b), scl, nsq,
+                   nterms);
   const int sq = nsq, K = nterms;
   const int mC = K / 2, mS = (K - 1) / 2;  // C to X^(2 mC), S to X^(2 mS + 1)
   {  // X slices into the first tile: one 8-column row chunk per thread and iteration
@@ -562,6 +578,271 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
   if (warp == 0) tc::tmem_free(tmem, ncols);
 }
 
+// ------------------------------------------------------------------ step exponential, stacked
+// The same step for blocks with up16(b) = R <= 64, with both halves of the M = 128 tile
+// holding rows.  X is sliced into both halves of a stacked tile XS, so that Y = XS X puts
+// Y's rows in lanes m and R + m; the two Horner chains run as one, T = [T_C; T_S] stacked,
+// T <- [I + c_C Y T_C; I + c_S Y T_S] from the single product T Y (T_C, T_S and Y are
+// polynomials in Y and commute), the sine series carried to the same number of terms as the
+// cosine (one more than it needs); S = T_S X from the same stacked T.  Every TMEM lane
+// quarter holds rows for each epilogue.  C and S end in R-row tiles, where the squarings
+// (as in k_tc_step) and the slab copy take them.  Shared memory: XS and T (stacked), two
+// R-row tiles (Y, then C; H's scratch, then S), the over-read margin of an R-row A tile.
+__host__ __device__ constexpr size_t tc_step_stk_smem(int b) {
+  return 8 * tc_stk_plane_bytes(b) + 2 * tc::tile_bytes(b) + tc::overread_bytes(b) + 1024;
+}
+
+__global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step_stk(DevSys s, int k, unsigned char *slab0) {
+  using tc::kTcThreads;
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __shared__ uint32_t tbase;
+  __shared__ __align__(8) uint64_t mbar[2];
+  __shared__ float2 fk[kMaxInt];
+  __shared__ float red[tc::kMaxB];
+  __shared__ float2 scl;
+  __shared__ int nsq, nterms;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c = blockIdx.x % s.C, i = blockIdx.x / s.C;
+  const int b = s.bs[k];
+  const int R = tc::up16(b);
+  const int pe = int(tc::plane_bytes(b) / 2), peS = int(tc_stk_plane_bytes(b) / 2);  // BF16 units
+  const uint32_t pl = uint32_t(tc::plane_bytes(b)), plS = uint32_t(tc_stk_plane_bytes(b));
+  const int ncols = tc::pow2_cols(6 * R);
+  unsigned char *base = tsm + ((1024 - (tc::saddr(tsm) & 1023)) & 1023);
+  __nv_bfloat16 *XS = reinterpret_cast<__nv_bfloat16 *>(base);
+  __nv_bfloat16 *T = reinterpret_cast<__nv_bfloat16 *>(base + 4 * plS);
+  __nv_bfloat16 *Yt = reinterpret_cast<__nv_bfloat16 *>(base + 8 * plS);
+  __nv_bfloat16 *Wt = reinterpret_cast<__nv_bfloat16 *>(base + 8 * plS + tc::tile_bytes(b));
+  const uint32_t aXS = tc::saddr(XS), aT = tc::saddr(T), aY = tc::saddr(Yt), aW = tc::saddr(Wt);
+  if (warp == 0) tc::tmem_alloc(&tbase, ncols);
+  if (tid == 0) tc::mbar_init(&mbar[0]), tc::mbar_init(&mbar[1]);
+  // H into Wt as scratch; XS, T and Yt as the staging area
+  float2 *H = reinterpret_cast<float2 *>(Wt);
+  tc_step_prologue(s, k, c, i, fk, red, H, base, 8 * plS + tc::tile_bytes(b), scl, nsq, nterms);
+  const int sq = nsq, K = nterms;
+  const int mC = K / 2;  // C to X^(2 mC), S to X^(2 mC + 1)
+  {  // X slices into both halves of XS: one 8-column row chunk per thread and iteration
+    const float2 sc = scl;
+    const int nch = R * (R / 8);
+    for (int t = tid; t < nch; t += kTcThreads) {
+      const int r = t / (R / 8), c0 = (t % (R / 8)) * 8;
+      float hi[8], lo[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int q = c0 + j;
+        float2 x = make_float2(0.f, 0.f);
+        if (r < b && q < b) x = dfv_mul(sc, H[r * b + q]);
+        hi[j] = x.x, lo[j] = x.y;
+      }
+      tc::store_row8(XS, peS, tc::tix(r, c0, R), hi, lo);
+      tc::store_row8(XS, peS, tc::tix(R + r, c0, R), hi, lo);
+    }
+  }
+  tc::fence_smem_async();
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tbase;
+  uint32_t phase[2] = {0u, 0u};
+  bool ok = true;
+  const int q4 = warp & 3, part = warp >> 2;  // lane quarter; 8-column chunks part, part+4, ...
+  const int L = 32 * q4 + lane;                // TMEM lane: row L of the top half or L - R of the bottom
+  const bool bot = L >= R, live = L < 2 * R;
+  const int m = bot ? L - R : L;
+  struct Out {
+    __nv_bfloat16 *dst;
+    int pe, row0;
+    float2 coef;
+    float diag;
+  };
+  // Epilogue of a stacked product (accumulator set 0): each live lane's row P (2^-16 times
+  // the three accumulator levels, double-float) goes out as coef P + diag I into the outputs
+  // of its half, as slices (row row0 + m of dst, plane stride pe), zero padding.
+  auto epi = [&](const Out *o0, int n0, const Out *o1, int n1) {
+    if (32 * q4 >= 2 * R) return;  // warp-uniform: no stacked row in this lane quarter
+    const Out *o = bot ? o1 : o0;
+    const int no = bot ? n1 : n0;
+    for (int c0 = 8 * part; c0 < R; c0 += 32) {
+      float a0[8], a1[8], a2[8];
+      const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + uint32_t(c0);
+      tc::ld8(ta, a0);
+      tc::ld8(ta + uint32_t(R), a1);
+      tc::ld8(ta + uint32_t(2 * R), a2);
+      tc::wait_ld();
+      if (!live || no == 0) continue;
+      float2 P[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const float2 p = tc::sum3(a0[j], a1[j], a2[j]);
+        P[j] = (m < b && c0 + j < b) ? make_float2(p.x * 0x1p-16f, p.y * 0x1p-16f) : make_float2(0.f, 0.f);
+      }
+      for (int u = 0; u < no; ++u) {
+        float hi[8], lo[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int q = c0 + j;
+          float2 v = make_float2(0.f, 0.f);
+          if (m < b && q < b) {
+            v = dfv_mul(o[u].coef, P[j]);
+            if (m == q) v = dfv_add(v, make_float2(o[u].diag, 0.f));
+          }
+          hi[j] = v.x, lo[j] = v.y;
+        }
+        tc::store_row8(o[u].dst, o[u].pe, tc::tix(o[u].row0 + m, c0, R), hi, lo);
+      }
+    }
+  };
+  auto sync_all = [&]() {  // epilogue writes -> the next MMAs, whole CTA
+    tc::fence_smem_async();
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+  };
+  auto wait_all = [&](int set) -> bool {
+    const bool done = tc::wait_parity(&mbar[set], phase[set]);
+    phase[set] ^= 1u;
+    const bool all = __syncthreads_and(done);
+    tc::fence_after();
+    return all;
+  };
+  const float2 one = make_float2(1.f, 0.f), zero = make_float2(0.f, 0.f);
+  // Y = X X (top and bottom halves alike); Y to Yt (when a chain step follows), the first
+  // Horner terms T_C = I + c Y (to T, or straight to Yt as C when no chain step follows) and
+  // T_S = I + c' Y (to T's bottom half); c = 0 when the series stops at the identity
+  if (tid == 0) {
+    tc::issue_product(tmem, 0, aXS, plS, aXS, plS, R, false, false);
+    tc::commit(&mbar[0]);
+  }
+  if (!wait_all(0)) ok = false;
+  if (ok) {
+    const float2 cC = mC >= 1 ? tc::horner_coef(2 * mC - 1) : zero, cS = mC >= 1 ? tc::horner_coef(2 * mC) : zero;
+    const Out top2[2] = {{Yt, pe, 0, one, 0.f}, {T, peS, 0, cC, 1.f}};
+    const Out top1[1] = {{Yt, pe, 0, cC, 1.f}};
+    const Out bot1[1] = {{T, peS, R, cS, 1.f}};
+    if (mC >= 2) epi(top2, 2, bot1, 1);
+    else epi(top1, 1, bot1, 1);
+    sync_all();
+  }
+  // the chains: T <- [I + c_(2j-1) T_C Y; I + c_(2j) T_S Y] for j = mC-1 .. 1; the last
+  // T_C (= C) goes to Yt, free once its product has run
+  for (int j = mC - 1; ok && j >= 1; --j) {
+    if (tid == 0) {
+      tc::issue_product(tmem, 0, aT, plS, aY, pl, R, false, false);
+      tc::commit(&mbar[0]);
+    }
+    if (!wait_all(0)) {
+      ok = false;
+      break;
+    }
+    const Out top[1] = {{j > 1 ? T : Yt, j > 1 ? peS : pe, 0, tc::horner_coef(2 * j - 1), 1.f}};
+    const Out btm[1] = {{T, peS, R, tc::horner_coef(2 * j), 1.f}};
+    epi(top, 1, btm, 1);
+    sync_all();
+  }
+  // S = T_S X (the bottom half of T times X, X from XS's top half) into Wt
+  if (ok) {
+    if (tid == 0) {
+      tc::issue_product(tmem, 0, aT, plS, aXS, plS, R, false, false);
+      tc::commit(&mbar[0]);
+    }
+    if (!wait_all(0)) ok = false;
+    if (ok) {
+      const Out btm[1] = {{Wt, pe, 0, one, 0.f}};
+      epi(nullptr, 0, btm, 1);
+      sync_all();
+    }
+  }
+  // squarings on R-row tiles: C' = C^2 - S^2 (sets 0 and 1), S' = 2 C S (set 0)
+  __nv_bfloat16 *Bf[4] = {Yt, Wt, XS, reinterpret_cast<__nv_bfloat16 *>(base + tc::tile_bytes(b))};
+  const uint32_t ba[4] = {aY, aW, aXS, aXS + uint32_t(tc::tile_bytes(b))};
+  __nv_bfloat16 *Ct = Yt, *St = Wt;
+  uint32_t aC = aY, aS = aW;
+  const uint32_t set_col[2] = {0u, uint32_t(3 * R)};
+  auto epi_sq = [&](int set, float2 coef, bool second, __nv_bfloat16 *dst) {
+    if (32 * q4 >= R) return;  // warp-uniform
+    const int r = 32 * q4 + lane;
+    for (int c0 = 8 * part; c0 < R; c0 += 32) {
+      float a0[8], a1[8], a2[8], b0[8], b1[8], b2[8];
+      const uint32_t ta = tmem + (uint32_t(32 * q4) << 16) + set_col[set] + uint32_t(c0);
+      tc::ld8(ta, a0);
+      tc::ld8(ta + uint32_t(R), a1);
+      tc::ld8(ta + uint32_t(2 * R), a2);
+      if (second) {
+        const uint32_t tb = tmem + (uint32_t(32 * q4) << 16) + set_col[1] + uint32_t(c0);
+        tc::ld8(tb, b0);
+        tc::ld8(tb + uint32_t(R), b1);
+        tc::ld8(tb + uint32_t(2 * R), b2);
+      }
+      tc::wait_ld();
+      if (r < R) {
+        float hi[8], lo[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int q = c0 + j;
+          float2 v = make_float2(0.f, 0.f);
+          if (r < b && q < b) {
+            const float2 p = tc::sum3(a0[j], a1[j], a2[j]);
+            v = make_float2(p.x * 0x1p-16f, p.y * 0x1p-16f);
+            if (second) {
+              const float2 p2 = tc::sum3(b0[j], b1[j], b2[j]);
+              v = dfv_add(v, make_float2(-p2.x * 0x1p-16f, -p2.y * 0x1p-16f));
+            }
+            v = dfv_mul(coef, v);
+          }
+          hi[j] = v.x, lo[j] = v.y;
+        }
+        tc::store_row8(dst, pe, tc::tix(r, c0, R), hi, lo);
+      }
+    }
+  };
+  for (int t = 0; ok && t < sq; ++t) {
+    __nv_bfloat16 *fr[2] = {nullptr, nullptr};
+    uint32_t fa[2] = {0u, 0u};
+    int nf = 0;
+    for (int u = 0; u < 4; ++u)
+      if (Bf[u] != Ct && Bf[u] != St && nf < 2) fr[nf] = Bf[u], fa[nf] = ba[u], ++nf;
+    if (tid == 0) {
+      tc::issue_product(tmem, set_col[0], aC, aC, pl, R, false, false);
+      tc::commit(&mbar[0]);
+      tc::issue_product(tmem, set_col[1], aS, aS, pl, R, false, false);
+      tc::commit(&mbar[1]);
+    }
+    const bool w0 = wait_all(0), w1 = wait_all(1);
+    if (!w0 || !w1) {
+      ok = false;
+      break;
+    }
+    epi_sq(0, one, true, fr[0]);
+    sync_all();
+    if (tid == 0) tc::issue_product(tmem, set_col[0], aC, aS, pl, R, false, false), tc::commit(&mbar[0]);
+    if (!wait_all(0)) {
+      ok = false;
+      break;
+    }
+    epi_sq(0, make_float2(2.f, 0.f), false, fr[1]);
+    sync_all();
+    Ct = fr[0], aC = fa[0], St = fr[1], aS = fa[1];
+  }
+  if (ok && tid == 0) {  // real products: Y, two per chain step, T_S X, 3 per squaring
+    const int nprod = 1 + 2 * max(mC - 1, 0) + 1 + 3 * sq;
+    atomicAdd(s.tc_flops, 20ull * (unsigned long long)nprod * (unsigned long long)(b * b * b));
+  }
+  if (ok) {  // the slab: C tile, then S tile (U = C - i S), 16-byte coalesced copies
+    uint4 *dst = reinterpret_cast<uint4 *>(slab0 + (size_t(c) * s.n + i) * tc::slab_bytes(b));
+    const int nv = int(tc::tile_bytes(b) / 16);
+    const uint4 *cs = reinterpret_cast<const uint4 *>(Ct), *ss = reinterpret_cast<const uint4 *>(St);
+    for (int v = tid; v < nv; v += kTcThreads) dst[v] = cs[v], dst[nv + v] = ss[v];
+  } else {
+    if (tid == 0) atomicOr(s.status, kTcTimeout);
+    tc::wait_parity(&mbar[0], phase[0]);  // bounded: let MMAs in flight drain before TMEM is freed
+    tc::wait_parity(&mbar[1], phase[1]);
+  }
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  if (warp == 0) tc::tmem_free(tmem, ncols);
+}
+
 // ------------------------------------------------------------------ Dyson product
 // One CTA per crystallite: A_{i+1} = U_i A_i for i < n, large block k of the mixed form.
 // The product is formed transposed, A_{i+1}^T = A_i^T U_i (U_i = C - i S is symmetric):
@@ -701,7 +982,6 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_dyson(DevSys s, int k,
 // Each epilogue lane writes its row's slices into both stacked tiles (negated in A2's lower
 // half) and its half of the double-float A_{i+1} element (re: .x and .z, im: .y and .w of the
 // float4 re.hi, im.hi, re.lo, im.lo).  Shared memory: A1, A2 (128 rows each), the U slab.
-__host__ __device__ constexpr size_t tc_stk_plane_bytes(int b) { return size_t(16) * tc::sbo_bytes(tc::up16(b)); }
 __host__ __device__ constexpr size_t tc_dyson_stk_smem(int b) {
   return 2 * 4 * tc_stk_plane_bytes(b) + tc::slab_bytes(b) + 1024;
 }
