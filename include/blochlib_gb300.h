@@ -65,16 +65,21 @@ typedef struct {
   double wr;       /* rotor speed, Hz (0 = static powder FID, as is rotor angle 0) */
   double rotb_deg; /* rotor angle, degrees */
   double start_t;  /* start time, s */
-  int precision;   /* 0 = FP64; 1 = mixed (propagators in double-float, hi + lo floats, for
-                      Hamiltonian blocks up to 74; Floquet eigenvalues and vectors and the
-                      powder sum in FP64, the Jacobi sweeps over the Cayley K in FP32;
-                      single-precision eigenframe, Q/R, Fave and FID terms; <= 1e-6 relative
-                      to FP64) */
+  int precision;   /* 0 = FP64; 1 = mixed, <= 1e-6 relative to FP64: for Hamiltonian blocks
+                      up to 39 the step exponential and the Dyson products in double-float
+                      (hi + lo floats); for blocks 40-74, with step_method 1 and no rf
+                      schedule, on the tensor cores as exact BF16 slice products (~2^-32 per
+                      product, double-float results); the Floquet decomposition with FP32
+                      Jacobi sweeps (FIDs of at most 64 rotor periods) and a double-float or
+                      FP64 Cayley transform, eigenvectors and eigenvalues; single-precision
+                      eigenframe, Q/R, Fave and FID terms; powder sum in FP64.  Blocks above
+                      74 stay FP64. */
   int step_method; /* step exponential exp(-i 2pi tau H): 0 = eigen-decomposition (Jacobi),
-                      1 = Taylor series with scaling and squaring; FP64, or double-float in
-                      the mixed form (blocks up to 8 with step_method 1, blocks 9-74 always) */
+                      1 = Taylor series with scaling and squaring; FP64, or in the mixed form
+                      as above (blocks up to 8 with step_method 1, blocks 9-74 always) */
   int fave_method; /* correlation over the rotor period: 0 = automatic (FFT for n <= 2048),
-                      1 = direct O(n^2) sum, 2 = zero-padded FFT; both FP64 */
+                      1 = direct O(n^2) sum, 2 = zero-padded FFT; FP64, single precision in
+                      the mixed form */
   int error_sample; /* mixed form: state the result's error.  The FID of this many crystallites
                       (spread evenly over the powder) is computed again in FP64 and in the mixed
                       form; their relative L2 difference is read with bl_last_error_statement.
