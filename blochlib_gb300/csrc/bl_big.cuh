@@ -693,7 +693,7 @@ __device__ void floquet_cta(const DevSys &s, int k, int c, FloqWork wk, int swee
     s.L[at(bo + r, c, s.Cpad)] = cmk(log(hypot(lam[r].x, lam[r].y)), atan2(lam[r].y, lam[r].x));
 }
 
-__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk);
+__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk, bool a64 = false);
 
 // One CTA per crystallite: unitary eigen-decomposition of a large block of A_n.
 __global__ void __launch_bounds__(kBigThreads) k_big_floquet(DevSys s, int k) {
@@ -1103,7 +1103,8 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
   return conv;
 }
 
-__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
+// a64: A_n is FP64 (double2, the huge-block path's storage) instead of double-float
+__device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk, bool a64) {
   __shared__ int piv_s;
   __shared__ double a_s;
   __shared__ int done_s;
@@ -1114,8 +1115,11 @@ __device__ void floquet_cta_df(const DevSys &s, int k, int c, FloqWork wk) {
   double2 *lam = wk.lam;
   double *red = wk.red;
   float2 *Kf = wk.Kf;
-  const float4 *U4 = reinterpret_cast<const float4 *>(s.A + size_t(s.n - 1) * s.S2 * s.Cpad);
-  auto Ug = [&](int r, int q) { return U4[big_at(s, b, bp, r * b + q, c)]; };
+  const double2 *An = s.A + size_t(s.n - 1) * s.S2 * s.Cpad;
+  const float4 *U4 = reinterpret_cast<const float4 *>(An);
+  auto Ug = [&](int r, int q) {
+    return a64 ? df_store(An[at(bp + r * b + q, c, s.Cpad)]) : U4[big_at(s, b, bp, r * b + q, c)];
+  };
   if (threadIdx.x == 0) a_s = 0.5, done_s = 0;
   __syncthreads();
   for (int pass = 0; pass < 2; ++pass) {

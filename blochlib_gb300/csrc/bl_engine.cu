@@ -2692,7 +2692,7 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
   }
   long cpad_all = ((long(J.Ceff) + 31) / 32) * 32;
   // huge blocks: one workspace for their batched products, at least one item of each use
-  // (exponential: 7 real b x b; Floquet: 2 complex b x b; eigenframe, Q/R: one complex
+  // (exponential: 7 real b x b; Floquet: 2 complex b x b, 3 in the mixed form; eigenframe, Q/R: one complex
   // matrix), else 1 GiB
   size_t huge_fixed = 0;
   {
@@ -2701,7 +2701,8 @@ Job::Job(Context &ctx, const SpinSystem &sys, const Powder &pw, const CMatrix &r
     for (int k = 0; k < nb; ++k) {
       const size_t b = size_t(L.size[k]);
       if (L.size[k] <= kMaxBigBlock) continue;
-      need = std::max(need, std::max(sizeof(double) * kHugeSlots * b * b, 2 * sizeof(double2) * b * b));
+      need = std::max(need, std::max(sizeof(double) * kHugeSlots * b * b,
+                                     (p.precision == 1 ? 3 : 2) * sizeof(double2) * b * b));
       bmin = bmin ? std::min(bmin, L.size[k]) : L.size[k];
     }
     for (int pr = 0; pr < J.npq + J.npr; ++pr) {
@@ -3218,7 +3219,8 @@ static void huge_step(JobImpl &J, DevSys &s, size_t kh) {
     auto sym = [&](int a, int bsl, int o, int akind, double alpha, int round, bool low, double c0, double c1,
                    double c2, double c3) {
       SymArgs g{ws, J.hsc.p, J.hsq.p, bb, b, a, bsl, o, akind, alpha, round, low ? 1 : 0, c0, c1, c2, c3};
-      k_huge_sym<<<dim3(gs, unsigned(items)), kHThreads, 0, st>>>(g);
+      if (s.mixed) k_huge_sym_df<<<dim3(gs, unsigned(items)), kHThreads, 0, st>>>(g);
+      else k_huge_sym<<<dim3(gs, unsigned(items)), kHThreads, 0, st>>>(g);
       ++J.launches;
     };
     k_huge_fk<<<unsigned((items + 127) / 128), 128, 0, st>>>(s, j0, items, J.hfk.p);
@@ -3263,8 +3265,12 @@ static void huge_dyson(JobImpl &J, DevSys &s, size_t kh) {
   const auto Ain = item_mat<const double2>(s.A, long(bp) - s.S2, s.S2, b, s.Cpad);
   const auto Aout = item_mat<double2>(s.A, bp, s.S2, b, s.Cpad);
   for (int i = 1; i < J.n; ++i) {
-    k_huge_zgemm<double2, false, double2, double2, double2>
-        <<<dim3(tiles(b, b), unsigned(s.C)), kHThreads, 0, st>>>(U, Ain, Aout, b, b, b, s.C, long(i) * s.C, 1.0);
+    if (s.mixed)  // double-float products, FP64 storage
+      k_huge_zgemm_df<<<dim3(tiles(b, b), unsigned(s.C)), kHThreads, 0, st>>>(U, Ain, Aout, b, b, b, s.C,
+                                                                              long(i) * s.C, 1.0);
+    else
+      k_huge_zgemm<double2, false, double2, double2, double2>
+          <<<dim3(tiles(b, b), unsigned(s.C)), kHThreads, 0, st>>>(U, Ain, Aout, b, b, b, s.C, long(i) * s.C, 1.0);
     ++J.launches;
   }
 }
@@ -3276,19 +3282,21 @@ static void huge_floquet_all(JobImpl &J, DevSys &s) {
   for (size_t g0 = 0; g0 < nh; g0 += kMaxHugeLaunch) {
     HugeFloq hf{};
     hf.n = int(std::min<size_t>(kMaxHugeLaunch, nh - g0));
+    hf.mats = s.floq32 ? 3 : 2;  // the mixed form's FP32 K takes half a third matrix
     size_t per_c = 0, smem = 0;
     for (int t = 0; t < hf.n; ++t) {
       const size_t b = size_t(J.L.size[J.huge_blocks[g0 + t]]);
-      per_c += 2 * b * b;
+      per_c += size_t(hf.mats) * b * b;
       smem = std::max(smem, huge_floquet_smem(int(b)));
     }
     const int per = int(std::min<size_t>(size_t(s.C), J.huge_ws_bytes / (sizeof(double2) * per_c)));
+    if (per < 1) throw Error(3, "the huge-block workspace holds no crystallite's Floquet matrices");
     long off = 0;
     for (int t = 0; t < hf.n; ++t) {
       const long b = J.L.size[J.huge_blocks[g0 + t]];
       hf.k[t] = J.huge_blocks[g0 + t];
       hf.ws[t] = off;
-      off += long(per) * 2 * b * b;
+      off += long(per) * hf.mats * b * b;
     }
     for (int c0 = 0; c0 < s.C; c0 += per) {
       k_huge_floquet<<<dim3(unsigned(std::min(per, s.C - c0)), unsigned(hf.n)), kHugeFloqThreads, smem,

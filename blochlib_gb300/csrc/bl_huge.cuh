@@ -91,6 +91,54 @@ __global__ void __launch_bounds__(kHThreads) k_huge_zgemm(HMat<const TA> A, HMat
     }
 }
 
+// The mixed form's Dyson product for huge blocks: O = alpha A B (FP64 storage, as
+// k_huge_zgemm<double2>) with double-float arithmetic on the FP32 pipe: operands split into
+// hi + lo floats as they are staged, each output a compensated complex dot product (cdf_mac),
+// rounded to FP64 once at the end (~2^-44 relative against FP64's 2^-53).
+__global__ void __launch_bounds__(kHThreads) k_huge_zgemm_df(HMat<const double2> A, HMat<const double2> B,
+                                                            HMat<double2> O, int m, int n, int k, int Cb, long j0,
+                                                            double alpha) {
+  __shared__ float4 As[kHK][kHT + 1], Bs[kHK][kHT + 1];
+  const long g = j0 + blockIdx.y;
+  const int c = int(g % Cb), sl = int(g / Cb);
+  const int tn = (n + kHT - 1) / kHT;
+  const int r0 = (blockIdx.x / tn) * kHT, q0 = (blockIdx.x % tn) * kHT;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  CdfAcc acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = CdfAcc{{0.f, 0.f}, {0.f, 0.f}};
+  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k0 = 0; k0 < k; k0 += kHK) {
+    for (int idx = threadIdx.x; idx < kHT * kHK; idx += kHThreads) {
+      const int rr = idx / kHK, kk = idx % kHK, r = r0 + rr, l = k0 + kk;
+      As[kk][rr] = (r < m && l < k) ? df_store(A(c, sl, r, l)) : z4;
+      const int kb = idx / kHT, qq = idx % kHT, lb = k0 + kb, q = q0 + qq;
+      Bs[kb][qq] = (lb < k && q < n) ? df_store(B(c, sl, lb, q)) : z4;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kHK; ++kk) {
+      float4 a[4], b[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) a[t] = As[kk][ty + 16 * t], b[t] = Bs[kk][tx + 16 * t];
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) cdf_mac(acc[x][y], a[x], b[y]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const int r = r0 + ty + 16 * x, q = q0 + tx + 16 * y;
+      if (r < m && q < n) O(c, sl, r, q) = cscale(df_load(cdf_fin(acc[x][y])), alpha);
+    }
+}
+
 // Arguments of k_huge_sym: workspace of kHugeSlots real b x b matrices per item (slot t of
 // item j at ws + (j*kHugeSlots + t)*bb) and per-item scale sc_j = 2 pi tau 2^-sq_j.
 struct SymArgs {
@@ -157,6 +205,65 @@ __global__ void __launch_bounds__(kHThreads) k_huge_sym(SymArgs g) {
       if (r >= b || q >= b || r > q) continue;  // upper triangle (r > q only on diagonal tiles)
       const long e = long(r) * b + q;
       double v = alpha * acc[x][y];
+      if (g.low) v += fma(g.c3, Y3[e], fma(g.c2, Y2[e], fma(g.c1, Y[e], r == q ? g.c0 : 0.0)));
+      O[e] = v;
+      if (r != q) O[long(q) * b + r] = v;
+    }
+}
+
+// k_huge_sym with double-float arithmetic (the mixed form): FP64 workspace, operands split
+// into hi + lo floats as they are staged, compensated dot products, the FP64 epilogue of
+// k_huge_sym (scale, low terms, mirrored store).
+__global__ void __launch_bounds__(kHThreads) k_huge_sym_df(SymArgs g) {
+  __shared__ float2 As[kHK][kHT + 1], Bs[kHK][kHT + 1];
+  const int j = blockIdx.y;
+  if (g.round >= 0 && g.sq[j] <= g.round) return;
+  const int b = g.b, tm = (b + kHT - 1) / kHT;
+  int ti, tj;
+  sym_tile(blockIdx.x, tm, ti, tj);
+  const int r0 = ti * kHT, q0 = tj * kHT;
+  double *base = g.ws + long(j) * kHugeSlots * g.bb;
+  const double *A = base + g.a * g.bb, *B = base + g.bsl * g.bb;
+  double *O = base + g.o * g.bb;
+  const double *Y = base + g.bb, *Y2 = base + 2 * g.bb, *Y3 = base + 3 * g.bb;
+  const double scj = g.sc[j];
+  const double alpha = g.akind == 0 ? g.alpha : (g.akind == 1 ? scj * scj : -scj);
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  DfAcc acc[4][4];
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) acc[x][y] = DfAcc{0.f, 0.f};
+  const float2 z2 = make_float2(0.f, 0.f);
+  for (int k0 = 0; k0 < b; k0 += kHK) {
+    for (int idx = threadIdx.x; idx < kHT * kHK; idx += kHThreads) {
+      const int rr = idx / kHK, kk = idx % kHK, r = r0 + rr, l = k0 + kk;
+      As[kk][rr] = (r < b && l < b) ? dfv_of(A[long(r) * b + l]) : z2;
+      const int kb = idx / kHT, qq = idx % kHT, lb = k0 + kb, q = q0 + qq;
+      Bs[kb][qq] = (lb < b && q < b) ? dfv_of(B[long(lb) * b + q]) : z2;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < kHK; ++kk) {
+      float2 a[4], bv[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) a[t] = As[kk][ty + 16 * t], bv[t] = Bs[kk][tx + 16 * t];
+#pragma unroll
+      for (int x = 0; x < 4; ++x)
+#pragma unroll
+        for (int y = 0; y < 4; ++y) df_dot(acc[x][y], a[x].x, a[x].y, bv[y].x, bv[y].y);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int x = 0; x < 4; ++x)
+#pragma unroll
+    for (int y = 0; y < 4; ++y) {
+      const int r = r0 + ty + 16 * x, q = q0 + tx + 16 * y;
+      if (r >= b || q >= b || r > q) continue;  // upper triangle (r > q only on diagonal tiles)
+      const long e = long(r) * b + q;
+      const float2 d = df_fin(acc[x][y]);
+      double v = alpha * (double(d.x) + double(d.y));
       if (g.low) v += fma(g.c3, Y3[e], fma(g.c2, Y2[e], fma(g.c1, Y[e], r == q ? g.c0 : 0.0)));
       O[e] = v;
       if (r != q) O[long(q) * b + r] = v;
@@ -306,6 +413,7 @@ __host__ __device__ constexpr size_t huge_floquet_smem(int b) {
 // Huge blocks of one Floquet launch and each one's workspace (2 b^2 per crystallite).
 struct HugeFloq {
   int n;
+  int mats;  // b x b double2 matrices per (crystallite, block): 2, or 3 with the FP32 K
   int k[kMaxHugeLaunch];
   long ws[kMaxHugeLaunch];
 };
@@ -320,6 +428,13 @@ __global__ void __launch_bounds__(kHugeFloqThreads) k_huge_floquet(DevSys s, Hug
   double2 *rot = reinterpret_cast<double2 *>(fsm), *fv = rot + 2 * np1, *lam = fv + b;
   double *red = reinterpret_cast<double *>(lam + b);
   int *rpair = reinterpret_cast<int *>(red + (b > kHugeFloqThreads ? b : kHugeFloqThreads));
-  double2 *Mm = ws + hf.ws[blockIdx.y] + size_t(blockIdx.x) * 2 * b * b;
-  floquet_cta<false, false>(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red, nullptr}, kHugeFloqSweeps0);
+  double2 *Mm = ws + hf.ws[blockIdx.y] + size_t(blockIdx.x) * hf.mats * b * b;
+  if (s.floq32)  // mixed form: FP32 sweeps, double-float Cayley solve, V and Rayleigh quotients
+    floquet_cta_df(s, k, c,
+                   FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red,
+                            reinterpret_cast<float2 *>(Mm + 2 * size_t(b) * b)},
+                   true);
+  else
+    floquet_cta<false, false>(s, k, c, FloqWork{Mm, Mm + size_t(b) * b, rot, fv, lam, rpair, red, nullptr},
+                              kHugeFloqSweeps0);
 }
