@@ -503,14 +503,15 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
         }
       }
       __syncthreads();
-      // columns p, q of K and V:  K <- K G, V <- V G  with G = [[c, sp], [-conj(sp), c]]
+      // columns p, q of K and V:  K <- K G, V <- V G  with G = [[c, sp], [-conj(sp), c]];
+      // the pair index runs fastest, so a warp's accesses stay within one row of K (or V)
       for (int e = threadIdx.x; e < np * b * 2; e += blockDim.x) {
-        const int t = e / (2 * b), rem2 = e % (2 * b), kk = rem2 % b;
+        const int t = e % np, rest = e / np, kk = rest % b;
         const int p = rpair(t, 0), q = rpair(t, 1);
         if (q >= b) continue;
         const double cc = rot(t, 0).x;
         const double2 sp = rot(t, 1), spc = cconj(sp);
-        if (rem2 < b) {
+        if (rest < b) {
           const R ccr = R(cc);
           const KC spr = cxm(R(sp.x), R(sp.y)), spcr = cxm(R(spc.x), R(spc.y));
           const KC xkp = Xk[kk * b + p], xkq = Xk[kk * b + q];
@@ -1049,10 +1050,10 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
       }
       __syncthreads();
       // columns p, q of K (FP32) and of V (double-float): X <- X G, G = [[c, sp], [-conj(sp), c]];
-      // one (pair, row) per iteration updates both
+      // one (pair, row) per iteration updates both; the pair index runs fastest, so a warp's
+      // accesses stay within one row of K and of V
       for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
-        int kk;
-        const int t = fdiv(e, invb, b, kk);
+        const int t = e % np, kk = e / np;
         const int p = rpair(t, 0), q = rpair(t, 1);
         if (q >= b) continue;
         const float4 cr = rot[2 * t], sp = rot[2 * t + 1];
