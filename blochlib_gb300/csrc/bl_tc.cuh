@@ -374,17 +374,19 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step(DevSys s, int k, 
                    nterms);
   const int sq = nsq, K = nterms;
   const int mC = K / 2, mS = (K - 1) / 2;  // C to X^(2 mC), S to X^(2 mS + 1)
-  {  // X slices into the first tile: one 8-column row chunk per thread and iteration
+  {  // X slices into the first tile: one 8-column row chunk per thread and iteration, rows
+     // fastest (a warp's 16-byte row stores fill whole row groups: no bank conflicts), H read
+     // down its columns (H is symmetric, its (r, q) and (q, r) sums alike), contiguous
     const float2 sc = scl;
     const int nch = R * (R / 8);
     for (int t = tid; t < nch; t += kTcThreads) {
-      const int r = t / (R / 8), c0 = (t % (R / 8)) * 8;
+      const int r = t % R, c0 = (t / R) * 8;
       float hi[8], lo[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int q = c0 + j;
         float2 x = make_float2(0.f, 0.f);
-        if (r < b && q < b) x = dfv_mul(sc, H[r * b + q]);
+        if (r < b && q < b) x = dfv_mul(sc, H[q * b + r]);
         hi[j] = x.x, lo[j] = x.y;
       }
       tc::store_row8(Bf[0], pe, tc::tix(r, c0, R), hi, lo);
@@ -621,17 +623,18 @@ __global__ void __launch_bounds__(tc::kTcThreads, 1) k_tc_step_stk(DevSys s, int
   tc_step_prologue(s, k, c, i, fk, red, H, base, 8 * plS + tc::tile_bytes(b), scl, nsq, nterms);
   const int sq = nsq, K = nterms;
   const int mC = K / 2;  // C to X^(2 mC), S to X^(2 mC + 1)
-  {  // X slices into both halves of XS: one 8-column row chunk per thread and iteration
+  {  // X slices into both halves of XS: one 8-column row chunk per thread and iteration, rows
+     // fastest, H read down its columns (as in k_tc_step)
     const float2 sc = scl;
     const int nch = R * (R / 8);
     for (int t = tid; t < nch; t += kTcThreads) {
-      const int r = t / (R / 8), c0 = (t % (R / 8)) * 8;
+      const int r = t % R, c0 = (t / R) * 8;
       float hi[8], lo[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const int q = c0 + j;
         float2 x = make_float2(0.f, 0.f);
-        if (r < b && q < b) x = dfv_mul(sc, H[r * b + q]);
+        if (r < b && q < b) x = dfv_mul(sc, H[q * b + r]);
         hi[j] = x.x, lo[j] = x.y;
       }
       tc::store_row8(XS, peS, tc::tix(r, c0, R), hi, lo);
