@@ -1,6 +1,7 @@
 // C ABI of the engine (include/blochlib_gb300.h).  Converts exceptions to bl_status.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -94,6 +95,7 @@ bl::FidParams to_params(const bl_p2p_params *p) {
 
 extern "C" {
 
+static void release_region(bl_ctx *ctx);
 static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder &pw, const bl::CMatrix &ro,
                           const bl::CMatrix &det, const bl::FidParams &p, double *fid_out, double *sw_out);
 
@@ -226,6 +228,7 @@ bl_status bl_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, 
   *out = nullptr;
   return guarded([&] {
     int N = sys->s().dim();
+    release_region(ctx);
     std::unique_ptr<bl_job> j(new bl_job);
     j->j.reset(new bl::Job(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
     *out = j.release();
@@ -238,6 +241,7 @@ bl_status bl_p2p_job_create(bl_ctx *ctx, const bl_system *sys, const bl_powder *
   *out = nullptr;
   return guarded([&] {
     int N = sys->s().dim();
+    release_region(ctx);
     std::unique_ptr<bl_job> j(new bl_job);
     j->j.reset(new bl::Job(ctx->c, sys->s(), pw->p, load_op(ro, N), load_op(det, N), to_params(params)));
     *out = j.release();
@@ -351,10 +355,24 @@ bl_status bl_probe_fp32(bl_ctx *ctx, double *tflops) {
   return guarded([&] { *tflops = bl::probe_fp32_tflops(ctx->c); });
 }
 
-// One FID with the job in the context's region when the whole powder fits one batch of the
-// budget (the layout and results of a freshly allocated job; the region is reused by the next
-// call).  Returns false, having done nothing, when it does not fit: the caller then runs a
-// job of its own (batched by the budget).
+// The context's region back to the device (a resident job sizes its batches from the free
+// memory, which the region would otherwise hold).
+static void release_region(bl_ctx *ctx) {
+  std::lock_guard<std::mutex> lock(ctx->mu);
+  if (ctx->region) {
+    cudaSetDevice(ctx->c.device);
+    cudaFree(ctx->region);
+  }
+  ctx->region = nullptr, ctx->region_bytes = 0;
+}
+
+// One FID with the job in the context's region: the whole powder in one batch when it fits
+// the budget, else batches sized to a region of the budget (the batches a job of its own
+// would run; results are independent of the batch).  The region stays with the context for
+// the next call, so a repeated call allocates and frees nothing (on c2, a job of its own
+// spent ~75 ms per call mapping and unmapping its ~170 GB of batch buffers).  Returns false,
+// having done nothing, when not even one batch fits: the caller then runs a job of its own,
+// which reports the error.
 static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder &pw, const bl::CMatrix &ro,
                           const bl::CMatrix &det, const bl::FidParams &p, double *fid_out, double *sw_out) {
   std::lock_guard<std::mutex> lock(ctx->mu);
@@ -364,20 +382,21 @@ static bool fid_in_region(bl_ctx *ctx, const bl::SpinSystem &s, const bl::Powder
   size_t fr = 0, tot = 0;
   if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return false;
   const size_t budget = ctx->c.hbm_budget ? ctx->c.hbm_budget : size_t(0.6 * double(fr + ctx->region_bytes));
-  if (full > budget) {  // batched job of its own: give it the region's memory back
+  const size_t want = std::min(full, budget);
+  if (want < lo) {  // not one batch: give the region's memory back to a job of its own
     if (ctx->region) cudaFree(ctx->region);
     ctx->region = nullptr, ctx->region_bytes = 0;
     return false;
   }
-  if (full > ctx->region_bytes) {
+  if (want > ctx->region_bytes) {
     if (ctx->region) cudaFree(ctx->region);
     ctx->region = nullptr, ctx->region_bytes = 0;
-    if (cudaMalloc(&ctx->region, full) != cudaSuccess) {
+    if (cudaMalloc(&ctx->region, want) != cudaSuccess) {
       cudaGetLastError();
       ctx->region = nullptr;
       return false;
     }
-    ctx->region_bytes = full;
+    ctx->region_bytes = want;
   }
   const size_t saved = ctx->c.hbm_budget;  // job_in_region sets the budget of the region
   struct Restore {

@@ -141,7 +141,11 @@ int bl_powder_size(const bl_powder *pw);
 bl_status bl_powder_get(const bl_powder *pw, double *theta, double *phi, double *gamma, double *weight);
 void bl_powder_destroy(bl_powder *pw);
 
-/* Powder FID: fid_out = 2*npts doubles; *sw_out = the sweep width actually used. */
+/* Powder FID: fid_out = 2*npts doubles; *sw_out = the sweep width actually used.  The call
+ * builds its job in a device region that the context keeps for the next call (the whole
+ * powder in one batch when it fits the context's budget, else batches sized to a region of
+ * the budget), so repeated calls allocate nothing; bl_job_create, bl_p2p_job_create and
+ * bl_ctx_destroy give the region back. */
 bl_status bl_powder_fid(bl_ctx *ctx, const bl_system *sys, const bl_powder *pw, const double *ro,
                         const double *det, const bl_fid_params *params, double *fid_out, double *sw_out);
 /* The stated error of the last FID this thread received (bl_powder_fid, or bl_server_poll
