@@ -89,11 +89,24 @@ def _c1_job(count=None):
 
 
 def test_batched_run_is_bitwise_identical_to_single_batch():
+    """Several batches (the one-shot call batches inside the context's kept region) equal one
+    batch bit for bit; a second call reuses the region, a resident job on the context takes
+    the region back, and the next one-shot call builds it again."""
     job, rows = _c1_job(200)
     one = gpu_fid(job, rows)
     small = bl.Context(0, hbm_budget=40 << 20)  # forces several crystallite batches
     many = gpu_fid(job, rows, ctx=small)
     np.testing.assert_array_equal(one, many)
+    np.testing.assert_array_equal(gpu_fid(job, rows, ctx=small), one)
+    lines, kv = parse_job(job)
+    s = bl.SolidSys(lines)
+    pw = bl.powder.from_arrays(theta=rows[:, 1], phi=rows[:, 0], gamma=rows[:, 2], weight=rows[:, 3])
+    res = bl.Job(s, pw, s.op(kv["rho"]), s.op(kv["det"]), int(kv["npts"]), float(kv["sw"]), float(kv["wr"]),
+                 float(kv["rotb"]), ctx=small)
+    res.run()
+    np.testing.assert_array_equal(res.read(), one)
+    res.close()
+    np.testing.assert_array_equal(gpu_fid(job, rows, ctx=small), one)
 
 
 def test_crystallite_alone_equals_crystallite_in_batch():
