@@ -975,34 +975,32 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
   const int bq = b + (b & 1);
   const int np = bq / 2;
   bool conv = false, polish = false;
+  const int nw = (blockDim.x + 31) / 32, wid = threadIdx.x >> 5, lid = threadIdx.x & 31;
   for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
-    double off = 0, dg = 0;
+    // off(K)^2 and diag(K)^2 for the stopping test: FP32 sums per thread (K is FP32), a fixed
+    // shuffle tree per warp, the warps' sums added in FP64 by one thread
+    float off = 0.f, dg = 0.f;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) {
       int q;
       const int r = fdiv(e, invb, b, q);
       const float2 v = Xk[e];
-      if (r < q) off += double(v.x) * v.x + double(v.y) * v.y;
-      else if (r == q) dg += double(v.x) * v.x;
+      if (r < q) off = fmaf(v.x, v.x, fmaf(v.y, v.y, off));
+      else if (r == q) dg = fmaf(v.x, v.x, dg);
     }
-    red[threadIdx.x] = off;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dg += __shfl_xor_sync(0xffffffffu, dg, o);
+    }
+    if (lid == 0) red[2 * wid] = off, red[2 * wid + 1] = dg;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double so = 0;
-      for (int t = 0; t < blockDim.x; ++t) so += red[t];
-      red[0] = so;
+      double so = 0, sd = 0;
+      for (int t = 0; t < nw; ++t) so += red[2 * t], sd += red[2 * t + 1];
+      red[2 * nw] = so, red[2 * nw + 1] = sd;
     }
     __syncthreads();
-    const double offs = red[0];
-    __syncthreads();
-    red[threadIdx.x] = dg;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double sd = 0;
-      for (int t = 0; t < blockDim.x; ++t) sd += red[t];
-      red[0] = sd;
-    }
-    __syncthreads();
-    const double dgs = red[0];
+    const double offs = red[2 * nw], dgs = red[2 * nw + 1];
     __syncthreads();
     const bool small = offs <= 1e-10 * dgs || offs == 0.0;
     if (small && (polish || offs == 0.0)) {
