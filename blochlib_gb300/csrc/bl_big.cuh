@@ -432,7 +432,10 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
   const int bq = b + (b & 1);  // players in the round-robin (one dummy when b is odd)
   const int np = bq / 2;
   bool conv = false, polish = false;
+  const int nw = (blockDim.x + 31) / 32, wid = threadIdx.x >> 5, lid = threadIdx.x & 31;
   for (int sweep = 0; sweep < max_sweeps && !conv; ++sweep) {
+    // off(K)^2 and diag(K)^2: FP64 sums per thread, a fixed shuffle tree per warp, the warps'
+    // sums added by one thread
     double off = 0, dg = 0;
     for (int e = threadIdx.x; e < bb; e += blockDim.x) {
       const int r = e / b, q = e % b;
@@ -440,25 +443,20 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
       if (r < q) off += v.x * v.x + v.y * v.y;
       else if (r == q) dg += v.x * v.x;
     }
-    red[threadIdx.x] = off;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dg += __shfl_xor_sync(0xffffffffu, dg, o);
+    }
+    if (lid == 0) red[2 * wid] = off, red[2 * wid + 1] = dg;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double so = 0;
-      for (int t = 0; t < blockDim.x; ++t) so += red[t];
-      red[0] = so;
+      double so = 0, sd = 0;
+      for (int t = 0; t < nw; ++t) so += red[2 * t], sd += red[2 * t + 1];
+      red[2 * nw] = so, red[2 * nw + 1] = sd;
     }
     __syncthreads();
-    const double offs = red[0];
-    __syncthreads();
-    red[threadIdx.x] = dg;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double sd = 0;
-      for (int t = 0; t < blockDim.x; ++t) sd += red[t];
-      red[0] = sd;
-    }
-    __syncthreads();
-    const double dgs = red[0];
+    const double offs = red[2 * nw], dgs = red[2 * nw + 1];
     __syncthreads();
     if (F32) {  // offs, dgs are the same in every thread: polish too
       const bool small = offs <= 1e-10 * dgs || offs == 0.0;
@@ -524,7 +522,8 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
         }
       }
       __syncthreads();
-      // rows p, q of K:  K <- G^H K
+      // rows p, q of K:  K <- G^H K; a non-trivial rotation then zeroes K_pq, K_qp and the
+      // imaginary parts of K_pp, K_qq (written by the items of columns p and q)
       for (int e = threadIdx.x; e < np * b; e += blockDim.x) {
         const int t = e / b, kk = e % b;
         const int p = rpair(t, 0), q = rpair(t, 1);
@@ -532,15 +531,13 @@ __device__ bool floquet_sweeps(KC *Xk, double2 *Mm, int b, int max_sweeps, const
         const R cc = R(rot(t, 0).x);
         const KC sp = cxm(R(rot(t, 1).x), R(rot(t, 1).y)), spc = cconj(sp);
         const KC xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
-        Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
-        Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
-      }
-      __syncthreads();
-      for (int t = threadIdx.x; t < np; t += blockDim.x) {
-        const int p = rpair(t, 0), q = rpair(t, 1);
-        if (q >= b || (rot(t, 1).x == 0.0 && rot(t, 1).y == 0.0)) continue;
-        Xk[p * b + q] = cxm(R(0), R(0)), Xk[q * b + p] = cxm(R(0), R(0));
-        Xk[p * b + p].y = R(0), Xk[q * b + q].y = R(0);
+        KC np_ = csub(cscale(xpk, cc), cmul(sp, xqk)), nq_ = cadd(cmul(spc, xpk), cscale(xqk, cc));
+        if ((kk == p || kk == q) && !(rot(t, 1).x == 0.0 && rot(t, 1).y == 0.0)) {
+          if (kk == p) np_.y = R(0), nq_ = cxm(R(0), R(0));
+          else np_ = cxm(R(0), R(0)), nq_.y = R(0);
+        }
+        Xk[p * b + kk] = np_;
+        Xk[q * b + kk] = nq_;
       }
       __syncthreads();
     }
@@ -1085,16 +1082,14 @@ __device__ bool floquet_sweeps_df(float2 *Xk, float4 *Vd, int b, int max_sweeps,
         const float cc = cr.x + cr.z;
         const float2 sp = make_float2(s4.x + s4.z, s4.y + s4.w), spc = cconj(sp);
         const float2 xpk = Xk[p * b + kk], xqk = Xk[q * b + kk];
-        Xk[p * b + kk] = csub(cscale(xpk, cc), cmul(sp, xqk));
-        Xk[q * b + kk] = cadd(cmul(spc, xpk), cscale(xqk, cc));
-      }
-      __syncthreads();
-      for (int t = threadIdx.x; t < np; t += blockDim.x) {
-        const int p = rpair(t, 0), q = rpair(t, 1);
-        const float4 s4 = rot[2 * t + 1];
-        if (q >= b || (s4.x == 0.f && s4.y == 0.f)) continue;
-        Xk[p * b + q] = make_float2(0.f, 0.f), Xk[q * b + p] = make_float2(0.f, 0.f);
-        Xk[p * b + p].y = 0.f, Xk[q * b + q].y = 0.f;
+        float2 np_ = csub(cscale(xpk, cc), cmul(sp, xqk)), nq_ = cadd(cmul(spc, xpk), cscale(xqk, cc));
+        // a non-trivial rotation zeroes K_pq, K_qp and the imaginary parts of K_pp, K_qq
+        if ((kk == p || kk == q) && !(s4.x == 0.f && s4.y == 0.f)) {
+          if (kk == p) np_.y = 0.f, nq_ = make_float2(0.f, 0.f);
+          else np_ = make_float2(0.f, 0.f), nq_.y = 0.f;
+        }
+        Xk[p * b + kk] = np_;
+        Xk[q * b + kk] = nq_;
       }
       __syncthreads();
     }
