@@ -318,3 +318,36 @@ def test_second_order_quadrupole_matches_oracle(seed, method):
     fid, sw_g = gpu_fid(job, rows, return_sw=True, step_method=method)
     assert sw_g == sw
     assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
+def test_tensor_core_blocks_of_41_and_50_mixed_within_1e6():
+    """2H + 6 1H with a strong 2H-1H J (total Fz conserved): blocks 1,7,22,41,50,41,22,7,1.
+    The mixed form runs the 41-blocks (up16 = 48: the stacked tiles' lower quarter has no rows)
+    and the 50-block (up16 = 64) on the stacked tensor-core step and Dyson kernels; <= 1e-6
+    against the oracle, and a crystallite alone equals it beside another bit for bit."""
+    rng = np.random.default_rng(4141)
+    lines = ["numspin 7", "T 2H 0"] + [f"T 1H {k}" for k in range(1, 7)]
+    a = rng.uniform(0, 360, 3)
+    lines.append(f"Q {rng.uniform(5e4, 1.5e5):.9g} {rng.uniform(0, 1):.9g} 0 {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    for k in range(1, 7):
+        a = rng.uniform(0, 360, 3)
+        lines.append(f"C {rng.uniform(-2e3, 2e3):.9g} {rng.uniform(-6e3, 6e3):.9g} {rng.uniform(0, 1):.9g} {k} "
+                     f"{a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    for i in range(7):
+        for j in range(i + 1, 7):
+            a = rng.uniform(0, 360, 3)
+            lines.append(f"D {rng.uniform(-1.2e4, 1.2e4):.9g} {i} {j} {a[0]:.9g} {a[1]:.9g} {a[2]:.9g}")
+    lines.append("J 60 0 1 1")
+    assert sorted(bl.SolidSys(lines).blocks())[-3:] == [41, 41, 50]
+    wr = 20e3
+    job = "\n".join(f"spin: {l}" for l in lines) + (
+        f"\nnpts: 300\nsw: {24 * wr!r}\nwr: {wr!r}\nrotb: {W.MAGIC_ANGLE!r}\nrho: Fx\ndet: Fp\n")
+    rows = np.stack([rng.uniform(0, 2 * np.pi, 2), np.arccos(rng.uniform(-1, 1, 2)), rng.uniform(0, 2 * np.pi, 2),
+                     rng.uniform(0.1, 1, 2)], axis=1)
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method="taylor", precision=1)
+    assert 0 < rel(fid, ref) <= 1e-6, rel(fid, ref)
+    masked = rows.copy()
+    masked[1, 3] = 0.0
+    np.testing.assert_array_equal(gpu_fid(job, rows[:1], step_method="taylor", precision=1),
+                                  gpu_fid(job, masked, step_method="taylor", precision=1))
