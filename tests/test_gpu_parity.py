@@ -351,3 +351,16 @@ def test_tensor_core_blocks_of_41_and_50_mixed_within_1e6():
     masked[1, 3] = 0.0
     np.testing.assert_array_equal(gpu_fid(job, rows[:1], step_method="taylor", precision=1),
                                   gpu_fid(job, masked, step_method="taylor", precision=1))
+
+
+def test_tensor_core_step_squarings_mixed_within_1e6():
+    """c2's spin system at 10 steps per rotor period: the scaled step norm is ~4, so every
+    tensor-core step (blocks 56 on the stacked kernel, 70 on the other) takes squarings;
+    <= 1e-6 against the oracle."""
+    cfg = W.config(2)
+    cfg = dict(cfg, sw=10 * cfg["wr"], npts=200)
+    job = W.job_text(cfg)
+    rows = np.stack(cfg["powder"], axis=1)[:2]
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method="taylor", precision=1)
+    assert 0 < rel(fid, ref) <= 1e-6, rel(fid, ref)
