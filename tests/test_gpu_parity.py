@@ -364,3 +364,17 @@ def test_tensor_core_step_squarings_mixed_within_1e6():
     ref, _ = oracle_fid(job, rows)
     fid = gpu_fid(job, rows, step_method="taylor", precision=1)
     assert 0 < rel(fid, ref) <= 1e-6, rel(fid, ref)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_few_steps_per_period_match_oracle(n, precision):
+    """1-3 steps per rotor period (the gamma loop sums 10, 5 and 3 shifted runs): Fave's
+    transforms of length 2-8, below the three-stage register passes (the plain load and the
+    one- and two-stage passes) in both forms."""
+    job, rows = random_system(7)
+    lines, kv = parse_job(job)
+    job = job.replace(f"sw: {kv['sw']}", f"sw: {n * float(kv['wr'])!r}")
+    ref, _ = oracle_fid(job, rows)
+    fid = gpu_fid(job, rows, step_method="taylor", precision=precision)
+    assert rel(fid, ref) <= (TOL if precision == 0 else 1e-6), rel(fid, ref)
