@@ -154,3 +154,22 @@ def test_small_requests_pass_a_blocked_large_head():
     for t in ts:
         np.testing.assert_array_equal(res[t][1], direct)
     srv.close()
+
+
+def test_tensor_core_request_is_the_same_alone_and_in_the_mix():
+    """A c2-sized mixed request (8 x 1H: its blocks 56 and 70 run on the tensor-core step and
+    Dyson kernels) gives the direct call's FID bit for bit, alone and among other requests
+    running on the other lanes."""
+    srv = bl.Server(0, lanes=4, pool_bytes=24 << 30)
+    probe = _job(W.config(2), 32)
+    t = srv.submit(**probe, precision=1, step_method="taylor")
+    alone = _wait(srv, [t], timeout=300)[t][1]
+    others = [srv.submit(**_job(W.config(3, 200 + i), 64), precision=i % 2, step_method="taylor") for i in range(6)]
+    tp = srv.submit(**probe, precision=1, step_method="taylor")
+    res = _wait(srv, others + [tp], timeout=300)
+    assert all(r[0] == srv.DONE for r in res.values())
+    np.testing.assert_array_equal(res[tp][1], alone)
+    direct = bl.oneFID(probe["sys"], probe["npts"], probe["sw"], probe["wr"], probe["rotb"], precision=1,
+                       step_method="taylor").FID(probe["pw"], probe["ro"], probe["det"])
+    np.testing.assert_array_equal(alone, direct)
+    srv.close()
