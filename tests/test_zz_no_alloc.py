@@ -54,6 +54,21 @@ def test_noalloc_matches_allocating_entry_point_twice(cfg, count):
         assert rel(fid, ref) <= TOL, rel(fid, ref)
 
 
+def test_noalloc_mixed_form_matches_allocating_entry_point():
+    """The mixed form (double-float step and Dyson, single-precision stages) through the
+    static scratch, in batches, gives bl_powder_fid's result."""
+    lib = bl.load()
+    ctx = bl.Context(0)
+    cfg = W.config(1)
+    s, pw, ro, det, _ = _inputs(cfg, 200)
+    params = bl.FidParams(cfg["npts"], cfg["sw"], cfg["wr"], cfg["rotb"], 0.0, 1, 1)
+    st, ref, _ = _call(lib.bl_powder_fid, ctx, s, pw, ro, det, params, cfg["npts"])
+    assert st == 0, lib.bl_last_error()
+    st, fid, _ = _call(lib.bl_powder_fid_noalloc, ctx, s, pw, ro, det, params, cfg["npts"])
+    assert st == 0, lib.bl_last_error()
+    assert rel(fid, ref) <= TOL, rel(fid, ref)
+
+
 def test_noalloc_rejects_a_job_beyond_its_scratch():
     lib = bl.load()
     ctx = bl.Context(0)
