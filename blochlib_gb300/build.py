@@ -52,7 +52,7 @@ def build_library(verbose=False, force=False):
     cuda = _cuda_home()
     nvcc = str(cuda / "bin" / "nvcc")
     BUILD.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + [ROOT / "include" / "blochlib_gb300.h"]
+    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [ROOT / "include" / "blochlib_gb300.h"]
     units = [
         (CSRC / "bl_engine.cu", [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                                  "-Xptxas", "-v" if verbose else "-O3"]),
